@@ -1,0 +1,258 @@
+"""Python face of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Loads oracle/_build/libtg_oracle.so (built by oracle/build_oracle.py) and reproduces pytreegrav's
+frontend ordering on top of it: self-gravity targets go in the tree's TreewalkIndices order,
+external targets (and self-gravity against a supplied tree) in their own Morton order, and results
+are scattered back to the caller's order (src/pytreegrav/frontend.py:244-288, 392-416, 514-555,
+659-680). Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module.
+"""
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+_LIB = None
+_i64 = ctypes.c_int64
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int64)
+
+
+class _Tree(ctypes.Structure):
+    _fields_ = [
+        ("npart", _i64),
+        ("num_nodes", _i64),
+        ("node_hi", _i64),
+        ("has_quads", ctypes.c_int),
+        ("has_coincident", ctypes.c_int),
+        ("coord", _dp),
+        ("mass", _dp),
+        ("size", _dp),
+        ("delta", _dp),
+        ("soft", _dp),
+        ("quad", _dp),
+        ("first", _ip),
+        ("next", _ip),
+        ("walk_idx", _ip),
+    ]
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = build_oracle.build()
+        L = ctypes.CDLL(path)
+        L.tgo_build.argtypes = [_dp, _dp, _dp, _i64, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_Tree)]
+        L.tgo_free.argtypes = [ctypes.POINTER(_Tree)]
+        L.tgo_fields.argtypes = [ctypes.POINTER(_Tree), _dp, _dp, _i64, ctypes.c_int, ctypes.c_int,
+                                 ctypes.c_int, ctypes.c_int, _i64, ctypes.c_double, ctypes.c_double,
+                                 _dp, ctypes.c_int]
+        L.tgo_walk_counts.argtypes = [ctypes.POINTER(_Tree), _dp, _dp, _i64, _i64, ctypes.c_double,
+                                      _ip, _ip, ctypes.c_int]
+        L.tgo_bruteforce.argtypes = [_dp, _dp, _i64, _dp, _dp, _dp, _i64, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_double, _dp, ctypes.c_int]
+        L.tgo_morton_keys.argtypes = [_dp, _i64, _dp, ctypes.c_double, _ip]
+        L.tgo_radix_argsort.argtypes = [_ip, _i64, _ip]
+        L.tgo_morton_order.argtypes = [_dp, _i64, _ip]
+        L.tgo_bounding_cube.argtypes = [_dp, _i64, _dp, _dp]
+        for k in ("tgo_force_kernel", "tgo_potential_kernel", "tgo_tidal_kernel"):
+            getattr(L, k).argtypes = [ctypes.c_double, ctypes.c_double]
+            getattr(L, k).restype = ctypes.c_double
+        _LIB = L
+    return _LIB
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+def _f64c(a, shape=None):
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+def bounding_cube(pos):
+    pos = _f64c(pos, (-1, 3))
+    c = np.zeros(3)
+    s = np.zeros(1)
+    lib().tgo_bounding_cube(_d(pos), len(pos), _d(c), _d(s))
+    return c, float(s[0])
+
+
+def morton_keys(pos, center, size):
+    pos = _f64c(pos, (-1, 3))
+    c = _f64c(center)
+    k = np.empty(len(pos), np.int64)
+    lib().tgo_morton_keys(_d(pos), len(pos), _d(c), float(size), _i(k))
+    return k
+
+
+def radix_argsort(keys):
+    keys = np.ascontiguousarray(keys, dtype=np.int64)
+    p = np.empty(len(keys), np.int64)
+    lib().tgo_radix_argsort(_i(keys), len(keys), _i(p))
+    return p
+
+
+def morton_order(pos):
+    pos = _f64c(pos, (-1, 3))
+    p = np.empty(len(pos), np.int64)
+    if len(pos):
+        lib().tgo_morton_order(_d(pos), len(pos), _i(p))
+    return p
+
+
+class OracleTree:
+    """Host copy of the oracle's octree, with pytreegrav's Octree attribute names."""
+
+    def __init__(self, pos, m=None, softening=None, quadrupole=False, compute_moments=True):
+        pos = _f64c(pos, (-1, 3))
+        n = len(pos)
+        mm = None if m is None else _f64c(m, (n,))
+        hh = np.zeros(n) if softening is None else _f64c(softening, (n,))
+        t = _Tree()
+        rc = lib().tgo_build(_d(pos), None if mm is None else _d(mm), _d(hh), n, int(quadrupole),
+                             int(compute_moments), ctypes.byref(t))
+        if rc:
+            raise RuntimeError(f"oracle build failed ({rc})")
+        self._t = t
+        nn = t.num_nodes
+        self.NumParticles = t.npart
+        self.NumNodes = nn
+        self.node_hi = t.node_hi
+        self.HasQuads = bool(t.has_quads)
+        self.HasCoincidentPoints = bool(t.has_coincident)
+        self.Coordinates = np.ctypeslib.as_array(t.coord, (nn, 3)).copy()
+        self.Masses = np.ctypeslib.as_array(t.mass, (nn,)).copy()
+        self.Sizes = np.ctypeslib.as_array(t.size, (nn,)).copy()
+        self.Deltas = np.ctypeslib.as_array(t.delta, (nn,)).copy()
+        self.Softenings = np.ctypeslib.as_array(t.soft, (nn,)).copy()
+        self.Quadrupoles = np.ctypeslib.as_array(t.quad, (nn, 3, 3)).copy() if t.has_quads else None
+        self.FirstSubnode = np.ctypeslib.as_array(t.first, (nn,)).copy()
+        self.NextBranch = np.ctypeslib.as_array(t.next, (nn,)).copy()
+        self.TreewalkIndices = np.ctypeslib.as_array(t.walk_idx, (n,)).copy()
+
+    def __del__(self):
+        try:
+            lib().tgo_free(ctypes.byref(self._t))
+        except Exception:
+            pass
+
+    def fields(self, pos, soft, potential=False, accel=False, tidal=False, quadrupole=False,
+               group_size=8, theta=0.7, G=1.0, nthreads=0):
+        """FieldsTarget_grouped on targets already in the order to be grouped."""
+        pos = _f64c(pos, (-1, 3))
+        soft = _f64c(soft, (len(pos),))
+        W = int(potential) + 3 * int(accel) + 9 * int(tidal)
+        out = np.zeros((len(pos), W))
+        rc = lib().tgo_fields(ctypes.byref(self._t), _d(pos), _d(soft), len(pos), int(potential),
+                              int(accel), int(tidal), int(quadrupole), int(group_size), float(theta),
+                              float(G), _d(out), int(nthreads))
+        if rc:
+            raise ValueError(f"oracle walk failed ({rc})")
+        res, o = {}, 0
+        if potential:
+            res["potential"] = out[:, 0].copy()
+            o = 1
+        if accel:
+            res["accel"] = out[:, o:o + 3].copy()
+            o += 3
+        if tidal:
+            res["tidal"] = out[:, o:o + 9].reshape(-1, 3, 3).copy()
+        return res
+
+    def walk_counts(self, pos, soft, group_size=8, theta=0.7, nthreads=0):
+        pos = _f64c(pos, (-1, 3))
+        soft = _f64c(soft, (len(pos),))
+        ng = (len(pos) + group_size - 1) // group_size
+        ni = np.zeros(ng, np.int64)
+        no = np.zeros(ng, np.int64)
+        lib().tgo_walk_counts(ctypes.byref(self._t), _d(pos), _d(soft), len(pos), int(group_size),
+                              float(theta), _i(ni), _i(no), int(nthreads))
+        return ni, no
+
+
+def bruteforce(pos_t, h_t, pos_s, m_s, h_s, potential=False, accel=False, tidal=False, mutual=False,
+               G=1.0, nthreads=0):
+    pos_t = _f64c(pos_t, (-1, 3))
+    pos_s = _f64c(pos_s, (-1, 3))
+    h_t = np.zeros(len(pos_t)) if h_t is None else _f64c(h_t, (len(pos_t),))
+    h_s = np.zeros(len(pos_s)) if h_s is None else _f64c(h_s, (len(pos_s),))
+    m_s = _f64c(m_s, (len(pos_s),))
+    W = int(potential) + 3 * int(accel) + 9 * int(tidal)
+    out = np.zeros((len(pos_t), W))
+    lib().tgo_bruteforce(_d(pos_t), _d(h_t), len(pos_t), _d(pos_s), _d(m_s), _d(h_s), len(pos_s),
+                         int(potential), int(accel), int(tidal), int(mutual), float(G), _d(out),
+                         int(nthreads))
+    res, o = {}, 0
+    if potential:
+        res["potential"] = out[:, 0].copy()
+        o = 1
+    if accel:
+        res["accel"] = out[:, o:o + 3].copy()
+        o += 3
+    if tidal:
+        res["tidal"] = out[:, o:o + 9].reshape(-1, 3, 3).copy()
+    return res
+
+
+def self_fields(pos, m, h, potential=False, accel=False, tidal=False, theta=0.7, quadrupole=False,
+                group_size=8, G=1.0, tree=None, nthreads=0):
+    """Potential/Accel/TidalTensor(method='tree') semantics (frontend.py:244-288)."""
+    pos = _f64c(pos, (-1, 3))
+    h = np.zeros(len(pos)) if h is None else _f64c(h, (len(pos),))
+    if tree is None:
+        tree = OracleTree(pos, m, h, quadrupole=quadrupole)
+        idx = tree.TreewalkIndices
+    else:
+        idx = morton_order(pos)
+    res = tree.fields(pos[idx], h[idx], potential, accel, tidal, quadrupole, group_size, theta, G,
+                      nthreads)
+    out = {}
+    for k, v in res.items():
+        o = np.empty_like(v)
+        o[idx] = v
+        out[k] = o
+    return out, tree
+
+
+def target_fields(pos_t, h_t, pos_s, m_s, h_s, potential=False, accel=False, tidal=False, theta=0.7,
+                  quadrupole=False, group_size=8, G=1.0, tree=None, nthreads=0):
+    """PotentialTarget/AccelTarget/TidalTensorTarget(method='tree') semantics (frontend.py:392-416)."""
+    pos_t = _f64c(pos_t, (-1, 3))
+    h_t = np.zeros(len(pos_t)) if h_t is None else _f64c(h_t, (len(pos_t),))
+    if tree is None:
+        tree = OracleTree(pos_s, m_s, h_s, quadrupole=quadrupole)
+    ts = morton_order(pos_t)
+    res = tree.fields(pos_t[ts], h_t[ts], potential, accel, tidal, quadrupole, group_size, theta, G,
+                      nthreads)
+    out = {}
+    for k, v in res.items():
+        o = np.empty_like(v)
+        o[ts] = v
+        out[k] = o
+    return out, tree
+
+
+def force_kernel(r, h):
+    return lib().tgo_force_kernel(float(r), float(h))
+
+
+def potential_kernel(r, h):
+    return lib().tgo_potential_kernel(float(r), float(h))
+
+
+def tidal_kernel(r, h):
+    return lib().tgo_tidal_kernel(float(r), float(h))
+
+
+def num_threads():
+    return os.cpu_count() or 1
