@@ -1,0 +1,136 @@
+/*
+ * pytreegrav_gb300 -- C ABI of the GB300 (sm_103a) Barnes-Hut gravity engine.
+ *
+ * Drop-in boundary for pytreegrav's tree and brute-force paths. Every entry point takes plain
+ * pointers and sizes, returns a tg_status, and runs on the CUDA stream passed as `stream`
+ * (a cudaStream_t; NULL = the legacy default stream). Arrays are C-contiguous float64:
+ * positions (n, 3), masses/softenings (n,), outputs (n, W) packed potential | accel(3) |
+ * tidal(9), only the requested fields, in the caller's order.
+ *
+ * `mem` says where the caller's arrays live: TG_MEM_HOST (pageable or pinned host memory; the
+ * library copies in and out on `stream` and synchronises before returning) or TG_MEM_DEVICE
+ * (device pointers; the call is asynchronous on `stream` except where noted).
+ *
+ * Citations name the pytreegrav interface each entry replaces (paths relative to the pytreegrav
+ * project).
+ */
+#ifndef PYTREEGRAV_GB300_H
+#define PYTREEGRAV_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    TG_OK = 0,
+    TG_ERR_BAD_ARG = 1,        /* ValueError/TypeError in the Python layer */
+    TG_ERR_NONFINITE = 2,      /* non-finite input (frontend.py:123-125) */
+    TG_ERR_OOM = 3,            /* device allocation failed */
+    TG_ERR_STACK_OVERFLOW = 4, /* a walk's node stack overflowed (result not written) */
+    TG_ERR_ITER_LIMIT = 5,     /* a bounded device loop ran out of iterations */
+    TG_ERR_QUEUE_TIMEOUT = 6,  /* a work queue did not drain within its bound */
+    TG_ERR_CUDA = 7,           /* a CUDA runtime call failed; see tg_last_error() */
+    TG_ERR_NO_QUADRUPOLES = 8  /* quadrupole walk on a monopole tree (frontend.py:28-37) */
+} tg_status;
+
+enum { TG_MEM_HOST = 0, TG_MEM_DEVICE = 1 };
+
+/* Field bits for tg_tree_fields / tg_bruteforce. */
+enum { TG_FIELD_POTENTIAL = 1, TG_FIELD_ACCEL = 2, TG_FIELD_TIDAL = 4 };
+
+/* Arithmetic of a walk or brute-force sum. */
+enum { TG_FP32 = 0, TG_FP64 = 1 };
+
+typedef struct tg_tree_s *tg_tree;
+
+/* Description of a built tree. Device pointers index the pytreegrav Octree arrays
+ * (octree.py:8-28): particles at [0, npart) in Morton order, nodes at [npart, node_hi). */
+typedef struct {
+    int64_t npart;          /* NumParticles */
+    int64_t num_nodes;      /* NumNodes: capacity, grown as octree.py:1188-1206, 1280-1298 */
+    int64_t node_hi;        /* one past the last allocated node */
+    int32_t has_quads;      /* HasQuads */
+    int32_t has_coincident; /* HasCoincidentPoints */
+    int32_t n_systems;      /* independent systems in the arena (1 unless batched) */
+    int32_t reserved;
+    const double *coord;    /* (node_hi, 3) Coordinates */
+    const double *mass;     /* (node_hi,) Masses */
+    const double *size;     /* (node_hi,) Sizes */
+    const double *delta;    /* (node_hi,) Deltas */
+    const double *soft;     /* (node_hi,) Softenings */
+    const double *quad;     /* (node_hi, 3, 3) Quadrupoles or NULL */
+    const int64_t *first;   /* (node_hi,) FirstSubnode */
+    const int64_t *next;    /* (node_hi,) NextBranch */
+    const int64_t *walk_idx;/* (npart,) TreewalkIndices */
+} tg_tree_info;
+
+/* Last CUDA error string recorded by this thread's most recent failing call. */
+const char *tg_last_error(void);
+
+/* ConstructTree(pos, m, softening, quadrupole, compute_moments) on the radix path
+ * (frontend.py:73-142 -> octree.py:664-723, 817-1091, 199-292).
+ * m == NULL: zero masses and compute_moments forced off (frontend.py:115-117).
+ * h == NULL: zero softenings. Synchronises `stream` (the node count is data dependent). */
+tg_status tg_tree_build(const double *pos, const double *m, const double *h, int64_t n,
+                        int quadrupole, int compute_moments, int mem, void *stream, tg_tree *out);
+
+/* Batched build: n_systems independent systems stored back to back; system s owns particles
+ * [offsets[s], offsets[s+1]). One segmented sort, one tree arena. Each system's tree equals the
+ * tree tg_tree_build would give for that system alone (node indices offset into the arena). */
+tg_status tg_tree_build_batched(const double *pos, const double *m, const double *h,
+                                const int64_t *offsets, int32_t n_systems, int quadrupole,
+                                int mem, void *stream, tg_tree *out);
+
+tg_status tg_tree_info_get(tg_tree tree, tg_tree_info *info);
+
+/* Copy the Octree arrays to host buffers sized for info.num_nodes rows (rows past node_hi are
+ * written as the reference leaves them: zeros, and -1 links). Any pointer may be NULL. */
+tg_status tg_tree_copy_out(tg_tree tree, double *coord, double *mass, double *size, double *delta,
+                           double *soft, double *quad, int64_t *first, int64_t *next,
+                           int64_t *walk_idx, void *stream);
+
+tg_status tg_tree_free(tg_tree tree);
+
+/* FieldsTarget_grouped (grouped_treewalk.py:350-397) at n targets.
+ * order: TG_ORDER_TREE -- targets are the tree's own particles (pos/h ignored, may be NULL),
+ *   results scattered back through TreewalkIndices (frontend.py:244-288);
+ *   TG_ORDER_MORTON -- targets are Morton-sorted by their own bounding cube first
+ *   (grouped_treewalk.py:269-275) and results scattered back (frontend.py:392-416);
+ *   TG_ORDER_GIVEN -- targets are grouped in the order given.
+ * theta > 0; group_size in {1,2,4,8,16,32}; precision TG_FP32 (default engine) or TG_FP64.
+ * grouping: TG_GROUP_BLOCKS -- groups of group_size consecutive targets in walk order, exactly
+ *   pytreegrav's grouping (grouped_treewalk.py:180-182), so the accepted node set is pytreegrav's;
+ *   TG_GROUP_TREE -- groups taken from the tree (subtrees and runs of siblings holding at most
+ *   group_size particles), never straddling a jump of the Morton curve; TG_ORDER_TREE only.
+ * theta_per_group: optional device array of one opening angle per group (NULL = theta). */
+enum { TG_ORDER_TREE = 0, TG_ORDER_MORTON = 1, TG_ORDER_GIVEN = 2 };
+enum { TG_GROUP_BLOCKS = 0, TG_GROUP_TREE = 1 };
+tg_status tg_tree_fields(tg_tree tree, const double *pos, const double *h, int64_t n, int fields,
+                         int quadrupole, double theta, double G, int group_size, int grouping,
+                         int order, int precision, const float *theta_per_group, int mem,
+                         double *out, void *stream);
+
+/* Interaction statistics of the last tg_tree_fields call on this tree: total interactions and
+ * node tests, the deepest node stack seen, and the number of groups. */
+tg_status tg_tree_last_walk_stats(tg_tree tree, int64_t *interactions, int64_t *node_tests,
+                                  int64_t *max_stack, int64_t *groups);
+
+/* _morton_order (grouped_treewalk.py:269-275): the stable permutation sorting points by their
+ * Morton keys in their own bounding cube. perm: int64 (n,). */
+tg_status tg_morton_order(const double *pos, int64_t n, int mem, int64_t *perm, void *stream);
+
+/* Brute force (bruteforce.py). mutual = 1: targets are the sources, self excluded by index
+ * (Potential/Accel/TidalTensor_bruteforce_parallel, bruteforce.py:86-116, 164-206, 319-350);
+ * mutual = 0: target form, r == 0 pairs skipped (bruteforce.py:7-50, 209-256, 353-386; pos_t/h_t
+ * used). precision TG_FP64 reproduces the CPU sums; TG_FP32 is the fast path (the numba-cuda
+ * CudaPotentialBruteforce/CudaAccelBruteforce, cuda.py:627-796). */
+tg_status tg_bruteforce(const double *pos_t, const double *h_t, int64_t nt, const double *pos_s,
+                        const double *m_s, const double *h_s, int64_t ns, int fields, int mutual,
+                        double G, int precision, int mem, double *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,24 @@
+/*
+ * pytreegrav_gb300 measurement utilities (not part of the pytreegrav boundary; used by bench.py).
+ */
+#ifndef PYTREEGRAV_GB300_MEASURE_H
+#define PYTREEGRAV_GB300_MEASURE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Kernels this library has launched since it was loaded (all entry points, all streams). */
+int64_t tg_launch_count(void);
+
+/* FP32 CUDA-core throughput of this GPU, measured: a grid of FFMA chains (8 independent chains per
+ * thread, every SM saturated) timed with CUDA events on `stream`. Writes TFLOP/s (2 flops per FMA)
+ * and the kernel's duration. */
+int tg_measure_fp32_fma(double *tflops, double *ms, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -51,6 +51,11 @@ def lib():
                                  _dp, ctypes.c_int]
         L.tgo_walk_counts.argtypes = [ctypes.POINTER(_Tree), _dp, _dp, _i64, _i64, ctypes.c_double,
                                       _ip, _ip, ctypes.c_int]
+        L.tgo_walk_counts_groups.argtypes = [ctypes.POINTER(_Tree), _dp, _dp, _ip, _ip, _i64, ctypes.c_double,
+                                             _ip, _ip, ctypes.c_int]
+        L.tgo_fields_groups.argtypes = [ctypes.POINTER(_Tree), _dp, _dp, _ip, _ip, _i64, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                        ctypes.c_double, _dp, ctypes.c_int]
         L.tgo_bruteforce.argtypes = [_dp, _dp, _i64, _dp, _dp, _dp, _i64, ctypes.c_int, ctypes.c_int,
                                      ctypes.c_int, ctypes.c_int, ctypes.c_double, _dp, ctypes.c_int]
         L.tgo_morton_keys.argtypes = [_dp, _i64, _dp, ctypes.c_double, _ip]
@@ -178,6 +183,100 @@ class OracleTree:
         lib().tgo_walk_counts(ctypes.byref(self._t), _d(pos), _d(soft), len(pos), int(group_size),
                               float(theta), _i(ni), _i(no), int(nthreads))
         return ni, no
+
+
+def fields_groups(tree, pos, soft, starts, counts, potential=False, accel=False, tidal=False, quadrupole=False,
+                  theta=0.7, G=1.0, nthreads=0):
+    """FP64 grouped walk over explicitly given groups; pos/soft in walk order, out in that order."""
+    pos = _f64c(pos, (-1, 3))
+    soft = _f64c(soft, (len(pos),))
+    starts = np.ascontiguousarray(starts, np.int64)
+    counts = np.ascontiguousarray(counts, np.int64)
+    W = int(potential) + 3 * int(accel) + 9 * int(tidal)
+    out = np.zeros((len(pos), W))
+    rc = lib().tgo_fields_groups(ctypes.byref(tree._t), _d(pos), _d(soft), _i(starts), _i(counts), len(starts),
+                                 int(potential), int(accel), int(tidal), int(quadrupole), float(theta), float(G),
+                                 _d(out), int(nthreads))
+    if rc:
+        raise ValueError(f"oracle walk failed ({rc})")
+    res, o = {}, 0
+    if potential:
+        res["potential"] = out[:, 0].copy()
+        o = 1
+    if accel:
+        res["accel"] = out[:, o:o + 3].copy()
+        o += 3
+    if tidal:
+        res["tidal"] = out[:, o:o + 9].reshape(-1, 3, 3).copy()
+    return res
+
+
+def tree_groups(tree, G=32):
+    """The engine's tree grouping restated: subtrees and runs of siblings of at most G particles,
+    a run never reaching into a large sibling's cell. Returns (starts, counts) in Morton order."""
+    N, node_hi = tree.NumParticles, tree.node_hi
+    first, nxt = tree.FirstSubnode, tree.NextBranch
+    pos = tree.Coordinates[:N]
+    size = tree.Sizes
+    geo = OracleTree(pos, None, None).Coordinates  # geometric cell centres, same topology
+
+    def children(f):
+        c, out = first[f], []
+        while c != nxt[f] and c >= 0:
+            out.append(c)
+            c = nxt[c]
+        return out
+
+    lo = np.zeros(node_hi, np.int64)
+    hi = np.zeros(node_hi, np.int64)
+    for f in range(node_hi - 1, N - 1, -1):
+        ch = children(f)
+        lo[f] = min(c if c < N else lo[c] for c in ch)
+        hi[f] = max(c + 1 if c < N else hi[c] for c in ch)
+    S, C = [], []
+    for f in range(N, node_hi):
+        if hi[f] - lo[f] <= G:
+            if f == N:
+                S.append(lo[f]); C.append(hi[f] - lo[f])
+            continue
+        ch = children(f)
+        big = [(geo[c] - 0.5 * size[c], geo[c] + 0.5 * size[c]) for c in ch if c >= N and hi[c] - lo[c] > G]
+        run_lo, run, rb = -1, 0, None
+        for c in ch:
+            l, h = (c, c + 1) if c < N else (lo[c], hi[c])
+            if h - l > G:
+                if run:
+                    S.append(run_lo); C.append(run)
+                run = 0
+                continue
+            b = (pos[l:h].min(0), pos[l:h].max(0))
+            if run:
+                nb = (np.minimum(rb[0], b[0]), np.maximum(rb[1], b[1]))
+                hits = any(np.all(nb[0] <= B[1]) and np.all(nb[1] >= B[0]) for B in big)
+                if run + (h - l) <= G and not hits:
+                    run += h - l
+                    rb = nb
+                    continue
+                S.append(run_lo); C.append(run)
+            run_lo, run, rb = l, h - l, b
+        if run:
+            S.append(run_lo); C.append(run)
+    S, C = np.array(S, np.int64), np.array(C, np.int64)
+    o = np.argsort(S)
+    return S[o], C[o]
+
+
+def walk_counts_groups(tree, pos, soft, starts, counts, theta=0.7, nthreads=0):
+    """Interactions and opened nodes per explicitly given group (pos/soft in walk order)."""
+    pos = _f64c(pos, (-1, 3))
+    soft = _f64c(soft, (len(pos),))
+    starts = np.ascontiguousarray(starts, np.int64)
+    counts = np.ascontiguousarray(counts, np.int64)
+    ni = np.zeros(len(starts), np.int64)
+    no = np.zeros(len(starts), np.int64)
+    lib().tgo_walk_counts_groups(ctypes.byref(tree._t), _d(pos), _d(soft), _i(starts), _i(counts), len(starts),
+                                 float(theta), _i(ni), _i(no), int(nthreads))
+    return ni, no
 
 
 def bruteforce(pos_t, h_t, pos_s, m_s, h_s, potential=False, accel=False, tidal=False, mutual=False,

@@ -648,6 +648,44 @@ static inline double rmin_to_box(const double *c, const double *bmin, const doub
     return sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
 }
 
+static void walk_group(const tgo_tree *t, const double *pos, const double *soft, int64_t a, int64_t b, field_set f,
+                       int W, double theta, double G, double *out) {
+    int64_t m = b - a;
+    double bmin[3], bmax[3], hmax;
+    group_bbox(pos, soft, a, b, bmin, bmax, &hmax);
+    double *acc = (double *)calloc(m * W, sizeof(double));
+    int64_t no = t->npart;
+    while (no > -1) {
+        double r_min = rmin_to_box(t->coord + 3 * no, bmin, bmax);
+        double h = pymax(t->soft[no], hmax);
+        if (no < t->npart || accept(r_min, h, t->size[no], t->delta[no], theta)) {
+            field_kernel(t, no, a, b, pos, soft, acc, W, f);
+            no = t->next[no];
+        } else {
+            no = t->first[no];
+        }
+    }
+    for (int64_t ti = a; ti < b; ti++)
+        for (int k = 0; k < W; k++) out[ti * W + k] = G * acc[(ti - a) * W + k];
+    free(acc);
+}
+
+/* The same walk over explicitly given groups [start, start + count) of pos. */
+int tgo_fields_groups(const tgo_tree *t, const double *pos, const double *soft, const int64_t *start,
+                      const int64_t *count, int64_t ngroups, int want_pot, int want_acc, int want_tidal,
+                      int quadrupole, double theta, double G, double *out, int nthreads) {
+    if (!(want_pot || want_acc || want_tidal)) return 1;
+    if (quadrupole && !t->has_quads) return 2;
+    field_set f = {want_pot, want_acc, want_tidal, quadrupole};
+    int W = want_pot + 3 * want_acc + 9 * want_tidal;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+    for (int64_t gi = 0; gi < ngroups; gi++) walk_group(t, pos, soft, start[gi], start[gi] + count[gi], f, W, theta, G, out);
+    return 0;
+}
+
 /* The traversal core built by _make_core (grouped_treewalk.py:163-241). */
 int tgo_fields(const tgo_tree *t, const double *pos, const double *soft, int64_t n, int want_pot,
                int want_acc, int want_tidal, int quadrupole, int64_t group_size, double theta,
@@ -697,6 +735,37 @@ int tgo_walk_counts(const tgo_tree *t, const double *pos, const double *soft, in
     for (int64_t gi = 0; gi < ngroups; gi++) {
         int64_t a = gi * group_size;
         int64_t b = a + group_size < n ? a + group_size : n;
+        double bmin[3], bmax[3], hmax;
+        group_bbox(pos, soft, a, b, bmin, bmax, &hmax);
+        int64_t ni = 0, no_open = 0;
+        int64_t no = t->npart;
+        while (no > -1) {
+            double r_min = rmin_to_box(t->coord + 3 * no, bmin, bmax);
+            double h = pymax(t->soft[no], hmax);
+            if (no < t->npart || accept(r_min, h, t->size[no], t->delta[no], theta)) {
+                ni++;
+                no = t->next[no];
+            } else {
+                no_open++;
+                no = t->first[no];
+            }
+        }
+        n_interactions[gi] = ni;
+        n_opened[gi] = no_open;
+    }
+    return 0;
+}
+
+/* Interaction counts of the same walk for explicitly given groups [start, start + count). */
+int tgo_walk_counts_groups(const tgo_tree *t, const double *pos, const double *soft, const int64_t *start,
+                           const int64_t *count, int64_t ngroups, double theta, int64_t *n_interactions,
+                           int64_t *n_opened, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+    for (int64_t gi = 0; gi < ngroups; gi++) {
+        int64_t a = start[gi], b = start[gi] + count[gi];
         double bmin[3], bmax[3], hmax;
         group_bbox(pos, soft, a, b, bmin, bmax, &hmax);
         int64_t ni = 0, no_open = 0;

@@ -52,10 +52,19 @@ int tgo_fields(const tgo_tree *t, const double *pos, const double *soft, int64_t
                int want_acc, int want_tidal, int quadrupole, int64_t group_size, double theta,
                double G, double *out, int nthreads);
 
+/* The same walk over explicitly given groups [start[g], start[g] + count[g]) of pos. */
+int tgo_fields_groups(const tgo_tree *t, const double *pos, const double *soft, const int64_t *start,
+                      const int64_t *count, int64_t ngroups, int want_pot, int want_acc, int want_tidal,
+                      int quadrupole, double theta, double G, double *out, int nthreads);
+
 /* Per-group interaction and opened-node counts of the same walk, for the cost model. */
 int tgo_walk_counts(const tgo_tree *t, const double *pos, const double *soft, int64_t n,
                     int64_t group_size, double theta, int64_t *n_interactions, int64_t *n_opened,
                     int nthreads);
+
+int tgo_walk_counts_groups(const tgo_tree *t, const double *pos, const double *soft, const int64_t *start,
+                           const int64_t *count, int64_t ngroups, double theta, int64_t *n_interactions,
+                           int64_t *n_opened, int nthreads);
 
 /* Brute force.  mode 0: target form (r == 0 pairs skipped, bruteforce.py:7-50, 209-256, 353-386);
  * mode 1: mutual form (self excluded by index, bruteforce.py:86-116, 164-206, 319-350).

@@ -1,0 +1,143 @@
+"""ctypes binding of libpytreegrav_gb300.so (the C ABI in include/pytreegrav_gb300.h).
+
+The library is built in-tree (pytreegrav_gb300/_build/) by pytreegrav_gb300.build. There is no CPU
+fallback: if the library is missing or cannot run, every compute call raises.
+"""
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libpytreegrav_gb300.so")
+
+TG_OK = 0
+TG_ERR_BAD_ARG = 1
+TG_ERR_NONFINITE = 2
+TG_ERR_OOM = 3
+TG_ERR_STACK_OVERFLOW = 4
+TG_ERR_ITER_LIMIT = 5
+TG_ERR_QUEUE_TIMEOUT = 6
+TG_ERR_CUDA = 7
+TG_ERR_NO_QUADRUPOLES = 8
+
+TG_MEM_HOST = 0
+TG_MEM_DEVICE = 1
+TG_FIELD_POTENTIAL = 1
+TG_FIELD_ACCEL = 2
+TG_FIELD_TIDAL = 4
+TG_FP32 = 0
+TG_FP64 = 1
+TG_ORDER_TREE = 0
+TG_ORDER_MORTON = 1
+TG_ORDER_GIVEN = 2
+TG_GROUP_BLOCKS = 0
+TG_GROUP_TREE = 1
+
+# every extern "C" symbol declared in include/pytreegrav_gb300.h
+EXPORTS = [
+    "tg_last_error",
+    "tg_tree_build",
+    "tg_tree_build_batched",
+    "tg_tree_info_get",
+    "tg_tree_copy_out",
+    "tg_tree_free",
+    "tg_tree_fields",
+    "tg_tree_last_walk_stats",
+    "tg_morton_order",
+    "tg_bruteforce",
+]
+
+
+class TreeInfo(ctypes.Structure):
+    _fields_ = [
+        ("npart", ctypes.c_int64),
+        ("num_nodes", ctypes.c_int64),
+        ("node_hi", ctypes.c_int64),
+        ("has_quads", ctypes.c_int32),
+        ("has_coincident", ctypes.c_int32),
+        ("n_systems", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("coord", ctypes.c_void_p),
+        ("mass", ctypes.c_void_p),
+        ("size", ctypes.c_void_p),
+        ("delta", ctypes.c_void_p),
+        ("soft", ctypes.c_void_p),
+        ("quad", ctypes.c_void_p),
+        ("first", ctypes.c_void_p),
+        ("next", ctypes.c_void_p),
+        ("walk_idx", ctypes.c_void_p),
+    ]
+
+
+class GravityError(RuntimeError):
+    """A device-side failure reported by the library (CUDA error, stack overflow, ...)."""
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def _declare(L):
+    vp, i64, i32, dbl = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_double
+    ci = ctypes.c_int
+    L.tg_last_error.argtypes = []
+    L.tg_last_error.restype = ctypes.c_char_p
+    L.tg_tree_build.argtypes = [vp, vp, vp, i64, ci, ci, ci, vp, ctypes.POINTER(vp)]
+    L.tg_tree_build_batched.argtypes = [vp, vp, vp, vp, i32, ci, ci, vp, ctypes.POINTER(vp)]
+    L.tg_tree_info_get.argtypes = [vp, ctypes.POINTER(TreeInfo)]
+    L.tg_tree_copy_out.argtypes = [vp] * 10 + [vp]
+    L.tg_tree_free.argtypes = [vp]
+    L.tg_tree_fields.argtypes = [vp, vp, vp, i64, ci, ci, dbl, dbl, ci, ci, ci, ci, vp, ci, vp, vp]
+    L.tg_tree_last_walk_stats.argtypes = [vp, vp, vp, vp, vp]
+    L.tg_morton_order.argtypes = [vp, i64, ci, vp, vp]
+    L.tg_bruteforce.argtypes = [vp, vp, i64, vp, vp, vp, i64, ci, ci, dbl, ci, ci, vp, vp]
+    for name in EXPORTS[1:]:
+        getattr(L, name).restype = ci
+
+
+def load(path=None):
+    """Load (once) and return the library; raises if it is missing."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            p = path or LIB_PATH
+            if not os.path.exists(p):
+                raise GravityError(
+                    f"pytreegrav_gb300: the CUDA library {p} is not built; run "
+                    "`python -m pytreegrav_gb300.build` (needs nvcc).")
+            L = ctypes.CDLL(p)
+            _declare(L)
+            _lib = L
+    return _lib
+
+
+def check(rc, what=""):
+    if rc == TG_OK:
+        return
+    L = load()
+    msg = f"{what}: " if what else ""
+    if rc == TG_ERR_BAD_ARG:
+        raise ValueError(msg + "invalid argument")
+    if rc == TG_ERR_NONFINITE:
+        raise RuntimeError(msg + "Invalid input detected - aborting treebuild to avoid going into an infinite loop!")
+    if rc == TG_ERR_OOM:
+        raise MemoryError(msg + "device allocation failed")
+    if rc == TG_ERR_NO_QUADRUPOLES:
+        raise ValueError(
+            "quadrupole=True requires a tree built with quadrupole moments: pass a tree from "
+            "ConstructTree(..., quadrupole=True), or evaluate with quadrupole=False.")
+    if rc == TG_ERR_STACK_OVERFLOW:
+        raise GravityError(msg + "tree walk node stack overflowed (result not written)")
+    if rc == TG_ERR_CUDA:
+        raise GravityError(msg + "CUDA error: " + (L.tg_last_error() or b"").decode())
+    raise GravityError(msg + f"status {rc}")
+
+
+def ptr(a):
+    """Host pointer of a C-contiguous numpy array (or None)."""
+    if a is None:
+        return None
+    return ctypes.c_void_p(a.ctypes.data)

@@ -1,0 +1,1254 @@
+// Octree build on the GPU, reproducing pytreegrav's radix build (octree.py:817-1175) bit for bit.
+//
+// pytreegrav splits Morton-sorted particles top-down with an explicit stack. Here the same tree is
+// derived in parallel from the sorted keys alone:
+//
+//   * L[i], the number of complete 3-bit digits keys i and i+1 share (capped at 21), fixes every
+//     node: a node at level k is a maximal run of >= 2 keys sharing their top 3k bits, so the nodes
+//     starting at particle i are exactly the levels L[i-1]+1 .. L[i]. A prefix sum of those counts
+//     enumerates all nodes; binary searches over the keys give each node's end and parent.
+//   * FirstSubnode/NextBranch follow from L in O(1): the element after a subtree ending at e is
+//     the outermost run starting at e (octree.py:1003-1009's sibling threading).
+//   * Runs whose 63-bit keys are identical are re-keyed relative to their cell and re-split, up to
+//     three rounds (octree.py:928-943, RekeySlice 1093-1126), then bucketed (BuildBucket 1128-1175).
+//   * Node indices: the serial split allocates a node's children when it pops the node, and pops
+//     in reverse preorder -- which sorts nodes by (end descending, depth ascending). Sorting every
+//     node by (its allocating parent's position in that order, its own start) therefore yields the
+//     reference's node numbering exactly.
+//   * Moments are rolled up bottom-up in FP64 with pytreegrav's summation order (particles in
+//     Morton order, then child nodes by descending index; octree.py:199-292), every operation
+//     rounded once (no FMA), so masses, centres of mass, Deltas and quadrupoles match bit for bit.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <type_traits>
+#include <vector>
+
+#include "tg_tree.cuh"
+
+namespace tg {
+
+__constant__ double c_octant[8][3] = {
+    {-0.25, -0.25, -0.25}, {0.25, -0.25, -0.25}, {-0.25, 0.25, -0.25}, {0.25, 0.25, -0.25},
+    {-0.25, -0.25, 0.25},  {0.25, -0.25, 0.25},  {-0.25, 0.25, 0.25},  {0.25, 0.25, 0.25},
+};
+
+// Link references before final numbering: >= 0 particle (arena index), -1 none, <= -2 node slot.
+__device__ __forceinline__ int64_t node_ref(int64_t slot) { return -(slot + 2); }
+
+__device__ __forceinline__ int64_t find_seg(const int64_t *off, int nseg, int64_t i) {
+    // last s with off[s] <= i
+    int lo = 0, hi = nseg;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (off[mid] <= i) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Bounding cube (octree.py:539-574): exact min/max through order-preserving integer atomics.
+__global__ void k_bbox_init(unsigned long long *mn, unsigned long long *mx, int nsys) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 3 * nsys) {
+        mn[i] = ~0ull;
+        mx[i] = 0ull;
+    }
+}
+
+constexpr int BB_THREADS = 256, BB_ITEMS = 8;
+
+__global__ void __launch_bounds__(BB_THREADS) k_bbox(const double *pos, int64_t n, const int64_t *sys_off, int nsys,
+                                                     unsigned long long *mn, unsigned long long *mx) {
+    int64_t tile0 = (int64_t)blockIdx.x * BB_THREADS * BB_ITEMS;
+    if (tile0 >= n) return;
+    int64_t tile1 = min(tile0 + (int64_t)BB_THREADS * BB_ITEMS, n) - 1;
+    int s0 = (int)find_seg(sys_off, nsys, tile0), s1 = (int)find_seg(sys_off, nsys, tile1);
+    if (s0 == s1) {
+        unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0, 0, 0};
+        for (int it = 0; it < BB_ITEMS; it++) {
+            int64_t i = tile0 + (int64_t)it * BB_THREADS + threadIdx.x;
+            if (i <= tile1) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    unsigned long long u = dbl_to_ordered(pos[3 * i + k]);
+                    lo[k] = min(lo[k], u);
+                    hi[k] = max(hi[k], u);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            for (int o = 16; o; o >>= 1) {
+                lo[k] = min(lo[k], __shfl_xor_sync(FULL, lo[k], o));
+                hi[k] = max(hi[k], __shfl_xor_sync(FULL, hi[k], o));
+            }
+        }
+        __shared__ unsigned long long slo[3][BB_THREADS / 32], shi[3][BB_THREADS / 32];
+        int w = threadIdx.x >> 5;
+        if (lane_id() == 0)
+            for (int k = 0; k < 3; k++) {
+                slo[k][w] = lo[k];
+                shi[k][w] = hi[k];
+            }
+        __syncthreads();
+        if (threadIdx.x < 3) {
+            int k = threadIdx.x;
+            unsigned long long a = ~0ull, b = 0;
+            for (int ww = 0; ww < BB_THREADS / 32; ww++) {
+                a = min(a, slo[k][ww]);
+                b = max(b, shi[k][ww]);
+            }
+            atomicMin(&mn[3 * s0 + k], a);
+            atomicMax(&mx[3 * s0 + k], b);
+        }
+    } else {
+        for (int it = 0; it < BB_ITEMS; it++) {
+            int64_t i = tile0 + (int64_t)it * BB_THREADS + threadIdx.x;
+            if (i <= tile1) {
+                int s = (int)find_seg(sys_off, nsys, i);
+                for (int k = 0; k < 3; k++) {
+                    unsigned long long u = dbl_to_ordered(pos[3 * i + k]);
+                    atomicMin(&mn[3 * s + k], u);
+                    atomicMax(&mx[3 * s + k], u);
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_bbox_finish(const unsigned long long *mn, const unsigned long long *mx, int nsys, double *center,
+                              double *size) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsys) return;
+    double lo[3], hi[3];
+    for (int k = 0; k < 3; k++) {
+        lo[k] = ordered_to_dbl(mn[3 * s + k]);
+        hi[k] = ordered_to_dbl(mx[3 * s + k]);
+        center[3 * s + k] = dmul(0.5, dadd(hi[k], lo[k]));
+    }
+    double sz = dsub(hi[0], lo[0]);
+    if (dsub(hi[1], lo[1]) > sz) sz = dsub(hi[1], lo[1]);
+    if (dsub(hi[2], lo[2]) > sz) sz = dsub(hi[2], lo[2]);
+    size[s] = sz;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Morton keys (octree.py:54-98), FP64 with every operation rounded once.
+__device__ __forceinline__ uint64_t spread_bits(uint64_t x) {
+    x &= 0x1FFFFFull;
+    x = (x | (x << 32)) & 0x1F00000000FFFFull;
+    x = (x | (x << 16)) & 0x1F0000FF0000FFull;
+    x = (x | (x << 8)) & 0x100F00F00F00F00Full;
+    x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+// int() truncation toward zero, then the clamp to [0, 2^21 - 1] (octree.py:85-96).
+__device__ __forceinline__ uint64_t quantize(double v) {
+    if (v >= 2097152.0) return (1u << MORTON_BITS) - 1;
+    if (!(v > -1.0)) return 0;
+    long long q = __double2ll_rz(v);
+    return q < 0 ? 0 : (uint64_t)q;
+}
+
+__device__ __forceinline__ uint64_t morton_key(double x, double y, double z, const double *c, double size) {
+    double inv = size > 0 ? ddiv(1.0, size) : 0.0;
+    double h = dmul(0.5, size);
+    double c0 = dsub(c[0], h), c1 = dsub(c[1], h), c2 = dsub(c[2], h);
+    uint64_t qx = quantize(dmul(dmul(dsub(x, c0), inv), 2097152.0));
+    uint64_t qy = quantize(dmul(dmul(dsub(y, c1), inv), 2097152.0));
+    uint64_t qz = quantize(dmul(dmul(dsub(z, c2), inv), 2097152.0));
+    return spread_bits(qx) | (spread_bits(qy) << 1) | (spread_bits(qz) << 2);
+}
+
+__global__ void k_keys(const double *pos, int64_t n, const int64_t *sys_off, int nsys, const double *center,
+                       const double *size, uint64_t *keys, uint64_t *keys_copy, uint32_t *vals) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int s = nsys > 1 ? (int)find_seg(sys_off, nsys, i) : 0;
+    uint64_t k = morton_key(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], center + 3 * s, size[s]);
+    keys[i] = k;
+    if (keys_copy) keys_copy[i] = k;
+    vals[i] = (uint32_t)i;
+}
+
+__global__ void k_sys_of(const uint32_t *vals, int64_t n, const int64_t *sys_off, int nsys, uint64_t *out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (uint64_t)find_seg(sys_off, nsys, vals[i]);
+}
+
+// _permute_particles (octree.py:577-603)
+__global__ void k_gather(const uint32_t *perm, int64_t n, const double *pos, const double *m, const double *h,
+                         const uint64_t *keys_in, double *coord, double *mass, double *soft, uint64_t *keys_sorted,
+                         int64_t *walk_idx) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int64_t o = perm[i];
+    coord[3 * i] = pos[3 * o];
+    coord[3 * i + 1] = pos[3 * o + 1];
+    coord[3 * i + 2] = pos[3 * o + 2];
+    mass[i] = m ? m[o] : 0.0;
+    soft[i] = h ? h[o] : 0.0;
+    keys_sorted[i] = keys_in[o];
+    walk_idx[i] = o;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Split rounds. A round works on segments: round 0 has one per system; a later round has one per
+// key-exhausted node of the previous round. Elements e of a round enumerate the segments'
+// particles in order.
+struct Segs {
+    int n = 0;
+    int64_t *lo = nullptr, *hi = nullptr;      // particle range
+    int64_t *root = nullptr;                   // existing root node slot, or -1 to create one
+    double *center = nullptr, *size = nullptr; // cell the keys are relative to
+    int32_t *depth0 = nullptr;                 // depth of the segment root
+    int64_t *next_ref = nullptr;               // NextBranch of the segment root
+    int32_t *sys = nullptr;                    // owning system
+    int64_t *eoff = nullptr;                   // element offsets (n + 1)
+};
+
+struct Nodes {  // node slots in discovery order
+    int64_t cap = 0, count = 0;
+    int64_t *lo = nullptr, *hi = nullptr, *parent = nullptr, *first = nullptr, *next = nullptr;
+    int64_t *aparent = nullptr, *rank = nullptr;  // allocating parent slot, sibling order key
+    int32_t *depth = nullptr, *sys = nullptr;
+    int8_t *level = nullptr;
+    double *center = nullptr, *size = nullptr;
+};
+
+__device__ __forceinline__ int pair_level(uint64_t a, uint64_t b) {
+    int c = __clzll((long long)(a ^ b));  // 64 when equal
+    int l = (c - 1) / 3;
+    return l > MAX_LEVEL ? MAX_LEVEL : l;
+}
+
+__device__ __forceinline__ uint64_t prefix(uint64_t key, int level) {
+    return level <= 0 ? 0 : (key >> (63 - 3 * level));
+}
+
+struct RoundView {
+    const int64_t *seg_lo, *seg_hi, *seg_root, *seg_next, *eoff;
+    const double *seg_center, *seg_size;
+    const int32_t *seg_depth0, *seg_sys;
+    int nseg;
+};
+
+__device__ __forceinline__ void elem_loc(const RoundView &v, int64_t e, int &s, int64_t &i) {
+    s = (int)find_seg(v.eoff, v.nseg, e);
+    i = v.seg_lo[s] + (e - v.eoff[s]);
+}
+
+__global__ void k_levels(RoundView v, int64_t E, const uint64_t *keys, int8_t *L) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    int s;
+    int64_t i;
+    elem_loc(v, e, s, i);
+    L[e] = (i + 1 < v.seg_hi[s]) ? (int8_t)pair_level(keys[i], keys[i + 1]) : (int8_t)-1;
+}
+
+// lowest level of a node starting at element e (e's particle i); root level 0 only at a segment
+// start whose root is created this round.
+__device__ __forceinline__ int lvl0(const RoundView &v, const int8_t *L, int s, int64_t e, int64_t i) {
+    if (i == v.seg_lo[s]) return v.seg_root[s] >= 0 ? 1 : 0;
+    return L[e - 1] + 1;
+}
+
+__global__ void k_counts(RoundView v, int64_t E, const int8_t *L, int64_t *cnt) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    int s;
+    int64_t i;
+    elem_loc(v, e, s, i);
+    int lo = lvl0(v, L, s, e, i);
+    int hi = L[e];
+    if (lo == 0 && hi < 0) hi = 0;  // a one-particle system still has its root
+    cnt[e] = hi >= lo ? (hi - lo + 1) : 0;
+}
+
+// last index in [a, b) with prefix(key, level) == p (keys sorted): upper bound - 1
+__device__ __forceinline__ int64_t upper_prefix(const uint64_t *keys, int64_t a, int64_t b, uint64_t p, int level) {
+    while (a < b) {
+        int64_t mid = (a + b) >> 1;
+        if (prefix(keys[mid], level) <= p) a = mid + 1;
+        else b = mid;
+    }
+    return a;
+}
+__device__ __forceinline__ int64_t lower_prefix(const uint64_t *keys, int64_t a, int64_t b, uint64_t p, int level) {
+    while (a < b) {
+        int64_t mid = (a + b) >> 1;
+        if (prefix(keys[mid], level) < p) a = mid + 1;
+        else b = mid;
+    }
+    return a;
+}
+
+// slot of the node at `level` containing particle i (level >= lvl0 of the segment root)
+__device__ __forceinline__ int64_t node_at(const RoundView &v, const int8_t *L, const int64_t *nstart,
+                                           int64_t slot_base, const uint64_t *keys, int s, int64_t i, int level) {
+    if (level == 0 && v.seg_root[s] >= 0) return v.seg_root[s];
+    int64_t lo = v.seg_lo[s];
+    int64_t p_lo = lower_prefix(keys, lo, i + 1, prefix(keys[i], level), level);
+    int64_t pe = v.eoff[s] + (p_lo - lo);
+    return slot_base + nstart[pe] + (level - lvl0(v, L, s, pe, p_lo));
+}
+
+// NextBranch reference of an element whose particle range ends at e_end (exclusive)
+__device__ __forceinline__ int64_t next_after(const RoundView &v, const int8_t *L, const int64_t *nstart,
+                                              int64_t slot_base, int s, int64_t e_end_particle) {
+    if (e_end_particle >= v.seg_hi[s]) return v.seg_next[s];
+    int64_t pe = v.eoff[s] + (e_end_particle - v.seg_lo[s]);
+    int outer = L[pe - 1] + 1;
+    return (outer <= L[pe]) ? node_ref(slot_base + nstart[pe]) : e_end_particle;
+}
+
+__global__ void k_nodes(RoundView v, int64_t E, const int8_t *L, const int64_t *nstart, const int64_t *cnt,
+                        int64_t slot_base, const uint64_t *keys, Nodes nd, int64_t *exhausted, int *n_exhausted,
+                        int64_t *root_first) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    int s;
+    int64_t i;
+    elem_loc(v, e, s, i);
+    int l0 = lvl0(v, L, s, e, i);
+    uint64_t key = keys[i];
+    int64_t seg_lo = v.seg_lo[s], seg_hi = v.seg_hi[s];
+    // existing segment root (a re-keyed node): its first child is the level-1 run at seg_lo
+    if (i == seg_lo && v.seg_root[s] >= 0) {
+        root_first[s] = (1 <= L[e]) ? node_ref(slot_base + nstart[e]) : i;
+    }
+    for (int64_t j = 0; j < cnt[e]; j++) {
+        int k = l0 + (int)j;
+        int64_t slot = slot_base + nstart[e] + j;
+        int64_t hi = (k == 0) ? seg_hi : upper_prefix(keys, i + 1, seg_hi, prefix(key, k), k);
+        nd.lo[slot] = i;
+        nd.hi[slot] = hi;
+        nd.level[slot] = (int8_t)k;
+        nd.depth[slot] = v.seg_depth0[s] + k;
+        nd.sys[slot] = v.seg_sys[s];
+        int64_t par = (k == 0) ? -1 : node_at(v, L, nstart, slot_base, keys, s, i, k - 1);
+        nd.parent[slot] = par;
+        nd.aparent[slot] = par;
+        nd.rank[slot] = i;
+        // geometric centre: iterate the digits from the segment cell (octree.py:974-978)
+        double c0 = v.seg_center[3 * s], c1 = v.seg_center[3 * s + 1], c2 = v.seg_center[3 * s + 2];
+        double sz = v.seg_size[s];
+        for (int q = 1; q <= k; q++) {
+            int d = (int)((key >> (63 - 3 * q)) & 7);
+            c0 = dadd(c0, dmul(sz, c_octant[d][0]));
+            c1 = dadd(c1, dmul(sz, c_octant[d][1]));
+            c2 = dadd(c2, dmul(sz, c_octant[d][2]));
+            sz = dmul(sz, 0.5);
+        }
+        nd.center[3 * slot] = c0;
+        nd.center[3 * slot + 1] = c1;
+        nd.center[3 * slot + 2] = c2;
+        nd.size[slot] = sz;
+        nd.next[slot] = next_after(v, L, nstart, slot_base, s, hi);
+        if (k == MAX_LEVEL) {
+            nd.first[slot] = -1;  // set by the re-key round or the bucket
+            int q = atomicAdd(n_exhausted, 1);
+            exhausted[q] = slot;
+        } else {
+            nd.first[slot] = (k + 1 <= L[e]) ? node_ref(slot + 1) : i;
+        }
+    }
+}
+
+__global__ void k_particles(RoundView v, int64_t E, const int8_t *L, const int64_t *nstart, int64_t slot_base,
+                            const uint64_t *keys, int64_t *p_parent, int64_t *p_next) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    int s;
+    int64_t i;
+    elem_loc(v, e, s, i);
+    int lprev = (i == v.seg_lo[s]) ? -1 : L[e - 1];
+    int K = max(lprev, (int)L[e]);
+    if (K >= MAX_LEVEL) return;  // inside a key-exhausted run: the next round places it
+    if (K < 0) K = 0;            // lone particle of its segment: child of the root
+    p_parent[i] = node_at(v, L, nstart, slot_base, keys, s, i, K);
+    p_next[i] = next_after(v, L, nstart, slot_base, s, i + 1);
+}
+
+__global__ void k_set_root_first(const int64_t *seg_root, const int64_t *root_first, int nseg, int64_t *nd_first) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nseg && seg_root[s] >= 0) nd_first[seg_root[s]] = root_first[s];
+}
+
+// Next round's segments from the exhausted node slots.
+__global__ void k_make_segs(const int64_t *exh, int n, Nodes nd, Segs sg) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    int64_t x = exh[q];
+    sg.lo[q] = nd.lo[x];
+    sg.hi[q] = nd.hi[x];
+    sg.root[q] = x;
+    sg.center[3 * q] = nd.center[3 * x];
+    sg.center[3 * q + 1] = nd.center[3 * x + 1];
+    sg.center[3 * q + 2] = nd.center[3 * x + 2];
+    sg.size[q] = nd.size[x];
+    sg.depth0[q] = nd.depth[x];
+    sg.next_ref[q] = nd.next[x];
+    sg.sys[q] = nd.sys[x];
+}
+
+__global__ void k_seg_sizes(const int64_t *lo, const int64_t *hi, int n, int64_t *sizes) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) sizes[q] = hi[q] - lo[q];
+}
+
+// RekeySlice (octree.py:1093-1126): keys relative to the node's cell, sorted stably per segment.
+__global__ void k_rekey_keys(RoundView v, int64_t E, const double *coord, uint64_t *k_sort, uint32_t *vals) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    int s;
+    int64_t i;
+    elem_loc(v, e, s, i);
+    k_sort[e] = morton_key(coord[3 * i], coord[3 * i + 1], coord[3 * i + 2], v.seg_center + 3 * s, v.seg_size[s]);
+    vals[e] = (uint32_t)e;
+}
+__global__ void k_rekey_segkeys(RoundView v, const uint32_t *vals, int64_t E, uint64_t *out) {
+    int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < E) out[a] = (uint64_t)find_seg(v.eoff, v.nseg, (int64_t)vals[a]);
+}
+// gather the permuted slice into temporaries (by element), then write back
+__global__ void k_rekey_gather(RoundView v, int64_t E, const uint32_t *vals, const double *coord, const double *mass,
+                               const double *soft, const int64_t *widx, const uint64_t *newkeys_by_elem, double *tc,
+                               double *tm, double *ts, int64_t *tw, uint64_t *tk) {
+    int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= E) return;
+    int64_t esrc = vals[a];
+    int s;
+    int64_t isrc;
+    elem_loc(v, esrc, s, isrc);
+    tc[3 * a] = coord[3 * isrc];
+    tc[3 * a + 1] = coord[3 * isrc + 1];
+    tc[3 * a + 2] = coord[3 * isrc + 2];
+    tm[a] = mass[isrc];
+    ts[a] = soft[isrc];
+    tw[a] = widx[isrc];
+    tk[a] = newkeys_by_elem[esrc];
+}
+__global__ void k_rekey_scatter(RoundView v, int64_t E, const double *tc, const double *tm, const double *ts,
+                                const int64_t *tw, const uint64_t *tk, double *coord, double *mass, double *soft,
+                                int64_t *widx, uint64_t *keys) {
+    int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= E) return;
+    int s;
+    int64_t i;
+    elem_loc(v, a, s, i);
+    coord[3 * i] = tc[3 * a];
+    coord[3 * i + 1] = tc[3 * a + 1];
+    coord[3 * i + 2] = tc[3 * a + 2];
+    mass[i] = tm[a];
+    soft[i] = ts[a];
+    widx[i] = tw[a];
+    keys[i] = tk[a];
+}
+
+// BuildBucket (octree.py:1128-1175) for the nodes still exhausted after three re-keys.
+__global__ void k_bucket_counts(const int64_t *exh, int n, const int64_t *nd_lo, const int64_t *nd_hi, int64_t *nchain) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    int64_t c = nd_hi[exh[q]] - nd_lo[exh[q]];
+    nchain[q] = c >= 2 ? (c - 2) / 7 : 0;
+}
+
+__global__ void k_bucket(const int64_t *exh, int n, const int64_t *chain_off, int64_t slot_base, Nodes nd,
+                         int64_t *p_parent, int64_t *p_next) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    int64_t x = exh[q];
+    int64_t lo = nd.lo[x], hi = nd.hi[x], c = hi - lo;
+    int64_t nch = c >= 2 ? (c - 2) / 7 : 0;
+    int64_t base = slot_base + chain_off[q];
+    int64_t xnext = nd.next[x];
+    nd.first[x] = lo;
+    double c0 = nd.center[3 * x], c1 = nd.center[3 * x + 1], c2 = nd.center[3 * x + 2], sz = nd.size[x];
+    for (int64_t j = 1; j <= nch; j++) {
+        int64_t sl = base + j - 1;
+        c0 = dadd(c0, dmul(sz, c_octant[7][0]));
+        c1 = dadd(c1, dmul(sz, c_octant[7][1]));
+        c2 = dadd(c2, dmul(sz, c_octant[7][2]));
+        sz = dmul(sz, 0.5);
+        nd.lo[sl] = lo + 7 * j;
+        nd.hi[sl] = hi;
+        nd.level[sl] = MAX_LEVEL;
+        nd.depth[sl] = nd.depth[x] + (int)j;
+        nd.sys[sl] = nd.sys[x];
+        nd.parent[sl] = (j == 1) ? x : sl - 1;
+        nd.aparent[sl] = x;
+        nd.rank[sl] = lo + 7 * j;
+        nd.center[3 * sl] = c0;
+        nd.center[3 * sl + 1] = c1;
+        nd.center[3 * sl + 2] = c2;
+        nd.size[sl] = sz;
+        nd.first[sl] = lo + 7 * j;
+        nd.next[sl] = xnext;
+    }
+    for (int64_t jj = 0; jj < c; jj++) {
+        int64_t owner = min(jj / 7, nch);
+        int64_t i = lo + jj;
+        p_parent[i] = owner == 0 ? x : base + owner - 1;
+        if (jj == c - 1) p_next[i] = xnext;
+        else if (owner < nch && jj == 7 * owner + 6) p_next[i] = node_ref(base + owner);
+        else p_next[i] = i + 1;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Index validation: every slot or particle reference the later kernels dereference is checked
+// once; a bad one stops the build with an error instead of an out-of-bounds access.
+__device__ __forceinline__ bool ref_ok(int64_t r, int64_t N, int64_t M) {
+    if (r >= 0) return r < N;
+    if (r == -1) return true;
+    return (-r - 2) < M;
+}
+__global__ void k_validate_slots(Nodes nd, int64_t M, const int64_t *p_parent, const int64_t *p_next, int64_t N,
+                                 int *bad) {
+    int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < M) {
+        bool ok = nd.parent[c] >= -1 && nd.parent[c] < M && nd.aparent[c] >= -1 && nd.aparent[c] < M &&
+                  ref_ok(nd.first[c], N, M) && ref_ok(nd.next[c], N, M) && nd.first[c] != -1 && nd.lo[c] >= 0 &&
+                  nd.hi[c] <= N && nd.lo[c] < nd.hi[c];
+        if (!ok) atomicOr(bad, 1);
+    }
+    if (c < N) {
+        bool ok = p_parent[c] >= 0 && p_parent[c] < M && ref_ok(p_next[c], N, M);
+        if (!ok) atomicOr(bad, 2);
+    }
+}
+__global__ void k_validate_links(int64_t NE, const int64_t *first, const int64_t *next, const int64_t *parent,
+                                 int *bad) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= NE) return;
+    bool ok = first[i] >= -1 && first[i] < NE && next[i] >= -1 && next[i] < NE && parent[i] >= -1 && parent[i] < NE;
+    if (!ok) atomicOr(bad, 4);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Numbering.
+struct NumberingBits {
+    int lb;  // bits of a system-local particle index
+    int db;  // bits of a depth
+};
+
+__global__ void k_number_keys(Nodes nd, int64_t count, const int64_t *sys_off, NumberingBits b, uint64_t *keys,
+                              uint32_t *vals, int64_t *root_slot_of_sys, int *nonroot_count) {
+    int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= count) return;
+    int s = nd.sys[c];
+    int64_t ap = nd.aparent[c];
+    if (ap < 0) {  // a system root
+        root_slot_of_sys[s] = c;
+        keys[c] = ~0ull;  // sorts last
+        vals[c] = (uint32_t)c;
+        return;
+    }
+    int64_t off = sys_off[s];
+    int64_t nsys_part = sys_off[s + 1] - off;
+    uint64_t k = ((uint64_t)s << (2 * b.lb + b.db)) | ((uint64_t)(nsys_part - (nd.hi[ap] - off)) << (b.lb + b.db)) |
+                 ((uint64_t)nd.depth[ap] << b.lb) | (uint64_t)(nd.rank[c] - off);
+    keys[c] = k;
+    vals[c] = (uint32_t)c;
+    atomicAdd(nonroot_count, 1);
+}
+
+__global__ void k_final_index(const uint32_t *vals, int64_t count, const int32_t *nd_sys, int64_t ntot,
+                              const int64_t *sys_node_off, int64_t *final_of_slot, const int64_t *root_slot_of_sys,
+                              int nsys) {
+    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < count) {
+        int64_t c = vals[q];
+        int s = nd_sys[c];
+        if (q < count - nsys) final_of_slot[c] = ntot + q + s + 1;
+    }
+    if (q < nsys) final_of_slot[root_slot_of_sys[q]] = ntot + sys_node_off[q];
+}
+
+__device__ __forceinline__ int64_t resolve(int64_t ref, const int64_t *final_of_slot) {
+    if (ref >= 0) return ref;
+    if (ref == -1) return -1;
+    return final_of_slot[-ref - 2];
+}
+
+__global__ void k_write_nodes(Nodes nd, int64_t count, const int64_t *final_of_slot, double *coord, double *size,
+                              int64_t *first, int64_t *next, int64_t *parent, int2 *range, double *cell, int64_t ntot) {
+    int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= count) return;
+    int64_t f = final_of_slot[c];
+    range[f - ntot] = make_int2((int)nd.lo[c], (int)nd.hi[c]);
+    cell[3 * (f - ntot)] = nd.center[3 * c];
+    cell[3 * (f - ntot) + 1] = nd.center[3 * c + 1];
+    cell[3 * (f - ntot) + 2] = nd.center[3 * c + 2];
+    coord[3 * f] = nd.center[3 * c];
+    coord[3 * f + 1] = nd.center[3 * c + 1];
+    coord[3 * f + 2] = nd.center[3 * c + 2];
+    size[f] = nd.size[c];
+    first[f] = resolve(nd.first[c], final_of_slot);
+    next[f] = resolve(nd.next[c], final_of_slot);
+    parent[f] = nd.parent[c] < 0 ? -1 : final_of_slot[nd.parent[c]];
+}
+
+__global__ void k_write_particles(int64_t ntot, const int64_t *p_parent, const int64_t *p_next,
+                                  const int64_t *final_of_slot, int64_t *first, int64_t *next, int64_t *parent,
+                                  double *size, double *delta) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntot) return;
+    first[i] = -1;
+    next[i] = resolve(p_next[i], final_of_slot);
+    parent[i] = final_of_slot[p_parent[i]];
+    size[i] = 0.0;
+    delta[i] = 0.0;
+}
+
+// Capacity bookkeeping for a bucket (octree.py:930-933): new_node_idx when the bucket is reached
+// plus the worst-case chain; new_node_idx there is 1 + the number of nodes the split allocated
+// earlier, i.e. the sorted position of the bucket's first allocation.
+__global__ void k_bucket_requirement(const int64_t *exh, int n, Nodes nd, const int64_t *sys_off, NumberingBits b,
+                                     const uint64_t *sorted_keys, int64_t count, int64_t ntot,
+                                     unsigned long long *req) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    int64_t x = exh[q];
+    int s = nd.sys[x];
+    int64_t off = sys_off[s], np = sys_off[s + 1] - off;
+    uint64_t key = ((uint64_t)s << (2 * b.lb + b.db)) | ((uint64_t)(np - (nd.hi[x] - off)) << (b.lb + b.db)) |
+                   ((uint64_t)nd.depth[x] << b.lb) | (uint64_t)(nd.lo[x] - off);
+    int64_t a = 0, z = count;
+    while (a < z) {
+        int64_t mid = (a + z) >> 1;
+        if (sorted_keys[mid] < key) a = mid + 1;
+        else z = mid;
+    }
+    // a = global sorted position; the system's earlier non-root nodes are those with smaller keys
+    // from the same system: subtract the count of keys of earlier systems.
+    uint64_t sys_key = (uint64_t)s << (2 * b.lb + b.db);
+    int64_t a0 = 0, z0 = count;
+    while (a0 < z0) {
+        int64_t mid = (a0 + z0) >> 1;
+        if (sorted_keys[mid] < sys_key) a0 = mid + 1;
+        else z0 = mid;
+    }
+    int64_t new_node_idx = np + 1 + (a - a0);
+    int64_t need = new_node_idx + (nd.hi[x] - nd.lo[x]) / 7 + 2;
+    atomicMax(&req[s], (unsigned long long)need);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Moments. Children are reached through FirstSubnode/NextBranch: a node's chain lists its
+// particle children and node children in digit order, and its node children carry consecutive
+// indices, so "descending index" is the reverse of their order in the chain.
+__global__ void k_count_node_children(int64_t ntot, int64_t mtot, const int64_t *parent, int *nchild) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= mtot) return;
+    int64_t p = parent[ntot + j];
+    if (p >= 0) atomicAdd(&nchild[p - ntot], 1);
+}
+
+struct MomentArgs {
+    int64_t ntot, mtot;
+    double *coord, *mass, *soft, *delta, *quad;  // quad: per node (9)
+    double *acc;                                  // per node (3)
+    const int64_t *first, *next, *parent;
+    int *nchild, *arrived;
+    int quads;
+};
+
+__device__ __forceinline__ void shift_quad(double *Q, double m, double r0, double r1, double r2) {
+    double rsq = dadd(dadd(dmul(r0, r0), dmul(r1, r1)), dmul(r2, r2));
+    double t;
+    t = dmul(m, dsub(dmul(dmul(3.0, r0), r0), rsq)); Q[0] = dadd(Q[0], t);
+    t = dmul(dmul(dmul(m, 3.0), r0), r1);           Q[1] = dadd(Q[1], t);
+    t = dmul(dmul(dmul(m, 3.0), r0), r2);           Q[2] = dadd(Q[2], t);
+    t = dmul(dmul(dmul(m, 3.0), r1), r0);           Q[3] = dadd(Q[3], t);
+    t = dmul(m, dsub(dmul(dmul(3.0, r1), r1), rsq)); Q[4] = dadd(Q[4], t);
+    t = dmul(dmul(dmul(m, 3.0), r1), r2);           Q[5] = dadd(Q[5], t);
+    t = dmul(dmul(dmul(m, 3.0), r2), r0);           Q[6] = dadd(Q[6], t);
+    t = dmul(dmul(dmul(m, 3.0), r2), r1);           Q[7] = dadd(Q[7], t);
+    t = dmul(m, dsub(dmul(dmul(3.0, r2), r2), rsq)); Q[8] = dadd(Q[8], t);
+}
+
+// One node's moments from its (finished) children: RollupMoments + RollupQuadrupoles restricted
+// to this node (octree.py:199-292).
+__device__ void node_moments(const MomentArgs &a, int64_t f) {
+    const int64_t stop = a.next[f];
+    double m = 0.0, ax = 0.0, ay = 0.0, az = 0.0, h = 0.0;
+    int64_t kids[8];
+    int nk = 0;
+    int steps = 0;
+    for (int64_t c = a.first[f]; c != stop && c >= 0 && steps < 9; c = a.next[c], steps++) {
+        if (c < a.ntot) {
+            double mi = __ldcg(a.mass + c);
+            m = dadd(m, mi);
+            ax = dadd(ax, dmul(mi, __ldcg(a.coord + 3 * c)));
+            ay = dadd(ay, dmul(mi, __ldcg(a.coord + 3 * c + 1)));
+            az = dadd(az, dmul(mi, __ldcg(a.coord + 3 * c + 2)));
+            h = pymax(h, __ldcg(a.soft + c));
+        } else if (nk < 8) {
+            kids[nk++] = c;
+        }
+    }
+    for (int q = nk - 1; q >= 0; q--) {
+        int64_t c = kids[q];
+        double mc = __ldcg(a.mass + c);
+        if (mc == 0.0) continue;
+        int64_t cj = c - a.ntot;
+        m = dadd(m, mc);
+        ax = dadd(ax, __ldcg(a.acc + 3 * cj));
+        ay = dadd(ay, __ldcg(a.acc + 3 * cj + 1));
+        az = dadd(az, __ldcg(a.acc + 3 * cj + 2));
+        h = pymax(h, __ldcg(a.soft + c));
+    }
+    int64_t j = f - a.ntot;
+    a.mass[f] = m;
+    a.soft[f] = h;
+    a.acc[3 * j] = ax;
+    a.acc[3 * j + 1] = ay;
+    a.acc[3 * j + 2] = az;
+    double com[3] = {a.coord[3 * f], a.coord[3 * f + 1], a.coord[3 * f + 2]};
+    if (m != 0.0) {
+        double inv = ddiv(1.0, m);
+        double accs[3] = {ax, ay, az};
+        double d2 = 0.0;
+        for (int k = 0; k < 3; k++) {
+            double cm = dmul(accs[k], inv);
+            double dx = dsub(cm, com[k]);
+            d2 = dadd(d2, dmul(dx, dx));
+            com[k] = cm;
+            a.coord[3 * f + k] = cm;
+        }
+        a.delta[f] = __dsqrt_rn(d2);
+    }
+    if (a.quads) {
+        double Q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        int qsteps = 0;
+        for (int64_t c = a.first[f]; c != stop && c >= 0 && qsteps < 9; c = a.next[c], qsteps++) {
+            if (c < a.ntot)
+                shift_quad(Q, __ldcg(a.mass + c), dsub(__ldcg(a.coord + 3 * c), com[0]),
+                           dsub(__ldcg(a.coord + 3 * c + 1), com[1]), dsub(__ldcg(a.coord + 3 * c + 2), com[2]));
+        }
+        for (int q = nk - 1; q >= 0; q--) {
+            int64_t c = kids[q];
+            double mc = __ldcg(a.mass + c);
+            if (mc == 0.0) continue;
+            int64_t cj = c - a.ntot;
+            for (int k = 0; k < 9; k++) Q[k] = dadd(Q[k], __ldcg(a.quad + 9 * cj + k));
+            shift_quad(Q, mc, dsub(__ldcg(a.coord + 3 * c), com[0]), dsub(__ldcg(a.coord + 3 * c + 1), com[1]),
+                       dsub(__ldcg(a.coord + 3 * c + 2), com[2]));
+        }
+        for (int k = 0; k < 9; k++) a.quad[9 * j + k] = Q[k];
+    }
+}
+
+// Bottom-up: every node whose children are all particles starts a thread; the last child to
+// finish a parent carries on with the parent (one pass, no level barriers).
+__global__ void k_moments(MomentArgs a) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.mtot || a.nchild[j] != 0) return;
+    int64_t f = a.ntot + j;
+    for (int64_t guard = 0; guard < a.mtot + 1; guard++) {
+        node_moments(a, f);
+        __threadfence();
+        int64_t p = a.parent[f];
+        if (p < 0) return;
+        int64_t pj = p - a.ntot;
+        int prev = atomicAdd(&a.arrived[pj], 1);
+        if (prev != a.nchild[pj] - 1) return;
+        __threadfence();
+        f = p;
+    }
+}
+
+// compute_moments=False: node masses/softenings hold only the particles folded in by the split.
+__global__ void k_fold_only(MomentArgs a) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.mtot) return;
+    int64_t f = a.ntot + j;
+    const int64_t stop = a.next[f];
+    double m = 0.0, h = 0.0;
+    int steps = 0;
+    for (int64_t c = a.first[f]; c != stop && c >= 0 && steps < 9; c = a.next[c], steps++) {
+        if (c < a.ntot) {
+            m = dadd(m, a.mass[c]);
+            h = pymax(h, a.soft[c]);
+        }
+    }
+    a.mass[f] = m;
+    a.soft[f] = h;
+}
+
+// ---------------------------------------------------------------------------------------------
+template <typename T>
+static tg_status dalloc(T **p, int64_t n, cudaStream_t s) {
+    *p = nullptr;
+    if (n <= 0) n = 1;
+    TG_CUDA(cudaMallocAsync((void **)p, sizeof(T) * n, s));
+    return TG_OK;
+}
+template <typename T>
+static void dfree(T *&p, cudaStream_t s) {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+}
+
+static tg_status segs_alloc(Segs &g, int n, cudaStream_t s) {
+    g.n = n;
+    TG_TRY(dalloc(&g.lo, n, s));
+    TG_TRY(dalloc(&g.hi, n, s));
+    TG_TRY(dalloc(&g.root, n, s));
+    TG_TRY(dalloc(&g.center, 3 * n, s));
+    TG_TRY(dalloc(&g.size, n, s));
+    TG_TRY(dalloc(&g.depth0, n, s));
+    TG_TRY(dalloc(&g.next_ref, n, s));
+    TG_TRY(dalloc(&g.sys, n, s));
+    TG_TRY(dalloc(&g.eoff, n + 1, s));
+    return TG_OK;
+}
+static void segs_free(Segs &g, cudaStream_t s) {
+    dfree(g.lo, s); dfree(g.hi, s); dfree(g.root, s); dfree(g.center, s); dfree(g.size, s);
+    dfree(g.depth0, s); dfree(g.next_ref, s); dfree(g.sys, s); dfree(g.eoff, s);
+    g.n = 0;
+}
+
+template <typename T>
+static tg_status grow_copy(T **p, int64_t old_n, int64_t new_n, int width, cudaStream_t s) {
+    T *q = nullptr;
+    TG_TRY(dalloc(&q, new_n * width, s));
+    if (*p && old_n > 0) TG_CUDA(cudaMemcpyAsync(q, *p, sizeof(T) * old_n * width, cudaMemcpyDeviceToDevice, s));
+    dfree(*p, s);
+    *p = q;
+    return TG_OK;
+}
+
+static tg_status nodes_reserve(Nodes &nd, int64_t need, cudaStream_t s) {
+    if (need <= nd.cap) return TG_OK;
+    int64_t nc = std::max<int64_t>(need, nd.cap + nd.cap / 2 + 64);
+    TG_TRY(grow_copy(&nd.lo, nd.count, nc, 1, s));
+    TG_TRY(grow_copy(&nd.hi, nd.count, nc, 1, s));
+    TG_TRY(grow_copy(&nd.parent, nd.count, nc, 1, s));
+    TG_TRY(grow_copy(&nd.first, nd.count, nc, 1, s));
+    TG_TRY(grow_copy(&nd.next, nd.count, nc, 1, s));
+    TG_TRY(grow_copy(&nd.aparent, nd.count, nc, 1, s));
+    TG_TRY(grow_copy(&nd.rank, nd.count, nc, 1, s));
+    TG_TRY(grow_copy(&nd.depth, nd.count, nc, 1, s));
+    TG_TRY(grow_copy(&nd.sys, nd.count, nc, 1, s));
+    TG_TRY(grow_copy(&nd.level, nd.count, nc, 1, s));
+    TG_TRY(grow_copy(&nd.center, nd.count, nc, 3, s));
+    TG_TRY(grow_copy(&nd.size, nd.count, nc, 1, s));
+    nd.cap = nc;
+    return TG_OK;
+}
+static void nodes_free(Nodes &nd, cudaStream_t s) {
+    dfree(nd.lo, s); dfree(nd.hi, s); dfree(nd.parent, s); dfree(nd.first, s); dfree(nd.next, s);
+    dfree(nd.aparent, s); dfree(nd.rank, s); dfree(nd.depth, s); dfree(nd.sys, s); dfree(nd.level, s);
+    dfree(nd.center, s); dfree(nd.size, s);
+}
+
+static RoundView view_of(const Segs &g) {
+    RoundView v;
+    v.seg_lo = g.lo; v.seg_hi = g.hi; v.seg_root = g.root; v.seg_next = g.next_ref; v.eoff = g.eoff;
+    v.seg_center = g.center; v.seg_size = g.size; v.seg_depth0 = g.depth0; v.seg_sys = g.sys; v.nseg = g.n;
+    return v;
+}
+
+static int bits_for(int64_t v) {
+    int b = 0;
+    while (b < 63 && ((int64_t)1 << b) <= v) b++;
+    return b;
+}
+
+static int64_t reference_capacity(int64_t npart, int64_t required) {
+    int64_t cap = (int64_t)(1.5 * (double)npart + 1.0);
+    while (cap < required) {
+        int64_t inc = (int64_t)((double)cap * 1.2 + 1.0) - cap;
+        cap += inc < 1 ? 1 : inc;
+    }
+    return cap;
+}
+
+__global__ void k_init_root_segs(Segs g, const int64_t *sys_off, const double *center, const double *size) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.n) return;
+    g.lo[s] = sys_off[s];
+    g.hi[s] = sys_off[s + 1];
+    g.root[s] = -1;
+    g.center[3 * s] = center[3 * s];
+    g.center[3 * s + 1] = center[3 * s + 1];
+    g.center[3 * s + 2] = center[3 * s + 2];
+    g.size[s] = size[s];
+    g.depth0[s] = 0;
+    g.next_ref[s] = -1;
+    g.sys[s] = s;
+}
+
+#define LAUNCH(n) div_up((n), 256), 256, 0, st
+
+// Build the whole arena. pos/m/h are device pointers (m/h may be null).
+tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const double *h,
+                     const std::vector<int64_t> &sys_off_host, int quadrupole, int compute_moments, cudaStream_t st) {
+    const int nsys = (int)sys_off_host.size() - 1;
+    const int64_t N = sys_off_host.back();
+    if (N < 1 || nsys < 1) return TG_ERR_BAD_ARG;
+    if (N > 0x7fffffffLL) return TG_ERR_BAD_ARG;
+    int64_t max_sys_n = 0;
+    for (int s = 0; s < nsys; s++) {
+        int64_t ns = sys_off_host[s + 1] - sys_off_host[s];
+        if (ns < 1) return TG_ERR_BAD_ARG;
+        max_sys_n = std::max(max_sys_n, ns);
+    }
+    NumberingBits nb{bits_for(max_sys_n), 7};
+    int sysbits = nsys > 1 ? bits_for(nsys - 1) : 0;
+    if (sysbits + 2 * nb.lb + nb.db > 64) return TG_ERR_BAD_ARG;
+
+    T->ntot = N;
+    T->nsys = nsys;
+    T->sys_off = sys_off_host;
+    T->has_quads = quadrupole;
+    T->compute_moments = compute_moments;
+    T->stream = st;
+
+    int64_t *sys_off = nullptr;
+    TG_TRY(dalloc(&sys_off, nsys + 1, st));
+    TG_CUDA(cudaMemcpyAsync(sys_off, sys_off_host.data(), sizeof(int64_t) * (nsys + 1), cudaMemcpyHostToDevice, st));
+
+    // 1. bounding cubes
+    unsigned long long *mn = nullptr, *mx = nullptr;
+    double *center = nullptr, *size = nullptr;
+    TG_TRY(dalloc(&mn, 3 * nsys, st));
+    TG_TRY(dalloc(&mx, 3 * nsys, st));
+    TG_TRY(dalloc(&center, 3 * nsys, st));
+    TG_TRY(dalloc(&size, nsys, st));
+    { k_bbox_init<<<LAUNCH(3 * nsys)>>>(mn, mx, nsys); tg::note_launch(); }
+    { k_bbox<<<div_up(N, BB_THREADS * BB_ITEMS), BB_THREADS, 0, st>>>(pos, N, sys_off, nsys, mn, mx); tg::note_launch(); }
+    { k_bbox_finish<<<LAUNCH(nsys)>>>(mn, mx, nsys, center, size); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
+
+    // 2. keys and stable sort (system id as the most significant digit when batched)
+    uint64_t *keys = nullptr, *keys_orig = nullptr;
+    uint32_t *perm = nullptr;
+    TG_TRY(dalloc(&keys, N, st));
+    TG_TRY(dalloc(&keys_orig, N, st));
+    TG_TRY(dalloc(&perm, N, st));
+    { k_keys<<<LAUNCH(N)>>>(pos, N, sys_off, nsys, center, size, keys, keys_orig, perm); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
+    TG_TRY(radix_sort_pairs(keys, perm, N, 63, st));
+    if (nsys > 1) {
+        { k_sys_of<<<LAUNCH(N)>>>(perm, N, sys_off, nsys, keys); tg::note_launch(); }
+        TG_TRY(radix_sort_pairs(keys, perm, N, sysbits, st));
+    }
+
+    // 3. arena element arrays; particles gathered into Morton order
+    const int64_t cap0 = N + N / 2 + 16;  // node slots, grown if needed
+    TG_TRY(dalloc(&T->walk_idx, N, st));
+    double *pc = nullptr, *pm = nullptr, *ps = nullptr;
+    TG_TRY(dalloc(&pc, 3 * N, st));
+    TG_TRY(dalloc(&pm, N, st));
+    TG_TRY(dalloc(&ps, N, st));
+    uint64_t *keys_sorted = keys;  // reuse
+    { k_gather<<<LAUNCH(N)>>>(perm, N, pos, m, h, keys_orig, pc, pm, ps, keys_sorted, T->walk_idx); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
+    dfree(keys_orig, st);
+
+    // 4. split rounds
+    Nodes nd;
+    TG_TRY(nodes_reserve(nd, cap0, st));
+    int64_t *p_parent = nullptr, *p_next = nullptr;
+    TG_TRY(dalloc(&p_parent, N, st));
+    TG_TRY(dalloc(&p_next, N, st));
+    Segs sg;
+    TG_TRY(segs_alloc(sg, nsys, st));
+    { k_init_root_segs<<<LAUNCH(nsys)>>>(sg, sys_off, center, size); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
+    int64_t *exh = nullptr;
+    int *n_exh_dev = nullptr;
+    int n_exh = 0;
+    int64_t *root_first = nullptr;
+    int has_coincident = 0;
+
+    for (int round = 0; round <= MORTON_MAX_ROUNDS; round++) {
+        // element offsets of the segments
+        int64_t *sizes = nullptr;
+        TG_TRY(dalloc(&sizes, sg.n, st));
+        { k_seg_sizes<<<LAUNCH(sg.n)>>>(sg.lo, sg.hi, sg.n, sizes); tg::note_launch(); }
+        TG_TRY(exclusive_scan_i64(sizes, sg.eoff, sg.n, sg.eoff + sg.n, st));
+        dfree(sizes, st);
+        int64_t E = 0;
+        TG_CUDA(cudaMemcpyAsync(&E, sg.eoff + sg.n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        TG_CUDA(cudaStreamSynchronize(st));
+        RoundView v = view_of(sg);
+
+        if (round > 0) {
+            // re-key the exhausted runs relative to their cells and sort each run stably
+            uint64_t *rk = nullptr, *rk_elem = nullptr;
+            uint32_t *rv = nullptr;
+            TG_TRY(dalloc(&rk, E, st));
+            TG_TRY(dalloc(&rk_elem, E, st));
+            TG_TRY(dalloc(&rv, E, st));
+            { k_rekey_keys<<<LAUNCH(E)>>>(v, E, pc, rk, rv); tg::note_launch(); }
+            TG_CUDA(cudaMemcpyAsync(rk_elem, rk, sizeof(uint64_t) * E, cudaMemcpyDeviceToDevice, st));
+            TG_TRY(radix_sort_pairs(rk, rv, E, 63, st));
+            if (sg.n > 1) {
+                { k_rekey_segkeys<<<LAUNCH(E)>>>(v, rv, E, rk); tg::note_launch(); }
+                TG_TRY(radix_sort_pairs(rk, rv, E, bits_for(sg.n - 1), st));
+            }
+            double *tc = nullptr, *tm = nullptr, *ts = nullptr;
+            int64_t *tw = nullptr;
+            uint64_t *tk = nullptr;
+            TG_TRY(dalloc(&tc, 3 * E, st));
+            TG_TRY(dalloc(&tm, E, st));
+            TG_TRY(dalloc(&ts, E, st));
+            TG_TRY(dalloc(&tw, E, st));
+            TG_TRY(dalloc(&tk, E, st));
+            { k_rekey_gather<<<LAUNCH(E)>>>(v, E, rv, pc, pm, ps, T->walk_idx, rk_elem, tc, tm, ts, tw, tk); tg::note_launch(); }
+            { k_rekey_scatter<<<LAUNCH(E)>>>(v, E, tc, tm, ts, tw, tk, pc, pm, ps, T->walk_idx, keys_sorted); tg::note_launch(); }
+            TG_CUDA(cudaGetLastError());
+            dfree(rk, st); dfree(rk_elem, st); dfree(rv, st);
+            dfree(tc, st); dfree(tm, st); dfree(ts, st); dfree(tw, st); dfree(tk, st);
+        }
+
+        int8_t *L = nullptr;
+        int64_t *cnt = nullptr, *nstart = nullptr, *total = nullptr;
+        TG_TRY(dalloc(&L, E, st));
+        TG_TRY(dalloc(&cnt, E, st));
+        TG_TRY(dalloc(&nstart, E, st));
+        TG_TRY(dalloc(&total, 1, st));
+        { k_levels<<<LAUNCH(E)>>>(v, E, keys_sorted, L); tg::note_launch(); }
+        { k_counts<<<LAUNCH(E)>>>(v, E, L, cnt); tg::note_launch(); }
+        TG_CUDA(cudaGetLastError());
+        TG_TRY(exclusive_scan_i64(cnt, nstart, E, total, st));
+        int64_t Mr = 0;
+        TG_CUDA(cudaMemcpyAsync(&Mr, total, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        TG_CUDA(cudaStreamSynchronize(st));
+        int64_t slot_base = nd.count;
+        TG_TRY(nodes_reserve(nd, slot_base + Mr, st));
+        dfree(exh, st);
+        dfree(n_exh_dev, st);
+        dfree(root_first, st);
+        TG_TRY(dalloc(&exh, std::max<int64_t>(Mr, 1), st));
+        TG_TRY(dalloc(&n_exh_dev, 1, st));
+        TG_TRY(dalloc(&root_first, sg.n, st));
+        TG_CUDA(cudaMemsetAsync(n_exh_dev, 0, sizeof(int), st));
+        { k_nodes<<<LAUNCH(E)>>>(v, E, L, nstart, cnt, slot_base, keys_sorted, nd, exh, n_exh_dev, root_first); tg::note_launch(); }
+        { k_particles<<<LAUNCH(E)>>>(v, E, L, nstart, slot_base, keys_sorted, p_parent, p_next); tg::note_launch(); }
+        if (round > 0) { k_set_root_first<<<LAUNCH(sg.n)>>>(sg.root, root_first, sg.n, nd.first); tg::note_launch(); }
+        TG_CUDA(cudaGetLastError());
+        nd.count = slot_base + Mr;
+        TG_CUDA(cudaMemcpyAsync(&n_exh, n_exh_dev, sizeof(int), cudaMemcpyDeviceToHost, st));
+        TG_CUDA(cudaStreamSynchronize(st));
+        dfree(L, st); dfree(cnt, st); dfree(nstart, st); dfree(total, st);
+        if (n_exh == 0) break;
+        if (round < MORTON_MAX_ROUNDS) {
+            segs_free(sg, st);
+            TG_TRY(segs_alloc(sg, n_exh, st));
+            { k_make_segs<<<LAUNCH(n_exh)>>>(exh, n_exh, nd, sg); tg::note_launch(); }
+            TG_CUDA(cudaGetLastError());
+        }
+    }
+    segs_free(sg, st);
+    dfree(root_first, st);
+
+    // 5. buckets for runs still exhausted after three re-keys
+    int n_bucket = (n_exh > 0) ? n_exh : 0;
+    if (n_bucket > 0) {
+        has_coincident = 1;
+        int64_t *nchain = nullptr, *choff = nullptr, *chtot = nullptr;
+        TG_TRY(dalloc(&nchain, n_bucket, st));
+        TG_TRY(dalloc(&choff, n_bucket, st));
+        TG_TRY(dalloc(&chtot, 1, st));
+        { k_bucket_counts<<<LAUNCH(n_bucket)>>>(exh, n_bucket, nd.lo, nd.hi, nchain); tg::note_launch(); }
+        TG_TRY(exclusive_scan_i64(nchain, choff, n_bucket, chtot, st));
+        int64_t nch = 0;
+        TG_CUDA(cudaMemcpyAsync(&nch, chtot, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        TG_CUDA(cudaStreamSynchronize(st));
+        int64_t slot_base = nd.count;
+        TG_TRY(nodes_reserve(nd, slot_base + nch, st));
+        { k_bucket<<<LAUNCH(n_bucket)>>>(exh, n_bucket, choff, slot_base, nd, p_parent, p_next); tg::note_launch(); }
+        TG_CUDA(cudaGetLastError());
+        nd.count = slot_base + nch;
+        dfree(nchain, st); dfree(choff, st); dfree(chtot, st);
+    }
+    T->has_coincident = has_coincident;
+
+    // 6. reference numbering
+    const int64_t M = nd.count;
+    T->mtot = M;
+    {
+        int *bad = nullptr;
+        TG_TRY(dalloc(&bad, 1, st));
+        TG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
+        { k_validate_slots<<<LAUNCH(std::max<int64_t>(M, N))>>>(nd, M, p_parent, p_next, N, bad); tg::note_launch(); }
+        int hbad = 0;
+        TG_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+        TG_CUDA(cudaStreamSynchronize(st));
+        dfree(bad, st);
+        if (hbad) {
+            set_last_error_msg("internal error: octree build produced an invalid node reference");
+            return TG_ERR_CUDA;
+        }
+    }
+    uint64_t *nkeys = nullptr;
+    uint32_t *nvals = nullptr;
+    int64_t *root_slot = nullptr, *final_of_slot = nullptr, *sys_node_off = nullptr;
+    int *nonroot = nullptr;
+    TG_TRY(dalloc(&nkeys, M, st));
+    TG_TRY(dalloc(&nvals, M, st));
+    TG_TRY(dalloc(&root_slot, nsys, st));
+    TG_TRY(dalloc(&final_of_slot, M, st));
+    TG_TRY(dalloc(&sys_node_off, nsys + 1, st));
+    TG_TRY(dalloc(&nonroot, 1, st));
+    TG_CUDA(cudaMemsetAsync(nonroot, 0, sizeof(int), st));
+    { k_number_keys<<<LAUNCH(M)>>>(nd, M, sys_off, nb, nkeys, nvals, root_slot, nonroot); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
+    TG_TRY(radix_sort_pairs(nkeys, nvals, M, 64, st));
+    // per-system node counts -> node offsets (roots first within each system's block)
+    std::vector<int64_t> node_cnt(nsys, 0);
+    {
+        std::vector<int32_t> sys_of_slot(M);
+        TG_CUDA(cudaMemcpyAsync(sys_of_slot.data(), nd.sys, sizeof(int32_t) * M, cudaMemcpyDeviceToHost, st));
+        TG_CUDA(cudaStreamSynchronize(st));
+        for (int64_t c = 0; c < M; c++) node_cnt[sys_of_slot[c]]++;
+    }
+    T->sys_node_off.assign(nsys + 1, 0);
+    for (int s = 0; s < nsys; s++) T->sys_node_off[s + 1] = T->sys_node_off[s] + node_cnt[s];
+    TG_CUDA(cudaMemcpyAsync(sys_node_off, T->sys_node_off.data(), sizeof(int64_t) * (nsys + 1), cudaMemcpyHostToDevice,
+                            st));
+    { k_final_index<<<LAUNCH(std::max<int64_t>(M, nsys))>>>(nvals, M, nd.sys, N, sys_node_off, final_of_slot, root_slot,
+                                                         nsys); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
+
+    // capacity (NumNodes) per system, from node_hi and bucket reservations
+    {
+        unsigned long long *req = nullptr;
+        TG_TRY(dalloc(&req, nsys, st));
+        TG_CUDA(cudaMemsetAsync(req, 0, sizeof(unsigned long long) * nsys, st));
+        if (n_bucket > 0) {
+            { k_bucket_requirement<<<LAUNCH(n_bucket)>>>(exh, n_bucket, nd, sys_off, nb, nkeys, M, N, req); tg::note_launch(); }
+            TG_CUDA(cudaGetLastError());
+        }
+        std::vector<unsigned long long> rq(nsys);
+        TG_CUDA(cudaMemcpyAsync(rq.data(), req, sizeof(unsigned long long) * nsys, cudaMemcpyDeviceToHost, st));
+        TG_CUDA(cudaStreamSynchronize(st));
+        T->sys_capacity.resize(nsys);
+        for (int s = 0; s < nsys; s++) {
+            int64_t np = sys_off_host[s + 1] - sys_off_host[s];
+            int64_t node_hi = np + node_cnt[s];
+            T->sys_capacity[s] = reference_capacity(np, std::max<int64_t>(node_hi, (int64_t)rq[s]));
+        }
+        dfree(req, st);
+    }
+    dfree(exh, st);
+    dfree(n_exh_dev, st);
+
+    // 7. final arrays
+    const int64_t NE = N + M;
+    TG_TRY(dalloc(&T->coord, 3 * NE, st));
+    TG_TRY(dalloc(&T->mass, NE, st));
+    TG_TRY(dalloc(&T->size, NE, st));
+    TG_TRY(dalloc(&T->delta, NE, st));
+    TG_TRY(dalloc(&T->soft, NE, st));
+    TG_TRY(dalloc(&T->first, NE, st));
+    TG_TRY(dalloc(&T->next, NE, st));
+    TG_TRY(dalloc(&T->parent, NE, st));
+    TG_CUDA(cudaMemcpyAsync(T->coord, pc, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, st));
+    TG_CUDA(cudaMemcpyAsync(T->mass, pm, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+    TG_CUDA(cudaMemcpyAsync(T->soft, ps, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+    TG_CUDA(cudaMemsetAsync(T->mass + N, 0, sizeof(double) * M, st));
+    TG_CUDA(cudaMemsetAsync(T->soft + N, 0, sizeof(double) * M, st));
+    TG_CUDA(cudaMemsetAsync(T->delta + N, 0, sizeof(double) * M, st));
+    dfree(pc, st); dfree(pm, st); dfree(ps, st);
+    TG_TRY(dalloc(&T->node_range, M, st));
+    TG_TRY(dalloc(&T->cell_center, 3 * M, st));
+    { k_write_nodes<<<LAUNCH(M)>>>(nd, M, final_of_slot, T->coord, T->size, T->first, T->next, T->parent,
+                                 T->node_range, T->cell_center, N); tg::note_launch(); }
+    { k_write_particles<<<LAUNCH(N)>>>(N, p_parent, p_next, final_of_slot, T->first, T->next, T->parent, T->size,
+                                     T->delta); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
+    {
+        int *bad = nullptr;
+        TG_TRY(dalloc(&bad, 1, st));
+        TG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
+        { k_validate_links<<<LAUNCH(NE)>>>(NE, T->first, T->next, T->parent, bad); tg::note_launch(); }
+        int hbad = 0;
+        TG_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+        TG_CUDA(cudaStreamSynchronize(st));
+        dfree(bad, st);
+        if (hbad) {
+            set_last_error_msg("internal error: octree links out of range");
+            return TG_ERR_CUDA;
+        }
+    }
+    nodes_free(nd, st);
+    dfree(p_parent, st); dfree(p_next, st); dfree(nkeys, st); dfree(nvals, st); dfree(root_slot, st);
+    dfree(final_of_slot, st); dfree(nonroot, st); dfree(keys, st); dfree(perm, st);
+
+    // 8. moments
+    MomentArgs a;
+    a.ntot = N;
+    a.mtot = M;
+    a.coord = T->coord; a.mass = T->mass; a.soft = T->soft; a.delta = T->delta;
+    a.first = T->first; a.next = T->next; a.parent = T->parent;
+    a.quads = (quadrupole && compute_moments) ? 1 : 0;
+    a.quad = nullptr;
+    a.acc = nullptr;
+    a.nchild = nullptr;
+    a.arrived = nullptr;
+    if (quadrupole) {
+        TG_TRY(dalloc(&T->quad, 9 * M, st));
+        TG_CUDA(cudaMemsetAsync(T->quad, 0, sizeof(double) * 9 * M, st));
+        a.quad = T->quad;
+    }
+    if (compute_moments) {
+        TG_TRY(dalloc(&a.acc, 3 * M, st));
+        TG_TRY(dalloc(&a.nchild, M, st));
+        TG_TRY(dalloc(&a.arrived, M, st));
+        TG_CUDA(cudaMemsetAsync(a.nchild, 0, sizeof(int) * M, st));
+        TG_CUDA(cudaMemsetAsync(a.arrived, 0, sizeof(int) * M, st));
+        { k_count_node_children<<<LAUNCH(M)>>>(N, M, T->parent, a.nchild); tg::note_launch(); }
+        { k_moments<<<LAUNCH(M)>>>(a); tg::note_launch(); }
+        TG_CUDA(cudaGetLastError());
+        dfree(a.acc, st); dfree(a.nchild, st); dfree(a.arrived, st);
+    } else {
+        { k_fold_only<<<LAUNCH(M)>>>(a); tg::note_launch(); }
+        TG_CUDA(cudaGetLastError());
+    }
+    dfree(sys_off, st); dfree(mn, st); dfree(mx, st); dfree(center, st); dfree(size, st);
+    TG_CUDA(cudaStreamSynchronize(st));
+    return TG_OK;
+}
+
+// _morton_order (grouped_treewalk.py:269-275): stable order of points by their keys in their own
+// bounding cube. perm receives uint32 indices.
+tg_status morton_order_device(const double *pos, int64_t n, uint32_t *perm, cudaStream_t st) {
+    if (n <= 0) return TG_OK;
+    if (n > 0x7fffffffLL) return TG_ERR_BAD_ARG;
+    std::vector<int64_t> off = {0, n};
+    int64_t *sys_off = nullptr;
+    unsigned long long *mn = nullptr, *mx = nullptr;
+    double *center = nullptr, *size = nullptr;
+    uint64_t *keys = nullptr;
+    TG_TRY(dalloc(&sys_off, 2, st));
+    TG_TRY(dalloc(&mn, 3, st));
+    TG_TRY(dalloc(&mx, 3, st));
+    TG_TRY(dalloc(&center, 3, st));
+    TG_TRY(dalloc(&size, 1, st));
+    TG_TRY(dalloc(&keys, n, st));
+    TG_CUDA(cudaMemcpyAsync(sys_off, off.data(), sizeof(int64_t) * 2, cudaMemcpyHostToDevice, st));
+    { k_bbox_init<<<1, 32, 0, st>>>(mn, mx, 1); tg::note_launch(); }
+    { k_bbox<<<div_up(n, BB_THREADS * BB_ITEMS), BB_THREADS, 0, st>>>(pos, n, sys_off, 1, mn, mx); tg::note_launch(); }
+    { k_bbox_finish<<<1, 32, 0, st>>>(mn, mx, 1, center, size); tg::note_launch(); }
+    { k_keys<<<LAUNCH(n)>>>(pos, n, sys_off, 1, center, size, keys, nullptr, perm); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
+    TG_TRY(radix_sort_pairs(keys, perm, n, 63, st));
+    dfree(sys_off, st); dfree(mn, st); dfree(mx, st); dfree(center, st); dfree(size, st); dfree(keys, st);
+    // the host vector `off` must outlive the copy
+    TG_CUDA(cudaStreamSynchronize(st));
+    return TG_OK;
+}
+
+}  // namespace tg

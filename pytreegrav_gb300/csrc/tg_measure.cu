@@ -1,0 +1,65 @@
+// Measurement utilities: kernel-launch counter and an FP32 FMA-throughput probe (the roofline
+// denominator for the FP32-bound walk; see include/pytreegrav_gb300_measure.h).
+#include <atomic>
+
+#include "../../include/pytreegrav_gb300_measure.h"
+#include "tg_common.cuh"
+
+namespace tg {
+static std::atomic<int64_t> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+}  // namespace tg
+
+namespace {
+constexpr int FMA_ITERS = 4096;
+constexpr int FMA_CHAINS = 8;
+
+__global__ void __launch_bounds__(256) k_fma_probe(float *sink, float a, float b) {
+    float v[FMA_CHAINS];
+#pragma unroll
+    for (int c = 0; c < FMA_CHAINS; c++) v[c] = threadIdx.x * 1e-3f + c;
+    for (int i = 0; i < FMA_ITERS; i++) {
+#pragma unroll
+        for (int c = 0; c < FMA_CHAINS; c++) v[c] = fmaf(v[c], a, b);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < FMA_CHAINS; c++) s += v[c];
+    if (s == 1234.5f) sink[0] = s;  // never true in practice; keeps the chains live
+}
+}  // namespace
+
+extern "C" {
+
+int64_t tg_launch_count(void) { return tg::g_launches.load(); }
+
+int tg_measure_fp32_fma(double *tflops, double *ms, void *stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    float *sink = nullptr;
+    TG_CUDA(cudaMalloc((void **)&sink, sizeof(float)));
+    int per_sm = 0;
+    TG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fma_probe, 256, 0));
+    const int blocks = per_sm * tg::num_sms() * 4;
+    cudaEvent_t e0, e1;
+    TG_CUDA(cudaEventCreate(&e0));
+    TG_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; rep++) {
+        TG_CUDA(cudaEventRecord(e0, st));
+        k_fma_probe<<<blocks, 256, 0, st>>>(sink, 0.999999f, 1e-7f);
+        TG_CUDA(cudaEventRecord(e1, st));
+        TG_CUDA(cudaEventSynchronize(e1));
+        float t = 0.f;
+        TG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+        if (rep > 0 && t < best) best = t;  // first launch is warm-up
+    }
+    double flops = 2.0 * FMA_ITERS * FMA_CHAINS * 256.0 * blocks;
+    *tflops = flops / (best * 1e-3) / 1e12;
+    *ms = best;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    return TG_OK;
+}
+
+}  // extern "C"

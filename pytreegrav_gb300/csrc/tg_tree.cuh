@@ -1,0 +1,75 @@
+// Device-resident octree and the walk arena derived from it.
+#pragma once
+
+#include <type_traits>
+#include <vector>
+
+#include "tg_common.cuh"
+
+namespace tg {
+
+// 32-byte FP64 quadruple (the CUDA double4 vector type is deprecated in CUDA 13).
+struct alignas(32) D4 {
+    double x, y, z, w;
+};
+template <typename T>
+using vec4 = typename std::conditional<sizeof(T) == 4, float4, D4>::type;
+
+// Walk arena: the octree repacked for the grouped walk. Nodes keep their final numbering
+// (node j = arena element npart_total + j) because pytreegrav's numbering already makes every
+// node's node-children contiguous; each node's particle children are copied into a contiguous
+// leaf range. Positions are split into a float "hi" part and the float rounding residual "lo",
+// so the walk can form source-target offsets relative to its group to ~2^-48 relative accuracy.
+template <typename T>
+struct Arena {
+    int64_t n_nodes = 0, n_leaves = 0;
+    // per node
+    vec4<T> *n_pos = nullptr;  // hi.xyz, M
+    vec4<T> *n_lo = nullptr;   // lo.xyz, hmax
+    vec4<T> *n_geo = nullptr;  // size, delta, hmax, 0
+    int4 *n_link = nullptr;     // first node child (arena node index), n node children, leaf start, n leaves
+    T *n_quad = nullptr;        // (n_nodes, 6): xx xy xz yy yz zz
+    // per leaf
+    vec4<T> *l_pos = nullptr;  // hi.xyz, m
+    vec4<T> *l_lo = nullptr;   // lo.xyz, h
+    bool built = false;
+    bool has_quad = false;
+};
+
+struct WalkStats {
+    int64_t interactions = 0, node_tests = 0, max_stack = 0, groups = 0;
+};
+
+}  // namespace tg
+
+struct tg_tree_s {
+    int64_t ntot = 0;       // particles in the arena (all systems)
+    int64_t mtot = 0;       // nodes in the arena (all systems)
+    int32_t nsys = 1;
+    int has_quads = 0;
+    int has_coincident = 0;
+    int compute_moments = 1;
+    std::vector<int64_t> sys_off;       // host: particle offsets per system (nsys + 1)
+    std::vector<int64_t> sys_node_off;  // host: node offsets per system (nsys + 1), roots first
+    std::vector<int64_t> sys_capacity;  // host: NumNodes per system (reference capacity rule)
+    cudaStream_t stream = nullptr;
+
+    // Octree arrays over the arena: particles [0, ntot), nodes [ntot, ntot + mtot).
+    double *coord = nullptr;   // 3 per element
+    double *mass = nullptr;
+    double *size = nullptr;
+    double *delta = nullptr;
+    double *soft = nullptr;
+    double *quad = nullptr;    // 9 per NODE (mtot rows), or null
+    int64_t *first = nullptr;
+    int64_t *next = nullptr;
+    int64_t *walk_idx = nullptr;  // per particle: index into the caller's input arrays
+    int64_t *parent = nullptr;    // per element: owning node (arena index), -1 for roots
+    int2 *node_range = nullptr;   // per node: particle range [lo, hi) of its subtree
+    double *cell_center = nullptr;  // per node: geometric centre of its cell (3)
+
+    tg::Arena<float> arena32;
+    tg::Arena<double> arena64;
+    tg::WalkStats last_stats;
+    int64_t *stats_dev = nullptr;  // 4 counters
+};

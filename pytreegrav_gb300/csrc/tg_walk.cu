@@ -1,0 +1,1055 @@
+// Grouped Barnes-Hut walk (pytreegrav grouped_treewalk.py:163-241 with the per-interaction kernel
+// of :45-155), one warp per group of consecutive Morton-ordered targets.
+//
+// Traversal: the warp pops up to 32 pending nodes from a per-warp stack in shared memory, tests
+// them in parallel against the group's bounding box (nearest-corner distance and the group's
+// maximum softening, as pytreegrav does), and votes with __ballot_sync: accepted nodes go to the
+// interaction list, opened nodes push their node children (contiguous indices) onto the stack and
+// append their particle children (a contiguous leaf range) to the interaction list.
+// The test runs in FP32 with an error bound; a node inside the bound is re-tested with the exact
+// FP64 expression on the tree's FP64 arrays, so the accepted set is exactly pytreegrav's.
+//
+// Evaluation: every 32 list entries are staged in shared memory as offsets from a group reference
+// point (hi/lo float pairs keep near-field offsets exact to FP32 rounding) and swept by all lanes:
+// lane = (target, slice), each slice takes every (32/group_size)-th source. Sources that cannot be
+// within any target's softening length (checked once per source against the group box) take the
+// point-mass path; the rest take the full softened path. Each lane sums a batch in registers and
+// adds the batch total into a Kahan-compensated accumulator.
+#include <type_traits>
+
+#include "tg_tree.cuh"
+
+namespace tg {
+
+constexpr int WALK_WARPS = 4;
+constexpr int STACK_CAP = 1536;
+constexpr int ILIST_CAP = 320;
+constexpr int NLIST_CAP = 64;
+
+// ---------------------------------------------------------------------------------------------
+// Softening kernels (kernel.py:5-75) in the walk's precision.
+template <typename T>
+__device__ __forceinline__ T force_kernel(T r, T h) {
+    if (r > h) return T(1) / (r * r * r);
+    T hinv = T(1) / h;
+    T q = r * hinv;
+    T h3 = hinv * hinv * hinv;
+    if (q <= T(0.5)) return (T(10.666666666666666666) + q * q * (T(-38.4) + T(32.0) * q)) * h3;
+    return (T(21.333333333333) - T(48.0) * q + T(38.4) * q * q - T(10.666666666667) * q * q * q -
+            T(0.066666666667) / (q * q * q)) * h3;
+}
+template <typename T>
+__device__ __forceinline__ T potential_kernel(T r, T h) {
+    if (h == T(0)) return T(-1) / r;
+    T hinv = T(1) / h;
+    T q = r * hinv;
+    if (q <= T(0.5)) return (T(-2.8) + q * q * (T(5.33333333333333333) + q * q * (T(6.4) * q - T(9.6)))) * hinv;
+    if (q <= T(1))
+        return (T(-3.2) + T(0.066666666666666666666) / q +
+                q * q * (T(10.666666666666666666666) + q * (T(-16.0) + q * (T(9.6) - T(2.1333333333333333333333) * q)))) *
+               hinv;
+    return T(-1) / r;
+}
+template <typename T>
+__device__ __forceinline__ T tidal_kernel(T r, T h) {
+    if (r > h) {
+        T r2 = r * r;
+        return T(3) / (r2 * r2 * r);
+    }
+    T hinv = T(1) / h;
+    T hinv2 = hinv * hinv;
+    T hinv5 = hinv2 * hinv2 * hinv;
+    T q = r * hinv;
+    if (q <= T(0.5)) return (T(76.8) - T(96.0) * q) * hinv5;
+    T qinv = T(1) / q;
+    T qinv3 = qinv * qinv * qinv;
+    return (T(48.0) * qinv - T(76.8) + T(32.0) * q - T(0.2) * qinv3 * qinv * qinv) * hinv5;
+}
+
+// One MUFU instruction (flush-to-zero; positions here are never denormal).
+__device__ __forceinline__ float rsqrt_t(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ double rsqrt_t(double x) { return rsqrt(x); }
+__device__ __forceinline__ float sqrt_t(float x) { return sqrtf(x); }
+__device__ __forceinline__ double sqrt_t(double x) { return sqrt(x); }
+
+// ---------------------------------------------------------------------------------------------
+// Arena packing.
+__device__ __forceinline__ void split_hi_lo(double x, float &hi, float &lo) {
+    hi = __double2float_rn(x);
+    lo = __double2float_rn(x - (double)hi);
+}
+__device__ __forceinline__ void split_hi_lo(double x, double &hi, double &lo) {
+    hi = x;
+    lo = 0.0;
+}
+
+__global__ void k_arena_links(int64_t ntot, int64_t mtot, const int64_t *first, const int64_t *next, int4 *link,
+                              int64_t *nleaf, int *bad) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= mtot) return;
+    int64_t f = ntot + j, stop = next[f];
+    int fc = -1, nc = 0, nl = 0, steps = 0;
+    for (int64_t c = first[f]; c != stop && c >= 0; c = next[c]) {
+        if (++steps > 8) {  // an octree node has at most 8 children
+            atomicOr(bad, 1);
+            break;
+        }
+        if (c < ntot) nl++;
+        else {
+            if (nc == 0) fc = (int)(c - ntot);
+            else if (c - ntot != fc + nc) atomicOr(bad, 2);  // node children must be consecutive
+            nc++;
+        }
+    }
+    if (nc > 0 && (fc < 0 || fc + nc > mtot)) atomicOr(bad, 4);
+    link[j] = make_int4(fc, nc, 0, nl);
+    nleaf[j] = nl;
+}
+
+template <typename T>
+__global__ void k_arena_fill(int64_t ntot, int64_t mtot, const int64_t *first, const int64_t *next,
+                             const double *coord, const double *mass, const double *soft, const double *size,
+                             const double *delta, const double *quad, const int64_t *leaf_start, Arena<T> ar) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= mtot) return;
+    int64_t f = ntot + j, stop = next[f];
+    int64_t ls = leaf_start[j];
+    int4 lk = ar.n_link[j];
+    lk.z = (int)ls;
+    ar.n_link[j] = lk;
+    T hx, hy, hz, lx, ly, lz;
+    split_hi_lo(coord[3 * f], hx, lx);
+    split_hi_lo(coord[3 * f + 1], hy, ly);
+    split_hi_lo(coord[3 * f + 2], hz, lz);
+    T hm = (T)soft[f];
+    ar.n_pos[j] = vec4<T>{hx, hy, hz, (T)mass[f]};
+    ar.n_lo[j] = vec4<T>{lx, ly, lz, hm};
+    ar.n_geo[j] = vec4<T>{(T)size[f], (T)delta[f], hm, T(0)};
+    if (ar.n_quad) {
+        const double *Q = quad + 9 * j;
+        T *q = ar.n_quad + 6 * j;
+        q[0] = (T)Q[0];
+        q[1] = (T)Q[1];
+        q[2] = (T)Q[2];
+        q[3] = (T)Q[4];
+        q[4] = (T)Q[5];
+        q[5] = (T)Q[8];
+    }
+    int64_t k = ls;
+    const int64_t kend = ls + lk.w;
+    for (int64_t c = first[f]; c != stop && c >= 0 && k < kend; c = next[c]) {
+        if (c < ntot) {
+            split_hi_lo(coord[3 * c], hx, lx);
+            split_hi_lo(coord[3 * c + 1], hy, ly);
+            split_hi_lo(coord[3 * c + 2], hz, lz);
+            ar.l_pos[k] = vec4<T>{hx, hy, hz, (T)mass[c]};
+            ar.l_lo[k] = vec4<T>{lx, ly, lz, (T)soft[c]};
+            k++;
+        }
+    }
+}
+
+template <typename T>
+tg_status build_arena(tg_tree_s *t, Arena<T> &ar, cudaStream_t st) {
+    if (ar.built) return TG_OK;
+    const int64_t M = t->mtot, N = t->ntot;
+    ar.n_nodes = M;
+    ar.n_leaves = N;
+    ar.has_quad = t->has_quads && t->quad;
+    TG_CUDA(cudaMallocAsync((void **)&ar.n_pos, sizeof(vec4<T>) * M, st));
+    TG_CUDA(cudaMallocAsync((void **)&ar.n_lo, sizeof(vec4<T>) * M, st));
+    TG_CUDA(cudaMallocAsync((void **)&ar.n_geo, sizeof(vec4<T>) * M, st));
+    TG_CUDA(cudaMallocAsync((void **)&ar.n_link, sizeof(int4) * M, st));
+    if (ar.has_quad) TG_CUDA(cudaMallocAsync((void **)&ar.n_quad, sizeof(T) * 6 * M, st));
+    TG_CUDA(cudaMallocAsync((void **)&ar.l_pos, sizeof(vec4<T>) * N, st));
+    TG_CUDA(cudaMallocAsync((void **)&ar.l_lo, sizeof(vec4<T>) * N, st));
+    int64_t *nleaf = nullptr, *lstart = nullptr, *ltot = nullptr;
+    int *bad = nullptr;
+    TG_CUDA(cudaMallocAsync((void **)&nleaf, sizeof(int64_t) * M, st));
+    TG_CUDA(cudaMallocAsync((void **)&lstart, sizeof(int64_t) * M, st));
+    TG_CUDA(cudaMallocAsync((void **)&ltot, sizeof(int64_t), st));
+    TG_CUDA(cudaMallocAsync((void **)&bad, sizeof(int), st));
+    TG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
+    { k_arena_links<<<div_up(M, 256), 256, 0, st>>>(N, M, t->first, t->next, ar.n_link, nleaf, bad); tg::note_launch(); }
+    TG_TRY(exclusive_scan_i64(nleaf, lstart, M, ltot, st));
+    int hbad = 0;
+    int64_t htot = 0;
+    TG_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TG_CUDA(cudaMemcpyAsync(&htot, ltot, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    TG_CUDA(cudaStreamSynchronize(st));
+    TG_CUDA(cudaFreeAsync(bad, st));
+    TG_CUDA(cudaFreeAsync(ltot, st));
+    if (hbad || htot != N) {
+        cudaFreeAsync(nleaf, st);
+        cudaFreeAsync(lstart, st);
+        set_last_error_msg("internal error: tree links do not form a valid octree for the walk arena");
+        return TG_ERR_CUDA;
+    }
+    { k_arena_fill<T><<<div_up(M, 256), 256, 0, st>>>(N, M, t->first, t->next, t->coord, t->mass, t->soft, t->size,
+                                                     t->delta, t->quad, lstart, ar); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
+    TG_CUDA(cudaFreeAsync(nleaf, st));
+    TG_CUDA(cudaFreeAsync(lstart, st));
+    ar.built = true;
+    return TG_OK;
+}
+
+template <typename T>
+void free_arena(Arena<T> &ar, cudaStream_t st) {
+    if (ar.n_pos) cudaFreeAsync(ar.n_pos, st);
+    if (ar.n_lo) cudaFreeAsync(ar.n_lo, st);
+    if (ar.n_geo) cudaFreeAsync(ar.n_geo, st);
+    if (ar.n_link) cudaFreeAsync(ar.n_link, st);
+    if (ar.n_quad) cudaFreeAsync(ar.n_quad, st);
+    if (ar.l_pos) cudaFreeAsync(ar.l_pos, st);
+    if (ar.l_lo) cudaFreeAsync(ar.l_lo, st);
+    ar = Arena<T>();
+}
+template tg_status build_arena<float>(tg_tree_s *, Arena<float> &, cudaStream_t);
+template tg_status build_arena<double>(tg_tree_s *, Arena<double> &, cudaStream_t);
+template void free_arena<float>(Arena<float> &, cudaStream_t);
+template void free_arena<double>(Arena<double> &, cudaStream_t);
+
+// ---------------------------------------------------------------------------------------------
+// Walk kernel.
+enum { F_POT = 1, F_ACC = 2, F_TID = 4 };
+
+template <typename T>
+struct WalkArgs {
+    Arena<T> ar;
+    int64_t ntot;
+    const double *tc, *ts, *tsize, *tdelta;  // tree FP64 arrays for exact acceptance
+    const double *tpos, *th;                   // targets in walk order (FP64)
+    const vec4<T> *thi, *tlo;                  // the same split into hi (x, y, z, h) and lo (x, y, z, 0)
+    const int64_t *scatter;                    // output row of walk-order target (null: identity)
+    const int2 *groups;                        // (first target, count)
+    const int *group_root;                     // arena node index of each group's tree root
+    const int *group_order;                    // queue position -> group (null: identity)
+    int64_t ngroups;
+    double theta;
+    const float *theta_group;
+    double G;
+    int out_fields;  // requested fields (bits) -> output packing
+    int out_w;
+    double *out;
+    int gs;  // group size (targets per group, divides 32)
+    int *queue;
+    int *status;
+    unsigned long long *stats;  // interactions, node tests, max stack, groups
+};
+
+template <typename T, bool QUAD>
+struct WarpSmem {
+    int stack[STACK_CAP];
+    int ilist[ILIST_CAP];
+    int nlist[QUAD ? NLIST_CAP : 1];
+    vec4<T> spos[32];   // offsets + mass for the point-mass sweep (near sources: mass 0, far away)
+    vec4<T> snear[32];  // offsets + mass of the near sources, swept with softening
+    T sh[32];
+    vec4<T> sq0[QUAD ? 32 : 1];  // quadrupole xx xy xz yy
+    T sq1[QUAD ? 64 : 1];        // quadrupole yz zz
+};
+
+template <typename T>
+struct Acc {
+    T v[10];  // pot | ax ay az | txx txy txz tyy tyz tzz
+};
+
+template <typename T, int FIELDS>
+__device__ __forceinline__ void point_mass(T m, T dx, T dy, T dz, T rinv, Acc<T> &p) {
+    T rinv2 = rinv * rinv;
+    T mr = m * rinv;
+    if (FIELDS & F_POT) p.v[0] -= mr;
+    if (FIELDS & (F_ACC | F_TID)) {
+        T mr3 = mr * rinv2;
+        if (FIELDS & F_ACC) {
+            p.v[1] += mr3 * dx;
+            p.v[2] += mr3 * dy;
+            p.v[3] += mr3 * dz;
+        }
+        if (FIELDS & F_TID) {
+            T q3 = T(3) * mr3 * rinv2;
+            T qx = q3 * dx, qy = q3 * dy;
+            p.v[4] += qx * dx - mr3;
+            p.v[5] += qx * dy;
+            p.v[6] += qx * dz;
+            p.v[7] += qy * dy - mr3;
+            p.v[8] += qy * dz;
+            p.v[9] += q3 * dz * dz - mr3;
+        }
+    }
+}
+
+// General interaction (grouped_treewalk.py:74-107): skips r == 0, softened when r < max(h_s, h_t).
+template <typename T, int FIELDS>
+__device__ __forceinline__ void softened(T m, T hs, T ht_target, T dx, T dy, T dz, T r2, Acc<T> &p) {
+    if (!(r2 > T(0))) return;
+    T rinv = rsqrt_t(r2);
+    T r = r2 * rinv;
+    T ht = hs > ht_target ? hs : ht_target;
+    if (!(r < ht)) {
+        point_mass<T, FIELDS>(m, dx, dy, dz, rinv, p);
+        return;
+    }
+    if (FIELDS & F_POT) p.v[0] += m * potential_kernel(r, ht);
+    if (FIELDS & (F_ACC | F_TID)) {
+        T K = m * force_kernel(r, ht);
+        if (FIELDS & F_ACC) {
+            p.v[1] += K * dx;
+            p.v[2] += K * dy;
+            p.v[3] += K * dz;
+        }
+        if (FIELDS & F_TID) {
+            T Q = m * tidal_kernel(r, ht);
+            p.v[4] += Q * dx * dx - K;
+            p.v[5] += Q * dx * dy;
+            p.v[6] += Q * dx * dz;
+            p.v[7] += Q * dy * dy - K;
+            p.v[8] += Q * dy * dz;
+            p.v[9] += Q * dz * dz - K;
+        }
+    }
+}
+
+// Quadrupole terms of an accepted node (grouped_treewalk.py:109-133).
+template <typename T, int FIELDS>
+__device__ __forceinline__ void quad_terms(const T *q, T dx, T dy, T dz, T rinv, Acc<T> &p) {
+    T rinv2 = rinv * rinv;
+    T r5inv = rinv2 * rinv2 * rinv;
+    T r7inv = r5inv * rinv2;
+    T qxx = q[0], qxy = q[1], qxz = q[2], qyy = q[3], qyz = q[4], qzz = q[5];
+    T qdx = qxx * dx + qxy * dy + qxz * dz;
+    T qdy = qxy * dx + qyy * dy + qyz * dz;
+    T qdz = qxz * dx + qyz * dy + qzz * dz;
+    T A = dx * qdx + dy * qdy + dz * qdz;
+    if (FIELDS & F_POT) p.v[0] += T(-0.5) * A * r5inv;
+    if (FIELDS & F_ACC) {
+        T qf = T(2.5) * A * r7inv;
+        p.v[1] += qf * dx - qdx * r5inv;
+        p.v[2] += qf * dy - qdy * r5inv;
+        p.v[3] += qf * dz - qdz * r5inv;
+    }
+    if (FIELDS & F_TID) {
+        T diag = T(-2.5) * A * r7inv;
+        T fac = T(17.5) * A * r7inv * rinv2;
+        p.v[4] += qxx * r5inv - T(10) * dx * qdx * r7inv + diag + fac * dx * dx;
+        p.v[7] += qyy * r5inv - T(10) * dy * qdy * r7inv + diag + fac * dy * dy;
+        p.v[9] += qzz * r5inv - T(10) * dz * qdz * r7inv + diag + fac * dz * dz;
+        p.v[5] += qxy * r5inv - T(5) * (dx * qdy + dy * qdx) * r7inv + fac * dx * dy;
+        p.v[6] += qxz * r5inv - T(5) * (dx * qdz + dz * qdx) * r7inv + fac * dx * dz;
+        p.v[8] += qyz * r5inv - T(5) * (dy * qdz + dz * qdy) * r7inv + fac * dy * dz;
+    }
+}
+
+template <int FIELDS>
+__device__ __forceinline__ constexpr bool comp(int c) {
+    return c == 0 ? (FIELDS & F_POT) : (c <= 3 ? (FIELDS & F_ACC) : (FIELDS & F_TID));
+}
+
+// Kahan-compensated add of a batch sum (float); plain add for double.
+template <typename T, int FIELDS>
+__device__ __forceinline__ void kahan_add(Acc<T> &S, Acc<T> &C, const Acc<T> &b) {
+#pragma unroll
+    for (int c = 0; c < 10; c++) {
+        if (!comp<FIELDS>(c)) continue;
+        if (sizeof(T) == 4) {
+            T y = b.v[c] - C.v[c];
+            T t = S.v[c] + y;
+            C.v[c] = (t - S.v[c]) - y;
+            S.v[c] = t;
+        } else {
+            S.v[c] += b.v[c];
+        }
+    }
+}
+
+// Exact FP64 acceptance, the expression of treewalk.py:22-25 on the group box r_min
+// (grouped_treewalk.py:209-231), each operation rounded once.
+__device__ __forceinline__ bool accept_exact(int64_t f, const double *tc, const double *ts, const double *tsize,
+                                             const double *tdelta, const double bmin[3], const double bmax[3],
+                                             double hmax, double theta) {
+    double d[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        double c = tc[3 * f + k];
+        d[k] = 0.0;
+        if (c < bmin[k]) d[k] = dsub(bmin[k], c);
+        else if (c > bmax[k]) d[k] = dsub(c, bmax[k]);
+    }
+    double r_min = __dsqrt_rn(dadd(dadd(dmul(d[0], d[0]), dmul(d[1], d[1])), dmul(d[2], d[2])));
+    double h = pymax(ts[f], hmax);
+    double size = tsize[f], delta = tdelta[f];
+    double crit = pymax(dadd(ddiv(size, theta), delta), dadd(dadd(h, dmul(size, 0.6)), delta));
+    return r_min > crit;
+}
+
+template <typename T, int FIELDS, bool QUAD>
+__global__ void __launch_bounds__(WALK_WARPS * 32) k_walk(WalkArgs<T> a) {
+    extern __shared__ unsigned char smem_raw[];
+    WarpSmem<T, QUAD> &sm = reinterpret_cast<WarpSmem<T, QUAD> *>(smem_raw)[threadIdx.x >> 5];
+    const int lane = lane_id();
+    const unsigned lt = lanemask_lt();
+    const int GS = a.gs;
+    const int tl = lane % GS;     // target of this lane within the group
+    const int slice = lane / GS;  // which interleaved share of each batch this lane sums
+    const int NSL = 32 / GS;
+    unsigned long long n_int = 0, n_tests = 0;
+    int max_sp = 0;
+
+    for (;;) {
+        int g = 0;
+        if (lane == 0) g = atomicAdd(a.queue, 1);
+        g = __shfl_sync(FULL, g, 0);
+        if (g >= a.ngroups) break;
+        if (a.group_order) g = a.group_order[g];
+        const int2 gr = a.groups[g];
+        const bool valid = tl < gr.y;
+        const int64_t t = gr.x + (valid ? tl : 0);
+        const vec4<T> thv = a.thi[t], tlv = a.tlo[t];
+        const double theta = a.theta_group ? (double)a.theta_group[g] : a.theta;
+        // group reference point: the first target's hi part; target offsets from it
+        const T gcx = __shfl_sync(FULL, thv.x, 0), gcy = __shfl_sync(FULL, thv.y, 0), gcz = __shfl_sync(FULL, thv.z, 0);
+        const T tx = (thv.x - gcx) + tlv.x, ty = (thv.y - gcy) + tlv.y, tz = (thv.z - gcz) + tlv.z;
+        const T th = thv.w;
+        // group box, relative (for the near-source test) and absolute (for the node tests)
+        T rbmin[3] = {tx, ty, tz}, rbmax[3] = {tx, ty, tz};
+        T abmin[3] = {thv.x, thv.y, thv.z}, abmax[3] = {thv.x, thv.y, thv.z};
+        T hmax_g = th;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                rbmin[k] = fmin(rbmin[k], __shfl_xor_sync(FULL, rbmin[k], o));
+                rbmax[k] = fmax(rbmax[k], __shfl_xor_sync(FULL, rbmax[k], o));
+                abmin[k] = fmin(abmin[k], __shfl_xor_sync(FULL, abmin[k], o));
+                abmax[k] = fmax(abmax[k], __shfl_xor_sync(FULL, abmax[k], o));
+            }
+            hmax_g = fmax(hmax_g, __shfl_xor_sync(FULL, hmax_g, o));
+        }
+        // FP64 box for the exact acceptance test, computed on first need
+        bool have_box_d = false;
+        double bmin[3], bmax[3], hmax_d = 0.0;
+        auto box_d = [&]() {
+            double px = a.tpos[3 * t], py = a.tpos[3 * t + 1], pz = a.tpos[3 * t + 2];
+            bmin[0] = bmax[0] = px;
+            bmin[1] = bmax[1] = py;
+            bmin[2] = bmax[2] = pz;
+            hmax_d = a.th[t];
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    bmin[k] = fmin(bmin[k], __shfl_xor_sync(FULL, bmin[k], o));
+                    bmax[k] = fmax(bmax[k], __shfl_xor_sync(FULL, bmax[k], o));
+                }
+                hmax_d = fmax(hmax_d, __shfl_xor_sync(FULL, hmax_d, o));
+            }
+            have_box_d = true;
+        };
+        const T gscale = fabs(abmin[0]) + fabs(abmin[1]) + fabs(abmin[2]) + fabs(abmax[0]) + fabs(abmax[1]) +
+                         fabs(abmax[2]);
+        const T inv_theta = (T)(1.0 / theta);
+        const T rel_eps = sizeof(T) == 4 ? T(1e-5) : T(0);
+        const T abs_eps = sizeof(T) == 4 ? T(1e-6) : T(0);
+        // softening-path threshold: a source whose squared distance to the box exceeds this cannot
+        // be within any target's softening length, nor coincide with a target
+        const T near_eps = (sizeof(T) == 4 ? T(4e-7) : T(1e-15)) * (gscale + T(1e-30));
+
+        Acc<T> S, C;
+#pragma unroll
+        for (int c = 0; c < 10; c++) S.v[c] = C.v[c] = T(0);
+
+        // evaluate list entries [0, cnt) of `list` (monopole: nodes >= 0, leaves as ~index)
+        // Each slice of lanes sweeps one contiguous chunk of GS staged sources. Sources that may lie
+        // within a softening length of the group (or coincide with a target) are staged as
+        // zero-mass points far away for the branch-free point-mass sweep and swept separately
+        // with the full softened kernel; empty slots of a short batch are staged the same way.
+        const T FAR = sizeof(T) == 4 ? T(1e18) : T(1e150);
+        auto eval_batch = [&](const int *list, int cnt) {
+            bool slow = false;
+            vec4<T> st = vec4<T>{FAR, FAR, FAR, T(0)};
+            if (lane < cnt) {
+                int e = list[lane];
+                vec4<T> p, q;
+                if (e >= 0) {
+                    p = a.ar.n_pos[e];
+                    q = a.ar.n_lo[e];
+                } else {
+                    p = a.ar.l_pos[~e];
+                    q = a.ar.l_lo[~e];
+                }
+                T sx = (p.x - gcx) + q.x, sy = (p.y - gcy) + q.y, sz = (p.z - gcz) + q.z;
+                T dx = fmax(fmax(rbmin[0] - sx, sx - rbmax[0]), T(0));
+                T dy = fmax(fmax(rbmin[1] - sy, sy - rbmax[1]), T(0));
+                T dz = fmax(fmax(rbmin[2] - sz, sz - rbmax[2]), T(0));
+                T d2 = dx * dx + dy * dy + dz * dz;
+                T hh = q.w > hmax_g ? q.w : hmax_g;
+                T lim = hh * T(1.001) + near_eps;
+                slow = !(d2 > lim * lim);
+                if (slow) {
+                    sm.snear[lane] = vec4<T>{sx, sy, sz, p.w};
+                    sm.sh[lane] = q.w;
+                } else {
+                    st = vec4<T>{sx, sy, sz, p.w};
+                }
+            }
+            sm.spos[lane] = st;
+            const unsigned slowmask = __ballot_sync(FULL, slow);
+            __syncwarp();
+            Acc<T> b;
+#pragma unroll
+            for (int c = 0; c < 10; c++) b.v[c] = T(0);
+            const vec4<T> *chunk = sm.spos + slice * GS;
+            if (GS == 32) {
+#pragma unroll 16
+                for (int i = 0; i < 32; i++) {
+                    vec4<T> s = chunk[i];
+                    T dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
+                    point_mass<T, FIELDS>(s.w, dx, dy, dz, rsqrt_t(dx * dx + dy * dy + dz * dz), b);
+                }
+            } else {
+#pragma unroll 4
+                for (int i = 0; i < GS; i++) {
+                    vec4<T> s = chunk[i];
+                    T dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
+                    point_mass<T, FIELDS>(s.w, dx, dy, dz, rsqrt_t(dx * dx + dy * dy + dz * dz), b);
+                }
+            }
+            const unsigned chunk_bits = GS == 32 ? FULL : ((1u << GS) - 1u) << (slice * GS);
+            for (unsigned mk = slowmask & chunk_bits; mk; mk &= mk - 1) {
+                int k = __ffs(mk) - 1;
+                vec4<T> s = sm.snear[k];
+                T dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
+                softened<T, FIELDS>(s.w, sm.sh[k], th, dx, dy, dz, dx * dx + dy * dy + dz * dz, b);
+            }
+            __syncwarp();
+            kahan_add<T, FIELDS>(S, C, b);
+            n_int += (unsigned long long)cnt * (unsigned long long)gr.y;
+        };
+        auto eval_nodes = [&](const int *list, int cnt) {
+            vec4<T> st = vec4<T>{FAR, FAR, FAR, T(0)}, q0 = vec4<T>{T(0), T(0), T(0), T(0)};
+            T q4 = T(0), q5 = T(0);
+            if (lane < cnt) {
+                int e = list[lane];
+                vec4<T> p = a.ar.n_pos[e], q = a.ar.n_lo[e];
+                st = vec4<T>{(p.x - gcx) + q.x, (p.y - gcy) + q.y, (p.z - gcz) + q.z, p.w};
+                const T *qq = a.ar.n_quad + 6 * (int64_t)e;
+                q0 = vec4<T>{qq[0], qq[1], qq[2], qq[3]};
+                q4 = qq[4];
+                q5 = qq[5];
+            }
+            sm.spos[lane] = st;
+            sm.sq0[lane] = q0;
+            sm.sq1[2 * lane] = q4;
+            sm.sq1[2 * lane + 1] = q5;
+            __syncwarp();
+            Acc<T> b;
+#pragma unroll
+            for (int c = 0; c < 10; c++) b.v[c] = T(0);
+            const int k0 = slice * GS;
+#pragma unroll 4
+            for (int i = 0; i < GS; i++) {
+                vec4<T> s = sm.spos[k0 + i];
+                vec4<T> qa = sm.sq0[k0 + i];
+                T qv[6] = {qa.x, qa.y, qa.z, qa.w, sm.sq1[2 * (k0 + i)], sm.sq1[2 * (k0 + i) + 1]};
+                T dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
+                T rinv = rsqrt_t(dx * dx + dy * dy + dz * dz);
+                point_mass<T, FIELDS>(s.w, dx, dy, dz, rinv, b);
+                quad_terms<T, FIELDS>(qv, dx, dy, dz, rinv, b);
+            }
+            __syncwarp();
+            kahan_add<T, FIELDS>(S, C, b);
+            n_int += (unsigned long long)cnt * (unsigned long long)gr.y;
+        };
+
+        int sp = 1, ni = 0, nn = 0;
+        if (lane == 0) sm.stack[0] = a.group_root[g];
+        __syncwarp();
+        bool overflow = false, runaway = false;
+        // a traversal tests every node at most once, and each step tests at least one
+        int64_t steps_left = a.ar.n_nodes + 2;
+        for (;;) {
+            if (--steps_left < 0) {
+                runaway = true;
+                break;
+            }
+            if (sp > 0) {
+                const int cnt = min(sp, 32);
+                const int node = lane < cnt ? sm.stack[sp - 1 - lane] : -1;
+                sp -= cnt;
+                bool acc = false, unsure = false;
+                int4 lk = make_int4(0, 0, 0, 0);
+                if (node >= 0) {
+                    n_tests++;
+                    vec4<T> p = a.ar.n_pos[node];
+                    vec4<T> gm = a.ar.n_geo[node];
+                    T dx = fmax(fmax(abmin[0] - p.x, p.x - abmax[0]), T(0));
+                    T dy = fmax(fmax(abmin[1] - p.y, p.y - abmax[1]), T(0));
+                    T dz = fmax(fmax(abmin[2] - p.z, p.z - abmax[2]), T(0));
+                    T r2 = dx * dx + dy * dy + dz * dz;
+                    T h = gm.z > hmax_g ? gm.z : hmax_g;
+                    T c1 = gm.x * inv_theta + gm.y, c2 = h + T(0.6) * gm.x + gm.y;
+                    T crit = c1 > c2 ? c1 : c2;
+                    T tol = rel_eps * crit + abs_eps * (gscale + fabs(p.x) + fabs(p.y) + fabs(p.z));
+                    T hiq = crit + tol, loq = crit - tol;
+                    if (sizeof(T) == 8) unsure = true;
+                    else if (r2 > hiq * hiq) acc = true;
+                    else if (loq > T(0) && r2 < loq * loq) acc = false;
+                    else unsure = true;
+                }
+                if (__any_sync(FULL, unsure)) {
+                    if (!have_box_d) box_d();
+                    if (unsure)
+                        acc = accept_exact(a.ntot + node, a.tc, a.ts, a.tsize, a.tdelta, bmin, bmax, hmax_d, theta);
+                }
+                const bool opn = node >= 0 && !acc;
+                if (opn) lk = a.ar.n_link[node];
+                const unsigned am = __ballot_sync(FULL, acc);
+                if (QUAD) {
+                    if (acc) sm.nlist[nn + __popc(am & lt)] = node;
+                    nn += __popc(am);
+                } else {
+                    if (acc) sm.ilist[ni + __popc(am & lt)] = node;
+                    ni += __popc(am);
+                }
+                const int nc = lk.y, nl = lk.w;
+                const int sc = warp_inclusive_scan(nc), sl = warp_inclusive_scan(nl);
+                const int totc = __shfl_sync(FULL, sc, 31), totl = __shfl_sync(FULL, sl, 31);
+                if (sp + totc > STACK_CAP) {
+                    overflow = true;
+                    break;
+                }
+                for (int j = 0, o = sp + sc - nc; j < nc; j++) sm.stack[o + j] = lk.x + j;
+                for (int j = 0, o = ni + sl - nl; j < nl; j++) sm.ilist[o + j] = ~(lk.z + j);
+                sp += totc;
+                ni += totl;
+                max_sp = max(max_sp, sp);
+                __syncwarp();
+            }
+            while (ni >= 32) {
+                eval_batch(sm.ilist + ni - 32, 32);
+                ni -= 32;
+            }
+            if (QUAD) {
+                while (nn >= 32) {
+                    eval_nodes(sm.nlist + nn - 32, 32);
+                    nn -= 32;
+                }
+            }
+            if (sp == 0) break;
+        }
+        if (overflow || runaway) {
+            if (lane == 0) atomicOr(a.status, 1 << (overflow ? TG_ERR_STACK_OVERFLOW : TG_ERR_ITER_LIMIT));
+            __syncwarp();
+            continue;
+        }
+        if (ni > 0) eval_batch(sm.ilist, ni);
+        if (QUAD && nn > 0) eval_nodes(sm.nlist, nn);
+
+        // combine the slices of each target and write G * field in the caller's order
+#pragma unroll
+        for (int c = 0; c < 10; c++) {
+            if (!comp<FIELDS>(c)) continue;
+            for (int o = GS; o < 32; o <<= 1) {
+                S.v[c] += __shfl_xor_sync(FULL, S.v[c], o);
+                C.v[c] += __shfl_xor_sync(FULL, C.v[c], o);
+            }
+        }
+        if (slice == 0 && valid) {
+            const int64_t row = a.scatter ? a.scatter[t] : t;
+            double *o = a.out + row * a.out_w;
+            int k = 0;
+            const double G = a.G;
+            auto val = [&](int c) { return G * ((double)S.v[c] - (double)C.v[c]); };
+            if (a.out_fields & F_POT) o[k++] = val(0);
+            if (a.out_fields & F_ACC) {
+                o[k] = val(1);
+                o[k + 1] = val(2);
+                o[k + 2] = val(3);
+                k += 3;
+            }
+            if (a.out_fields & F_TID) {
+                double txx = val(4), txy = val(5), txz = val(6), tyy = val(7), tyz = val(8), tzz = val(9);
+                o[k] = txx; o[k + 1] = txy; o[k + 2] = txz;
+                o[k + 3] = txy; o[k + 4] = tyy; o[k + 5] = tyz;
+                o[k + 6] = txz; o[k + 7] = tyz; o[k + 8] = tzz;
+            }
+        }
+        __syncwarp();
+    }
+    // statistics (interactions are counted per batch entry; each covers the group's targets)
+    if (lane == 0 && a.stats) {
+        atomicAdd(a.stats + 0, n_int);
+        atomicMax(a.stats + 2, (unsigned long long)max_sp);
+    }
+    unsigned long long tests = n_tests;
+    for (int o = 16; o; o >>= 1) tests += __shfl_xor_sync(FULL, tests, o);
+    if (lane == 0 && a.stats) atomicAdd(a.stats + 1, tests);
+}
+
+__global__ void k_make_groups(const int64_t *sys_off, int nsys, int gs, const int64_t *group_off, const int *sys_root,
+                              int2 *groups, int *group_root) {
+    int s = blockIdx.x;
+    if (s >= nsys) return;
+    int64_t a = sys_off[s], b = sys_off[s + 1];
+    int64_t g0 = group_off[s];
+    for (int64_t t = a + (int64_t)threadIdx.x * gs; t < b; t += (int64_t)blockDim.x * gs) {
+        int64_t g = g0 + (t - a) / gs;
+        groups[g] = make_int2((int)t, (int)((b - t) < gs ? (b - t) : gs));
+        group_root[g] = sys_root[s];
+    }
+}
+
+// Engine grouping: groups are taken from the tree, so a group never straddles a jump of the Morton
+// curve. A system root with at most G particles is one group. Every node with more than G
+// particles emits its children, in order, packed greedily into runs of at most G particles; a child
+// with more than G particles breaks the run (it emits its own children), and a child joins the run
+// only if the run's bounding box stays clear of every such large sibling's cell -- a group whose
+// box reached into a dense sibling would open that sibling down to its particles.
+__global__ void k_tree_groups(int64_t ntot, int64_t mtot, const int2 *node_range, const double *cell,
+                              const double *size, const double *coord, const int64_t *first, const int64_t *next,
+                              const int64_t *parent, int G, const int64_t *sys_off, const int64_t *sys_node_off,
+                              int nsys, int2 *groups, int *group_root, unsigned long long *count) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= mtot) return;
+    const int2 r = node_range[j];
+    const int64_t f = ntot + j;
+    int s = 0;
+    if (nsys > 1) {
+        int lo = 0, hi = nsys;
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (sys_off[mid] <= r.x) lo = mid;
+            else hi = mid;
+        }
+        s = lo;
+    }
+    const int root = (int)sys_node_off[s];
+    auto emit = [&](int lo, int cnt) {
+        unsigned long long q = atomicAdd(count, 1ull);
+        groups[q] = make_int2(lo, cnt);
+        group_root[q] = root;
+    };
+    if (r.y - r.x <= G) {
+        if (parent[f] < 0) emit(r.x, r.y - r.x);
+        return;
+    }
+    // children (at most 8) and the cells of the large ones
+    int clo[8], chi[8], nch = 0;
+    double bmin[8][3], bmax[8][3];
+    int nbig = 0;
+    for (int64_t c = first[f]; c != next[f] && c >= 0 && nch < 8; c = next[c]) {
+        if (c < ntot) {
+            clo[nch] = (int)c;
+            chi[nch] = (int)c + 1;
+        } else {
+            int2 cr = node_range[c - ntot];
+            clo[nch] = cr.x;
+            chi[nch] = cr.y;
+            if (cr.y - cr.x > G) {
+                double hs = 0.5 * size[c];
+                for (int k = 0; k < 3; k++) {
+                    bmin[nbig][k] = cell[3 * (c - ntot) + k] - hs;
+                    bmax[nbig][k] = cell[3 * (c - ntot) + k] + hs;
+                }
+                nbig++;
+            }
+        }
+        nch++;
+    }
+    int run_lo = -1, run_cnt = 0;
+    double rlo[3], rhi[3];
+    for (int q = 0; q < nch; q++) {
+        int sz = chi[q] - clo[q];
+        if (sz > G) {
+            if (run_cnt) emit(run_lo, run_cnt);
+            run_cnt = 0;
+            continue;
+        }
+        double lo3[3], hi3[3];
+        for (int k = 0; k < 3; k++) lo3[k] = hi3[k] = coord[3 * (int64_t)clo[q] + k];
+        for (int p = clo[q] + 1; p < chi[q]; p++)
+            for (int k = 0; k < 3; k++) {
+                double v = coord[3 * (int64_t)p + k];
+                lo3[k] = fmin(lo3[k], v);
+                hi3[k] = fmax(hi3[k], v);
+            }
+        if (run_cnt) {
+            double nlo[3], nhi[3];
+            for (int k = 0; k < 3; k++) {
+                nlo[k] = fmin(rlo[k], lo3[k]);
+                nhi[k] = fmax(rhi[k], hi3[k]);
+            }
+            bool hits = false;
+            for (int b = 0; b < nbig && !hits; b++) {
+                bool overlap = true;
+                for (int k = 0; k < 3; k++) overlap = overlap && nlo[k] <= bmax[b][k] && nhi[k] >= bmin[b][k];
+                hits = overlap;
+            }
+            if (run_cnt + sz <= G && !hits) {
+                run_cnt += sz;
+                for (int k = 0; k < 3; k++) {
+                    rlo[k] = nlo[k];
+                    rhi[k] = nhi[k];
+                }
+                continue;
+            }
+            emit(run_lo, run_cnt);
+        }
+        run_lo = clo[q];
+        run_cnt = sz;
+        for (int k = 0; k < 3; k++) {
+            rlo[k] = lo3[k];
+            rhi[k] = hi3[k];
+        }
+    }
+    if (run_cnt) emit(run_lo, run_cnt);
+}
+
+// Queue key for reference grouping: the group's bounding-box diagonal, largest first (as float
+// bits, which order like the floats for non-negative values), so the few groups that straddle a
+// Morton-curve jump -- and open most of the tree -- start first instead of forming the tail.
+__global__ void k_group_cost_keys(const double *tpos, const int2 *groups, int64_t ngroups, uint64_t *keys,
+                                  uint32_t *vals) {
+    int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ngroups) return;
+    int2 gr = groups[g];
+    double lo[3], hi[3];
+    for (int k = 0; k < 3; k++) lo[k] = hi[k] = tpos[3 * (int64_t)gr.x + k];
+    for (int t = 1; t < gr.y; t++)
+        for (int k = 0; k < 3; k++) {
+            double v = tpos[3 * ((int64_t)gr.x + t) + k];
+            lo[k] = fmin(lo[k], v);
+            hi[k] = fmax(hi[k], v);
+        }
+    float d = (float)sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                          (hi[2] - lo[2]) * (hi[2] - lo[2]));
+    keys[g] = (uint64_t)(0xffffffffu - __float_as_uint(d));
+    vals[g] = (uint32_t)g;
+}
+__global__ void k_group_start_keys(const int2 *groups, int64_t ngroups, uint64_t *keys, uint32_t *vals) {
+    int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ngroups) return;
+    keys[g] = (uint32_t)groups[g].x;
+    vals[g] = (uint32_t)g;
+}
+__global__ void k_permute_groups(const uint32_t *perm, int64_t ngroups, const int2 *gin, const int *rin, int2 *gout,
+                                 int *rout) {
+    int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ngroups) return;
+    gout[g] = gin[perm[g]];
+    rout[g] = rin[perm[g]];
+}
+
+// Targets in walk order split once per walk into hi/lo parts in the walk precision.
+template <typename T>
+__global__ void k_prep_targets(const double *tpos, const double *th, int64_t n, vec4<T> *thi, vec4<T> *tlo) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    T hx, hy, hz, lx, ly, lz;
+    split_hi_lo(tpos[3 * i], hx, lx);
+    split_hi_lo(tpos[3 * i + 1], hy, ly);
+    split_hi_lo(tpos[3 * i + 2], hz, lz);
+    thi[i] = vec4<T>{hx, hy, hz, (T)th[i]};
+    tlo[i] = vec4<T>{lx, ly, lz, T(0)};
+}
+
+template <typename T, int FIELDS, bool QUAD>
+static tg_status launch_walk(WalkArgs<T> &a, cudaStream_t st) {
+    size_t smem = sizeof(WarpSmem<T, QUAD>) * WALK_WARPS;
+    auto kern = k_walk<T, FIELDS, QUAD>;
+    TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    TG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WALK_WARPS * 32, smem));
+    if (per_sm < 1) per_sm = 1;
+    int64_t blocks = (int64_t)per_sm * num_sms();
+    int64_t need = (a.ngroups + WALK_WARPS - 1) / WALK_WARPS;
+    if (blocks > need) blocks = need;
+    if (blocks < 1) blocks = 1;
+    { kern<<<(unsigned)blocks, WALK_WARPS * 32, smem, st>>>(a); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
+    return TG_OK;
+}
+
+template <typename T>
+static tg_status dispatch_walk(WalkArgs<T> &a, int fields, bool quad, cudaStream_t st) {
+    // Fields computed: potential and/or acceleration alone, or everything when the tidal tensor is
+    // wanted (its setup already contains the other two).
+    int fc = (fields & F_TID) ? (F_POT | F_ACC | F_TID) : fields;
+    if (quad) {
+        switch (fc) {
+            case F_POT: return launch_walk<T, F_POT, true>(a, st);
+            case F_ACC: return launch_walk<T, F_ACC, true>(a, st);
+            case F_POT | F_ACC: return launch_walk<T, F_POT | F_ACC, true>(a, st);
+            default: return launch_walk<T, F_POT | F_ACC | F_TID, true>(a, st);
+        }
+    }
+    switch (fc) {
+        case F_POT: return launch_walk<T, F_POT, false>(a, st);
+        case F_ACC: return launch_walk<T, F_ACC, false>(a, st);
+        case F_POT | F_ACC: return launch_walk<T, F_POT | F_ACC, false>(a, st);
+        default: return launch_walk<T, F_POT | F_ACC | F_TID, false>(a, st);
+    }
+}
+
+// Walk targets already in walk order (tpos/th on the device). groups/group_root describe the
+// grouping; scatter maps walk order to output rows.
+tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t ntargets, const int2 *groups,
+                   const int *group_root, const int *group_order, int64_t ngroups, const int64_t *scatter, int fields,
+                   int quadrupole, double theta, double G, int group_size, int precision, const float *theta_group,
+                   double *out, cudaStream_t st) {
+    int w = ((fields & F_POT) ? 1 : 0) + ((fields & F_ACC) ? 3 : 0) + ((fields & F_TID) ? 9 : 0);
+    if (!t->stats_dev) TG_CUDA(cudaMalloc((void **)&t->stats_dev, sizeof(unsigned long long) * 4));
+    int *scratch = nullptr;
+    TG_CUDA(cudaMallocAsync((void **)&scratch, sizeof(int) * 2, st));
+    TG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int) * 2, st));
+    TG_CUDA(cudaMemsetAsync(t->stats_dev, 0, sizeof(unsigned long long) * 4, st));
+    tg_status rc = TG_OK;
+    if (precision == TG_FP64) {
+        TG_TRY(build_arena(t, t->arena64, st));
+        WalkArgs<double> a;
+        a.ar = t->arena64;
+        a.ntot = t->ntot;
+        a.tc = t->coord; a.ts = t->soft; a.tsize = t->size; a.tdelta = t->delta;
+        a.tpos = tpos; a.th = th; a.scatter = scatter; a.groups = groups; a.group_root = group_root;
+        a.group_order = group_order;
+        a.ngroups = ngroups; a.theta = theta; a.theta_group = theta_group; a.G = G;
+        a.out_fields = fields; a.out_w = w; a.out = out; a.gs = group_size;
+        a.queue = scratch; a.status = scratch + 1; a.stats = (unsigned long long *)t->stats_dev;
+        vec4<double> *thi = nullptr, *tlo = nullptr;
+        TG_CUDA(cudaMallocAsync((void **)&thi, sizeof(vec4<double>) * std::max<int64_t>(ntargets, 1), st));
+        TG_CUDA(cudaMallocAsync((void **)&tlo, sizeof(vec4<double>) * std::max<int64_t>(ntargets, 1), st));
+        { k_prep_targets<double><<<div_up(ntargets, 256), 256, 0, st>>>(tpos, th, ntargets, thi, tlo); tg::note_launch(); }
+        a.thi = thi;
+        a.tlo = tlo;
+        rc = dispatch_walk<double>(a, fields, quadrupole != 0, st);
+        cudaFreeAsync(thi, st);
+        cudaFreeAsync(tlo, st);
+    } else {
+        TG_TRY(build_arena(t, t->arena32, st));
+        WalkArgs<float> a;
+        a.ar = t->arena32;
+        a.ntot = t->ntot;
+        a.tc = t->coord; a.ts = t->soft; a.tsize = t->size; a.tdelta = t->delta;
+        a.tpos = tpos; a.th = th; a.scatter = scatter; a.groups = groups; a.group_root = group_root;
+        a.group_order = group_order;
+        a.ngroups = ngroups; a.theta = theta; a.theta_group = theta_group; a.G = G;
+        a.out_fields = fields; a.out_w = w; a.out = out; a.gs = group_size;
+        a.queue = scratch; a.status = scratch + 1; a.stats = (unsigned long long *)t->stats_dev;
+        vec4<float> *thi = nullptr, *tlo = nullptr;
+        TG_CUDA(cudaMallocAsync((void **)&thi, sizeof(vec4<float>) * std::max<int64_t>(ntargets, 1), st));
+        TG_CUDA(cudaMallocAsync((void **)&tlo, sizeof(vec4<float>) * std::max<int64_t>(ntargets, 1), st));
+        { k_prep_targets<float><<<div_up(ntargets, 256), 256, 0, st>>>(tpos, th, ntargets, thi, tlo); tg::note_launch(); }
+        a.thi = thi;
+        a.tlo = tlo;
+        rc = dispatch_walk<float>(a, fields, quadrupole != 0, st);
+        cudaFreeAsync(thi, st);
+        cudaFreeAsync(tlo, st);
+    }
+    if (rc != TG_OK) return rc;
+    int status = 0;
+    TG_CUDA(cudaMemcpyAsync(&status, scratch + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    unsigned long long stats[4];
+    TG_CUDA(cudaMemcpyAsync(stats, t->stats_dev, sizeof(stats), cudaMemcpyDeviceToHost, st));
+    TG_CUDA(cudaFreeAsync(scratch, st));
+    TG_CUDA(cudaStreamSynchronize(st));
+    t->last_stats.interactions = (int64_t)stats[0];
+    t->last_stats.node_tests = (int64_t)stats[1];
+    t->last_stats.max_stack = (int64_t)stats[2];
+    t->last_stats.groups = ngroups;
+    if (status & (1 << TG_ERR_STACK_OVERFLOW)) return TG_ERR_STACK_OVERFLOW;
+    if (status & (1 << TG_ERR_ITER_LIMIT)) return TG_ERR_ITER_LIMIT;
+    return TG_OK;
+}
+
+tg_status make_tree_groups(tg_tree_s *t, int G, int2 **groups, int **group_root, int64_t *ngroups,
+                           cudaStream_t st) {
+    const int64_t N = t->ntot, M = t->mtot;
+    int64_t *d_sys = nullptr, *d_node = nullptr;
+    unsigned long long *cnt = nullptr;
+    int2 *g0 = nullptr;
+    int *r0 = nullptr;
+    TG_CUDA(cudaMallocAsync((void **)&g0, sizeof(int2) * N, st));
+    TG_CUDA(cudaMallocAsync((void **)&r0, sizeof(int) * N, st));
+    TG_CUDA(cudaMallocAsync((void **)&cnt, sizeof(unsigned long long), st));
+    TG_CUDA(cudaMallocAsync((void **)&d_sys, sizeof(int64_t) * (t->nsys + 1), st));
+    TG_CUDA(cudaMallocAsync((void **)&d_node, sizeof(int64_t) * (t->nsys + 1), st));
+    TG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), st));
+    TG_CUDA(cudaMemcpyAsync(d_sys, t->sys_off.data(), sizeof(int64_t) * (t->nsys + 1), cudaMemcpyHostToDevice, st));
+    TG_CUDA(cudaMemcpyAsync(d_node, t->sys_node_off.data(), sizeof(int64_t) * (t->nsys + 1), cudaMemcpyHostToDevice,
+                            st));
+    { k_tree_groups<<<div_up(M, 256), 256, 0, st>>>(N, M, t->node_range, t->cell_center, t->size, t->coord, t->first,
+                                                  t->next, t->parent, G, d_sys, d_node, t->nsys, g0, r0, cnt); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
+    unsigned long long ng = 0;
+    TG_CUDA(cudaMemcpyAsync(&ng, cnt, sizeof(ng), cudaMemcpyDeviceToHost, st));
+    TG_CUDA(cudaStreamSynchronize(st));
+    // deterministic Morton order of the groups (their emission order depends on thread timing)
+    uint64_t *keys = nullptr;
+    uint32_t *vals = nullptr;
+    TG_CUDA(cudaMallocAsync((void **)&keys, sizeof(uint64_t) * ng, st));
+    TG_CUDA(cudaMallocAsync((void **)&vals, sizeof(uint32_t) * ng, st));
+    TG_CUDA(cudaMallocAsync((void **)groups, sizeof(int2) * std::max<unsigned long long>(ng, 1), st));
+    TG_CUDA(cudaMallocAsync((void **)group_root, sizeof(int) * std::max<unsigned long long>(ng, 1), st));
+    { k_group_start_keys<<<div_up(ng, 256), 256, 0, st>>>(g0, ng, keys, vals); tg::note_launch(); }
+    TG_TRY(radix_sort_pairs(keys, vals, ng, 32, st));
+    { k_permute_groups<<<div_up(ng, 256), 256, 0, st>>>(vals, ng, g0, r0, *groups, *group_root); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
+    TG_CUDA(cudaFreeAsync(keys, st));
+    TG_CUDA(cudaFreeAsync(vals, st));
+    TG_CUDA(cudaFreeAsync(g0, st));
+    TG_CUDA(cudaFreeAsync(r0, st));
+    TG_CUDA(cudaFreeAsync(cnt, st));
+    TG_CUDA(cudaFreeAsync(d_sys, st));
+    TG_CUDA(cudaFreeAsync(d_node, st));
+    *ngroups = (int64_t)ng;
+    return TG_OK;
+}
+
+// Largest-first queue order of consecutive-block groups (see k_group_cost_keys).
+tg_status make_cost_order(const double *tpos, const int2 *groups, int64_t ngroups, int **order, cudaStream_t st) {
+    uint64_t *keys = nullptr;
+    TG_CUDA(cudaMallocAsync((void **)&keys, sizeof(uint64_t) * std::max<int64_t>(ngroups, 1), st));
+    TG_CUDA(cudaMallocAsync((void **)order, sizeof(int) * std::max<int64_t>(ngroups, 1), st));
+    { k_group_cost_keys<<<div_up(ngroups, 256), 256, 0, st>>>(tpos, groups, ngroups, keys, (uint32_t *)*order); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
+    TG_TRY(radix_sort_pairs(keys, (uint32_t *)*order, ngroups, 32, st));
+    TG_CUDA(cudaFreeAsync(keys, st));
+    return TG_OK;
+}
+
+tg_status make_groups(tg_tree_s *t, const std::vector<int64_t> &sys_off_host, int gs, int2 **groups,
+                      int **group_root, int64_t *ngroups, cudaStream_t st) {
+    int nsys = (int)sys_off_host.size() - 1;
+    std::vector<int64_t> goff(nsys + 1, 0);
+    std::vector<int> roots(nsys);
+    for (int s = 0; s < nsys; s++) {
+        goff[s + 1] = goff[s] + (sys_off_host[s + 1] - sys_off_host[s] + gs - 1) / gs;
+        roots[s] = (int)t->sys_node_off[s];
+    }
+    *ngroups = goff[nsys];
+    int64_t *d_sys = nullptr, *d_goff = nullptr;
+    int *d_roots = nullptr;
+    TG_CUDA(cudaMallocAsync((void **)groups, sizeof(int2) * std::max<int64_t>(*ngroups, 1), st));
+    TG_CUDA(cudaMallocAsync((void **)group_root, sizeof(int) * std::max<int64_t>(*ngroups, 1), st));
+    TG_CUDA(cudaMallocAsync((void **)&d_sys, sizeof(int64_t) * (nsys + 1), st));
+    TG_CUDA(cudaMallocAsync((void **)&d_goff, sizeof(int64_t) * (nsys + 1), st));
+    TG_CUDA(cudaMallocAsync((void **)&d_roots, sizeof(int) * nsys, st));
+    TG_CUDA(cudaMemcpyAsync(d_sys, sys_off_host.data(), sizeof(int64_t) * (nsys + 1), cudaMemcpyHostToDevice, st));
+    TG_CUDA(cudaMemcpyAsync(d_goff, goff.data(), sizeof(int64_t) * (nsys + 1), cudaMemcpyHostToDevice, st));
+    TG_CUDA(cudaMemcpyAsync(d_roots, roots.data(), sizeof(int) * nsys, cudaMemcpyHostToDevice, st));
+    { k_make_groups<<<nsys, 256, 0, st>>>(d_sys, nsys, gs, d_goff, d_roots, *groups, *group_root); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
+    TG_CUDA(cudaFreeAsync(d_sys, st));
+    TG_CUDA(cudaFreeAsync(d_goff, st));
+    TG_CUDA(cudaFreeAsync(d_roots, st));
+    // the host vectors above must outlive the async copies
+    TG_CUDA(cudaStreamSynchronize(st));
+    return TG_OK;
+}
+
+}  // namespace tg

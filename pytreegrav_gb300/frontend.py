@@ -1,0 +1,272 @@
+"""pytreegrav's public gravity API (src/pytreegrav/frontend.py) on the GB300 engine.
+
+Same function names, arguments, defaults, return shapes, ordering and exceptions as pytreegrav's
+tree and brute-force paths; every computation runs on the GPU through libpytreegrav_gb300.
+
+Differences a caller can see, all deliberate:
+  * ``parallel`` is accepted and ignored: the GPU path is always parallel, and results do not
+    depend on it (pytreegrav's own parallel and serial walks are bit-identical too).
+  * ``precision`` (keyword, extension): the tree walk evaluates interactions in FP32 with
+    compensated accumulation by default ("fp32"); "fp64" evaluates them in FP64. Either way the
+    tree (keys, topology, moments) is bit-identical to pytreegrav's and the accepted node set is
+    pytreegrav's exactly. Brute force defaults to FP64 (bit-identical sums) for device="cpu" and
+    FP32 for device="cuda", matching what each device meant in pytreegrav.
+  * ``morton_order=False``/``radix=False`` in ConstructTree still build the radix tree (pytreegrav
+    documents both builds as giving identical fields on generic data); ``vel`` (the velocity tree
+    used only by the correlation functions) is not provided.
+"""
+
+import warnings
+
+import numpy as np
+from numpy import zeros
+
+from .tree import Octree, bruteforce, morton_order
+
+SYMMETRIC_NMIN = 1000
+
+
+def _f64(a):
+    """Cast to float64 without collapsing a length-1 array to a scalar (frontend.py:20-25)."""
+    return np.asarray(a, dtype=np.float64)
+
+
+def checkTreeQuadrupoles(tree, quadrupole):
+    """Raise ValueError if a quadrupole treewalk is requested on a tree that lacks them."""
+    if quadrupole and not tree.HasQuads:
+        raise ValueError(
+            "quadrupole=True requires a tree built with quadrupole moments: pass a tree from "
+            "ConstructTree(..., quadrupole=True), or evaluate with quadrupole=False.")
+
+
+def valueTestMethod(method):
+    """Raise TypeError/ValueError unless method is one of 'adaptive', 'bruteforce', 'tree'."""
+    methods = ["adaptive", "bruteforce", "tree"]
+    if type(method) != str:
+        raise TypeError("Invalid method type %s, must be str" % type(method))
+    if method not in methods:
+        raise ValueError("Invalid method %s. Must be one of: %s" % (method, str(methods)))
+
+
+def warn_if_coincident_positions(tree, softening=None):
+    """Warn if the build found particle positions coincident to floating-point precision."""
+    if not tree.HasCoincidentPoints:
+        return
+    if softening is not None and np.any(softening > 0):
+        warnings.warn("Warning: Particle positions are non-unique. Softening will determine the answer for "
+                      "overlapping particles.")
+        return
+    warnings.warn("Warning: Particle positions are non-unique. The answer will be singular or garbage for "
+                  "overlapping particles.")
+
+
+def _check_device(device, quadrupole):
+    if device not in ("cpu", "cuda"):
+        raise ValueError(f"device must be 'cpu' or 'cuda', got {device!r}")
+    if device == "cuda" and quadrupole:
+        raise ValueError("device='cuda' is monopole only; pass quadrupole=False")
+
+
+def _bf_precision(device):
+    return "fp32" if device == "cuda" else "fp64"
+
+
+def _check_tree(tree):
+    if not isinstance(tree, Octree):
+        raise TypeError("tree must be an Octree built by pytreegrav_gb300.ConstructTree")
+
+
+def ConstructTree(pos, m=None, softening=None, quadrupole=False, vel=None, compute_moments=True, morton_order=True,
+                  radix=True):
+    """Build a tree of the particle data on the GPU for subsequent field evaluation.
+
+    Same arguments as pytreegrav.ConstructTree (frontend.py:73-142). Returns an Octree whose arrays
+    are bit-identical to pytreegrav's radix build.
+    """
+    if vel is not None:
+        raise NotImplementedError("the velocity-carrying DynamicOctree (vel=...) is not provided by pytreegrav_gb300")
+    pos = np.atleast_2d(_f64(pos))
+    if m is None:
+        compute_moments = False
+    else:
+        m = np.atleast_1d(_f64(m))
+    if softening is None:
+        softening = zeros(len(pos))
+    softening = np.atleast_1d(_f64(softening))
+    finite = np.all(np.isfinite(pos)) and np.all(np.isfinite(softening)) and (m is None or np.all(np.isfinite(m)))
+    if not finite:
+        print("Invalid input detected - aborting treebuild to avoid going into an infinite loop!")
+        raise RuntimeError("Invalid input detected - aborting treebuild to avoid going into an infinite loop!")
+    tree = Octree(pos, m, softening, quadrupole=quadrupole, compute_moments=compute_moments)
+    warn_if_coincident_positions(tree, softening)
+    return tree
+
+
+def _self_field(key, pos, m, softening, G, theta, tree, return_tree, method, quadrupole, group_size, device,
+                precision, parallel_threshold):
+    valueTestMethod(method)
+    pos = np.atleast_2d(_f64(pos))
+    m = np.atleast_1d(_f64(m))
+    if softening is None:
+        softening = np.zeros_like(m)
+    softening = np.atleast_1d(_f64(softening))
+    if method == "adaptive":
+        method = "tree" if (tree is not None or len(pos) > parallel_threshold) else "bruteforce"
+    if device is not None:
+        _check_device(device, quadrupole)
+    if method == "bruteforce":
+        res = bruteforce(None, None, pos, m, softening, mutual=True, G=G, precision=_bf_precision(device),
+                         **{key: True})[key]
+        if return_tree:
+            tree = None
+    else:
+        if tree is None:
+            tree = ConstructTree(pos, m, softening, quadrupole=quadrupole)
+            checkTreeQuadrupoles(tree, quadrupole)
+            res = tree.fields(potential=key == "potential", accel=key == "accel", tidal=key == "tidal",
+                              quadrupole=quadrupole, group_size=group_size, theta=theta, G=G, order="tree",
+                              precision=precision)[key]
+        else:
+            _check_tree(tree)
+            checkTreeQuadrupoles(tree, quadrupole)
+            # targets sorted by their own Morton order, not the tree's stored permutation
+            res = tree.fields(pos, softening, potential=key == "potential", accel=key == "accel",
+                              tidal=key == "tidal", quadrupole=quadrupole, group_size=group_size, theta=theta, G=G,
+                              order="morton", precision=precision)[key]
+    if return_tree:
+        return res, tree
+    return res
+
+
+def _target_field(key, pos_target, pos_source, m_source, softening_target, softening_source, G, theta, tree,
+                  return_tree, method, quadrupole, group_size, precision):
+    valueTestMethod(method)
+    if tree is None and (pos_source is None or m_source is None):
+        raise ValueError("Must pass either pos_source & m_source or source tree.")
+    pos_target = np.atleast_2d(_f64(pos_target))
+    if softening_target is None:
+        softening_target = zeros(len(pos_target))
+    softening_target = np.atleast_1d(_f64(softening_target))
+    if pos_source is not None:
+        pos_source = np.atleast_2d(_f64(pos_source))
+        m_source = np.atleast_1d(_f64(m_source))
+        if softening_source is None:
+            softening_source = zeros(len(pos_source))
+        softening_source = np.atleast_1d(_f64(softening_source))
+    if method == "adaptive":
+        if pos_source is None or len(pos_target) * len(pos_source) > 10**6:
+            method = "tree"
+        else:
+            method = "bruteforce"
+    if method == "bruteforce":
+        res = bruteforce(pos_target, softening_target, pos_source, m_source, softening_source, mutual=False, G=G,
+                         precision="fp64", **{key: True})[key]
+        if return_tree:
+            tree = None
+    else:
+        if tree is None:
+            tree = ConstructTree(pos_source, m_source, softening_source, quadrupole=quadrupole)
+        _check_tree(tree)
+        checkTreeQuadrupoles(tree, quadrupole)
+        res = tree.fields(pos_target, softening_target, potential=key == "potential", accel=key == "accel",
+                          tidal=key == "tidal", quadrupole=quadrupole, group_size=group_size, theta=theta, G=G,
+                          order="morton", precision=precision)[key]
+    if return_tree:
+        return res, tree
+    return res
+
+
+def Potential(pos, m, softening=None, G=1.0, theta=0.7, tree=None, return_tree=False, parallel=False,
+              method="adaptive", quadrupole=False, group_size=8, device="cpu", *, precision="fp32"):
+    """Gravitational potential of N particles at their own positions (frontend.py:145-293)."""
+    return _self_field("potential", pos, m, softening, G, theta, tree, return_tree, method, quadrupole, group_size,
+                       device, precision, 4000 if parallel else 1000)
+
+
+def Accel(pos, m, softening=None, G=1.0, theta=0.7, tree=None, return_tree=False, parallel=False,
+          method="adaptive", quadrupole=False, group_size=8, device="cpu", *, precision="fp32"):
+    """Gravitational acceleration of N particles at their own positions (frontend.py:421-560)."""
+    return _self_field("accel", pos, m, softening, G, theta, tree, return_tree, method, quadrupole, group_size,
+                       device, precision, 4000 if parallel else 1000)
+
+
+def TidalTensor(pos, m, softening=None, G=1.0, theta=0.7, tree=None, return_tree=False, parallel=False,
+                method="adaptive", quadrupole=False, group_size=8, *, precision="fp32"):
+    """Tidal tensor T_ij = dg_i/dx_j at the particle positions (frontend.py:688-789)."""
+    return _self_field("tidal", pos, m, softening, G, theta, tree, return_tree, method, quadrupole, group_size,
+                       None, precision, 4000 if parallel else 1000)
+
+
+def PotentialTarget(pos_target, pos_source, m_source, softening_target=None, softening_source=None, G=1.0,
+                    theta=0.7, tree=None, return_tree=False, parallel=False, method="adaptive", quadrupole=False,
+                    group_size=8, *, precision="fp32"):
+    """Potential at arbitrary target points from a set of sources (frontend.py:296-418)."""
+    return _target_field("potential", pos_target, pos_source, m_source, softening_target, softening_source, G, theta,
+                         tree, return_tree, method, quadrupole, group_size, precision)
+
+
+def AccelTarget(pos_target, pos_source, m_source, softening_target=None, softening_source=None, G=1.0, theta=0.7,
+                tree=None, return_tree=False, parallel=False, method="adaptive", quadrupole=False, group_size=8, *,
+                precision="fp32"):
+    """Acceleration at arbitrary target points from a set of sources (frontend.py:563-685)."""
+    return _target_field("accel", pos_target, pos_source, m_source, softening_target, softening_source, G, theta,
+                         tree, return_tree, method, quadrupole, group_size, precision)
+
+
+def TidalTensorTarget(pos_target, pos_source, m_source, softening_target=None, softening_source=None, G=1.0,
+                      theta=0.7, tree=None, return_tree=False, parallel=False, method="adaptive", quadrupole=False,
+                      group_size=8, *, precision="fp32"):
+    """Tidal tensor at arbitrary target points from a set of sources (frontend.py:792-901)."""
+    return _target_field("tidal", pos_target, pos_source, m_source, softening_target, softening_source, G, theta,
+                         tree, return_tree, method, quadrupole, group_size, precision)
+
+
+class Field:
+    """A reusable gravitational field: tree built once on the GPU, evaluated many times, any subset of
+    potential/accel/tidal from a single traversal (frontend.py:904-1044)."""
+
+    def __init__(self, pos, m, softening=None, G=1.0, theta=0.7, quadrupole=False, group_size=8, parallel=False, *,
+                 precision="fp32"):
+        pos = np.atleast_2d(_f64(pos))
+        m = np.atleast_1d(_f64(m))
+        if softening is None:
+            softening = np.zeros_like(m)
+        softening = np.atleast_1d(_f64(softening))
+        self.G = G
+        self.theta = theta
+        self.quadrupole = quadrupole
+        self.group_size = group_size
+        self.parallel = parallel
+        self.precision = precision
+        self.tree = ConstructTree(pos, m, softening, quadrupole=quadrupole)
+
+    def __repr__(self):
+        return (f"<pytreegrav.Field: {self.tree.NumParticles} particles, "
+                f"{'quadrupole' if self.quadrupole else 'monopole'}, theta={self.theta}, "
+                f"G={self.G}, group_size={self.group_size}, parallel={self.parallel}>")
+
+    def evaluate(self, potential=False, accel=False, tidal=False, pos_target=None, softening_target=None, theta=None,
+                 parallel=None, group_size=None, precision=None):
+        if not (potential or accel or tidal):
+            raise ValueError("request at least one of potential=True, accel=True, tidal=True")
+        theta = self.theta if theta is None else theta
+        group_size = self.group_size if group_size is None else group_size
+        precision = self.precision if precision is None else precision
+        kw = dict(potential=potential, accel=accel, tidal=tidal, quadrupole=self.quadrupole, group_size=group_size,
+                  theta=theta, G=self.G, precision=precision)
+        if pos_target is None:
+            return self.tree.fields(order="tree", **kw)
+        pos_target = np.atleast_2d(_f64(pos_target))
+        if softening_target is None:
+            softening_target = zeros(len(pos_target))
+        softening_target = np.atleast_1d(_f64(softening_target))
+        return self.tree.fields(pos_target, softening_target, order="morton", **kw)
+
+    def potential(self, pos_target=None, **kwargs):
+        return self.evaluate(potential=True, pos_target=pos_target, **kwargs)["potential"]
+
+    def accel(self, pos_target=None, **kwargs):
+        return self.evaluate(accel=True, pos_target=pos_target, **kwargs)["accel"]
+
+    def tidal(self, pos_target=None, **kwargs):
+        return self.evaluate(tidal=True, pos_target=pos_target, **kwargs)["tidal"]

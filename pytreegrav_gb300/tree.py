@@ -1,0 +1,203 @@
+"""Device-resident octree with pytreegrav's Octree interface (src/pytreegrav/octree.py:8-28, 664-723).
+
+The tree lives on the GPU as the arrays pytreegrav defines -- particles at [0, NumParticles) in
+Morton order, nodes after them in pytreegrav's own numbering -- plus a walk arena derived from them.
+The attribute arrays (Coordinates, Masses, ...) are copied to the host on first access, padded to
+NumNodes rows exactly as pytreegrav leaves its spare capacity (zeros, and -1 links).
+"""
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+FIELD_KEYS = ("potential", "accel", "tidal")
+
+
+def _as_f64(a, shape=None):
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+class Octree:
+    """An octree built on the GPU by ConstructTree.
+
+    Attributes mirror pytreegrav's Octree jitclass: NumParticles, NumNodes, HasQuads,
+    HasCoincidentPoints, Coordinates, Masses, Sizes, Deltas, Softenings, Quadrupoles,
+    FirstSubnode, NextBranch, TreewalkIndices.
+    """
+
+    def __init__(self, pos, m=None, softening=None, quadrupole=False, compute_moments=True):
+        L = _lib.load()
+        pos = _as_f64(pos, (-1, 3))
+        n = len(pos)
+        m = None if m is None else _as_f64(m, (n,))
+        softening = None if softening is None else _as_f64(softening, (n,))
+        handle = ctypes.c_void_p()
+        rc = L.tg_tree_build(_lib.ptr(pos), _lib.ptr(m), _lib.ptr(softening), n, int(bool(quadrupole)),
+                             int(bool(compute_moments)), _lib.TG_MEM_HOST, None, ctypes.byref(handle))
+        _lib.check(rc, "ConstructTree")
+        self._h = handle
+        self._host = None
+        info = _lib.TreeInfo()
+        _lib.check(L.tg_tree_info_get(self._h, ctypes.byref(info)))
+        self.NumParticles = int(info.npart)
+        self.NumNodes = int(info.num_nodes)
+        self.node_hi = int(info.node_hi)
+        self.HasQuads = bool(quadrupole)
+        self.HasCoincidentPoints = bool(info.has_coincident)
+
+    @classmethod
+    def _from_handle(cls, handle, quadrupole):
+        self = cls.__new__(cls)
+        L = _lib.load()
+        self._h = handle
+        self._host = None
+        info = _lib.TreeInfo()
+        _lib.check(L.tg_tree_info_get(self._h, ctypes.byref(info)))
+        self.NumParticles = int(info.npart)
+        self.NumNodes = int(info.num_nodes)
+        self.node_hi = int(info.node_hi)
+        self.HasQuads = bool(quadrupole)
+        self.HasCoincidentPoints = bool(info.has_coincident)
+        return self
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().tg_tree_free(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # -- host copies of the Octree arrays ------------------------------------------------------
+    def _arrays(self):
+        if self._host is None:
+            nn, n = self.NumNodes, self.NumParticles
+            a = {
+                "Coordinates": np.empty((nn, 3)),
+                "Masses": np.empty(nn),
+                "Sizes": np.empty(nn),
+                "Deltas": np.empty(nn),
+                "Softenings": np.empty(nn),
+                "Quadrupoles": np.empty((nn, 3, 3)) if self.HasQuads else None,
+                "FirstSubnode": np.empty(nn, np.int64),
+                "NextBranch": np.empty(nn, np.int64),
+                "TreewalkIndices": np.empty(n, np.int64),
+            }
+            p = _lib.ptr
+            rc = _lib.load().tg_tree_copy_out(self._h, p(a["Coordinates"]), p(a["Masses"]), p(a["Sizes"]),
+                                              p(a["Deltas"]), p(a["Softenings"]), p(a["Quadrupoles"]),
+                                              p(a["FirstSubnode"]), p(a["NextBranch"]), p(a["TreewalkIndices"]),
+                                              None)
+            _lib.check(rc, "copy_out")
+            self._host = a
+        return self._host
+
+    def __getattr__(self, name):
+        if name in ("Coordinates", "Masses", "Sizes", "Deltas", "Softenings", "Quadrupoles", "FirstSubnode",
+                    "NextBranch", "TreewalkIndices"):
+            return self._arrays()[name]
+        raise AttributeError(name)
+
+    # -- evaluation ------------------------------------------------------------------------------
+    def fields(self, pos=None, soft=None, potential=False, accel=False, tidal=False, quadrupole=False,
+               group_size=8, theta=0.7, G=1.0, order="tree", precision="fp32", theta_per_group=None,
+               grouping="blocks"):
+        """Any subset of {potential, accel, tidal} from one traversal (FieldsTarget_grouped).
+
+        order="tree": the tree's own particles are the targets (pos/soft ignored); "morton": targets
+        are Morton-sorted by their own bounding cube before grouping; "given": grouped as passed.
+        grouping="blocks": group_size consecutive targets per group (pytreegrav's grouping);
+        "tree": groups taken from the tree (order="tree" only).
+        Results come back in the caller's order (the tree's input order for order="tree").
+        """
+        fields = (_lib.TG_FIELD_POTENTIAL * bool(potential) + _lib.TG_FIELD_ACCEL * bool(accel)
+                  + _lib.TG_FIELD_TIDAL * bool(tidal))
+        if fields == 0:
+            raise ValueError("request at least one of potential=True, accel=True, tidal=True")
+        if quadrupole and not self.HasQuads:
+            _lib.check(_lib.TG_ERR_NO_QUADRUPOLES)
+        W = int(bool(potential)) + 3 * int(bool(accel)) + 9 * int(bool(tidal))
+        ord_code = {"tree": _lib.TG_ORDER_TREE, "morton": _lib.TG_ORDER_MORTON, "given": _lib.TG_ORDER_GIVEN}[order]
+        prec = {"fp32": _lib.TG_FP32, "fp64": _lib.TG_FP64}[precision]
+        if ord_code == _lib.TG_ORDER_TREE:
+            n = self.NumParticles
+            pos_p = soft_p = None
+        else:
+            pos = _as_f64(pos, (-1, 3))
+            n = len(pos)
+            soft = np.zeros(n) if soft is None else _as_f64(soft, (n,))
+            pos_p, soft_p = _lib.ptr(pos), _lib.ptr(soft)
+        out = np.empty((n, W))
+        if n == 0:
+            return _split(out, potential, accel, tidal)
+        tpg = None
+        if theta_per_group is not None:
+            tpg = ctypes.c_void_p(int(theta_per_group))  # a device pointer (float32, one per group)
+        grp = {"blocks": _lib.TG_GROUP_BLOCKS, "tree": _lib.TG_GROUP_TREE}[grouping]
+        rc = _lib.load().tg_tree_fields(self._h, pos_p, soft_p, n, fields, int(bool(quadrupole)), float(theta),
+                                        float(G), int(group_size), grp, ord_code, prec, tpg, _lib.TG_MEM_HOST,
+                                        _lib.ptr(out), None)
+        _lib.check(rc, "tree walk")
+        return _split(out, potential, accel, tidal)
+
+    def last_walk_stats(self):
+        """(interactions, node tests, deepest stack, groups) of the last walk on this tree."""
+        v = [ctypes.c_int64() for _ in range(4)]
+        _lib.check(_lib.load().tg_tree_last_walk_stats(self._h, *[ctypes.byref(x) for x in v]))
+        return tuple(int(x.value) for x in v)
+
+
+def _split(out, potential, accel, tidal):
+    res, o = {}, 0
+    if potential:
+        res["potential"] = out[:, 0].copy()
+        o = 1
+    if accel:
+        res["accel"] = np.ascontiguousarray(out[:, o:o + 3])
+        o += 3
+    if tidal:
+        res["tidal"] = np.ascontiguousarray(out[:, o:o + 9]).reshape(-1, 3, 3)
+    return res
+
+
+def morton_order(pos):
+    """Stable permutation sorting points by Morton key in their own bounding cube (_morton_order)."""
+    pos = _as_f64(pos, (-1, 3))
+    perm = np.empty(len(pos), np.int64)
+    if len(pos):
+        _lib.check(_lib.load().tg_morton_order(_lib.ptr(pos), len(pos), _lib.TG_MEM_HOST, _lib.ptr(perm), None),
+                   "morton_order")
+    return perm
+
+
+def bruteforce(pos_t, h_t, pos_s, m_s, h_s, potential=False, accel=False, tidal=False, mutual=False, G=1.0,
+               precision="fp64"):
+    """Direct summation on the GPU. mutual=True: targets are the sources, self excluded by index."""
+    fields = 1 * bool(potential) + 2 * bool(accel) + 4 * bool(tidal)
+    if fields == 0:
+        raise ValueError("request at least one field")
+    pos_s = _as_f64(pos_s, (-1, 3))
+    ns = len(pos_s)
+    m_s = _as_f64(m_s, (ns,))
+    h_s = np.zeros(ns) if h_s is None else _as_f64(h_s, (ns,))
+    if mutual:
+        pos_t, h_t = pos_s, h_s
+    else:
+        pos_t = _as_f64(pos_t, (-1, 3))
+        h_t = np.zeros(len(pos_t)) if h_t is None else _as_f64(h_t, (len(pos_t),))
+    nt = len(pos_t)
+    W = int(bool(potential)) + 3 * int(bool(accel)) + 9 * int(bool(tidal))
+    out = np.empty((nt, W))
+    if nt:
+        prec = {"fp32": _lib.TG_FP32, "fp64": _lib.TG_FP64}[precision]
+        rc = _lib.load().tg_bruteforce(_lib.ptr(pos_t), _lib.ptr(h_t), nt, _lib.ptr(pos_s), _lib.ptr(m_s),
+                                       _lib.ptr(h_s), ns, fields, int(bool(mutual)), float(G), prec,
+                                       _lib.TG_MEM_HOST, _lib.ptr(out), None)
+        _lib.check(rc, "bruteforce")
+    return _split(out, potential, accel, tidal)

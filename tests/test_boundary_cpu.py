@@ -1,0 +1,99 @@
+"""CPU-side checks of the drop-in boundary: the C ABI library loads and exports every symbol the
+header declares, and the frontend validates arguments exactly like pytreegrav before any GPU work."""
+
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from pytreegrav_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    src = open(os.path.join(ROOT, "include", "pytreegrav_gb300.h")).read()
+    return sorted(set(re.findall(r"^(?:tg_status|const char \*)\s*(tg_\w+)\s*\(", src, re.M)))
+
+
+def test_header_and_binding_agree():
+    assert header_symbols() == sorted(_lib.EXPORTS)
+
+
+def test_library_builds_loads_and_exports_every_symbol():
+    from pytreegrav_gb300 import build
+
+    path = build.build()
+    L = ctypes.CDLL(path)
+    for name in header_symbols():
+        assert hasattr(L, name), name
+
+
+def test_status_mapping():
+    with pytest.raises(ValueError):
+        _lib.check(_lib.TG_ERR_BAD_ARG)
+    with pytest.raises(ValueError, match="quadrupole"):
+        _lib.check(_lib.TG_ERR_NO_QUADRUPOLES)
+    with pytest.raises(MemoryError):
+        _lib.check(_lib.TG_ERR_OOM)
+    with pytest.raises(RuntimeError, match="Invalid input"):
+        _lib.check(_lib.TG_ERR_NONFINITE)
+    with pytest.raises(_lib.GravityError, match="stack"):
+        _lib.check(_lib.TG_ERR_STACK_OVERFLOW)
+
+
+@pytest.mark.parametrize("fn", ["Potential", "Accel", "TidalTensor"])
+def test_invalid_method_raises(fn):
+    import pytreegrav_gb300 as tg
+
+    x = np.random.default_rng(0).random((10, 3))
+    m = np.ones(10)
+    with pytest.raises(ValueError):
+        getattr(tg, fn)(x, m, method="nonsense")
+    with pytest.raises(TypeError):
+        getattr(tg, fn)(x, m, method=3)
+
+
+@pytest.mark.parametrize("fn", ["PotentialTarget", "AccelTarget", "TidalTensorTarget"])
+def test_target_forms_need_sources_or_tree(fn):
+    import pytreegrav_gb300 as tg
+
+    x = np.random.default_rng(0).random((10, 3))
+    with pytest.raises(ValueError, match="Must pass either"):
+        getattr(tg, fn)(x, None, None)
+    with pytest.raises(ValueError):
+        getattr(tg, fn)(x, x, np.ones(10), method="nonsense")
+
+
+@pytest.mark.parametrize("fn", ["Potential", "Accel"])
+def test_frontend_rejects_bad_device_combinations(fn):
+    import pytreegrav_gb300 as tg
+
+    x = np.random.default_rng(0).random((500, 3))
+    m = np.ones(500)
+    with pytest.raises(ValueError, match="must be 'cpu' or 'cuda'"):
+        getattr(tg, fn)(x, m, device="gpu")
+    with pytest.raises(ValueError, match="monopole only"):
+        getattr(tg, fn)(x, m, device="cuda", quadrupole=True)
+
+
+def test_nonfinite_input_raises_before_the_gpu():
+    import pytreegrav_gb300 as tg
+
+    x = np.random.default_rng(0).random((100, 3))
+    x[3, 1] = np.nan
+    with pytest.raises(RuntimeError, match="Invalid input"):
+        tg.ConstructTree(x, np.ones(100))
+
+
+def test_quadrupole_guard():
+    import pytreegrav_gb300 as tg
+
+    class Fake:
+        HasQuads = False
+
+    with pytest.raises(ValueError, match="quadrupole"):
+        tg.checkTreeQuadrupoles(Fake(), True)
+    tg.checkTreeQuadrupoles(Fake(), False)

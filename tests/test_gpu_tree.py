@@ -1,0 +1,148 @@
+"""GPU octree build vs the oracle and the golden fixtures: keys, permutation, topology, geometry,
+moments and quadrupoles bit-exact, including re-key rounds, buckets and the reference's capacity."""
+
+import hashlib
+
+import numpy as np
+import pytest
+
+import gen
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TREE_FIELDS = ["Coordinates", "Masses", "Sizes", "Deltas", "Softenings", "Quadrupoles", "FirstSubnode",
+               "NextBranch", "TreewalkIndices"]
+SMALL_CASES = ["uniform2000q", "plummer3000", "rekey302q", "dup250q", "origin5", "tiny1q", "tiny2q", "tiny3q",
+               "lattice216"]
+
+
+@pytest.fixture(scope="module")
+def tg():
+    import pytreegrav_gb300 as tg
+
+    return tg
+
+
+def digest(a):
+    a = np.ascontiguousarray(a)
+    return hashlib.sha256(a.dtype.str.encode() + str(a.shape).encode() + a.tobytes()).hexdigest()
+
+
+def assert_tree_equal(t, ref, quad, label=""):
+    assert t.NumParticles == ref.NumParticles
+    assert t.NumNodes == ref.NumNodes, f"{label}: capacity {t.NumNodes} vs {ref.NumNodes}"
+    assert t.HasCoincidentPoints == ref.HasCoincidentPoints
+    for f in TREE_FIELDS:
+        if f == "Quadrupoles" and not quad:
+            continue
+        a, b = getattr(t, f), getattr(ref, f)
+        if not np.array_equal(a, b):
+            bad = np.argwhere(np.atleast_1d(a != b).reshape(len(a), -1).any(1))[:5].ravel()
+            raise AssertionError(f"{label}: {f} differs at rows {bad.tolist()}")
+
+
+@pytest.mark.parametrize("case", SMALL_CASES)
+def test_tree_matches_golden(tg, golden_trees, case):
+    g = golden_trees
+    quad = bool(g[case + "/quad"])
+    import warnings
+
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        t = tg.ConstructTree(g[case + "/pos"], g[case + "/m"], g[case + "/h"], quadrupole=quad)
+    p = case + "/tree/"
+    assert t.NumNodes == g[p + "NumNodes"]
+    assert t.HasCoincidentPoints == bool(g[p + "HasCoincidentPoints"])
+    for f in TREE_FIELDS:
+        if f == "Quadrupoles" and not quad:
+            continue
+        assert np.array_equal(getattr(t, f), g[p + f]), f"{case}: {f}"
+    assert np.array_equal(tg.morton_order(g[case + "/pos"]), g[case + "/perm"])
+
+
+def test_geometric_only_tree(tg, golden_trees):
+    g = golden_trees
+    t = tg.ConstructTree(g["nomoments500/pos"])
+    for f in TREE_FIELDS:
+        if f == "Quadrupoles":
+            continue
+        assert np.array_equal(getattr(t, f), g["nomoments500/tree/" + f]), f
+
+
+def test_large_tree_digests(tg, golden_bigtree):
+    g = golden_bigtree
+    s1, s2, s3 = (int(v) for v in g["plummer40k/seeds"])
+    x = gen.concentrated(s1, 40000)
+    t = tg.ConstructTree(x, gen.masses(s2, 40000), gen.softenings(s3, 40000, 0.01), quadrupole=True)
+    p = "plummer40k/serial/"
+    assert t.NumNodes == g[p + "NumNodes"]
+    for f in TREE_FIELDS:
+        assert digest(getattr(t, f)) == str(g[p + f + "__sha256"]), f
+
+
+@pytest.mark.parametrize("kind,n", [("uniform", 100_000), ("plummer", 1_000_000), ("clustered", 300_000)])
+def test_full_size_tree_bit_exact_vs_oracle(tg, kind, n):
+    rng = np.random.default_rng(n)
+    if kind == "uniform":
+        x = rng.random((n, 3))
+    elif kind == "plummer":
+        u = rng.random(n)
+        r = 1 / np.sqrt(u ** (-2 / 3) - 1)
+        d = rng.normal(size=(n, 3))
+        x = d / np.linalg.norm(d, axis=1)[:, None] * r[:, None]
+    else:
+        c = rng.uniform(-10, 10, (16, 3))
+        x = c[rng.integers(0, 16, n)] + rng.normal(size=(n, 3)) * 0.05
+    m = rng.random(n) / n
+    h = rng.random(n) * 0.01
+    t = tg.ConstructTree(x, m, h, quadrupole=True)
+    ref = O.OracleTree(x, m, h, quadrupole=True)
+    assert_tree_equal(t, ref, True, kind)
+
+
+def test_duplicates_and_rekey_paths_vs_oracle(tg):
+    rng = np.random.default_rng(3)
+    base = rng.random((3000, 3))
+    x = np.vstack([base, base[:400], base[:5], 0.25 + 1e-9 * rng.random((200, 3))])
+    n = len(x)
+    m = rng.random(n) / n
+    h = np.full(n, 0.01)
+    import warnings
+
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        t = tg.ConstructTree(x, m, h, quadrupole=True)
+    ref = O.OracleTree(x, m, h, quadrupole=True)
+    assert t.HasCoincidentPoints
+    assert_tree_equal(t, ref, True, "dups")
+
+
+def test_links_reach_every_particle_once(tg):
+    """Fully opening the tree via FirstSubnode/NextBranch visits each particle exactly once."""
+    for n in (1, 2, 997, 5000):
+        x = np.random.default_rng(n).random((n, 3))
+        t = tg.ConstructTree(x, np.full(n, 1.0 / n), np.zeros(n))
+        first, nxt, npart = t.FirstSubnode, t.NextBranch, t.NumParticles
+        seen, no = [], npart
+        for _ in range(4 * t.NumNodes + 16):
+            if no <= -1:
+                break
+            if no < npart:
+                seen.append(no)
+                no = nxt[no]
+            else:
+                no = first[no]
+        assert np.array_equal(np.sort(seen), np.arange(n))
+
+
+def test_root_quadrupole_matches_analytic(tg):
+    for n in (8, 50, 500, 5000):
+        rng = np.random.default_rng(0)
+        x, m = rng.random((n, 3)), rng.random(n)
+        t = tg.ConstructTree(x, m, np.zeros(n), quadrupole=True)
+        root = t.NumParticles
+        com = t.Coordinates[root]
+        r = x - com
+        Qref = 3.0 * np.einsum("i,ik,il->kl", m, r, r) - np.eye(3) * np.sum(m * np.sum(r**2, 1))
+        assert np.max(np.abs(t.Quadrupoles[root] - Qref)) / np.max(np.abs(Qref)) < 1e-10
