@@ -10,6 +10,9 @@
 extern "C" {
 #endif
 
+/* Traversal steps (warp-wide stack pops) of the last walk on a tree (opaque tg_tree handle). */
+int64_t tg_tree_last_walk_steps(void *tree);
+
 /* Kernels this library has launched since it was loaded (all entry points, all streams). */
 int64_t tg_launch_count(void);
 

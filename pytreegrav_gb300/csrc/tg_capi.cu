@@ -314,6 +314,10 @@ tg_status tg_tree_last_walk_stats(tg_tree t, int64_t *interactions, int64_t *nod
     return TG_OK;
 }
 
+int64_t tg_tree_last_walk_steps(tg_tree t) {
+    return t ? t->last_stats.steps : 0;
+}
+
 tg_status tg_morton_order(const double *pos, int64_t n, int mem, int64_t *perm, void *stream) {
     if (!perm || (!pos && n > 0) || n < 0) return TG_ERR_BAD_ARG;
     if (n == 0) return TG_OK;

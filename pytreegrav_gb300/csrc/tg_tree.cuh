@@ -24,11 +24,13 @@ template <typename T>
 struct Arena {
     int64_t n_nodes = 0, n_leaves = 0;
     // per node
-    vec4<T> *n_pos = nullptr;  // hi.xyz, M
-    vec4<T> *n_lo = nullptr;   // lo.xyz, hmax
-    vec4<T> *n_geo = nullptr;  // size, delta, hmax, 0
-    int4 *n_link = nullptr;     // first node child (arena node index), n node children, leaf start, n leaves
-    T *n_quad = nullptr;        // (n_nodes, 6): xx xy xz yy yz zz
+    // traversal record, two per node: (hi.x, hi.y, hi.z, size), (delta, hmax, first node child << 4 |
+    // node children, leaf start << 4 | leaves) -- the integers stored as the bit pattern of T
+    vec4<T> *n_trav = nullptr;
+    vec4<T> *n_pos = nullptr;   // interaction record: hi.xyz, M
+    vec4<T> *n_lo = nullptr;    // lo.xyz, hmax
+    vec4<T> *n_quad = nullptr;  // two per node: (xx, xy, xz, yy), (yz, zz, 0, 0)
+    int4 *n_link = nullptr;     // first node child, node children, leaf start, leaves (build scratch)
     // per leaf
     vec4<T> *l_pos = nullptr;  // hi.xyz, m
     vec4<T> *l_lo = nullptr;   // lo.xyz, h
@@ -37,7 +39,7 @@ struct Arena {
 };
 
 struct WalkStats {
-    int64_t interactions = 0, node_tests = 0, max_stack = 0, groups = 0;
+    int64_t interactions = 0, node_tests = 0, max_stack = 0, groups = 0, steps = 0;
 };
 
 }  // namespace tg

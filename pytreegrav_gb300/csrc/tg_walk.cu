@@ -22,9 +22,16 @@
 namespace tg {
 
 constexpr int WALK_WARPS = 4;
-constexpr int STACK_CAP = 1536;
+constexpr int STACK_SMALL = 1024;  // per-warp node stack; a walk that overflows it is rerun with
+constexpr int STACK_LARGE = 4096;  // the large stack (fewer resident warps)
 constexpr int ILIST_CAP = 320;
 constexpr int NLIST_CAP = 64;
+
+// Integers carried in a traversal record, as the bit pattern of the record's element type.
+__device__ __forceinline__ float int_bits(int v, float) { return __int_as_float(v); }
+__device__ __forceinline__ double int_bits(int v, double) { return __longlong_as_double((long long)v); }
+__device__ __forceinline__ int bits_int(float x) { return __float_as_int(x); }
+__device__ __forceinline__ int bits_int(double x) { return (int)__double_as_longlong(x); }
 
 // ---------------------------------------------------------------------------------------------
 // Softening kernels (kernel.py:5-75) in the walk's precision.
@@ -128,16 +135,13 @@ __global__ void k_arena_fill(int64_t ntot, int64_t mtot, const int64_t *first, c
     T hm = (T)soft[f];
     ar.n_pos[j] = vec4<T>{hx, hy, hz, (T)mass[f]};
     ar.n_lo[j] = vec4<T>{lx, ly, lz, hm};
-    ar.n_geo[j] = vec4<T>{(T)size[f], (T)delta[f], hm, T(0)};
+    const int fc = lk.y > 0 ? lk.x : 0;
+    ar.n_trav[2 * j] = vec4<T>{hx, hy, hz, (T)size[f]};
+    ar.n_trav[2 * j + 1] = vec4<T>{(T)delta[f], hm, int_bits((fc << 4) | lk.y, T(0)), int_bits(((int)ls << 4) | lk.w, T(0))};
     if (ar.n_quad) {
         const double *Q = quad + 9 * j;
-        T *q = ar.n_quad + 6 * j;
-        q[0] = (T)Q[0];
-        q[1] = (T)Q[1];
-        q[2] = (T)Q[2];
-        q[3] = (T)Q[4];
-        q[4] = (T)Q[5];
-        q[5] = (T)Q[8];
+        ar.n_quad[2 * j] = vec4<T>{(T)Q[0], (T)Q[1], (T)Q[2], (T)Q[4]};
+        ar.n_quad[2 * j + 1] = vec4<T>{(T)Q[5], (T)Q[8], T(0), T(0)};
     }
     int64_t k = ls;
     const int64_t kend = ls + lk.w;
@@ -160,11 +164,15 @@ tg_status build_arena(tg_tree_s *t, Arena<T> &ar, cudaStream_t st) {
     ar.n_nodes = M;
     ar.n_leaves = N;
     ar.has_quad = t->has_quads && t->quad;
+    if (M >= (1 << 27) || N >= (1 << 27)) {  // node and leaf indices are packed with 4 count bits
+        set_last_error_msg("tree too large for the walk arena (2^27 nodes or particles)");
+        return TG_ERR_BAD_ARG;
+    }
     TG_CUDA(cudaMallocAsync((void **)&ar.n_pos, sizeof(vec4<T>) * M, st));
     TG_CUDA(cudaMallocAsync((void **)&ar.n_lo, sizeof(vec4<T>) * M, st));
-    TG_CUDA(cudaMallocAsync((void **)&ar.n_geo, sizeof(vec4<T>) * M, st));
+    TG_CUDA(cudaMallocAsync((void **)&ar.n_trav, sizeof(vec4<T>) * 2 * M, st));
     TG_CUDA(cudaMallocAsync((void **)&ar.n_link, sizeof(int4) * M, st));
-    if (ar.has_quad) TG_CUDA(cudaMallocAsync((void **)&ar.n_quad, sizeof(T) * 6 * M, st));
+    if (ar.has_quad) TG_CUDA(cudaMallocAsync((void **)&ar.n_quad, sizeof(vec4<T>) * 2 * M, st));
     TG_CUDA(cudaMallocAsync((void **)&ar.l_pos, sizeof(vec4<T>) * N, st));
     TG_CUDA(cudaMallocAsync((void **)&ar.l_lo, sizeof(vec4<T>) * N, st));
     int64_t *nleaf = nullptr, *lstart = nullptr, *ltot = nullptr;
@@ -202,7 +210,7 @@ template <typename T>
 void free_arena(Arena<T> &ar, cudaStream_t st) {
     if (ar.n_pos) cudaFreeAsync(ar.n_pos, st);
     if (ar.n_lo) cudaFreeAsync(ar.n_lo, st);
-    if (ar.n_geo) cudaFreeAsync(ar.n_geo, st);
+    if (ar.n_trav) cudaFreeAsync(ar.n_trav, st);
     if (ar.n_link) cudaFreeAsync(ar.n_link, st);
     if (ar.n_quad) cudaFreeAsync(ar.n_quad, st);
     if (ar.l_pos) cudaFreeAsync(ar.l_pos, st);
@@ -242,16 +250,15 @@ struct WalkArgs {
     unsigned long long *stats;  // interactions, node tests, max stack, groups
 };
 
-template <typename T, bool QUAD>
+template <typename T, bool QUAD, int STACK>
 struct WarpSmem {
-    int stack[STACK_CAP];
+    int stack[STACK];
     int ilist[ILIST_CAP];
     int nlist[QUAD ? NLIST_CAP : 1];
     vec4<T> spos[32];   // offsets + mass for the point-mass sweep (near sources: mass 0, far away)
     vec4<T> snear[32];  // offsets + mass of the near sources, swept with softening
     T sh[32];
-    vec4<T> sq0[QUAD ? 32 : 1];  // quadrupole xx xy xz yy
-    T sq1[QUAD ? 64 : 1];        // quadrupole yz zz
+    vec4<T> sq[QUAD ? 64 : 1];   // quadrupole records of the staged nodes
 };
 
 template <typename T>
@@ -387,17 +394,17 @@ __device__ __forceinline__ bool accept_exact(int64_t f, const double *tc, const 
     return r_min > crit;
 }
 
-template <typename T, int FIELDS, bool QUAD>
-__global__ void __launch_bounds__(WALK_WARPS * 32) k_walk(WalkArgs<T> a) {
+template <typename T, int FIELDS, bool QUAD, int STACK>
+__global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2) k_walk(WalkArgs<T> a) {
     extern __shared__ unsigned char smem_raw[];
-    WarpSmem<T, QUAD> &sm = reinterpret_cast<WarpSmem<T, QUAD> *>(smem_raw)[threadIdx.x >> 5];
+    WarpSmem<T, QUAD, STACK> &sm = reinterpret_cast<WarpSmem<T, QUAD, STACK> *>(smem_raw)[threadIdx.x >> 5];
     const int lane = lane_id();
     const unsigned lt = lanemask_lt();
     const int GS = a.gs;
     const int tl = lane % GS;     // target of this lane within the group
     const int slice = lane / GS;  // which interleaved share of each batch this lane sums
     const int NSL = 32 / GS;
-    unsigned long long n_int = 0, n_tests = 0;
+    unsigned long long n_int = 0, n_tests = 0, n_steps = 0;
     int max_sp = 0;
 
     for (;;) {
@@ -531,21 +538,17 @@ __global__ void __launch_bounds__(WALK_WARPS * 32) k_walk(WalkArgs<T> a) {
             n_int += (unsigned long long)cnt * (unsigned long long)gr.y;
         };
         auto eval_nodes = [&](const int *list, int cnt) {
-            vec4<T> st = vec4<T>{FAR, FAR, FAR, T(0)}, q0 = vec4<T>{T(0), T(0), T(0), T(0)};
-            T q4 = T(0), q5 = T(0);
+            vec4<T> st = vec4<T>{FAR, FAR, FAR, T(0)}, q0 = vec4<T>{T(0), T(0), T(0), T(0)}, q1 = q0;
             if (lane < cnt) {
                 int e = list[lane];
                 vec4<T> p = a.ar.n_pos[e], q = a.ar.n_lo[e];
+                q0 = a.ar.n_quad[2 * e];
+                q1 = a.ar.n_quad[2 * e + 1];
                 st = vec4<T>{(p.x - gcx) + q.x, (p.y - gcy) + q.y, (p.z - gcz) + q.z, p.w};
-                const T *qq = a.ar.n_quad + 6 * (int64_t)e;
-                q0 = vec4<T>{qq[0], qq[1], qq[2], qq[3]};
-                q4 = qq[4];
-                q5 = qq[5];
             }
             sm.spos[lane] = st;
-            sm.sq0[lane] = q0;
-            sm.sq1[2 * lane] = q4;
-            sm.sq1[2 * lane + 1] = q5;
+            sm.sq[2 * lane] = q0;
+            sm.sq[2 * lane + 1] = q1;
             __syncwarp();
             Acc<T> b;
 #pragma unroll
@@ -554,8 +557,8 @@ __global__ void __launch_bounds__(WALK_WARPS * 32) k_walk(WalkArgs<T> a) {
 #pragma unroll 4
             for (int i = 0; i < GS; i++) {
                 vec4<T> s = sm.spos[k0 + i];
-                vec4<T> qa = sm.sq0[k0 + i];
-                T qv[6] = {qa.x, qa.y, qa.z, qa.w, sm.sq1[2 * (k0 + i)], sm.sq1[2 * (k0 + i) + 1]};
+                vec4<T> qa = sm.sq[2 * (k0 + i)], qb = sm.sq[2 * (k0 + i) + 1];
+                T qv[6] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y};
                 T dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
                 T rinv = rsqrt_t(dx * dx + dy * dy + dz * dz);
                 point_mass<T, FIELDS>(s.w, dx, dy, dz, rinv, b);
@@ -578,23 +581,26 @@ __global__ void __launch_bounds__(WALK_WARPS * 32) k_walk(WalkArgs<T> a) {
                 break;
             }
             if (sp > 0) {
+                n_steps++;
                 const int cnt = min(sp, 32);
                 const int node = lane < cnt ? sm.stack[sp - 1 - lane] : -1;
                 sp -= cnt;
                 bool acc = false, unsure = false;
-                int4 lk = make_int4(0, 0, 0, 0);
+                vec4<T> r1 = vec4<T>{T(0), T(0), T(0), T(0)};
                 if (node >= 0) {
                     n_tests++;
-                    vec4<T> p = a.ar.n_pos[node];
-                    vec4<T> gm = a.ar.n_geo[node];
+                    const vec4<T> p = a.ar.n_trav[2 * node];
+                    r1 = a.ar.n_trav[2 * node + 1];
                     T dx = fmax(fmax(abmin[0] - p.x, p.x - abmax[0]), T(0));
                     T dy = fmax(fmax(abmin[1] - p.y, p.y - abmax[1]), T(0));
                     T dz = fmax(fmax(abmin[2] - p.z, p.z - abmax[2]), T(0));
                     T r2 = dx * dx + dy * dy + dz * dz;
-                    T h = gm.z > hmax_g ? gm.z : hmax_g;
-                    T c1 = gm.x * inv_theta + gm.y, c2 = h + T(0.6) * gm.x + gm.y;
+                    T h = r1.y > hmax_g ? r1.y : hmax_g;
+                    T c1 = p.w * inv_theta + r1.x, c2 = h + T(0.6) * p.w + r1.x;
                     T crit = c1 > c2 ? c1 : c2;
-                    T tol = rel_eps * crit + abs_eps * (gscale + fabs(p.x) + fabs(p.y) + fabs(p.z));
+                    // FP32 error bound: node positions near the boundary are within gscale + 2 crit of
+                    // the origin, so the relative term covers their rounding
+                    T tol = rel_eps * crit + abs_eps * gscale;
                     T hiq = crit + tol, loq = crit - tol;
                     if (sizeof(T) == 8) unsure = true;
                     else if (r2 > hiq * hiq) acc = true;
@@ -607,7 +613,7 @@ __global__ void __launch_bounds__(WALK_WARPS * 32) k_walk(WalkArgs<T> a) {
                         acc = accept_exact(a.ntot + node, a.tc, a.ts, a.tsize, a.tdelta, bmin, bmax, hmax_d, theta);
                 }
                 const bool opn = node >= 0 && !acc;
-                if (opn) lk = a.ar.n_link[node];
+                const int cbits = opn ? bits_int(r1.z) : 0, lbits = opn ? bits_int(r1.w) : 0;
                 const unsigned am = __ballot_sync(FULL, acc);
                 if (QUAD) {
                     if (acc) sm.nlist[nn + __popc(am & lt)] = node;
@@ -616,15 +622,18 @@ __global__ void __launch_bounds__(WALK_WARPS * 32) k_walk(WalkArgs<T> a) {
                     if (acc) sm.ilist[ni + __popc(am & lt)] = node;
                     ni += __popc(am);
                 }
-                const int nc = lk.y, nl = lk.w;
-                const int sc = warp_inclusive_scan(nc), sl = warp_inclusive_scan(nl);
-                const int totc = __shfl_sync(FULL, sc, 31), totl = __shfl_sync(FULL, sl, 31);
-                if (sp + totc > STACK_CAP) {
+                const int nc = cbits & 15, nl = lbits & 15;
+                const int both = warp_inclusive_scan(nc | (nl << 16));  // both counts in one scan
+                const int sc = both & 0xffff, sl = both >> 16;
+                const int tot = __shfl_sync(FULL, both, 31);
+                const int totc = tot & 0xffff, totl = tot >> 16;
+                if (sp + totc > STACK) {
                     overflow = true;
                     break;
                 }
-                for (int j = 0, o = sp + sc - nc; j < nc; j++) sm.stack[o + j] = lk.x + j;
-                for (int j = 0, o = ni + sl - nl; j < nl; j++) sm.ilist[o + j] = ~(lk.z + j);
+                const int fc = cbits >> 4, ls = lbits >> 4;
+                for (int j = 0, o = sp + sc - nc; j < nc; j++) sm.stack[o + j] = fc + j;
+                for (int j = 0, o = ni + sl - nl; j < nl; j++) sm.ilist[o + j] = ~(ls + j);
                 sp += totc;
                 ni += totl;
                 max_sp = max(max_sp, sp);
@@ -685,6 +694,7 @@ __global__ void __launch_bounds__(WALK_WARPS * 32) k_walk(WalkArgs<T> a) {
     if (lane == 0 && a.stats) {
         atomicAdd(a.stats + 0, n_int);
         atomicMax(a.stats + 2, (unsigned long long)max_sp);
+        atomicAdd(a.stats + 3, n_steps);
     }
     unsigned long long tests = n_tests;
     for (int o = 16; o; o >>= 1) tests += __shfl_xor_sync(FULL, tests, o);
@@ -858,10 +868,10 @@ __global__ void k_prep_targets(const double *tpos, const double *th, int64_t n, 
     tlo[i] = vec4<T>{lx, ly, lz, T(0)};
 }
 
-template <typename T, int FIELDS, bool QUAD>
+template <typename T, int FIELDS, bool QUAD, int STACK>
 static tg_status launch_walk(WalkArgs<T> &a, cudaStream_t st) {
-    size_t smem = sizeof(WarpSmem<T, QUAD>) * WALK_WARPS;
-    auto kern = k_walk<T, FIELDS, QUAD>;
+    size_t smem = sizeof(WarpSmem<T, QUAD, STACK>) * WALK_WARPS;
+    auto kern = k_walk<T, FIELDS, QUAD, STACK>;
     TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     TG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WALK_WARPS * 32, smem));
@@ -875,25 +885,44 @@ static tg_status launch_walk(WalkArgs<T> &a, cudaStream_t st) {
     return TG_OK;
 }
 
-template <typename T>
+template <typename T, int STACK>
 static tg_status dispatch_walk(WalkArgs<T> &a, int fields, bool quad, cudaStream_t st) {
     // Fields computed: potential and/or acceleration alone, or everything when the tidal tensor is
     // wanted (its setup already contains the other two).
     int fc = (fields & F_TID) ? (F_POT | F_ACC | F_TID) : fields;
     if (quad) {
         switch (fc) {
-            case F_POT: return launch_walk<T, F_POT, true>(a, st);
-            case F_ACC: return launch_walk<T, F_ACC, true>(a, st);
-            case F_POT | F_ACC: return launch_walk<T, F_POT | F_ACC, true>(a, st);
-            default: return launch_walk<T, F_POT | F_ACC | F_TID, true>(a, st);
+            case F_POT: return launch_walk<T, F_POT, true, STACK>(a, st);
+            case F_ACC: return launch_walk<T, F_ACC, true, STACK>(a, st);
+            case F_POT | F_ACC: return launch_walk<T, F_POT | F_ACC, true, STACK>(a, st);
+            default: return launch_walk<T, F_POT | F_ACC | F_TID, true, STACK>(a, st);
         }
     }
     switch (fc) {
-        case F_POT: return launch_walk<T, F_POT, false>(a, st);
-        case F_ACC: return launch_walk<T, F_ACC, false>(a, st);
-        case F_POT | F_ACC: return launch_walk<T, F_POT | F_ACC, false>(a, st);
-        default: return launch_walk<T, F_POT | F_ACC | F_TID, false>(a, st);
+        case F_POT: return launch_walk<T, F_POT, false, STACK>(a, st);
+        case F_ACC: return launch_walk<T, F_ACC, false, STACK>(a, st);
+        case F_POT | F_ACC: return launch_walk<T, F_POT | F_ACC, false, STACK>(a, st);
+        default: return launch_walk<T, F_POT | F_ACC | F_TID, false, STACK>(a, st);
     }
+}
+
+// Run the walk with the small stack; if any group overflowed it, rerun everything with the large one.
+template <typename T>
+static tg_status walk_with_fallback(WalkArgs<T> &a, int fields, bool quad, int *scratch, cudaStream_t st,
+                                    int *status_out) {
+    TG_TRY((dispatch_walk<T, STACK_SMALL>(a, fields, quad, st)));
+    int status = 0;
+    TG_CUDA(cudaMemcpyAsync(&status, scratch + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TG_CUDA(cudaStreamSynchronize(st));
+    if (status & (1 << TG_ERR_STACK_OVERFLOW)) {
+        TG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int) * 2, st));
+        if (a.stats) TG_CUDA(cudaMemsetAsync(a.stats, 0, sizeof(unsigned long long) * 4, st));
+        TG_TRY((dispatch_walk<T, STACK_LARGE>(a, fields, quad, st)));
+        TG_CUDA(cudaMemcpyAsync(&status, scratch + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        TG_CUDA(cudaStreamSynchronize(st));
+    }
+    *status_out = status;
+    return TG_OK;
 }
 
 // Walk targets already in walk order (tpos/th on the device). groups/group_root describe the
@@ -909,6 +938,7 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
     TG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int) * 2, st));
     TG_CUDA(cudaMemsetAsync(t->stats_dev, 0, sizeof(unsigned long long) * 4, st));
     tg_status rc = TG_OK;
+    int status = 0;
     if (precision == TG_FP64) {
         TG_TRY(build_arena(t, t->arena64, st));
         WalkArgs<double> a;
@@ -926,7 +956,7 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         { k_prep_targets<double><<<div_up(ntargets, 256), 256, 0, st>>>(tpos, th, ntargets, thi, tlo); tg::note_launch(); }
         a.thi = thi;
         a.tlo = tlo;
-        rc = dispatch_walk<double>(a, fields, quadrupole != 0, st);
+        rc = walk_with_fallback<double>(a, fields, quadrupole != 0, scratch, st, &status);
         cudaFreeAsync(thi, st);
         cudaFreeAsync(tlo, st);
     } else {
@@ -946,13 +976,11 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         { k_prep_targets<float><<<div_up(ntargets, 256), 256, 0, st>>>(tpos, th, ntargets, thi, tlo); tg::note_launch(); }
         a.thi = thi;
         a.tlo = tlo;
-        rc = dispatch_walk<float>(a, fields, quadrupole != 0, st);
+        rc = walk_with_fallback<float>(a, fields, quadrupole != 0, scratch, st, &status);
         cudaFreeAsync(thi, st);
         cudaFreeAsync(tlo, st);
     }
     if (rc != TG_OK) return rc;
-    int status = 0;
-    TG_CUDA(cudaMemcpyAsync(&status, scratch + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
     unsigned long long stats[4];
     TG_CUDA(cudaMemcpyAsync(stats, t->stats_dev, sizeof(stats), cudaMemcpyDeviceToHost, st));
     TG_CUDA(cudaFreeAsync(scratch, st));
@@ -961,6 +989,7 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
     t->last_stats.node_tests = (int64_t)stats[1];
     t->last_stats.max_stack = (int64_t)stats[2];
     t->last_stats.groups = ngroups;
+    t->last_stats.steps = (int64_t)stats[3];
     if (status & (1 << TG_ERR_STACK_OVERFLOW)) return TG_ERR_STACK_OVERFLOW;
     if (status & (1 << TG_ERR_ITER_LIMIT)) return TG_ERR_ITER_LIMIT;
     return TG_OK;
