@@ -1,0 +1,343 @@
+"""Benchmark: Accel particles/s on a 1e6-particle Plummer sphere (GB300).
+
+One step = build the octree of 1e6 Plummer particles (a=1, r<50, m=1/N, h=0.005, quadrupoles) on
+the GPU and evaluate the acceleration of every particle with the FP32 grouped walk at theta=0.7,
+inputs resident in HBM. Prints one JSON line (rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm on the host cores (the C restatement under oracle/,
+all threads): pytreegrav's own implementation is numba-compiled Python and numba is absent here.
+Multi-GPU runs are independent replicas (one system per rank, no collective in the data path).
+"""
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Accel particles/s, 1e6 Plummer: learned-θ vs plain walk at same RMS force error"
+UNIT = "particles/s"
+N_DEFAULT = 1_000_000
+THETA = 0.7
+SOFT = 0.005
+GROUP = 32
+SEED = 20261203
+
+# FP32 flops per interaction, counted from the walk kernel's arithmetic with add/sub/mul = 1,
+# FMA = 2, rsqrt = 1 (pytreegrav_gb300/csrc/tg_walk.cu, point_mass and quad_terms):
+#   monopole acceleration: 3 sub + r^2 (1 mul + 2 fma) + rsqrt + rinv^2, m*rinv, *rinv^2 (3 mul)
+#   + 3 fma = 18; quadrupole node, acceleration: +38 (Q.dx 15, A 5, r^-5 and r^-7 4, 2.5*A*r^-7 2,
+#   three components of qf*dx - qdx*r^-5 accumulated, 12).
+FLOPS_MONO_ACC = 18
+FLOPS_QUAD_ACC = 18 + 38
+
+
+def plummer(n, seed):
+    """Plummer sphere, a=1, truncated at r<50, isotropic directions (seeded)."""
+    rng = np.random.default_rng(seed)
+    out = np.empty((0, 3))
+    while len(out) < n:
+        k = n - len(out)
+        u = rng.random(k)
+        r = 1.0 / np.sqrt(u ** (-2.0 / 3.0) - 1.0)
+        d = rng.normal(size=(k, 3))
+        p = d / np.linalg.norm(d, axis=1)[:, None] * r[:, None]
+        out = np.vstack([out, p[r < 50]])
+    return np.ascontiguousarray(out[:n])
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (SM clock, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"tg_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def read_traffic():
+    """DRAM bytes per walk launch from the committed ncu summary (profiles/), or None."""
+    path = os.path.join(ROOT, "profiles", "walk_plummer1e6.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return int(float(line.split(":", 1)[1].strip().split()[0]))
+            except ValueError:
+                return None
+    return None
+
+
+def _bind(L):
+    i64, dbl, vp = ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
+    L.tg_launch_count.restype = i64
+    L.tg_launch_count.argtypes = []
+    L.tg_measure_fp32_fma.argtypes = [ctypes.POINTER(dbl), ctypes.POINTER(dbl), vp]
+    L.tg_tree_last_walk_kernel_ms.restype = dbl
+    L.tg_tree_last_walk_kernel_ms.argtypes = [vp]
+    L.tg_tree_last_walk_quad_interactions.restype = i64
+    L.tg_tree_last_walk_quad_interactions.argtypes = [vp]
+    return L
+
+
+def gpu_step(L, _lib, dpos, dm, dh, out, n, stream):
+    """One step on device-resident arrays: build + FP32 quadrupole Accel walk (tree grouping)."""
+    vp = ctypes.c_void_p
+    h = vp()
+    rc = L.tg_tree_build(vp(dpos.data_ptr()), vp(dm.data_ptr()), vp(dh.data_ptr()), n, 1, 1, _lib.TG_MEM_DEVICE,
+                         vp(stream), ctypes.byref(h))
+    _lib.check(rc, "build")
+    rc = L.tg_tree_fields(h, None, None, n, _lib.TG_FIELD_ACCEL, 1, THETA, 1.0, GROUP, _lib.TG_GROUP_TREE,
+                          _lib.TG_ORDER_TREE, _lib.TG_FP32, None, _lib.TG_MEM_DEVICE, vp(out.data_ptr()), vp(stream))
+    _lib.check(rc, "walk")
+    v = [ctypes.c_int64() for _ in range(4)]
+    L.tg_tree_last_walk_stats(h, *[ctypes.byref(x) for x in v])
+    st = {"interactions": v[0].value, "node_tests": v[1].value, "groups": v[3].value,
+          "quad_interactions": L.tg_tree_last_walk_quad_interactions(h),
+          "kernel_ms": L.tg_tree_last_walk_kernel_ms(h)}
+    L.tg_tree_free(h)
+    return st
+
+
+def cpu_baseline(x, m, h, nthreads):
+    """The reference algorithm on the host cores (oracle/, FP64, pytreegrav's grouping of 8): a full
+    tree build plus the walk of every 4th group of 8 targets, extrapolated to all targets."""
+    from oracle import oracle as O
+
+    n = len(x)
+    t0 = time.perf_counter()
+    t = O.OracleTree(x, m, h, quadrupole=True)
+    t1 = time.perf_counter()
+    idx = t.TreewalkIndices
+    starts = np.arange(0, n, 32, dtype=np.int64)
+    counts = np.minimum(8, n - starts)
+    O.fields_groups(t, x[idx], h[idx], starts, counts, accel=True, quadrupole=True, theta=THETA,
+                    nthreads=nthreads)
+    t2 = time.perf_counter()
+    sampled = int(counts.sum())
+    step = (t1 - t0) + (t2 - t1) * n / sampled
+    return {"value": n / step, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"full build of N={n} + FP64 grouped walk (group_size=8, theta={THETA}, quadrupole) of "
+                      f"every 4th group ({sampled} targets), extrapolated; {step:.2f} s per step"}
+
+
+def run_ours(args):
+    import torch
+
+    from pytreegrav_gb300 import _lib
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    L = _bind(_lib.load())
+    stream = torch.cuda.current_stream().cuda_stream
+    n = args.n
+    x = plummer(n, SEED + rank)  # one independent replica per rank
+    m = np.full(n, 1.0 / n)
+    h = np.full(n, SOFT)
+    dpos = torch.from_numpy(x).cuda()
+    dm = torch.from_numpy(m).cuda()
+    dh = torch.from_numpy(h).cuda()
+    out = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2 (129 MB)
+
+    for _ in range(args.warmup):
+        gpu_step(L, _lib, dpos, dm, dh, out, n, stream)
+    torch.cuda.synchronize()
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stats = []
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = L.tg_launch_count()
+    t_region = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()  # evict the previous step's data from L2 (outside the step events)
+        ev[k][0].record()
+        stats.append(gpu_step(L, _lib, dpos, dm, dh, out, n, stream))
+        ev[k][1].record()
+    torch.cuda.synchronize()
+    t_region = time.perf_counter() - t_region
+    if dist:
+        dist.barrier()
+    launches = L.tg_launch_count() - launches0
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = statistics.mean(step_ms)
+    if dist:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = n * ws / (ms * 1e-3)
+    if rank != 0:
+        return None
+
+    # accuracy of the timed configuration against FP64 direct summation on 1e4 sampled targets
+    import pytreegrav_gb300 as tg
+
+    acc = out.cpu().numpy()
+    rng = np.random.default_rng(7)
+    samp = rng.choice(n, 10_000, replace=False)
+    ref = tg.bruteforce(x[samp], h[samp], x, m, h, accel=True, precision="fp64")["accel"]
+    err = acc[samp] - ref
+    rms_err = float(np.sqrt(np.mean(np.sum(err**2, 1))) / np.sqrt(np.mean(np.sum(ref**2, 1))))
+    max_err = float(np.max(np.sqrt(np.sum(err**2, 1))) / np.sqrt(np.mean(np.sum(ref**2, 1))))
+
+    # roofline of the dominant kernel (the walk): algorithmic FP32 flops / its own device time
+    st = stats[-1]
+    walk_ms = statistics.mean(s["kernel_ms"] for s in stats)
+    flops = FLOPS_MONO_ACC * (st["interactions"] - st["quad_interactions"]) + FLOPS_QUAD_ACC * st["quad_interactions"]
+    peak_tf, peak_ms = ctypes.c_double(), ctypes.c_double()
+    L.tg_measure_fp32_fma(ctypes.byref(peak_tf), ctypes.byref(peak_ms), ctypes.c_void_p(stream))
+    achieved = flops / (walk_ms * 1e-3) / 1e12
+    roofline = {"bound": "fp32", "achieved": round(achieved, 3), "peak": round(peak_tf.value, 3), "unit": "TFLOP/s",
+                "frac": round(achieved / peak_tf.value, 4), "traffic": read_traffic(), "kernel": "k_walk",
+                "peak_source": "measured: FFMA-chain probe on this GPU (tg_measure_fp32_fma); MEASURED_PEAKS.json "
+                               "has no FP32 CUDA-core figure",
+                "kernel_ms": round(walk_ms, 4), "flops_per_launch": flops,
+                "interactions_per_s": round(st["interactions"] / (walk_ms * 1e-3), 1)}
+
+    # end to end through the public API, inputs in pinned host memory, result read back
+    pin_x = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
+    pin_m = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    pin_h = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    pin_x.numpy()[:] = x
+    pin_m.numpy()[:] = m
+    pin_h.numpy()[:] = h
+    kw = dict(theta=THETA, method="tree", quadrupole=True, group_size=GROUP, grouping="tree")
+    for _ in range(2):
+        tg.Accel(pin_x.numpy(), pin_m.numpy(), pin_h.numpy(), **kw)
+    e2e_t = []
+    for _ in range(max(3, min(args.steps, 10))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        a = tg.Accel(pin_x.numpy(), pin_m.numpy(), pin_h.numpy(), **kw)
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e = {"value": n / statistics.median(e2e_t), "unit": UNIT, "h2d_bytes_per_step": int(x.nbytes + m.nbytes + h.nbytes),
+           "d2h_bytes_per_step": int(a.nbytes), "api": "pytreegrav_gb300.Accel(pos, m, h, theta=0.7, quadrupole=True, "
+           "method='tree', group_size=32, grouping='tree')", "ms_per_step": round(1e3 * statistics.median(e2e_t), 3)}
+
+    base = cpu_baseline(x, m, h, os.cpu_count() or 1)
+    return {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Plummer sphere, a=1, r<50)",
+        "config": {"workload": f"Accel, N={n} Plummer (m=1/N, h={SOFT}), theta={THETA}, quadrupole, FP32 walk with FP64 "
+                               f"tree build and moments, tree grouping <= {GROUP} targets/warp",
+                   "variant": "plain global-theta walk (the learned-theta walk is not built yet)",
+                   "step": "octree build + Accel walk, inputs resident in HBM",
+                   "l2": "flushed between timed steps (256 MiB write, outside the step events)",
+                   "parallelism": f"replicas x{ws}", "region_s": round(t_region, 4)},
+        "accuracy": {"rms_rel_vs_fp64_bruteforce": rms_err, "max_rel_vs_fp64_bruteforce": max_err,
+                     "sample_targets": 10_000},
+        "walk": {"interactions_per_target": st["interactions"] / n, "node_tests": st["node_tests"],
+                 "groups": st["groups"], "quad_interactions": st["quad_interactions"]},
+        "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+    }
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return None
+    n = args.n
+    x = plummer(n, SEED)
+    m = np.full(n, 1.0 / n)
+    h = np.full(n, SOFT)
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_baseline(x, m, h, cores)
+    vals = [cpu_baseline(x, m, h, cores) for _ in range(args.steps)]
+    value = statistics.mean(v["value"] for v in vals)
+    base = dict(vals[-1])
+    base["value"] = value
+    return {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1e3 * n / value, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Plummer sphere, a=1, r<50)",
+            "impl": "reference",
+            "config": {"workload": f"Accel, N={n} Plummer (m=1/N, h={SOFT}), theta={THETA}, quadrupole",
+                       "implementation": "C restatement of pytreegrav's radix build and grouped walk (oracle/), "
+                                         "all host threads; pytreegrav itself needs numba, absent on this machine"},
+            "cpu_baseline": base, "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0,
+                                          "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    res = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -13,6 +13,12 @@ extern "C" {
 /* Traversal steps (warp-wide stack pops) of the last walk on a tree (opaque tg_tree handle). */
 int64_t tg_tree_last_walk_steps(void *tree);
 
+/* Quadrupole node interactions (target-node pairs) of the last walk on a tree. */
+int64_t tg_tree_last_walk_quad_interactions(void *tree);
+
+/* Device time of the last walk's kernel launch on a tree (CUDA events on the launching stream). */
+double tg_tree_last_walk_kernel_ms(void *tree);
+
 /* Kernels this library has launched since it was loaded (all entry points, all streams). */
 int64_t tg_launch_count(void);
 

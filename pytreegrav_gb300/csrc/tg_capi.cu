@@ -318,6 +318,14 @@ int64_t tg_tree_last_walk_steps(tg_tree t) {
     return t ? t->last_stats.steps : 0;
 }
 
+int64_t tg_tree_last_walk_quad_interactions(tg_tree t) {
+    return t ? t->last_stats.quad_interactions : 0;
+}
+
+double tg_tree_last_walk_kernel_ms(tg_tree t) {
+    return t ? (double)t->last_stats.kernel_ms : 0.0;
+}
+
 tg_status tg_morton_order(const double *pos, int64_t n, int mem, int64_t *perm, void *stream) {
     if (!perm || (!pos && n > 0) || n < 0) return TG_ERR_BAD_ARG;
     if (n == 0) return TG_OK;

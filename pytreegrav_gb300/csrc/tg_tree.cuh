@@ -39,7 +39,8 @@ struct Arena {
 };
 
 struct WalkStats {
-    int64_t interactions = 0, node_tests = 0, max_stack = 0, groups = 0, steps = 0;
+    int64_t interactions = 0, node_tests = 0, max_stack = 0, groups = 0, steps = 0, quad_interactions = 0;
+    float kernel_ms = 0.f;  // device time of the walk kernel launch(es)
 };
 
 }  // namespace tg
@@ -73,5 +74,5 @@ struct tg_tree_s {
     tg::Arena<float> arena32;
     tg::Arena<double> arena64;
     tg::WalkStats last_stats;
-    int64_t *stats_dev = nullptr;  // 4 counters
+    int64_t *stats_dev = nullptr;  // 8 counters
 };

@@ -247,7 +247,7 @@ struct WalkArgs {
     int gs;  // group size (targets per group, divides 32)
     int *queue;
     int *status;
-    unsigned long long *stats;  // interactions, node tests, max stack, groups
+    unsigned long long *stats;  // interactions, node tests, max stack, steps, quadrupole-node interactions
 };
 
 template <typename T, bool QUAD, int STACK>
@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2)
     const int tl = lane % GS;     // target of this lane within the group
     const int slice = lane / GS;  // which interleaved share of each batch this lane sums
     const int NSL = 32 / GS;
-    unsigned long long n_int = 0, n_tests = 0, n_steps = 0;
+    unsigned long long n_int = 0, n_tests = 0, n_steps = 0, n_qint = 0;
     int max_sp = 0;
 
     for (;;) {
@@ -567,6 +567,7 @@ __global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2)
             __syncwarp();
             kahan_add<T, FIELDS>(S, C, b);
             n_int += (unsigned long long)cnt * (unsigned long long)gr.y;
+            n_qint += (unsigned long long)cnt * (unsigned long long)gr.y;
         };
 
         int sp = 1, ni = 0, nn = 0;
@@ -695,6 +696,7 @@ __global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2)
         atomicAdd(a.stats + 0, n_int);
         atomicMax(a.stats + 2, (unsigned long long)max_sp);
         atomicAdd(a.stats + 3, n_steps);
+        atomicAdd(a.stats + 4, n_qint);
     }
     unsigned long long tests = n_tests;
     for (int o = 16; o; o >>= 1) tests += __shfl_xor_sync(FULL, tests, o);
@@ -909,18 +911,28 @@ static tg_status dispatch_walk(WalkArgs<T> &a, int fields, bool quad, cudaStream
 // Run the walk with the small stack; if any group overflowed it, rerun everything with the large one.
 template <typename T>
 static tg_status walk_with_fallback(WalkArgs<T> &a, int fields, bool quad, int *scratch, cudaStream_t st,
-                                    int *status_out) {
+                                    int *status_out, float *kernel_ms) {
+    cudaEvent_t e0, e1;
+    TG_CUDA(cudaEventCreate(&e0));
+    TG_CUDA(cudaEventCreate(&e1));
+    TG_CUDA(cudaEventRecord(e0, st));
     TG_TRY((dispatch_walk<T, STACK_SMALL>(a, fields, quad, st)));
+    TG_CUDA(cudaEventRecord(e1, st));
     int status = 0;
     TG_CUDA(cudaMemcpyAsync(&status, scratch + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
     TG_CUDA(cudaStreamSynchronize(st));
     if (status & (1 << TG_ERR_STACK_OVERFLOW)) {
         TG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int) * 2, st));
-        if (a.stats) TG_CUDA(cudaMemsetAsync(a.stats, 0, sizeof(unsigned long long) * 4, st));
+        if (a.stats) TG_CUDA(cudaMemsetAsync(a.stats, 0, sizeof(unsigned long long) * 8, st));
+        TG_CUDA(cudaEventRecord(e0, st));
         TG_TRY((dispatch_walk<T, STACK_LARGE>(a, fields, quad, st)));
+        TG_CUDA(cudaEventRecord(e1, st));
         TG_CUDA(cudaMemcpyAsync(&status, scratch + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
         TG_CUDA(cudaStreamSynchronize(st));
     }
+    TG_CUDA(cudaEventElapsedTime(kernel_ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
     *status_out = status;
     return TG_OK;
 }
@@ -932,13 +944,14 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
                    int quadrupole, double theta, double G, int group_size, int precision, const float *theta_group,
                    double *out, cudaStream_t st) {
     int w = ((fields & F_POT) ? 1 : 0) + ((fields & F_ACC) ? 3 : 0) + ((fields & F_TID) ? 9 : 0);
-    if (!t->stats_dev) TG_CUDA(cudaMalloc((void **)&t->stats_dev, sizeof(unsigned long long) * 4));
+    if (!t->stats_dev) TG_CUDA(cudaMalloc((void **)&t->stats_dev, sizeof(unsigned long long) * 8));
     int *scratch = nullptr;
     TG_CUDA(cudaMallocAsync((void **)&scratch, sizeof(int) * 2, st));
     TG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int) * 2, st));
-    TG_CUDA(cudaMemsetAsync(t->stats_dev, 0, sizeof(unsigned long long) * 4, st));
+    TG_CUDA(cudaMemsetAsync(t->stats_dev, 0, sizeof(unsigned long long) * 8, st));
     tg_status rc = TG_OK;
     int status = 0;
+    float kms = 0.f;
     if (precision == TG_FP64) {
         TG_TRY(build_arena(t, t->arena64, st));
         WalkArgs<double> a;
@@ -956,7 +969,7 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         { k_prep_targets<double><<<div_up(ntargets, 256), 256, 0, st>>>(tpos, th, ntargets, thi, tlo); tg::note_launch(); }
         a.thi = thi;
         a.tlo = tlo;
-        rc = walk_with_fallback<double>(a, fields, quadrupole != 0, scratch, st, &status);
+        rc = walk_with_fallback<double>(a, fields, quadrupole != 0, scratch, st, &status, &kms);
         cudaFreeAsync(thi, st);
         cudaFreeAsync(tlo, st);
     } else {
@@ -976,12 +989,12 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         { k_prep_targets<float><<<div_up(ntargets, 256), 256, 0, st>>>(tpos, th, ntargets, thi, tlo); tg::note_launch(); }
         a.thi = thi;
         a.tlo = tlo;
-        rc = walk_with_fallback<float>(a, fields, quadrupole != 0, scratch, st, &status);
+        rc = walk_with_fallback<float>(a, fields, quadrupole != 0, scratch, st, &status, &kms);
         cudaFreeAsync(thi, st);
         cudaFreeAsync(tlo, st);
     }
     if (rc != TG_OK) return rc;
-    unsigned long long stats[4];
+    unsigned long long stats[8];
     TG_CUDA(cudaMemcpyAsync(stats, t->stats_dev, sizeof(stats), cudaMemcpyDeviceToHost, st));
     TG_CUDA(cudaFreeAsync(scratch, st));
     TG_CUDA(cudaStreamSynchronize(st));
@@ -990,6 +1003,8 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
     t->last_stats.max_stack = (int64_t)stats[2];
     t->last_stats.groups = ngroups;
     t->last_stats.steps = (int64_t)stats[3];
+    t->last_stats.quad_interactions = (int64_t)stats[4];
+    t->last_stats.kernel_ms = kms;
     if (status & (1 << TG_ERR_STACK_OVERFLOW)) return TG_ERR_STACK_OVERFLOW;
     if (status & (1 << TG_ERR_ITER_LIMIT)) return TG_ERR_ITER_LIMIT;
     return TG_OK;

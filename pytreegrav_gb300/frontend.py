@@ -11,6 +11,11 @@ Differences a caller can see, all deliberate:
     tree (keys, topology, moments) is bit-identical to pytreegrav's and the accepted node set is
     pytreegrav's exactly. Brute force defaults to FP64 (bit-identical sums) for device="cpu" and
     FP32 for device="cuda", matching what each device meant in pytreegrav.
+  * ``grouping`` (keyword, extension): "blocks" (default) groups ``group_size`` consecutive
+    Morton-ordered targets per traversal, pytreegrav's grouping, so the accepted node set is
+    pytreegrav's exactly; "tree" takes groups of at most ``group_size`` particles from the tree
+    itself (self-gravity with a freshly built tree only), which never straddle a jump of the Morton
+    curve and is the engine's fast path.
   * ``morton_order=False``/``radix=False`` in ConstructTree still build the radix tree (pytreegrav
     documents both builds as giving identical fields on generic data); ``vel`` (the velocity tree
     used only by the correlation functions) is not provided.
@@ -103,7 +108,7 @@ def ConstructTree(pos, m=None, softening=None, quadrupole=False, vel=None, compu
 
 
 def _self_field(key, pos, m, softening, G, theta, tree, return_tree, method, quadrupole, group_size, device,
-                precision, parallel_threshold):
+                precision, parallel_threshold, grouping="blocks"):
     valueTestMethod(method)
     pos = np.atleast_2d(_f64(pos))
     m = np.atleast_1d(_f64(m))
@@ -125,7 +130,7 @@ def _self_field(key, pos, m, softening, G, theta, tree, return_tree, method, qua
             checkTreeQuadrupoles(tree, quadrupole)
             res = tree.fields(potential=key == "potential", accel=key == "accel", tidal=key == "tidal",
                               quadrupole=quadrupole, group_size=group_size, theta=theta, G=G, order="tree",
-                              precision=precision)[key]
+                              precision=precision, grouping=grouping)[key]
         else:
             _check_tree(tree)
             checkTreeQuadrupoles(tree, quadrupole)
@@ -177,24 +182,25 @@ def _target_field(key, pos_target, pos_source, m_source, softening_target, softe
 
 
 def Potential(pos, m, softening=None, G=1.0, theta=0.7, tree=None, return_tree=False, parallel=False,
-              method="adaptive", quadrupole=False, group_size=8, device="cpu", *, precision="fp32"):
+              method="adaptive", quadrupole=False, group_size=8, device="cpu", *, precision="fp32",
+              grouping="blocks"):
     """Gravitational potential of N particles at their own positions (frontend.py:145-293)."""
     return _self_field("potential", pos, m, softening, G, theta, tree, return_tree, method, quadrupole, group_size,
-                       device, precision, 4000 if parallel else 1000)
+                       device, precision, 4000 if parallel else 1000, grouping)
 
 
 def Accel(pos, m, softening=None, G=1.0, theta=0.7, tree=None, return_tree=False, parallel=False,
-          method="adaptive", quadrupole=False, group_size=8, device="cpu", *, precision="fp32"):
+          method="adaptive", quadrupole=False, group_size=8, device="cpu", *, precision="fp32", grouping="blocks"):
     """Gravitational acceleration of N particles at their own positions (frontend.py:421-560)."""
     return _self_field("accel", pos, m, softening, G, theta, tree, return_tree, method, quadrupole, group_size,
-                       device, precision, 4000 if parallel else 1000)
+                       device, precision, 4000 if parallel else 1000, grouping)
 
 
 def TidalTensor(pos, m, softening=None, G=1.0, theta=0.7, tree=None, return_tree=False, parallel=False,
-                method="adaptive", quadrupole=False, group_size=8, *, precision="fp32"):
+                method="adaptive", quadrupole=False, group_size=8, *, precision="fp32", grouping="blocks"):
     """Tidal tensor T_ij = dg_i/dx_j at the particle positions (frontend.py:688-789)."""
     return _self_field("tidal", pos, m, softening, G, theta, tree, return_tree, method, quadrupole, group_size,
-                       None, precision, 4000 if parallel else 1000)
+                       None, precision, 4000 if parallel else 1000, grouping)
 
 
 def PotentialTarget(pos_target, pos_source, m_source, softening_target=None, softening_source=None, G=1.0,
@@ -226,7 +232,7 @@ class Field:
     potential/accel/tidal from a single traversal (frontend.py:904-1044)."""
 
     def __init__(self, pos, m, softening=None, G=1.0, theta=0.7, quadrupole=False, group_size=8, parallel=False, *,
-                 precision="fp32"):
+                 precision="fp32", grouping="blocks"):
         pos = np.atleast_2d(_f64(pos))
         m = np.atleast_1d(_f64(m))
         if softening is None:
@@ -238,6 +244,7 @@ class Field:
         self.group_size = group_size
         self.parallel = parallel
         self.precision = precision
+        self.grouping = grouping
         self.tree = ConstructTree(pos, m, softening, quadrupole=quadrupole)
 
     def __repr__(self):
@@ -255,7 +262,7 @@ class Field:
         kw = dict(potential=potential, accel=accel, tidal=tidal, quadrupole=self.quadrupole, group_size=group_size,
                   theta=theta, G=self.G, precision=precision)
         if pos_target is None:
-            return self.tree.fields(order="tree", **kw)
+            return self.tree.fields(order="tree", grouping=self.grouping, **kw)
         pos_target = np.atleast_2d(_f64(pos_target))
         if softening_target is None:
             softening_target = zeros(len(pos_target))
