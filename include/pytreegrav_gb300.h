@@ -121,6 +121,19 @@ tg_status tg_tree_last_walk_stats(tg_tree tree, int64_t *interactions, int64_t *
  * Morton keys in their own bounding cube. perm: int64 (n,). */
 tg_status tg_morton_order(const double *pos, int64_t n, int mem, int64_t *perm, void *stream);
 
+/* No counterpart in the reference: tg_morton_order for callers that cannot allocate device memory
+ * (a host that owns every device allocation through its own pool, or a latency-critical path that
+ * must not enter an allocator). pos (n x 3 doubles) and perm (n int64) are device pointers on the
+ * current device; every temporary lives in one fixed scratch array of TG_NOALLOC_SCRATCH_BYTES that
+ * the library holds on each GPU that loads it, until exit. n above TG_NOALLOC_MAX_POINTS returns
+ * TG_ERR_BAD_ARG. All calls on a device share that array: calls whose GPU work overlaps race, so
+ * order them (e.g. one stream). The first call on a device looks the array up; make it before
+ * any stream capture on that device. Returns when perm is written (the stream is synchronised).
+ * The result equals tg_morton_order's. */
+#define TG_NOALLOC_MAX_POINTS 262144
+#define TG_NOALLOC_SCRATCH_BYTES 6358528
+tg_status tg_morton_order_noalloc(const double *pos, int64_t n, int64_t *perm, void *stream);
+
 /* Brute force (bruteforce.py). mutual = 1: targets are the sources, self excluded by index
  * (Potential/Accel/TidalTensor_bruteforce_parallel, bruteforce.py:86-116, 164-206, 319-350);
  * mutual = 0: target form, r == 0 pairs skipped (bruteforce.py:7-50, 209-256, 353-386; pos_t/h_t

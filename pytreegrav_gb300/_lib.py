@@ -35,6 +35,7 @@ TG_ORDER_MORTON = 1
 TG_ORDER_GIVEN = 2
 TG_GROUP_BLOCKS = 0
 TG_GROUP_TREE = 1
+TG_NOALLOC_MAX_POINTS = 262144
 
 # every extern "C" symbol declared in include/pytreegrav_gb300.h
 EXPORTS = [
@@ -47,6 +48,7 @@ EXPORTS = [
     "tg_tree_fields",
     "tg_tree_last_walk_stats",
     "tg_morton_order",
+    "tg_morton_order_noalloc",
     "tg_bruteforce",
 ]
 
@@ -93,6 +95,7 @@ def _declare(L):
     L.tg_tree_fields.argtypes = [vp, vp, vp, i64, ci, ci, dbl, dbl, ci, ci, ci, ci, vp, ci, vp, vp]
     L.tg_tree_last_walk_stats.argtypes = [vp, vp, vp, vp, vp]
     L.tg_morton_order.argtypes = [vp, i64, ci, vp, vp]
+    L.tg_morton_order_noalloc.argtypes = [vp, i64, vp, vp]
     L.tg_bruteforce.argtypes = [vp, vp, i64, vp, vp, vp, i64, ci, ci, dbl, ci, ci, vp, vp]
     for name in EXPORTS[1:]:
         getattr(L, name).restype = ci
