@@ -279,6 +279,17 @@ __device__ __forceinline__ int64_t upper_prefix(const uint64_t *keys, int64_t a,
     }
     return a;
 }
+// upper_prefix over [a, b) by galloping from a: cheap when the answer lies near a.
+__device__ __forceinline__ int64_t gallop_upper_prefix(const uint64_t *keys, int64_t a, int64_t b, uint64_t p,
+                                                       int level) {
+    int64_t step = 1;
+    while (a + step - 1 < b && prefix(keys[a + step - 1], level) <= p) {
+        a += step;
+        step <<= 1;
+    }
+    int64_t e = a + step - 1;
+    return upper_prefix(keys, a, e < b ? e : b, p, level);
+}
 __device__ __forceinline__ int64_t lower_prefix(const uint64_t *keys, int64_t a, int64_t b, uint64_t p, int level) {
     while (a < b) {
         int64_t mid = (a + b) >> 1;
@@ -307,11 +318,14 @@ __device__ __forceinline__ int64_t next_after(const RoundView &v, const int8_t *
     return (outer <= L[pe]) ? node_ref(slot_base + nstart[pe]) : e_end_particle;
 }
 
+// Node slots beyond nd.cap are not written (the host sees the round's node total, grows the slot
+// arrays and runs the round's node kernels again); so are exhausted-run entries beyond exh_cap.
 __global__ void k_nodes(RoundView v, int64_t E, const int8_t *L, const int64_t *nstart, const int64_t *cnt,
-                        int64_t slot_base, const uint64_t *keys, Nodes nd, int64_t *exhausted, int *n_exhausted,
-                        int64_t *root_first) {
+                        int64_t slot_base, const uint64_t *keys, Nodes nd, int64_t *exhausted,
+                        unsigned long long *n_exhausted, int64_t exh_cap, int64_t *root_first) {
     int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
+    if (slot_base + nstart[e] + cnt[e] > nd.cap) return;
     int s;
     int64_t i;
     elem_loc(v, e, s, i);
@@ -322,41 +336,54 @@ __global__ void k_nodes(RoundView v, int64_t E, const int8_t *L, const int64_t *
     if (i == seg_lo && v.seg_root[s] >= 0) {
         root_first[s] = (1 <= L[e]) ? node_ref(slot_base + nstart[e]) : i;
     }
-    for (int64_t j = 0; j < cnt[e]; j++) {
+    // geometric centres: the digits are applied from the segment cell down (octree.py:974-978);
+    // the element's nodes are consecutive levels, so one pass over the digits serves them all
+    double c0 = v.seg_center[3 * s], c1 = v.seg_center[3 * s + 1], c2 = v.seg_center[3 * s + 2];
+    double sz = v.seg_size[s];
+    int at = 0;  // level the running centre belongs to
+    const int64_t nc = cnt[e];
+    const int64_t slot0 = slot_base + nstart[e];
+    for (int64_t j = 0; j < nc; j++) {
         int k = l0 + (int)j;
-        int64_t slot = slot_base + nstart[e] + j;
-        int64_t hi = (k == 0) ? seg_hi : upper_prefix(keys, i + 1, seg_hi, prefix(key, k), k);
-        nd.lo[slot] = i;
-        nd.hi[slot] = hi;
-        nd.level[slot] = (int8_t)k;
-        nd.depth[slot] = v.seg_depth0[s] + k;
-        nd.sys[slot] = v.seg_sys[s];
-        int64_t par = (k == 0) ? -1 : node_at(v, L, nstart, slot_base, keys, s, i, k - 1);
-        nd.parent[slot] = par;
-        nd.aparent[slot] = par;
-        nd.rank[slot] = i;
-        // geometric centre: iterate the digits from the segment cell (octree.py:974-978)
-        double c0 = v.seg_center[3 * s], c1 = v.seg_center[3 * s + 1], c2 = v.seg_center[3 * s + 2];
-        double sz = v.seg_size[s];
-        for (int q = 1; q <= k; q++) {
-            int d = (int)((key >> (63 - 3 * q)) & 7);
+        int64_t slot = slot0 + j;
+        for (; at < k; at++) {
+            int d = (int)((key >> (63 - 3 * (at + 1))) & 7);
             c0 = dadd(c0, dmul(sz, c_octant[d][0]));
             c1 = dadd(c1, dmul(sz, c_octant[d][1]));
             c2 = dadd(c2, dmul(sz, c_octant[d][2]));
             sz = dmul(sz, 0.5);
         }
+        nd.lo[slot] = i;
+        nd.level[slot] = (int8_t)k;
+        nd.depth[slot] = v.seg_depth0[s] + k;
+        nd.sys[slot] = v.seg_sys[s];
+        // the element's nodes are nested runs starting at i: all but the first have the
+        // previous slot as parent
+        int64_t par = (k == 0) ? -1 : (j > 0 ? slot - 1 : node_at(v, L, nstart, slot_base, keys, s, i, k - 1));
+        nd.parent[slot] = par;
+        nd.aparent[slot] = par;
+        nd.rank[slot] = i;
         nd.center[3 * slot] = c0;
         nd.center[3 * slot + 1] = c1;
         nd.center[3 * slot + 2] = c2;
         nd.size[slot] = sz;
-        nd.next[slot] = next_after(v, L, nstart, slot_base, s, hi);
         if (k == MAX_LEVEL) {
             nd.first[slot] = -1;  // set by the re-key round or the bucket
-            int q = atomicAdd(n_exhausted, 1);
-            exhausted[q] = slot;
+            unsigned long long q = atomicAdd(n_exhausted, 1ull);
+            if ((int64_t)q < exh_cap) exhausted[q] = slot;
         } else {
             nd.first[slot] = (k + 1 <= L[e]) ? node_ref(slot + 1) : i;
         }
+    }
+    // run ends, deepest first: a shallower run ends at or after the deeper one, so each search
+    // gallops on from the previous end
+    int64_t hi = i + 1;
+    for (int64_t j = nc - 1; j >= 0; j--) {
+        int k = l0 + (int)j;
+        int64_t slot = slot0 + j;
+        hi = (k == 0) ? seg_hi : gallop_upper_prefix(keys, hi, seg_hi, prefix(key, k), k);
+        nd.hi[slot] = hi;
+        nd.next[slot] = next_after(v, L, nstart, slot_base, s, hi);
     }
 }
 
@@ -509,26 +536,60 @@ __device__ __forceinline__ bool ref_ok(int64_t r, int64_t N, int64_t M) {
     if (r == -1) return true;
     return (-r - 2) < M;
 }
-__global__ void k_validate_slots(Nodes nd, int64_t M, const int64_t *p_parent, const int64_t *p_next, int64_t N,
-                                 int *bad) {
-    int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < M) {
-        bool ok = nd.parent[c] >= -1 && nd.parent[c] < M && nd.aparent[c] >= -1 && nd.aparent[c] < M &&
-                  ref_ok(nd.first[c], N, M) && ref_ok(nd.next[c], N, M) && nd.first[c] != -1 && nd.lo[c] >= 0 &&
-                  nd.hi[c] <= N && nd.lo[c] < nd.hi[c];
-        if (!ok) atomicOr(bad, 1);
-    }
-    if (c < N) {
-        bool ok = p_parent[c] >= 0 && p_parent[c] < M && ref_ok(p_next[c], N, M);
-        if (!ok) atomicOr(bad, 2);
-    }
-}
 __global__ void k_validate_links(int64_t NE, const int64_t *first, const int64_t *next, const int64_t *parent,
                                  int *bad) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= NE) return;
     bool ok = first[i] >= -1 && first[i] < NE && next[i] >= -1 && next[i] < NE && parent[i] >= -1 && parent[i] < NE;
     if (!ok) atomicOr(bad, 4);
+}
+
+// Values the host reads back after a split round, gathered so that one copy (one synchronisation)
+// serves them all. depth_hist counts node slots per depth; depths >= DEPTH_CAP share the last bin.
+constexpr int DEPTH_CAP = 48;
+struct BuildSummary {
+    unsigned long long nodes;  // node slots made by the round (its scan total)
+    unsigned long long n_exh;  // key-exhausted runs found by the round
+    int bad;                   // invalid references (bit flags)
+    int pad;
+    int depth_hist[DEPTH_CAP + 1];
+};
+
+// Slot validation (as above) plus the depth histogram, over the slots [0, M) with
+// M = M_base + *M_round (clamped to the slot capacity).
+__global__ void k_summarize_slots(Nodes nd, int64_t M_base, const unsigned long long *M_round, const int64_t *p_parent,
+                                  const int64_t *p_next, int64_t N, BuildSummary *sum) {
+    __shared__ int hist[DEPTH_CAP + 1];
+    for (int b = threadIdx.x; b <= DEPTH_CAP; b += blockDim.x) hist[b] = 0;
+    __syncthreads();
+    int64_t M = M_base + (M_round ? (int64_t)*M_round : 0);
+    if (M > nd.cap) M = nd.cap;
+    int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < M) {
+        bool ok = nd.parent[c] >= -1 && nd.parent[c] < M && nd.aparent[c] >= -1 && nd.aparent[c] < M &&
+                  ref_ok(nd.first[c], N, M) && ref_ok(nd.next[c], N, M) && nd.first[c] != -1 && nd.lo[c] >= 0 &&
+                  nd.hi[c] <= N && nd.lo[c] < nd.hi[c];
+        if (!ok) atomicOr(&sum->bad, 1);
+        int d = nd.depth[c];
+        atomicAdd(&hist[d < 0 ? 0 : (d > DEPTH_CAP ? DEPTH_CAP : d)], 1);
+    }
+    if (c < N) {
+        bool ok = p_parent[c] >= 0 && p_parent[c] < M && ref_ok(p_next[c], N, M);
+        if (!ok) atomicOr(&sum->bad, 2);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b <= DEPTH_CAP; b += blockDim.x)
+        if (hist[b]) atomicAdd(&sum->depth_hist[b], hist[b]);
+}
+
+// Node slots per system -> node offsets (exclusive scan done by the caller).
+__global__ void k_sys_node_counts(const int32_t *nd_sys, int64_t M, int64_t *cnt) {
+    int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < M) atomicAdd((unsigned long long *)&cnt[nd_sys[c]], 1ull);
+}
+__global__ void k_single_sys_node_off(int64_t *sys_node_off, int64_t M) {
+    sys_node_off[0] = 0;
+    sys_node_off[1] = M;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -538,15 +599,16 @@ struct NumberingBits {
     int db;  // bits of a depth
 };
 
-__global__ void k_number_keys(Nodes nd, int64_t count, const int64_t *sys_off, NumberingBits b, uint64_t *keys,
-                              uint32_t *vals, int64_t *root_slot_of_sys, int *nonroot_count) {
+// root_key sorts after every other key (1 << the key width, or all ones when the width is 64).
+__global__ void k_number_keys(Nodes nd, int64_t count, const int64_t *sys_off, NumberingBits b, uint64_t root_key,
+                              uint64_t *keys, uint32_t *vals, int64_t *root_slot_of_sys, int *nonroot_count) {
     int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= count) return;
     int s = nd.sys[c];
     int64_t ap = nd.aparent[c];
     if (ap < 0) {  // a system root
         root_slot_of_sys[s] = c;
-        keys[c] = ~0ull;  // sorts last
+        keys[c] = root_key;
         vals[c] = (uint32_t)c;
         return;
     }
@@ -577,11 +639,25 @@ __device__ __forceinline__ int64_t resolve(int64_t ref, const int64_t *final_of_
     return final_of_slot[-ref - 2];
 }
 
+// Besides the node arrays, files every node into the list of its depth (lvl_list, sections at
+// lvl_off[d]; depths >= DEPTH_CAP share the last section) for the level-by-level moment pass.
 __global__ void k_write_nodes(Nodes nd, int64_t count, const int64_t *final_of_slot, double *coord, double *size,
-                              int64_t *first, int64_t *next, int64_t *parent, int2 *range, double *cell, int64_t ntot) {
+                              int64_t *first, int64_t *next, int64_t *parent, int2 *range, double *cell, int64_t ntot,
+                              const int *lvl_off, int *lvl_cursor, int32_t *lvl_list, int8_t *fdepth) {
     int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= count) return;
     int64_t f = final_of_slot[c];
+    {
+        int d = nd.depth[c];
+        d = d < 0 ? 0 : (d > DEPTH_CAP ? DEPTH_CAP : d);
+        unsigned peers = __match_any_sync(__activemask(), d);
+        int leader = __ffs(peers) - 1;
+        int base = 0;
+        if (lane_id() == leader) base = atomicAdd(&lvl_cursor[d], __popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        lvl_list[lvl_off[d] + base + __popc(peers & lanemask_lt())] = (int32_t)(f - ntot);
+        fdepth[f - ntot] = (int8_t)d;
+    }
     range[f - ntot] = make_int2((int)nd.lo[c], (int)nd.hi[c]);
     cell[3 * (f - ntot)] = nd.center[3 * c];
     cell[3 * (f - ntot) + 1] = nd.center[3 * c + 1];
@@ -675,35 +751,45 @@ __device__ __forceinline__ void shift_quad(double *Q, double m, double r0, doubl
 }
 
 // One node's moments from its (finished) children: RollupMoments + RollupQuadrupoles restricted
-// to this node (octree.py:199-292).
+// to this node (octree.py:199-292). The children (at most 8: octants, or a bucket node's 7
+// particles and 1 node) are gathered first, then visited in fixed, unrolled slots: threads of a
+// warp whose nodes differ in their mix of children then part only for one slot's short body
+// and meet again after it, instead of running their loops apart. Summation order as in the
+// reference: particle children in chain (Morton) order, then node children in reverse chain
+// order (descending index), zero-mass nodes skipped.
 __device__ void node_moments(const MomentArgs &a, int64_t f) {
     const int64_t stop = a.next[f];
+    const int64_t ne = a.ntot + a.mtot;
+    int64_t ch[8];
+    int n = 0;
+    for (int64_t c = a.first[f]; c != stop && c >= 0 && c < ne && n < 8; c = a.next[c]) ch[n++] = c;
     double m = 0.0, ax = 0.0, ay = 0.0, az = 0.0, h = 0.0;
-    int64_t kids[8];
-    int nk = 0;
-    int steps = 0;
-    for (int64_t c = a.first[f]; c != stop && c >= 0 && steps < 9; c = a.next[c], steps++) {
-        if (c < a.ntot) {
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        if (q < n && ch[q] < a.ntot) {
+            const int64_t c = ch[q];
             double mi = __ldcg(a.mass + c);
             m = dadd(m, mi);
             ax = dadd(ax, dmul(mi, __ldcg(a.coord + 3 * c)));
             ay = dadd(ay, dmul(mi, __ldcg(a.coord + 3 * c + 1)));
             az = dadd(az, dmul(mi, __ldcg(a.coord + 3 * c + 2)));
             h = pymax(h, __ldcg(a.soft + c));
-        } else if (nk < 8) {
-            kids[nk++] = c;
         }
     }
-    for (int q = nk - 1; q >= 0; q--) {
-        int64_t c = kids[q];
-        double mc = __ldcg(a.mass + c);
-        if (mc == 0.0) continue;
-        int64_t cj = c - a.ntot;
-        m = dadd(m, mc);
-        ax = dadd(ax, __ldcg(a.acc + 3 * cj));
-        ay = dadd(ay, __ldcg(a.acc + 3 * cj + 1));
-        az = dadd(az, __ldcg(a.acc + 3 * cj + 2));
-        h = pymax(h, __ldcg(a.soft + c));
+#pragma unroll
+    for (int q = 7; q >= 0; q--) {
+        if (q < n && ch[q] >= a.ntot) {
+            const int64_t c = ch[q];
+            double mc = __ldcg(a.mass + c);
+            if (mc != 0.0) {
+                int64_t cj = c - a.ntot;
+                m = dadd(m, mc);
+                ax = dadd(ax, __ldcg(a.acc + 3 * cj));
+                ay = dadd(ay, __ldcg(a.acc + 3 * cj + 1));
+                az = dadd(az, __ldcg(a.acc + 3 * cj + 2));
+                h = pymax(h, __ldcg(a.soft + c));
+            }
+        }
     }
     int64_t j = f - a.ntot;
     a.mass[f] = m;
@@ -716,6 +802,7 @@ __device__ void node_moments(const MomentArgs &a, int64_t f) {
         double inv = ddiv(1.0, m);
         double accs[3] = {ax, ay, az};
         double d2 = 0.0;
+#pragma unroll
         for (int k = 0; k < 3; k++) {
             double cm = dmul(accs[k], inv);
             double dx = dsub(cm, com[k]);
@@ -727,41 +814,183 @@ __device__ void node_moments(const MomentArgs &a, int64_t f) {
     }
     if (a.quads) {
         double Q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-        int qsteps = 0;
-        for (int64_t c = a.first[f]; c != stop && c >= 0 && qsteps < 9; c = a.next[c], qsteps++) {
-            if (c < a.ntot)
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            if (q < n && ch[q] < a.ntot) {
+                const int64_t c = ch[q];
                 shift_quad(Q, __ldcg(a.mass + c), dsub(__ldcg(a.coord + 3 * c), com[0]),
                            dsub(__ldcg(a.coord + 3 * c + 1), com[1]), dsub(__ldcg(a.coord + 3 * c + 2), com[2]));
+            }
         }
-        for (int q = nk - 1; q >= 0; q--) {
-            int64_t c = kids[q];
-            double mc = __ldcg(a.mass + c);
-            if (mc == 0.0) continue;
-            int64_t cj = c - a.ntot;
-            for (int k = 0; k < 9; k++) Q[k] = dadd(Q[k], __ldcg(a.quad + 9 * cj + k));
-            shift_quad(Q, mc, dsub(__ldcg(a.coord + 3 * c), com[0]), dsub(__ldcg(a.coord + 3 * c + 1), com[1]),
-                       dsub(__ldcg(a.coord + 3 * c + 2), com[2]));
+#pragma unroll
+        for (int q = 7; q >= 0; q--) {
+            if (q < n && ch[q] >= a.ntot) {
+                const int64_t c = ch[q];
+                double mc = __ldcg(a.mass + c);
+                if (mc != 0.0) {
+                    int64_t cj = c - a.ntot;
+#pragma unroll
+                    for (int k = 0; k < 9; k++) Q[k] = dadd(Q[k], __ldcg(a.quad + 9 * cj + k));
+                    shift_quad(Q, mc, dsub(__ldcg(a.coord + 3 * c), com[0]), dsub(__ldcg(a.coord + 3 * c + 1), com[1]),
+                               dsub(__ldcg(a.coord + 3 * c + 2), com[2]));
+                }
+            }
         }
+#pragma unroll
         for (int k = 0; k < 9; k++) a.quad[9 * j + k] = Q[k];
     }
 }
 
-// Bottom-up: every node whose children are all particles starts a thread; the last child to
-// finish a parent carries on with the parent (one pass, no level barriers).
-__global__ void k_moments(MomentArgs a) {
-    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= a.mtot || a.nchild[j] != 0) return;
+// Level by level, deepest first: one launch per depth over that depth's node list, so every lane
+// of a warp works on a node (FP64 throughput is scarce on this GPU, and a warp instruction costs
+// the same with one lane active as with 32). Children are finished by the previous launch.
+__global__ void k_moments_level(MomentArgs a, const int32_t *list, int count) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) node_moments(a, a.ntot + list[i]);
+}
+
+// One quadrupole entry e = 3a + b of shift_quad's update for a child of mass m at offset r.
+__device__ __forceinline__ double quad_term(int e, double m, double r0, double r1, double r2) {
+    const int ia = e / 3, ib = e - 3 * ia;
+    const double ra = ia == 0 ? r0 : (ia == 1 ? r1 : r2);
+    if (ia == ib) {
+        double rsq = dadd(dadd(dmul(r0, r0), dmul(r1, r1)), dmul(r2, r2));
+        return dmul(m, dsub(dmul(dmul(3.0, ra), ra), rsq));
+    }
+    const double rb = ib == 0 ? r0 : (ib == 1 ? r1 : r2);
+    return dmul(dmul(dmul(m, 3.0), ra), rb);
+}
+
+// Small levels (latency-bound: too few nodes to hide a thread's long FP64 chain): 16 lanes per
+// node. Lanes 0-4 each carry one of the mass pass's sums (mass, three mass-weighted coordinates,
+// softening max) and lanes 0-8 one quadrupole entry each; every sum takes its terms in the same
+// order as node_moments, so the results are identical.
+__global__ void k_moments_level_coop(MomentArgs a, const int32_t *list, int count) {
+    const int lane = threadIdx.x & 31, sub = lane & 15, half = lane >> 4;
+    const int node = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 4);
+    if (node >= count) return;  // whole half-warps leave together
+    const unsigned hmask = 0xFFFFu << (16 * half);
+    const int64_t f = a.ntot + list[node];
+    const int64_t stop = a.next[f];
+    const int64_t ne = a.ntot + a.mtot;
+    int64_t ch[8];
+    int n = 0;
+    for (int64_t c = a.first[f]; c != stop && c >= 0 && c < ne && n < 8; c = a.next[c]) ch[n++] = c;
+    double v = 0.0;
+    if (sub < 5) {
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            if (q < n && ch[q] < a.ntot) {
+                const int64_t c = ch[q];
+                double mi = __ldcg(a.mass + c);
+                if (sub == 0) v = dadd(v, mi);
+                else if (sub < 4) v = dadd(v, dmul(mi, __ldcg(a.coord + 3 * c + sub - 1)));
+                else v = pymax(v, __ldcg(a.soft + c));
+            }
+        }
+#pragma unroll
+        for (int q = 7; q >= 0; q--) {
+            if (q < n && ch[q] >= a.ntot) {
+                const int64_t c = ch[q];
+                double mc = __ldcg(a.mass + c);
+                if (mc != 0.0) {
+                    const int64_t cj = c - a.ntot;
+                    if (sub == 0) v = dadd(v, mc);
+                    else if (sub < 4) v = dadd(v, __ldcg(a.acc + 3 * cj + sub - 1));
+                    else v = pymax(v, __ldcg(a.soft + c));
+                }
+            }
+        }
+    }
+    const double m = __shfl_sync(hmask, v, 0, 16);
+    const double ax = __shfl_sync(hmask, v, 1, 16), ay = __shfl_sync(hmask, v, 2, 16);
+    const double az = __shfl_sync(hmask, v, 3, 16), h = __shfl_sync(hmask, v, 4, 16);
+    const int64_t j = f - a.ntot;
+    double com0 = 0.0, com1 = 0.0, com2 = 0.0;
+    if (sub == 0) {
+        a.mass[f] = m;
+        a.soft[f] = h;
+        a.acc[3 * j] = ax;
+        a.acc[3 * j + 1] = ay;
+        a.acc[3 * j + 2] = az;
+        double com[3] = {a.coord[3 * f], a.coord[3 * f + 1], a.coord[3 * f + 2]};
+        if (m != 0.0) {
+            double inv = ddiv(1.0, m);
+            double accs[3] = {ax, ay, az};
+            double d2 = 0.0;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                double cm = dmul(accs[k], inv);
+                double dx = dsub(cm, com[k]);
+                d2 = dadd(d2, dmul(dx, dx));
+                com[k] = cm;
+                a.coord[3 * f + k] = cm;
+            }
+            a.delta[f] = __dsqrt_rn(d2);
+        }
+        com0 = com[0]; com1 = com[1]; com2 = com[2];
+    }
+    com0 = __shfl_sync(hmask, com0, 0, 16);
+    com1 = __shfl_sync(hmask, com1, 0, 16);
+    com2 = __shfl_sync(hmask, com2, 0, 16);
+    if (a.quads && sub < 9) {
+        double Q = 0.0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            if (q < n && ch[q] < a.ntot) {
+                const int64_t c = ch[q];
+                Q = dadd(Q, quad_term(sub, __ldcg(a.mass + c), dsub(__ldcg(a.coord + 3 * c), com0),
+                                      dsub(__ldcg(a.coord + 3 * c + 1), com1), dsub(__ldcg(a.coord + 3 * c + 2), com2)));
+            }
+        }
+#pragma unroll
+        for (int q = 7; q >= 0; q--) {
+            if (q < n && ch[q] >= a.ntot) {
+                const int64_t c = ch[q];
+                double mc = __ldcg(a.mass + c);
+                if (mc != 0.0) {
+                    Q = dadd(Q, __ldcg(a.quad + 9 * (c - a.ntot) + sub));
+                    Q = dadd(Q, quad_term(sub, mc, dsub(__ldcg(a.coord + 3 * c), com0),
+                                          dsub(__ldcg(a.coord + 3 * c + 1), com1), dsub(__ldcg(a.coord + 3 * c + 2), com2)));
+                }
+            }
+        }
+        a.quad[9 * j + sub] = Q;
+    }
+}
+
+// Nodes at depth >= DEPTH_CAP (chains of re-keyed cells and coincident-point buckets, whose depth
+// is unbounded): every such node without node children starts a thread; the last child to finish
+// a parent carries on with the parent, up to the first ancestor above DEPTH_CAP, which the level
+// pass then handles.
+__global__ void k_moments_deep(MomentArgs a, const int32_t *list, int count, const int8_t *fdepth) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    int64_t j = list[i];
+    if (a.nchild[j] != 0) return;
     int64_t f = a.ntot + j;
     for (int64_t guard = 0; guard < a.mtot + 1; guard++) {
         node_moments(a, f);
         __threadfence();
         int64_t p = a.parent[f];
-        if (p < 0) return;
+        if (p < a.ntot || p >= a.ntot + a.mtot) return;
         int64_t pj = p - a.ntot;
+        if (fdepth[pj] < DEPTH_CAP) return;
         int prev = atomicAdd(&a.arrived[pj], 1);
         if (prev != a.nchild[pj] - 1) return;
         __threadfence();
         f = p;
+    }
+}
+
+// Section offsets of the level lists from the depth histogram; cursors reset.
+__global__ void k_level_offsets(const BuildSummary *sum, int *lvl_off, int *lvl_cursor) {
+    if (threadIdx.x != 0) return;
+    int run = 0;
+    for (int d = 0; d <= DEPTH_CAP; d++) {
+        lvl_off[d] = run;
+        lvl_cursor[d] = 0;
+        run += sum->depth_hist[d];
     }
 }
 
@@ -788,7 +1017,7 @@ template <typename T>
 static tg_status dalloc(T **p, int64_t n, cudaStream_t s) {
     *p = nullptr;
     if (n <= 0) n = 1;
-    TG_CUDA(cudaMallocAsync((void **)p, sizeof(T) * n, s));
+    TG_CUDA(tg::dev_malloc((void **)p, sizeof(T) * n, s));
     return TG_OK;
 }
 template <typename T>
@@ -966,21 +1195,31 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     { k_init_root_segs<<<LAUNCH(nsys)>>>(sg, sys_off, center, size); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
     int64_t *exh = nullptr;
-    int *n_exh_dev = nullptr;
     int n_exh = 0;
     int64_t *root_first = nullptr;
     int has_coincident = 0;
+    // What the host reads back after a round; final (covering every slot) once a round leaves no
+    // key-exhausted run. The common case, one round and no buckets, synchronises here once.
+    BuildSummary *sum = nullptr;
+    TG_TRY(dalloc(&sum, 1, st));
+    BuildSummary hs;
+    memset(&hs, 0, sizeof(hs));
+    bool summary_final = false;
 
     for (int round = 0; round <= MORTON_MAX_ROUNDS; round++) {
-        // element offsets of the segments
-        int64_t *sizes = nullptr;
-        TG_TRY(dalloc(&sizes, sg.n, st));
-        { k_seg_sizes<<<LAUNCH(sg.n)>>>(sg.lo, sg.hi, sg.n, sizes); tg::note_launch(); }
-        TG_TRY(exclusive_scan_i64(sizes, sg.eoff, sg.n, sg.eoff + sg.n, st));
-        dfree(sizes, st);
-        int64_t E = 0;
-        TG_CUDA(cudaMemcpyAsync(&E, sg.eoff + sg.n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-        TG_CUDA(cudaStreamSynchronize(st));
+        // element offsets of the segments; round 0's segments are the systems
+        int64_t E = N;
+        if (round == 0) {
+            TG_CUDA(cudaMemcpyAsync(sg.eoff, sys_off, sizeof(int64_t) * (nsys + 1), cudaMemcpyDeviceToDevice, st));
+        } else {
+            int64_t *sizes = nullptr;
+            TG_TRY(dalloc(&sizes, sg.n, st));
+            { k_seg_sizes<<<LAUNCH(sg.n)>>>(sg.lo, sg.hi, sg.n, sizes); tg::note_launch(); }
+            TG_TRY(exclusive_scan_i64(sizes, sg.eoff, sg.n, sg.eoff + sg.n, st));
+            dfree(sizes, st);
+            TG_CUDA(cudaMemcpyAsync(&E, sg.eoff + sg.n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+            TG_CUDA(cudaStreamSynchronize(st));
+        }
         RoundView v = view_of(sg);
 
         if (round > 0) {
@@ -1013,36 +1252,53 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
         }
 
         int8_t *L = nullptr;
-        int64_t *cnt = nullptr, *nstart = nullptr, *total = nullptr;
+        int64_t *cnt = nullptr, *nstart = nullptr;
         TG_TRY(dalloc(&L, E, st));
         TG_TRY(dalloc(&cnt, E, st));
         TG_TRY(dalloc(&nstart, E, st));
-        TG_TRY(dalloc(&total, 1, st));
+        TG_CUDA(cudaMemsetAsync(sum, 0, sizeof(BuildSummary), st));
         { k_levels<<<LAUNCH(E)>>>(v, E, keys_sorted, L); tg::note_launch(); }
         { k_counts<<<LAUNCH(E)>>>(v, E, L, cnt); tg::note_launch(); }
         TG_CUDA(cudaGetLastError());
-        TG_TRY(exclusive_scan_i64(cnt, nstart, E, total, st));
-        int64_t Mr = 0;
-        TG_CUDA(cudaMemcpyAsync(&Mr, total, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-        TG_CUDA(cudaStreamSynchronize(st));
-        int64_t slot_base = nd.count;
-        TG_TRY(nodes_reserve(nd, slot_base + Mr, st));
+        TG_TRY(exclusive_scan_i64(cnt, nstart, E, (int64_t *)&sum->nodes, st));
+        const int64_t slot_base = nd.count;
         dfree(exh, st);
-        dfree(n_exh_dev, st);
         dfree(root_first, st);
-        TG_TRY(dalloc(&exh, std::max<int64_t>(Mr, 1), st));
-        TG_TRY(dalloc(&n_exh_dev, 1, st));
+        int64_t exh_cap = std::max<int64_t>(nd.cap - slot_base, 1);
+        TG_TRY(dalloc(&exh, exh_cap, st));
         TG_TRY(dalloc(&root_first, sg.n, st));
-        TG_CUDA(cudaMemsetAsync(n_exh_dev, 0, sizeof(int), st));
-        { k_nodes<<<LAUNCH(E)>>>(v, E, L, nstart, cnt, slot_base, keys_sorted, nd, exh, n_exh_dev, root_first); tg::note_launch(); }
-        { k_particles<<<LAUNCH(E)>>>(v, E, L, nstart, slot_base, keys_sorted, p_parent, p_next); tg::note_launch(); }
-        if (round > 0) { k_set_root_first<<<LAUNCH(sg.n)>>>(sg.root, root_first, sg.n, nd.first); tg::note_launch(); }
-        TG_CUDA(cudaGetLastError());
+        // The round's nodes, particle links and the summary, read back with one copy. Slots that
+        // do not fit are skipped by k_nodes; the host then grows the arrays and runs it again.
+        auto run_round = [&]() -> tg_status {
+            { k_nodes<<<LAUNCH(E)>>>(v, E, L, nstart, cnt, slot_base, keys_sorted, nd, exh, &sum->n_exh, exh_cap,
+                                     root_first); tg::note_launch(); }
+            { k_particles<<<LAUNCH(E)>>>(v, E, L, nstart, slot_base, keys_sorted, p_parent, p_next); tg::note_launch(); }
+            if (round > 0) { k_set_root_first<<<LAUNCH(sg.n)>>>(sg.root, root_first, sg.n, nd.first); tg::note_launch(); }
+            { k_summarize_slots<<<LAUNCH(std::max<int64_t>(nd.cap, N))>>>(nd, slot_base, &sum->nodes, p_parent, p_next,
+                                                                       N, sum); tg::note_launch(); }
+            TG_CUDA(cudaGetLastError());
+            TG_CUDA(cudaMemcpyAsync(&hs, sum, sizeof(BuildSummary), cudaMemcpyDeviceToHost, st));
+            TG_CUDA(cudaStreamSynchronize(st));
+            return TG_OK;
+        };
+        TG_TRY(run_round());
+        const int64_t Mr = (int64_t)hs.nodes;
+        if (slot_base + Mr > nd.cap) {
+            TG_TRY(nodes_reserve(nd, slot_base + Mr, st));
+            dfree(exh, st);
+            exh_cap = std::max<int64_t>(Mr, 1);
+            TG_TRY(dalloc(&exh, exh_cap, st));
+            TG_CUDA(cudaMemsetAsync(&sum->n_exh, 0, sizeof(unsigned long long), st));
+            TG_CUDA(cudaMemsetAsync(&sum->bad, 0, sizeof(int) * (2 + DEPTH_CAP + 1), st));
+            TG_TRY(run_round());
+        }
         nd.count = slot_base + Mr;
-        TG_CUDA(cudaMemcpyAsync(&n_exh, n_exh_dev, sizeof(int), cudaMemcpyDeviceToHost, st));
-        TG_CUDA(cudaStreamSynchronize(st));
-        dfree(L, st); dfree(cnt, st); dfree(nstart, st); dfree(total, st);
-        if (n_exh == 0) break;
+        n_exh = (int)hs.n_exh;
+        dfree(L, st); dfree(cnt, st); dfree(nstart, st);
+        if (n_exh == 0) {
+            summary_final = true;
+            break;
+        }
         if (round < MORTON_MAX_ROUNDS) {
             segs_free(sg, st);
             TG_TRY(segs_alloc(sg, n_exh, st));
@@ -1076,22 +1332,20 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     T->has_coincident = has_coincident;
 
     // 6. reference numbering
+    if (!summary_final) {  // buckets were made after the last summary: validate every slot again
+        TG_CUDA(cudaMemsetAsync(sum, 0, sizeof(BuildSummary), st));
+        { k_summarize_slots<<<LAUNCH(std::max<int64_t>(nd.count, N))>>>(nd, nd.count, nullptr, p_parent, p_next, N,
+                                                                      sum); tg::note_launch(); }
+        TG_CUDA(cudaGetLastError());
+        TG_CUDA(cudaMemcpyAsync(&hs, sum, sizeof(BuildSummary), cudaMemcpyDeviceToHost, st));
+        TG_CUDA(cudaStreamSynchronize(st));
+    }
+    if (hs.bad) {
+        set_last_error_msg("internal error: octree build produced an invalid node reference");
+        return TG_ERR_CUDA;
+    }
     const int64_t M = nd.count;
     T->mtot = M;
-    {
-        int *bad = nullptr;
-        TG_TRY(dalloc(&bad, 1, st));
-        TG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
-        { k_validate_slots<<<LAUNCH(std::max<int64_t>(M, N))>>>(nd, M, p_parent, p_next, N, bad); tg::note_launch(); }
-        int hbad = 0;
-        TG_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
-        TG_CUDA(cudaStreamSynchronize(st));
-        dfree(bad, st);
-        if (hbad) {
-            set_last_error_msg("internal error: octree build produced an invalid node reference");
-            return TG_ERR_CUDA;
-        }
-    }
     uint64_t *nkeys = nullptr;
     uint32_t *nvals = nullptr;
     int64_t *root_slot = nullptr, *final_of_slot = nullptr, *sys_node_off = nullptr;
@@ -1103,49 +1357,41 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     TG_TRY(dalloc(&sys_node_off, nsys + 1, st));
     TG_TRY(dalloc(&nonroot, 1, st));
     TG_CUDA(cudaMemsetAsync(nonroot, 0, sizeof(int), st));
-    { k_number_keys<<<LAUNCH(M)>>>(nd, M, sys_off, nb, nkeys, nvals, root_slot, nonroot); tg::note_launch(); }
+    const int key_bits = sysbits + 2 * nb.lb + nb.db;
+    const int sort_bits = key_bits < 64 ? key_bits + 1 : 64;
+    const uint64_t root_key = key_bits < 64 ? (1ull << key_bits) : ~0ull;
+    { k_number_keys<<<LAUNCH(M)>>>(nd, M, sys_off, nb, root_key, nkeys, nvals, root_slot, nonroot); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
-    TG_TRY(radix_sort_pairs(nkeys, nvals, M, 64, st));
-    // per-system node counts -> node offsets (roots first within each system's block)
-    std::vector<int64_t> node_cnt(nsys, 0);
-    {
-        std::vector<int32_t> sys_of_slot(M);
-        TG_CUDA(cudaMemcpyAsync(sys_of_slot.data(), nd.sys, sizeof(int32_t) * M, cudaMemcpyDeviceToHost, st));
-        TG_CUDA(cudaStreamSynchronize(st));
-        for (int64_t c = 0; c < M; c++) node_cnt[sys_of_slot[c]]++;
+    TG_TRY(radix_sort_pairs(nkeys, nvals, M, sort_bits, st));
+    // per-system node offsets (roots first within each system's block), on the device; the host
+    // copy is read with the final synchronisation
+    if (nsys == 1) {
+        { k_single_sys_node_off<<<1, 1, 0, st>>>(sys_node_off, M); tg::note_launch(); }
+        T->sys_node_off = {0, M};
+    } else {
+        int64_t *ncnt = nullptr;
+        TG_TRY(dalloc(&ncnt, nsys, st));
+        TG_CUDA(cudaMemsetAsync(ncnt, 0, sizeof(int64_t) * nsys, st));
+        { k_sys_node_counts<<<LAUNCH(M)>>>(nd.sys, M, ncnt); tg::note_launch(); }
+        TG_CUDA(cudaGetLastError());
+        TG_TRY(exclusive_scan_i64(ncnt, sys_node_off, nsys, sys_node_off + nsys, st));
+        dfree(ncnt, st);
+        T->sys_node_off.assign(nsys + 1, 0);
     }
-    T->sys_node_off.assign(nsys + 1, 0);
-    for (int s = 0; s < nsys; s++) T->sys_node_off[s + 1] = T->sys_node_off[s] + node_cnt[s];
-    TG_CUDA(cudaMemcpyAsync(sys_node_off, T->sys_node_off.data(), sizeof(int64_t) * (nsys + 1), cudaMemcpyHostToDevice,
-                            st));
     { k_final_index<<<LAUNCH(std::max<int64_t>(M, nsys))>>>(nvals, M, nd.sys, N, sys_node_off, final_of_slot, root_slot,
                                                          nsys); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
-
-    // capacity (NumNodes) per system, from node_hi and bucket reservations
-    {
-        unsigned long long *req = nullptr;
+    // capacity (NumNodes) per system: bucket reservations, read with the final synchronisation
+    unsigned long long *req = nullptr;
+    if (n_bucket > 0) {
         TG_TRY(dalloc(&req, nsys, st));
         TG_CUDA(cudaMemsetAsync(req, 0, sizeof(unsigned long long) * nsys, st));
-        if (n_bucket > 0) {
-            { k_bucket_requirement<<<LAUNCH(n_bucket)>>>(exh, n_bucket, nd, sys_off, nb, nkeys, M, N, req); tg::note_launch(); }
-            TG_CUDA(cudaGetLastError());
-        }
-        std::vector<unsigned long long> rq(nsys);
-        TG_CUDA(cudaMemcpyAsync(rq.data(), req, sizeof(unsigned long long) * nsys, cudaMemcpyDeviceToHost, st));
-        TG_CUDA(cudaStreamSynchronize(st));
-        T->sys_capacity.resize(nsys);
-        for (int s = 0; s < nsys; s++) {
-            int64_t np = sys_off_host[s + 1] - sys_off_host[s];
-            int64_t node_hi = np + node_cnt[s];
-            T->sys_capacity[s] = reference_capacity(np, std::max<int64_t>(node_hi, (int64_t)rq[s]));
-        }
-        dfree(req, st);
+        { k_bucket_requirement<<<LAUNCH(n_bucket)>>>(exh, n_bucket, nd, sys_off, nb, nkeys, M, N, req); tg::note_launch(); }
+        TG_CUDA(cudaGetLastError());
     }
     dfree(exh, st);
-    dfree(n_exh_dev, st);
 
-    // 7. final arrays
+    // 7. final arrays; every node also goes into the list of its depth
     const int64_t NE = N + M;
     TG_TRY(dalloc(&T->coord, 3 * NE, st));
     TG_TRY(dalloc(&T->mass, NE, st));
@@ -1164,30 +1410,26 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     dfree(pc, st); dfree(pm, st); dfree(ps, st);
     TG_TRY(dalloc(&T->node_range, M, st));
     TG_TRY(dalloc(&T->cell_center, 3 * M, st));
+    int *lvl = nullptr;  // section offsets, then cursors, of the depth lists
+    int32_t *lvl_list = nullptr;
+    int8_t *fdepth = nullptr;
+    TG_TRY(dalloc(&lvl, 2 * (DEPTH_CAP + 1), st));
+    TG_TRY(dalloc(&lvl_list, M, st));
+    TG_TRY(dalloc(&fdepth, M, st));
+    { k_level_offsets<<<1, 32, 0, st>>>(sum, lvl, lvl + DEPTH_CAP + 1); tg::note_launch(); }
     { k_write_nodes<<<LAUNCH(M)>>>(nd, M, final_of_slot, T->coord, T->size, T->first, T->next, T->parent,
-                                 T->node_range, T->cell_center, N); tg::note_launch(); }
+                                 T->node_range, T->cell_center, N, lvl, lvl + DEPTH_CAP + 1, lvl_list, fdepth); tg::note_launch(); }
     { k_write_particles<<<LAUNCH(N)>>>(N, p_parent, p_next, final_of_slot, T->first, T->next, T->parent, T->size,
                                      T->delta); tg::note_launch(); }
+    TG_CUDA(cudaMemsetAsync(&sum->bad, 0, sizeof(int), st));
+    { k_validate_links<<<LAUNCH(NE)>>>(NE, T->first, T->next, T->parent, &sum->bad); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
-    {
-        int *bad = nullptr;
-        TG_TRY(dalloc(&bad, 1, st));
-        TG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
-        { k_validate_links<<<LAUNCH(NE)>>>(NE, T->first, T->next, T->parent, bad); tg::note_launch(); }
-        int hbad = 0;
-        TG_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
-        TG_CUDA(cudaStreamSynchronize(st));
-        dfree(bad, st);
-        if (hbad) {
-            set_last_error_msg("internal error: octree links out of range");
-            return TG_ERR_CUDA;
-        }
-    }
     nodes_free(nd, st);
     dfree(p_parent, st); dfree(p_next, st); dfree(nkeys, st); dfree(nvals, st); dfree(root_slot, st);
     dfree(final_of_slot, st); dfree(nonroot, st); dfree(keys, st); dfree(perm, st);
 
-    // 8. moments
+    // 8. moments: nodes deeper than DEPTH_CAP by climbing, then one launch per depth, deepest first
+    // (the moment kernels bound every link they follow, so they may run before the link check is read)
     MomentArgs a;
     a.ntot = N;
     a.mtot = M;
@@ -1204,21 +1446,59 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
         a.quad = T->quad;
     }
     if (compute_moments) {
+        int off[DEPTH_CAP + 1];
+        for (int d = 0, run = 0; d <= DEPTH_CAP; d++) {
+            off[d] = run;
+            run += hs.depth_hist[d];
+        }
         TG_TRY(dalloc(&a.acc, 3 * M, st));
-        TG_TRY(dalloc(&a.nchild, M, st));
-        TG_TRY(dalloc(&a.arrived, M, st));
-        TG_CUDA(cudaMemsetAsync(a.nchild, 0, sizeof(int) * M, st));
-        TG_CUDA(cudaMemsetAsync(a.arrived, 0, sizeof(int) * M, st));
-        { k_count_node_children<<<LAUNCH(M)>>>(N, M, T->parent, a.nchild); tg::note_launch(); }
-        { k_moments<<<LAUNCH(M)>>>(a); tg::note_launch(); }
+        const int ndeep = hs.depth_hist[DEPTH_CAP];
+        if (ndeep > 0) {
+            TG_TRY(dalloc(&a.nchild, M, st));
+            TG_TRY(dalloc(&a.arrived, M, st));
+            TG_CUDA(cudaMemsetAsync(a.nchild, 0, sizeof(int) * M, st));
+            TG_CUDA(cudaMemsetAsync(a.arrived, 0, sizeof(int) * M, st));
+            { k_count_node_children<<<LAUNCH(M)>>>(N, M, T->parent, a.nchild); tg::note_launch(); }
+            { k_moments_deep<<<div_up(ndeep, 128), 128, 0, st>>>(a, lvl_list + off[DEPTH_CAP], ndeep, fdepth); tg::note_launch(); }
+        }
+        // a level with few nodes is latency-bound: 16 lanes per node there; one thread per node
+        // on the large levels, which are FP64-throughput-bound
+        const int few = 128 * num_sms();
+        for (int d = DEPTH_CAP - 1; d >= 0; d--) {
+            const int c = hs.depth_hist[d];
+            if (c <= 0) continue;
+            if (c < few) { k_moments_level_coop<<<div_up((int64_t)c * 16, 128), 128, 0, st>>>(a, lvl_list + off[d], c); tg::note_launch(); }
+            else { k_moments_level<<<div_up(c, 128), 128, 0, st>>>(a, lvl_list + off[d], c); tg::note_launch(); }
+        }
         TG_CUDA(cudaGetLastError());
         dfree(a.acc, st); dfree(a.nchild, st); dfree(a.arrived, st);
     } else {
         { k_fold_only<<<LAUNCH(M)>>>(a); tg::note_launch(); }
         TG_CUDA(cudaGetLastError());
     }
+
+    // 9. the one closing synchronisation: link check, per-system node offsets, bucket reservations
+    int links_bad = 0;
+    std::vector<unsigned long long> rq(nsys, 0);
+    TG_CUDA(cudaMemcpyAsync(&links_bad, &sum->bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (nsys > 1)
+        TG_CUDA(cudaMemcpyAsync(T->sys_node_off.data(), sys_node_off, sizeof(int64_t) * (nsys + 1),
+                                cudaMemcpyDeviceToHost, st));
+    if (req) TG_CUDA(cudaMemcpyAsync(rq.data(), req, sizeof(unsigned long long) * nsys, cudaMemcpyDeviceToHost, st));
+    dfree(req, st); dfree(sum, st); dfree(sys_node_off, st);
+    dfree(lvl, st); dfree(lvl_list, st); dfree(fdepth, st);
     dfree(sys_off, st); dfree(mn, st); dfree(mx, st); dfree(center, st); dfree(size, st);
     TG_CUDA(cudaStreamSynchronize(st));
+    if (links_bad) {
+        set_last_error_msg("internal error: octree links out of range");
+        return TG_ERR_CUDA;
+    }
+    T->sys_capacity.resize(nsys);
+    for (int s = 0; s < nsys; s++) {
+        int64_t np = sys_off_host[s + 1] - sys_off_host[s];
+        int64_t node_hi = np + (T->sys_node_off[s + 1] - T->sys_node_off[s]);
+        T->sys_capacity[s] = reference_capacity(np, std::max<int64_t>(node_hi, (int64_t)rq[s]));
+    }
     return TG_OK;
 }
 

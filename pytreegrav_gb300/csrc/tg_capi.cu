@@ -70,7 +70,7 @@ tg_status stage_in(const double *src, int64_t count, int mem, cudaStream_t st, D
         b.ptr = src;
         return TG_OK;
     }
-    TG_CUDA(cudaMallocAsync((void **)&b.owned, sizeof(double) * std::max<int64_t>(count, 1), st));
+    TG_CUDA(tg::dev_malloc((void **)&b.owned, sizeof(double) * std::max<int64_t>(count, 1), st));
     TG_CUDA(cudaMemcpyAsync(b.owned, src, sizeof(double) * count, cudaMemcpyHostToDevice, st));
     b.ptr = b.owned;
     return TG_OK;
@@ -78,7 +78,7 @@ tg_status stage_in(const double *src, int64_t count, int mem, cudaStream_t st, D
 
 tg_status check_finite(const double *const *arrs, const int64_t *counts, int k, cudaStream_t st) {
     int *flag = nullptr;
-    TG_CUDA(cudaMallocAsync((void **)&flag, sizeof(int), st));
+    TG_CUDA(tg::dev_malloc((void **)&flag, sizeof(int), st));
     TG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
     for (int q = 0; q < k; q++)
         if (arrs[q] && counts[q] > 0) { k_nonfinite<<<div_up(counts[q], 256), 256, 0, st>>>(arrs[q], counts[q], flag); tg::note_launch(); }
@@ -99,8 +99,7 @@ void destroy(tg_tree_s *t) {
     f(t->first); f(t->next); f(t->walk_idx); f(t->parent); f(t->node_range); f(t->cell_center);
     free_arena(t->arena32, st);
     free_arena(t->arena64, st);
-    if (t->stats_dev) cudaFree(t->stats_dev);
-    cudaStreamSynchronize(st);
+    if (t->stats_dev) cudaFreeAsync(t->stats_dev, st);
     delete t;
 }
 
@@ -250,7 +249,7 @@ tg_status tg_tree_fields(tg_tree t, const double *pos, const double *h, int64_t 
             TG_TRY(make_groups(t, t->sys_off, group_size, &groups, &groot, &ngroups, st));
             TG_TRY(make_cost_order(t->coord, groups, ngroups, &gorder, st));
         }
-        if (mem == TG_MEM_HOST) TG_CUDA(cudaMallocAsync((void **)&dout, sizeof(double) * nt * W, st));
+        if (mem == TG_MEM_HOST) TG_CUDA(tg::dev_malloc((void **)&dout, sizeof(double) * nt * W, st));
         else dout = out;
         rc = run_walk(t, t->coord, t->soft, nt, groups, groot, gorder, ngroups, t->walk_idx, fields, quadrupole, theta,
                       G, group_size, precision, theta_per_group, dout, st);
@@ -267,24 +266,24 @@ tg_status tg_tree_fields(tg_tree t, const double *pos, const double *h, int64_t 
         int64_t *scatter = nullptr;
         if (order == TG_ORDER_MORTON) {
             uint32_t *perm = nullptr;
-            TG_CUDA(cudaMallocAsync((void **)&perm, sizeof(uint32_t) * n, st));
+            TG_CUDA(tg::dev_malloc((void **)&perm, sizeof(uint32_t) * n, st));
             TG_TRY(morton_order_device(dp.ptr, n, perm, st));
-            TG_CUDA(cudaMallocAsync((void **)&sp, sizeof(double) * 3 * n, st));
-            TG_CUDA(cudaMallocAsync((void **)&sh, sizeof(double) * n, st));
-            TG_CUDA(cudaMallocAsync((void **)&scatter, sizeof(int64_t) * n, st));
+            TG_CUDA(tg::dev_malloc((void **)&sp, sizeof(double) * 3 * n, st));
+            TG_CUDA(tg::dev_malloc((void **)&sh, sizeof(double) * n, st));
+            TG_CUDA(tg::dev_malloc((void **)&scatter, sizeof(int64_t) * n, st));
             { k_gather_targets<<<div_up(n, 256), 256, 0, st>>>(perm, n, dp.ptr, dh.ptr, sp, sh); tg::note_launch(); }
             { k_u32_to_i64<<<div_up(n, 256), 256, 0, st>>>(perm, n, scatter); tg::note_launch(); }
             TG_CUDA(cudaGetLastError());
             TG_CUDA(cudaFreeAsync(perm, st));
         } else {
-            TG_CUDA(cudaMallocAsync((void **)&sh, sizeof(double) * n, st));
+            TG_CUDA(tg::dev_malloc((void **)&sh, sizeof(double) * n, st));
             if (dh.ptr) TG_CUDA(cudaMemcpyAsync(sh, dh.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
             else TG_CUDA(cudaMemsetAsync(sh, 0, sizeof(double) * n, st));
         }
         std::vector<int64_t> toff = {0, n};
         TG_TRY(make_groups(t, toff, group_size, &groups, &groot, &ngroups, st));
         TG_TRY(make_cost_order(sp ? sp : dp.ptr, groups, ngroups, &gorder, st));
-        if (mem == TG_MEM_HOST) TG_CUDA(cudaMallocAsync((void **)&dout, sizeof(double) * nt * W, st));
+        if (mem == TG_MEM_HOST) TG_CUDA(tg::dev_malloc((void **)&dout, sizeof(double) * nt * W, st));
         else dout = out;
         rc = run_walk(t, sp ? sp : dp.ptr, sh, nt, groups, groot, gorder, ngroups, scatter, fields, quadrupole, theta, G,
                       group_size, precision, theta_per_group, dout, st);
@@ -337,9 +336,9 @@ tg_status tg_morton_order(const double *pos, int64_t n, int mem, int64_t *perm, 
     TG_TRY(check_finite(arrs, counts, 1, st));
     uint32_t *p32 = nullptr;
     int64_t *p64 = nullptr;
-    TG_CUDA(cudaMallocAsync((void **)&p32, sizeof(uint32_t) * n, st));
+    TG_CUDA(tg::dev_malloc((void **)&p32, sizeof(uint32_t) * n, st));
     TG_TRY(morton_order_device(dp.ptr, n, p32, st));
-    if (mem == TG_MEM_HOST) TG_CUDA(cudaMallocAsync((void **)&p64, sizeof(int64_t) * n, st));
+    if (mem == TG_MEM_HOST) TG_CUDA(tg::dev_malloc((void **)&p64, sizeof(int64_t) * n, st));
     else p64 = perm;
     { k_u32_to_i64<<<div_up(n, 256), 256, 0, st>>>(p32, n, p64); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
@@ -379,18 +378,18 @@ tg_status tg_bruteforce(const double *pos_t, const double *h_t, int64_t nt, cons
     }
     double *zt = nullptr, *zs = nullptr;
     if (!dht.ptr) {
-        TG_CUDA(cudaMallocAsync((void **)&zt, sizeof(double) * nt, st));
+        TG_CUDA(tg::dev_malloc((void **)&zt, sizeof(double) * nt, st));
         TG_CUDA(cudaMemsetAsync(zt, 0, sizeof(double) * nt, st));
         dht.ptr = zt;
     }
     if (!dhs.ptr) {
-        TG_CUDA(cudaMallocAsync((void **)&zs, sizeof(double) * std::max<int64_t>(ns, 1), st));
+        TG_CUDA(tg::dev_malloc((void **)&zs, sizeof(double) * std::max<int64_t>(ns, 1), st));
         TG_CUDA(cudaMemsetAsync(zs, 0, sizeof(double) * std::max<int64_t>(ns, 1), st));
         dhs.ptr = zs;
         if (mutual) dht.ptr = zs;
     }
     double *dout = out;
-    if (mem == TG_MEM_HOST) TG_CUDA(cudaMallocAsync((void **)&dout, sizeof(double) * nt * W, st));
+    if (mem == TG_MEM_HOST) TG_CUDA(tg::dev_malloc((void **)&dout, sizeof(double) * nt * W, st));
     tg_status rc = run_bruteforce(dpt.ptr, dht.ptr, nt, dps.ptr, dms.ptr, dhs.ptr, ns, fields, mutual, G, precision,
                                   dout, st);
     if (rc == TG_OK && mem == TG_MEM_HOST)

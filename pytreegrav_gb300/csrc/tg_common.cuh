@@ -85,6 +85,16 @@ tg_status radix_sort_pairs(uint64_t *keys, uint32_t *vals, int64_t n, int bits, 
 
 int num_sms();
 
+// Stream-ordered device allocation from the library's own memory pool on the current device.
+// The pool keeps up to TG_POOL_KEEP_BYTES of freed memory mapped for later calls (a build and a
+// walk allocate and free their temporaries on every call; with the driver's default threshold of
+// zero, that memory would be unmapped at each synchronisation and mapped again by the next call).
+// Free with cudaFreeAsync.
+#ifndef TG_POOL_KEEP_BYTES
+#define TG_POOL_KEEP_BYTES (4ull << 30)
+#endif
+cudaError_t dev_malloc(void **p, size_t bytes, cudaStream_t s);
+
 // Counts kernel launches (every launch site calls it; read through tg_launch_count()).
 void note_launch();
 

@@ -5,6 +5,7 @@
 // 8-bit digits, one tile of 4096 keys per CTA, ranks made stable by processing each warp's slice
 // in order with __match_any_sync, and per-(digit, tile) offsets from a digit-major scan.
 #include <cstdio>
+#include <mutex>
 
 #include "tg_common.cuh"
 
@@ -27,6 +28,36 @@ int num_sms() {
         if (sms <= 0) sms = 1;
     }
     return sms;
+}
+
+cudaError_t dev_malloc(void **p, size_t bytes, cudaStream_t s) {
+    constexpr int MAX_DEVICES = 64;
+    static std::mutex mu;
+    static cudaMemPool_t pools[MAX_DEVICES] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= MAX_DEVICES) return cudaMallocAsync(p, bytes, s);
+    cudaMemPool_t pool;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!pools[dev]) {
+            cudaMemPoolProps props = {};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            e = cudaMemPoolCreate(&pools[dev], &props);
+            if (e != cudaSuccess) {
+                pools[dev] = nullptr;
+                return e;
+            }
+            unsigned long long keep = TG_POOL_KEEP_BYTES;
+            e = cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+            if (e != cudaSuccess) return e;
+        }
+        pool = pools[dev];
+    }
+    return cudaMallocFromPoolAsync(p, bytes, pool, s);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -118,7 +149,7 @@ static tg_status exclusive_scan(const T *in, T *out, int64_t n, T *total_dev, cu
     }
     int64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
     T *sums = nullptr;
-    TG_CUDA(cudaMallocAsync((void **)&sums, sizeof(T) * nb, s));
+    TG_CUDA(tg::dev_malloc((void **)&sums, sizeof(T) * nb, s));
     { scan_block_sums<T><<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, sums); tg::note_launch(); }
     { scan_sums_single<T><<<1, SCAN_THREADS, 0, s>>>(sums, nb, total_dev); tg::note_launch(); }
     { scan_apply<T><<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, out, n, sums); tg::note_launch(); }
@@ -222,9 +253,9 @@ tg_status radix_sort_pairs(uint64_t *keys, uint32_t *vals, int64_t n, int bits, 
     uint64_t *k2 = nullptr;
     uint32_t *v2 = nullptr;
     int *hist = nullptr;
-    TG_CUDA(cudaMallocAsync((void **)&k2, sizeof(uint64_t) * n, s));
-    TG_CUDA(cudaMallocAsync((void **)&v2, sizeof(uint32_t) * n, s));
-    TG_CUDA(cudaMallocAsync((void **)&hist, sizeof(int) * (int64_t)RS_BINS * ntiles, s));
+    TG_CUDA(tg::dev_malloc((void **)&k2, sizeof(uint64_t) * n, s));
+    TG_CUDA(tg::dev_malloc((void **)&v2, sizeof(uint32_t) * n, s));
+    TG_CUDA(tg::dev_malloc((void **)&hist, sizeof(int) * (int64_t)RS_BINS * ntiles, s));
     uint64_t *kin = keys, *kout = k2;
     uint32_t *vin = vals, *vout = v2;
     for (int shift = 0; shift < bits; shift += 8) {

@@ -168,19 +168,19 @@ tg_status build_arena(tg_tree_s *t, Arena<T> &ar, cudaStream_t st) {
         set_last_error_msg("tree too large for the walk arena (2^27 nodes or particles)");
         return TG_ERR_BAD_ARG;
     }
-    TG_CUDA(cudaMallocAsync((void **)&ar.n_pos, sizeof(vec4<T>) * M, st));
-    TG_CUDA(cudaMallocAsync((void **)&ar.n_lo, sizeof(vec4<T>) * M, st));
-    TG_CUDA(cudaMallocAsync((void **)&ar.n_trav, sizeof(vec4<T>) * 2 * M, st));
-    TG_CUDA(cudaMallocAsync((void **)&ar.n_link, sizeof(int4) * M, st));
-    if (ar.has_quad) TG_CUDA(cudaMallocAsync((void **)&ar.n_quad, sizeof(vec4<T>) * 2 * M, st));
-    TG_CUDA(cudaMallocAsync((void **)&ar.l_pos, sizeof(vec4<T>) * N, st));
-    TG_CUDA(cudaMallocAsync((void **)&ar.l_lo, sizeof(vec4<T>) * N, st));
+    TG_CUDA(tg::dev_malloc((void **)&ar.n_pos, sizeof(vec4<T>) * M, st));
+    TG_CUDA(tg::dev_malloc((void **)&ar.n_lo, sizeof(vec4<T>) * M, st));
+    TG_CUDA(tg::dev_malloc((void **)&ar.n_trav, sizeof(vec4<T>) * 2 * M, st));
+    TG_CUDA(tg::dev_malloc((void **)&ar.n_link, sizeof(int4) * M, st));
+    if (ar.has_quad) TG_CUDA(tg::dev_malloc((void **)&ar.n_quad, sizeof(vec4<T>) * 2 * M, st));
+    TG_CUDA(tg::dev_malloc((void **)&ar.l_pos, sizeof(vec4<T>) * N, st));
+    TG_CUDA(tg::dev_malloc((void **)&ar.l_lo, sizeof(vec4<T>) * N, st));
     int64_t *nleaf = nullptr, *lstart = nullptr, *ltot = nullptr;
     int *bad = nullptr;
-    TG_CUDA(cudaMallocAsync((void **)&nleaf, sizeof(int64_t) * M, st));
-    TG_CUDA(cudaMallocAsync((void **)&lstart, sizeof(int64_t) * M, st));
-    TG_CUDA(cudaMallocAsync((void **)&ltot, sizeof(int64_t), st));
-    TG_CUDA(cudaMallocAsync((void **)&bad, sizeof(int), st));
+    TG_CUDA(tg::dev_malloc((void **)&nleaf, sizeof(int64_t) * M, st));
+    TG_CUDA(tg::dev_malloc((void **)&lstart, sizeof(int64_t) * M, st));
+    TG_CUDA(tg::dev_malloc((void **)&ltot, sizeof(int64_t), st));
+    TG_CUDA(tg::dev_malloc((void **)&bad, sizeof(int), st));
     TG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
     { k_arena_links<<<div_up(M, 256), 256, 0, st>>>(N, M, t->first, t->next, ar.n_link, nleaf, bad); tg::note_launch(); }
     TG_TRY(exclusive_scan_i64(nleaf, lstart, M, ltot, st));
@@ -944,9 +944,9 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
                    int quadrupole, double theta, double G, int group_size, int precision, const float *theta_group,
                    double *out, cudaStream_t st) {
     int w = ((fields & F_POT) ? 1 : 0) + ((fields & F_ACC) ? 3 : 0) + ((fields & F_TID) ? 9 : 0);
-    if (!t->stats_dev) TG_CUDA(cudaMalloc((void **)&t->stats_dev, sizeof(unsigned long long) * 8));
+    if (!t->stats_dev) TG_CUDA(tg::dev_malloc((void **)&t->stats_dev, sizeof(unsigned long long) * 8, st));
     int *scratch = nullptr;
-    TG_CUDA(cudaMallocAsync((void **)&scratch, sizeof(int) * 2, st));
+    TG_CUDA(tg::dev_malloc((void **)&scratch, sizeof(int) * 2, st));
     TG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int) * 2, st));
     TG_CUDA(cudaMemsetAsync(t->stats_dev, 0, sizeof(unsigned long long) * 8, st));
     tg_status rc = TG_OK;
@@ -964,8 +964,8 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         a.out_fields = fields; a.out_w = w; a.out = out; a.gs = group_size;
         a.queue = scratch; a.status = scratch + 1; a.stats = (unsigned long long *)t->stats_dev;
         vec4<double> *thi = nullptr, *tlo = nullptr;
-        TG_CUDA(cudaMallocAsync((void **)&thi, sizeof(vec4<double>) * std::max<int64_t>(ntargets, 1), st));
-        TG_CUDA(cudaMallocAsync((void **)&tlo, sizeof(vec4<double>) * std::max<int64_t>(ntargets, 1), st));
+        TG_CUDA(tg::dev_malloc((void **)&thi, sizeof(vec4<double>) * std::max<int64_t>(ntargets, 1), st));
+        TG_CUDA(tg::dev_malloc((void **)&tlo, sizeof(vec4<double>) * std::max<int64_t>(ntargets, 1), st));
         { k_prep_targets<double><<<div_up(ntargets, 256), 256, 0, st>>>(tpos, th, ntargets, thi, tlo); tg::note_launch(); }
         a.thi = thi;
         a.tlo = tlo;
@@ -984,8 +984,8 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         a.out_fields = fields; a.out_w = w; a.out = out; a.gs = group_size;
         a.queue = scratch; a.status = scratch + 1; a.stats = (unsigned long long *)t->stats_dev;
         vec4<float> *thi = nullptr, *tlo = nullptr;
-        TG_CUDA(cudaMallocAsync((void **)&thi, sizeof(vec4<float>) * std::max<int64_t>(ntargets, 1), st));
-        TG_CUDA(cudaMallocAsync((void **)&tlo, sizeof(vec4<float>) * std::max<int64_t>(ntargets, 1), st));
+        TG_CUDA(tg::dev_malloc((void **)&thi, sizeof(vec4<float>) * std::max<int64_t>(ntargets, 1), st));
+        TG_CUDA(tg::dev_malloc((void **)&tlo, sizeof(vec4<float>) * std::max<int64_t>(ntargets, 1), st));
         { k_prep_targets<float><<<div_up(ntargets, 256), 256, 0, st>>>(tpos, th, ntargets, thi, tlo); tg::note_launch(); }
         a.thi = thi;
         a.tlo = tlo;
@@ -1017,11 +1017,11 @@ tg_status make_tree_groups(tg_tree_s *t, int G, int2 **groups, int **group_root,
     unsigned long long *cnt = nullptr;
     int2 *g0 = nullptr;
     int *r0 = nullptr;
-    TG_CUDA(cudaMallocAsync((void **)&g0, sizeof(int2) * N, st));
-    TG_CUDA(cudaMallocAsync((void **)&r0, sizeof(int) * N, st));
-    TG_CUDA(cudaMallocAsync((void **)&cnt, sizeof(unsigned long long), st));
-    TG_CUDA(cudaMallocAsync((void **)&d_sys, sizeof(int64_t) * (t->nsys + 1), st));
-    TG_CUDA(cudaMallocAsync((void **)&d_node, sizeof(int64_t) * (t->nsys + 1), st));
+    TG_CUDA(tg::dev_malloc((void **)&g0, sizeof(int2) * N, st));
+    TG_CUDA(tg::dev_malloc((void **)&r0, sizeof(int) * N, st));
+    TG_CUDA(tg::dev_malloc((void **)&cnt, sizeof(unsigned long long), st));
+    TG_CUDA(tg::dev_malloc((void **)&d_sys, sizeof(int64_t) * (t->nsys + 1), st));
+    TG_CUDA(tg::dev_malloc((void **)&d_node, sizeof(int64_t) * (t->nsys + 1), st));
     TG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), st));
     TG_CUDA(cudaMemcpyAsync(d_sys, t->sys_off.data(), sizeof(int64_t) * (t->nsys + 1), cudaMemcpyHostToDevice, st));
     TG_CUDA(cudaMemcpyAsync(d_node, t->sys_node_off.data(), sizeof(int64_t) * (t->nsys + 1), cudaMemcpyHostToDevice,
@@ -1035,10 +1035,10 @@ tg_status make_tree_groups(tg_tree_s *t, int G, int2 **groups, int **group_root,
     // deterministic Morton order of the groups (their emission order depends on thread timing)
     uint64_t *keys = nullptr;
     uint32_t *vals = nullptr;
-    TG_CUDA(cudaMallocAsync((void **)&keys, sizeof(uint64_t) * ng, st));
-    TG_CUDA(cudaMallocAsync((void **)&vals, sizeof(uint32_t) * ng, st));
-    TG_CUDA(cudaMallocAsync((void **)groups, sizeof(int2) * std::max<unsigned long long>(ng, 1), st));
-    TG_CUDA(cudaMallocAsync((void **)group_root, sizeof(int) * std::max<unsigned long long>(ng, 1), st));
+    TG_CUDA(tg::dev_malloc((void **)&keys, sizeof(uint64_t) * ng, st));
+    TG_CUDA(tg::dev_malloc((void **)&vals, sizeof(uint32_t) * ng, st));
+    TG_CUDA(tg::dev_malloc((void **)groups, sizeof(int2) * std::max<unsigned long long>(ng, 1), st));
+    TG_CUDA(tg::dev_malloc((void **)group_root, sizeof(int) * std::max<unsigned long long>(ng, 1), st));
     { k_group_start_keys<<<div_up(ng, 256), 256, 0, st>>>(g0, ng, keys, vals); tg::note_launch(); }
     TG_TRY(radix_sort_pairs(keys, vals, ng, 32, st));
     { k_permute_groups<<<div_up(ng, 256), 256, 0, st>>>(vals, ng, g0, r0, *groups, *group_root); tg::note_launch(); }
@@ -1057,8 +1057,8 @@ tg_status make_tree_groups(tg_tree_s *t, int G, int2 **groups, int **group_root,
 // Largest-first queue order of consecutive-block groups (see k_group_cost_keys).
 tg_status make_cost_order(const double *tpos, const int2 *groups, int64_t ngroups, int **order, cudaStream_t st) {
     uint64_t *keys = nullptr;
-    TG_CUDA(cudaMallocAsync((void **)&keys, sizeof(uint64_t) * std::max<int64_t>(ngroups, 1), st));
-    TG_CUDA(cudaMallocAsync((void **)order, sizeof(int) * std::max<int64_t>(ngroups, 1), st));
+    TG_CUDA(tg::dev_malloc((void **)&keys, sizeof(uint64_t) * std::max<int64_t>(ngroups, 1), st));
+    TG_CUDA(tg::dev_malloc((void **)order, sizeof(int) * std::max<int64_t>(ngroups, 1), st));
     { k_group_cost_keys<<<div_up(ngroups, 256), 256, 0, st>>>(tpos, groups, ngroups, keys, (uint32_t *)*order); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
     TG_TRY(radix_sort_pairs(keys, (uint32_t *)*order, ngroups, 32, st));
@@ -1078,11 +1078,11 @@ tg_status make_groups(tg_tree_s *t, const std::vector<int64_t> &sys_off_host, in
     *ngroups = goff[nsys];
     int64_t *d_sys = nullptr, *d_goff = nullptr;
     int *d_roots = nullptr;
-    TG_CUDA(cudaMallocAsync((void **)groups, sizeof(int2) * std::max<int64_t>(*ngroups, 1), st));
-    TG_CUDA(cudaMallocAsync((void **)group_root, sizeof(int) * std::max<int64_t>(*ngroups, 1), st));
-    TG_CUDA(cudaMallocAsync((void **)&d_sys, sizeof(int64_t) * (nsys + 1), st));
-    TG_CUDA(cudaMallocAsync((void **)&d_goff, sizeof(int64_t) * (nsys + 1), st));
-    TG_CUDA(cudaMallocAsync((void **)&d_roots, sizeof(int) * nsys, st));
+    TG_CUDA(tg::dev_malloc((void **)groups, sizeof(int2) * std::max<int64_t>(*ngroups, 1), st));
+    TG_CUDA(tg::dev_malloc((void **)group_root, sizeof(int) * std::max<int64_t>(*ngroups, 1), st));
+    TG_CUDA(tg::dev_malloc((void **)&d_sys, sizeof(int64_t) * (nsys + 1), st));
+    TG_CUDA(tg::dev_malloc((void **)&d_goff, sizeof(int64_t) * (nsys + 1), st));
+    TG_CUDA(tg::dev_malloc((void **)&d_roots, sizeof(int) * nsys, st));
     TG_CUDA(cudaMemcpyAsync(d_sys, sys_off_host.data(), sizeof(int64_t) * (nsys + 1), cudaMemcpyHostToDevice, st));
     TG_CUDA(cudaMemcpyAsync(d_goff, goff.data(), sizeof(int64_t) * (nsys + 1), cudaMemcpyHostToDevice, st));
     TG_CUDA(cudaMemcpyAsync(d_roots, roots.data(), sizeof(int) * nsys, cudaMemcpyHostToDevice, st));
