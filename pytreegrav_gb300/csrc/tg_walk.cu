@@ -11,7 +11,9 @@
 //
 // Evaluation: every 32 list entries are staged in shared memory as offsets from a group reference
 // point (hi/lo float pairs keep near-field offsets exact to FP32 rounding) and swept by all lanes:
-// lane = (target, slice), each slice takes every (32/group_size)-th source. Sources that cannot be
+// lane = (target, slice): a group of n targets takes P lanes per slice, P the smallest power of two
+// >= n (at most group_size), and each of the 32/P slices sweeps its own share of every batch, so
+// small groups keep the warp busy. Sources that cannot be
 // within any target's softening length (checked once per source against the group box) take the
 // point-mass path; the rest take the full softened path. Each lane sums a batch in registers and
 // adds the batch total into a Kahan-compensated accumulator.
@@ -400,10 +402,6 @@ __global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2)
     WarpSmem<T, QUAD, STACK> &sm = reinterpret_cast<WarpSmem<T, QUAD, STACK> *>(smem_raw)[threadIdx.x >> 5];
     const int lane = lane_id();
     const unsigned lt = lanemask_lt();
-    const int GS = a.gs;
-    const int tl = lane % GS;     // target of this lane within the group
-    const int slice = lane / GS;  // which interleaved share of each batch this lane sums
-    const int NSL = 32 / GS;
     unsigned long long n_int = 0, n_tests = 0, n_steps = 0, n_qint = 0;
     int max_sp = 0;
 
@@ -414,6 +412,12 @@ __global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2)
         if (g >= a.ngroups) break;
         if (a.group_order) g = a.group_order[g];
         const int2 gr = a.groups[g];
+        // lanes per target slot: the smallest power of two holding the group (at most a.gs); the
+        // other lanes of the warp take interleaved shares of every source batch
+        int GS = a.gs;
+        while (GS > 1 && (GS >> 1) >= gr.y) GS >>= 1;
+        const int tl = lane & (GS - 1);  // target of this lane within the group
+        const int slice = lane / GS;     // which share of each batch this lane sums
         const bool valid = tl < gr.y;
         const int64_t t = gr.x + (valid ? tl : 0);
         const vec4<T> thv = a.thi[t], tlv = a.tlo[t];
