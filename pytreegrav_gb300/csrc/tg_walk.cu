@@ -354,6 +354,24 @@ __device__ __forceinline__ void quad_terms(const T *q, T dx, T dy, T dz, T rinv,
     }
 }
 
+// Acceleration of an accepted node, monopole and quadrupole together (the sum of point_mass and
+// quad_terms for F_ACC): a += dx (m r^-3 + 2.5 A r^-7) - (Q dx) r^-5, with A = dx.Q.dx.
+template <typename T>
+__device__ __forceinline__ void acc_mono_quad(T m, const T *q, T dx, T dy, T dz, T rinv, Acc<T> &p) {
+    T rinv2 = rinv * rinv;
+    T r3inv = rinv * rinv2;
+    T r5inv = r3inv * rinv2;
+    T r7inv = r5inv * rinv2;
+    T qdx = q[0] * dx + q[1] * dy + q[2] * dz;
+    T qdy = q[1] * dx + q[3] * dy + q[4] * dz;
+    T qdz = q[2] * dx + q[4] * dy + q[5] * dz;
+    T A = dx * qdx + dy * qdy + dz * qdz;
+    T sc = fma(T(2.5) * A, r7inv, m * r3inv);
+    p.v[1] = fma(-qdx, r5inv, fma(sc, dx, p.v[1]));
+    p.v[2] = fma(-qdy, r5inv, fma(sc, dy, p.v[2]));
+    p.v[3] = fma(-qdz, r5inv, fma(sc, dz, p.v[3]));
+}
+
 template <int FIELDS>
 __device__ __forceinline__ constexpr bool comp(int c) {
     return c == 0 ? (FIELDS & F_POT) : (c <= 3 ? (FIELDS & F_ACC) : (FIELDS & F_TID));
@@ -565,8 +583,12 @@ __global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2)
                 T qv[6] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y};
                 T dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
                 T rinv = rsqrt_t(dx * dx + dy * dy + dz * dz);
-                point_mass<T, FIELDS>(s.w, dx, dy, dz, rinv, b);
-                quad_terms<T, FIELDS>(qv, dx, dy, dz, rinv, b);
+                if (FIELDS == F_ACC) {
+                    acc_mono_quad(s.w, qv, dx, dy, dz, rinv, b);
+                } else {
+                    point_mass<T, FIELDS>(s.w, dx, dy, dz, rinv, b);
+                    quad_terms<T, FIELDS>(qv, dx, dy, dz, rinv, b);
+                }
             }
             __syncwarp();
             kahan_add<T, FIELDS>(S, C, b);
