@@ -135,15 +135,20 @@ def _bind(L):
     return L
 
 
-def gpu_step(L, _lib, dpos, dm, dh, out, n, stream):
-    """One step on device-resident arrays: build + FP32 quadrupole Accel walk (tree grouping)."""
+def gpu_step(L, _lib, dpos, dm, dh, out, n, stream, model=None, log10_lambda=0.0):
+    """One step on device-resident arrays: build + FP32 quadrupole Accel walk (tree grouping), with
+    the learned acceptance test when `model` (a library model handle) is given, else plain theta."""
     vp = ctypes.c_void_p
     h = vp()
     rc = L.tg_tree_build(vp(dpos.data_ptr()), vp(dm.data_ptr()), vp(dh.data_ptr()), n, 1, 1, _lib.TG_MEM_DEVICE,
                          vp(stream), ctypes.byref(h))
     _lib.check(rc, "build")
-    rc = L.tg_tree_fields(h, None, None, n, _lib.TG_FIELD_ACCEL, 1, THETA, 1.0, GROUP, _lib.TG_GROUP_TREE,
-                          _lib.TG_ORDER_TREE, _lib.TG_FP32, None, _lib.TG_MEM_DEVICE, vp(out.data_ptr()), vp(stream))
+    if model is not None:
+        rc = L.tg_tree_fields_learned(h, _lib.TG_FIELD_ACCEL, 1, 1.0, GROUP, model, float(log10_lambda), THETA,
+                                      _lib.TG_MEM_DEVICE, vp(out.data_ptr()), vp(stream))
+    else:
+        rc = L.tg_tree_fields(h, None, None, n, _lib.TG_FIELD_ACCEL, 1, THETA, 1.0, GROUP, _lib.TG_GROUP_TREE,
+                              _lib.TG_ORDER_TREE, _lib.TG_FP32, None, _lib.TG_MEM_DEVICE, vp(out.data_ptr()), vp(stream))
     _lib.check(rc, "walk")
     v = [ctypes.c_int64() for _ in range(4)]
     L.tg_tree_last_walk_stats(h, *[ctypes.byref(x) for x in v])
@@ -198,52 +203,67 @@ def run_ours(args):
     dm = torch.from_numpy(m).cuda()
     dh = torch.from_numpy(h).cuda()
     out = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    out_plain = torch.empty((n, 3), dtype=torch.float64, device="cuda")
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2 (129 MB)
+    from pytreegrav_gb300 import theta as th
 
-    for _ in range(args.warmup):
-        gpu_step(L, _lib, dpos, dm, dh, out, n, stream)
-    torch.cuda.synchronize()
+    model = th.ThetaModel.load()
+    mh = model.handle()
+    l10 = th.default_lambda(model, True)
 
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    stats = []
+    def timed(step_fn, dest, count_launches=False):
+        for _ in range(args.warmup):
+            step_fn(dest)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        stats = []
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        l0 = L.tg_launch_count()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.zero_()  # evict the previous step's data from L2 (outside the step events)
+            ev[k][0].record()
+            stats.append(step_fn(dest))
+            ev[k][1].record()
+        torch.cuda.synchronize()
+        region = time.perf_counter() - t0
+        if dist:
+            dist.barrier()
+        ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+        if dist:
+            tt = torch.tensor([ms], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            ms = float(tt.item())
+        return ms, stats, region, L.tg_launch_count() - l0
+
+    learned_step = lambda dest: gpu_step(L, _lib, dpos, dm, dh, dest, n, stream, mh, l10)
+    plain_step = lambda dest: gpu_step(L, _lib, dpos, dm, dh, dest, n, stream)
     clocks = ClockSampler(local)
     clocks.start()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    launches0 = L.tg_launch_count()
-    t_region = time.perf_counter()
-    for k in range(args.steps):
-        flush.zero_()  # evict the previous step's data from L2 (outside the step events)
-        ev[k][0].record()
-        stats.append(gpu_step(L, _lib, dpos, dm, dh, out, n, stream))
-        ev[k][1].record()
-    torch.cuda.synchronize()
-    t_region = time.perf_counter() - t_region
-    if dist:
-        dist.barrier()
-    launches = L.tg_launch_count() - launches0
+    ms, stats, t_region, launches = timed(learned_step, out)
     clk = clocks.stop()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    ms = statistics.mean(step_ms)
-    if dist:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms_plain, stats_plain, _, _ = timed(plain_step, out_plain)
     value = n * ws / (ms * 1e-3)
     if rank != 0:
         return None
 
-    # accuracy of the timed configuration against FP64 direct summation on 1e4 sampled targets
+    # accuracy of both walks against FP64 direct summation on the same 1e4 sampled targets
     import pytreegrav_gb300 as tg
 
-    acc = out.cpu().numpy()
     rng = np.random.default_rng(7)
     samp = rng.choice(n, 10_000, replace=False)
     ref = tg.bruteforce(x[samp], h[samp], x, m, h, accel=True, precision="fp64")["accel"]
-    err = acc[samp] - ref
-    rms_err = float(np.sqrt(np.mean(np.sum(err**2, 1))) / np.sqrt(np.mean(np.sum(ref**2, 1))))
-    max_err = float(np.max(np.sqrt(np.sum(err**2, 1))) / np.sqrt(np.mean(np.sum(ref**2, 1))))
+    rms_ref = np.sqrt(np.mean(np.sum(ref**2, 1)))
+
+    def accuracy(o):
+        err = o.cpu().numpy()[samp] - ref
+        return {"rms_rel_vs_fp64_bruteforce": float(np.sqrt(np.mean(np.sum(err**2, 1))) / rms_ref),
+                "max_rel_vs_fp64_bruteforce": float(np.max(np.sqrt(np.sum(err**2, 1))) / rms_ref),
+                "sample_targets": len(samp)}
+
+    acc_learned, acc_plain = accuracy(out), accuracy(out_plain)
 
     # roofline of the dominant kernel (the walk): algorithmic FP32 flops / its own device time
     st = stats[-1]
@@ -258,6 +278,20 @@ def run_ours(args):
                                "has no FP32 CUDA-core figure",
                 "kernel_ms": round(walk_ms, 4), "flops_per_launch": flops,
                 "interactions_per_s": round(st["interactions"] / (walk_ms * 1e-3), 1)}
+    sp = stats_plain[-1]
+    walk_ms_plain = statistics.mean(s["kernel_ms"] for s in stats_plain)
+    flops_plain = (FLOPS_MONO_ACC * (sp["interactions"] - sp["quad_interactions"])
+                   + FLOPS_QUAD_ACC * sp["quad_interactions"])
+    plain = {"value": round(n / (ms_plain * 1e-3), 1), "ms_per_step": round(ms_plain, 4),
+             "walk_kernel_ms": round(walk_ms_plain, 4), "walk_particles_per_s": round(n / (walk_ms_plain * 1e-3), 1),
+             "interactions_per_target": sp["interactions"] / n, "accuracy": acc_plain,
+             "walk_frac_of_fp32_peak": round(flops_plain / (walk_ms_plain * 1e-3) / 1e12 / peak_tf.value, 4)}
+    learned = {"walk_kernel_ms": round(walk_ms, 4), "walk_particles_per_s": round(n / (walk_ms * 1e-3), 1),
+               "walk_speedup_vs_plain": round(walk_ms_plain / walk_ms, 3),
+               "step_speedup_vs_plain": round(ms_plain / ms, 3),
+               "error_ratio_vs_plain": round(acc_learned["rms_rel_vs_fp64_bruteforce"]
+                                             / acc_plain["rms_rel_vs_fp64_bruteforce"], 3),
+               "log10_lambda": l10, "model": os.path.relpath(th.DEFAULT_MODEL, ROOT), "theta_cap": model.theta_max}
 
     # end to end through the public API, inputs in pinned host memory, result read back
     pin_x = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
@@ -266,7 +300,7 @@ def run_ours(args):
     pin_x.numpy()[:] = x
     pin_m.numpy()[:] = m
     pin_h.numpy()[:] = h
-    kw = dict(theta=THETA, method="tree", quadrupole=True, group_size=GROUP, grouping="tree")
+    kw = dict(theta=THETA, method="tree", quadrupole=True, learned=True)
     for _ in range(2):
         tg.Accel(pin_x.numpy(), pin_m.numpy(), pin_h.numpy(), **kw)
     e2e_t = []
@@ -278,7 +312,7 @@ def run_ours(args):
         e2e_t.append(time.perf_counter() - t0)
     e2e = {"value": n / statistics.median(e2e_t), "unit": UNIT, "h2d_bytes_per_step": int(x.nbytes + m.nbytes + h.nbytes),
            "d2h_bytes_per_step": int(a.nbytes), "api": "pytreegrav_gb300.Accel(pos, m, h, theta=0.7, quadrupole=True, "
-           "method='tree', group_size=32, grouping='tree')", "ms_per_step": round(1e3 * statistics.median(e2e_t), 3)}
+           "method='tree', learned=True)", "ms_per_step": round(1e3 * statistics.median(e2e_t), 3)}
 
     base = cpu_baseline(x, m, h, os.cpu_count() or 1)
     return {
@@ -287,12 +321,14 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Plummer sphere, a=1, r<50)",
         "config": {"workload": f"Accel, N={n} Plummer (m=1/N, h={SOFT}), theta={THETA}, quadrupole, FP32 walk with FP64 "
                                f"tree build and moments, tree grouping <= {GROUP} targets/warp",
-                   "variant": "plain global-theta walk (the learned-theta walk is not built yet)",
-                   "step": "octree build + Accel walk, inputs resident in HBM",
+                   "variant": "learned: each group's acceptance test from the packaged 16-64-64-1 network (a "
+                              "mass-aware tolerance per group, angle cap 1.2, calibrated lambda); the plain "
+                              "theta=0.7 walk is timed the same way under 'plain'",
+                   "step": "octree build + learned Accel walk (features, BF16 inference, walk), inputs resident "
+                           "in HBM",
                    "l2": "flushed between timed steps (256 MiB write, outside the step events)",
                    "parallelism": f"replicas x{ws}", "region_s": round(t_region, 4)},
-        "accuracy": {"rms_rel_vs_fp64_bruteforce": rms_err, "max_rel_vs_fp64_bruteforce": max_err,
-                     "sample_targets": 10_000},
+        "accuracy": acc_learned, "learned": learned, "plain": plain,
         "walk": {"interactions_per_target": st["interactions"] / n, "node_tests": st["node_tests"],
                  "groups": st["groups"], "quad_interactions": st["quad_interactions"]},
         "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,

@@ -52,6 +52,31 @@ EXPORTS = [
     "tg_bruteforce",
 ]
 
+# every extern "C" symbol declared in include/pytreegrav_gb300_theta.h
+THETA_EXPORTS = [
+    "tg_tree_groups",
+    "tg_tree_groups_copy",
+    "tg_tree_record_group_stats",
+    "tg_tree_last_group_stats",
+    "tg_theta_features",
+    "tg_mlp_forward",
+    "tg_mlp_backward",
+    "tg_adam_step",
+    "tg_theta_loss",
+    "tg_theta_tolerances",
+    "tg_theta_model_create",
+    "tg_theta_model_free",
+    "tg_theta_infer",
+    "tg_tree_fields_grouped",
+    "tg_tree_fields_learned",
+]
+TG_THETA_NFEAT = 16
+TG_MLP_H = 64
+TG_MLP_NPARAM = TG_MLP_H * TG_THETA_NFEAT + TG_MLP_H + TG_MLP_H * TG_MLP_H + TG_MLP_H + TG_MLP_H + 1
+TG_THETA_FEAT_LAMBDA = 13
+TG_THETA_KIND_ANGLE = 0
+TG_THETA_KIND_TOLERANCE = 1
+
 
 class TreeInfo(ctypes.Structure):
     _fields_ = [
@@ -98,6 +123,24 @@ def _declare(L):
     L.tg_morton_order_noalloc.argtypes = [vp, i64, vp, vp]
     L.tg_bruteforce.argtypes = [vp, vp, i64, vp, vp, vp, i64, ci, ci, dbl, ci, ci, vp, vp]
     for name in EXPORTS[1:]:
+        getattr(L, name).restype = ci
+    flt = ctypes.c_float
+    L.tg_tree_groups.argtypes = [vp, ci, vp, vp]
+    L.tg_tree_groups_copy.argtypes = [vp, ci, vp, vp, vp, ci, vp]
+    L.tg_tree_record_group_stats.argtypes = [vp, ci]
+    L.tg_tree_last_group_stats.argtypes = [vp, vp, ci, vp]
+    L.tg_theta_features.argtypes = [vp, ci, ci, vp, vp]
+    L.tg_mlp_forward.argtypes = [vp, vp, i64, vp, vp, vp]
+    L.tg_mlp_backward.argtypes = [vp, vp, vp, vp, i64, vp, vp, vp]
+    L.tg_adam_step.argtypes = [vp, vp, vp, vp, i64, flt, flt, flt, flt, ci, vp]
+    L.tg_theta_loss.argtypes = [vp, vp, vp, vp, i64, ci, flt, flt, flt, flt, vp, vp, vp]
+    L.tg_theta_tolerances.argtypes = [vp, ci, ci, vp, vp, vp]
+    L.tg_theta_model_create.argtypes = [vp, vp, vp, ci, flt, flt, flt, ci, ctypes.POINTER(vp)]
+    L.tg_theta_model_free.argtypes = [vp]
+    L.tg_theta_infer.argtypes = [vp, vp, i64, flt, vp, vp]
+    L.tg_tree_fields_grouped.argtypes = [vp, ci, ci, dbl, ci, dbl, vp, vp, ci, vp, vp]
+    L.tg_tree_fields_learned.argtypes = [vp, ci, ci, dbl, ci, vp, flt, dbl, ci, vp, vp]
+    for name in THETA_EXPORTS:
         getattr(L, name).restype = ci
 
 

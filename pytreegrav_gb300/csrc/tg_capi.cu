@@ -17,11 +17,10 @@ void free_arena(Arena<T> &ar, cudaStream_t st);
 tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t ntargets, const int2 *groups,
                    const int *group_root, const int *group_order, int64_t ngroups, const int64_t *scatter, int fields,
                    int quadrupole, double theta, double G, int group_size, int precision, const float *theta_group,
-                   double *out, cudaStream_t st);
+                   const float *tol_group, double *out, cudaStream_t st);
 tg_status make_groups(tg_tree_s *t, const std::vector<int64_t> &sys_off_host, int gs, int2 **groups,
                       int **group_root, int64_t *ngroups, cudaStream_t st);
-tg_status make_tree_groups(tg_tree_s *t, int G, int2 **groups, int **group_root, int64_t *ngroups,
-                           cudaStream_t st);
+tg_status tree_groups(tg_tree_s *t, int G, cudaStream_t st);
 tg_status make_cost_order(const double *tpos, const int2 *groups, int64_t ngroups, int **order, cudaStream_t st);
 tg_status run_bruteforce(const double *pt, const double *ht, int64_t nt, const double *ps, const double *ms,
                          const double *hs, int64_t ns, int fields, int mutual, double G, int precision, double *out,
@@ -100,6 +99,7 @@ void destroy(tg_tree_s *t) {
     free_arena(t->arena32, st);
     free_arena(t->arena64, st);
     if (t->stats_dev) cudaFreeAsync(t->stats_dev, st);
+    f(t->groups); f(t->group_root); f(t->group_node); f(t->gstats);
     delete t;
 }
 
@@ -243,16 +243,23 @@ tg_status tg_tree_fields(tg_tree t, const double *pos, const double *h, int64_t 
     tg_status rc = TG_OK;
     if (order == TG_ORDER_TREE) {
         nt = t->ntot;
-        if (grouping == TG_GROUP_TREE) {
-            TG_TRY(make_tree_groups(t, group_size, &groups, &groot, &ngroups, st));
+        const int2 *wg = nullptr;
+        const int *wr = nullptr;
+        if (grouping == TG_GROUP_TREE) {  // kept on the tree, not freed here
+            TG_TRY(tree_groups(t, group_size, st));
+            wg = t->groups;
+            wr = t->group_root;
+            ngroups = t->ngroups;
         } else {
             TG_TRY(make_groups(t, t->sys_off, group_size, &groups, &groot, &ngroups, st));
             TG_TRY(make_cost_order(t->coord, groups, ngroups, &gorder, st));
+            wg = groups;
+            wr = groot;
         }
         if (mem == TG_MEM_HOST) TG_CUDA(tg::dev_malloc((void **)&dout, sizeof(double) * nt * W, st));
         else dout = out;
-        rc = run_walk(t, t->coord, t->soft, nt, groups, groot, gorder, ngroups, t->walk_idx, fields, quadrupole, theta,
-                      G, group_size, precision, theta_per_group, dout, st);
+        rc = run_walk(t, t->coord, t->soft, nt, wg, wr, gorder, ngroups, t->walk_idx, fields, quadrupole, theta,
+                      G, group_size, precision, theta_per_group, nullptr, dout, st);
     } else if (order == TG_ORDER_MORTON || order == TG_ORDER_GIVEN) {
         if (t->nsys != 1 || !pos || n < 1) return TG_ERR_BAD_ARG;
         nt = n;
@@ -286,7 +293,7 @@ tg_status tg_tree_fields(tg_tree t, const double *pos, const double *h, int64_t 
         if (mem == TG_MEM_HOST) TG_CUDA(tg::dev_malloc((void **)&dout, sizeof(double) * nt * W, st));
         else dout = out;
         rc = run_walk(t, sp ? sp : dp.ptr, sh, nt, groups, groot, gorder, ngroups, scatter, fields, quadrupole, theta, G,
-                      group_size, precision, theta_per_group, dout, st);
+                      group_size, precision, theta_per_group, nullptr, dout, st);
         if (sp) cudaFreeAsync(sp, st);
         if (sh) cudaFreeAsync(sh, st);
         if (scatter) cudaFreeAsync(scatter, st);

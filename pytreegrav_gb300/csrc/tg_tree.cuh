@@ -75,4 +75,18 @@ struct tg_tree_s {
     tg::Arena<double> arena64;
     tg::WalkStats last_stats;
     int64_t *stats_dev = nullptr;  // 8 counters
+
+    // Tree grouping (TG_GROUP_TREE, TG_ORDER_TREE) at group size groups_G, made on first use and
+    // kept: groups as (first target, count) in start order, each group's system root and the node
+    // whose subtree holds it.
+    int groups_G = 0;
+    int64_t ngroups = 0;
+    int2 *groups = nullptr;
+    int *group_root = nullptr;
+    int *group_node = nullptr;
+    // Per-group walk counters, three per group (list entries evaluated as point masses, entries
+    // evaluated as quadrupole nodes, nodes tested), written by walks while record_group_stats is set.
+    int record_group_stats = 0;
+    unsigned *gstats = nullptr;
+    int64_t gstats_n = 0;
 };

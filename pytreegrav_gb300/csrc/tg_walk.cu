@@ -242,6 +242,10 @@ struct WalkArgs {
     int64_t ngroups;
     double theta;
     const float *theta_group;
+    // per group error tolerance (null or <= 0: pytreegrav's geometric criterion). A group with a
+    // tolerance tau accepts a node once r exceeds both s/theta and (M s^p / tau)^(1/(p+2)) (plus
+    // delta), p = 3 with quadrupoles and 2 without: the size of the first neglected multipole term.
+    const float *tol_group;
     double G;
     int out_fields;  // requested fields (bits) -> output packing
     int out_w;
@@ -250,6 +254,7 @@ struct WalkArgs {
     int *queue;
     int *status;
     unsigned long long *stats;  // interactions, node tests, max stack, steps, quadrupole-node interactions
+    unsigned *gstats;           // per group (3): point-mass entries, quadrupole entries, nodes tested; or null
 };
 
 template <typename T, bool QUAD, int STACK>
@@ -394,6 +399,9 @@ __device__ __forceinline__ void kahan_add(Acc<T> &S, Acc<T> &C, const Acc<T> &b)
     }
 }
 
+__device__ __forceinline__ float pow_fifth(float q) { return q > 0.f ? __powf(q, 0.2f) : 0.f; }
+__device__ __forceinline__ double pow_fifth(double q) { return q > 0.0 ? pow(q, 0.2) : 0.0; }
+
 // Exact FP64 acceptance, the expression of treewalk.py:22-25 on the group box r_min
 // (grouped_treewalk.py:209-231), each operation rounded once.
 __device__ __forceinline__ bool accept_exact(int64_t f, const double *tc, const double *ts, const double *tsize,
@@ -482,6 +490,9 @@ __global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2)
         const T gscale = fabs(abmin[0]) + fabs(abmin[1]) + fabs(abmin[2]) + fabs(abmax[0]) + fabs(abmax[1]) +
                          fabs(abmax[2]);
         const T inv_theta = (T)(1.0 / theta);
+        const float tolg = a.tol_group ? a.tol_group[g] : 0.f;
+        const bool mass_aware = tolg > 0.f;  // warp-uniform
+        const T inv_tol = mass_aware ? (T)(1.0 / (double)tolg) : T(0);
         const T rel_eps = sizeof(T) == 4 ? T(1e-5) : T(0);
         const T abs_eps = sizeof(T) == 4 ? T(1e-6) : T(0);
         // softening-path threshold: a source whose squared distance to the box exceeds this cannot
@@ -596,6 +607,7 @@ __global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2)
             n_qint += (unsigned long long)cnt * (unsigned long long)gr.y;
         };
 
+        unsigned g_mono = 0, g_quad = 0, g_tests = 0;  // this group's counters (warp-uniform)
         int sp = 1, ni = 0, nn = 0;
         if (lane == 0) sm.stack[0] = a.group_root[g];
         __syncwarp();
@@ -610,6 +622,7 @@ __global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2)
             if (sp > 0) {
                 n_steps++;
                 const int cnt = min(sp, 32);
+                g_tests += cnt;
                 const int node = lane < cnt ? sm.stack[sp - 1 - lane] : -1;
                 sp -= cnt;
                 bool acc = false, unsure = false;
@@ -624,12 +637,18 @@ __global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2)
                     T r2 = dx * dx + dy * dy + dz * dz;
                     T h = r1.y > hmax_g ? r1.y : hmax_g;
                     T c1 = p.w * inv_theta + r1.x, c2 = h + T(0.6) * p.w + r1.x;
+                    if (mass_aware) {
+                        const T q = a.ar.n_pos[node].w * (QUAD ? p.w * p.w * p.w : p.w * p.w) * inv_tol;
+                        const T rc = QUAD ? pow_fifth(q) : sqrt(sqrt(q));
+                        c1 = fmax(p.w * inv_theta, rc) + r1.x;
+                    }
                     T crit = c1 > c2 ? c1 : c2;
                     // FP32 error bound: node positions near the boundary are within gscale + 2 crit of
                     // the origin, so the relative term covers their rounding
                     T tol = rel_eps * crit + abs_eps * gscale;
                     T hiq = crit + tol, loq = crit - tol;
-                    if (sizeof(T) == 8) unsure = true;
+                    if (mass_aware) acc = r2 > crit * crit;  // no pytreegrav decision to reproduce
+                    else if (sizeof(T) == 8) unsure = true;
                     else if (r2 > hiq * hiq) acc = true;
                     else if (loq > T(0) && r2 < loq * loq) acc = false;
                     else unsure = true;
@@ -669,11 +688,13 @@ __global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2)
             while (ni >= 32) {
                 eval_batch(sm.ilist + ni - 32, 32);
                 ni -= 32;
+                g_mono += 32;
             }
             if (QUAD) {
                 while (nn >= 32) {
                     eval_nodes(sm.nlist + nn - 32, 32);
                     nn -= 32;
+                    g_quad += 32;
                 }
             }
             if (sp == 0) break;
@@ -685,6 +706,13 @@ __global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2)
         }
         if (ni > 0) eval_batch(sm.ilist, ni);
         if (QUAD && nn > 0) eval_nodes(sm.nlist, nn);
+        g_mono += ni;
+        g_quad += QUAD ? nn : 0;
+        if (a.gstats && lane == 0) {
+            a.gstats[3 * g] = g_mono;
+            a.gstats[3 * g + 1] = g_quad;
+            a.gstats[3 * g + 2] = g_tests;
+        }
 
         // combine the slices of each target and write G * field in the caller's order
 #pragma unroll
@@ -751,7 +779,7 @@ __global__ void k_make_groups(const int64_t *sys_off, int nsys, int gs, const in
 __global__ void k_tree_groups(int64_t ntot, int64_t mtot, const int2 *node_range, const double *cell,
                               const double *size, const double *coord, const int64_t *first, const int64_t *next,
                               const int64_t *parent, int G, const int64_t *sys_off, const int64_t *sys_node_off,
-                              int nsys, int2 *groups, int *group_root, unsigned long long *count) {
+                              int nsys, int2 *groups, int *group_root, int *group_node, unsigned long long *count) {
     int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= mtot) return;
     const int2 r = node_range[j];
@@ -767,10 +795,11 @@ __global__ void k_tree_groups(int64_t ntot, int64_t mtot, const int2 *node_range
         s = lo;
     }
     const int root = (int)sys_node_off[s];
-    auto emit = [&](int lo, int cnt) {
+    auto emit = [&](int lo, int cnt) {  // a group inside node j's subtree
         unsigned long long q = atomicAdd(count, 1ull);
         groups[q] = make_int2(lo, cnt);
         group_root[q] = root;
+        group_node[q] = (int)j;
     };
     if (r.y - r.x <= G) {
         if (parent[f] < 0) emit(r.x, r.y - r.x);
@@ -875,12 +904,13 @@ __global__ void k_group_start_keys(const int2 *groups, int64_t ngroups, uint64_t
     keys[g] = (uint32_t)groups[g].x;
     vals[g] = (uint32_t)g;
 }
-__global__ void k_permute_groups(const uint32_t *perm, int64_t ngroups, const int2 *gin, const int *rin, int2 *gout,
-                                 int *rout) {
+__global__ void k_permute_groups(const uint32_t *perm, int64_t ngroups, const int2 *gin, const int *rin, const int *nin,
+                                 int2 *gout, int *rout, int *nout) {
     int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= ngroups) return;
     gout[g] = gin[perm[g]];
     rout[g] = rin[perm[g]];
+    if (nin) nout[g] = nin[perm[g]];
 }
 
 // Targets in walk order split once per walk into hi/lo parts in the walk precision.
@@ -968,7 +998,7 @@ static tg_status walk_with_fallback(WalkArgs<T> &a, int fields, bool quad, int *
 tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t ntargets, const int2 *groups,
                    const int *group_root, const int *group_order, int64_t ngroups, const int64_t *scatter, int fields,
                    int quadrupole, double theta, double G, int group_size, int precision, const float *theta_group,
-                   double *out, cudaStream_t st) {
+                   const float *tol_group, double *out, cudaStream_t st) {
     int w = ((fields & F_POT) ? 1 : 0) + ((fields & F_ACC) ? 3 : 0) + ((fields & F_TID) ? 9 : 0);
     if (!t->stats_dev) TG_CUDA(tg::dev_malloc((void **)&t->stats_dev, sizeof(unsigned long long) * 8, st));
     int *scratch = nullptr;
@@ -978,6 +1008,18 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
     tg_status rc = TG_OK;
     int status = 0;
     float kms = 0.f;
+    unsigned *gstats = nullptr;
+    if (t->record_group_stats) {
+        if (t->gstats_n < ngroups) {
+            if (t->gstats) cudaFreeAsync(t->gstats, st);
+            t->gstats = nullptr;
+            t->gstats_n = 0;
+            TG_CUDA(tg::dev_malloc((void **)&t->gstats, sizeof(unsigned) * 3 * std::max<int64_t>(ngroups, 1), st));
+            t->gstats_n = ngroups;
+        }
+        TG_CUDA(cudaMemsetAsync(t->gstats, 0, sizeof(unsigned) * 3 * std::max<int64_t>(ngroups, 1), st));
+        gstats = t->gstats;
+    }
     if (precision == TG_FP64) {
         TG_TRY(build_arena(t, t->arena64, st));
         WalkArgs<double> a;
@@ -986,9 +1028,10 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         a.tc = t->coord; a.ts = t->soft; a.tsize = t->size; a.tdelta = t->delta;
         a.tpos = tpos; a.th = th; a.scatter = scatter; a.groups = groups; a.group_root = group_root;
         a.group_order = group_order;
-        a.ngroups = ngroups; a.theta = theta; a.theta_group = theta_group; a.G = G;
+        a.ngroups = ngroups; a.theta = theta; a.theta_group = theta_group; a.tol_group = tol_group; a.G = G;
         a.out_fields = fields; a.out_w = w; a.out = out; a.gs = group_size;
         a.queue = scratch; a.status = scratch + 1; a.stats = (unsigned long long *)t->stats_dev;
+        a.gstats = gstats;
         vec4<double> *thi = nullptr, *tlo = nullptr;
         TG_CUDA(tg::dev_malloc((void **)&thi, sizeof(vec4<double>) * std::max<int64_t>(ntargets, 1), st));
         TG_CUDA(tg::dev_malloc((void **)&tlo, sizeof(vec4<double>) * std::max<int64_t>(ntargets, 1), st));
@@ -1006,9 +1049,10 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         a.tc = t->coord; a.ts = t->soft; a.tsize = t->size; a.tdelta = t->delta;
         a.tpos = tpos; a.th = th; a.scatter = scatter; a.groups = groups; a.group_root = group_root;
         a.group_order = group_order;
-        a.ngroups = ngroups; a.theta = theta; a.theta_group = theta_group; a.G = G;
+        a.ngroups = ngroups; a.theta = theta; a.theta_group = theta_group; a.tol_group = tol_group; a.G = G;
         a.out_fields = fields; a.out_w = w; a.out = out; a.gs = group_size;
         a.queue = scratch; a.status = scratch + 1; a.stats = (unsigned long long *)t->stats_dev;
+        a.gstats = gstats;
         vec4<float> *thi = nullptr, *tlo = nullptr;
         TG_CUDA(tg::dev_malloc((void **)&thi, sizeof(vec4<float>) * std::max<int64_t>(ntargets, 1), st));
         TG_CUDA(tg::dev_malloc((void **)&tlo, sizeof(vec4<float>) * std::max<int64_t>(ntargets, 1), st));
@@ -1036,15 +1080,21 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
     return TG_OK;
 }
 
-tg_status make_tree_groups(tg_tree_s *t, int G, int2 **groups, int **group_root, int64_t *ngroups,
-                           cudaStream_t st) {
+// The tree grouping at group size G, made once per tree and size and kept on the tree.
+tg_status tree_groups(tg_tree_s *t, int G, cudaStream_t st) {
+    if (t->groups && t->groups_G == G) return TG_OK;
+    if (t->groups) cudaFreeAsync(t->groups, st);
+    if (t->group_root) cudaFreeAsync(t->group_root, st);
+    if (t->group_node) cudaFreeAsync(t->group_node, st);
+    t->groups = nullptr; t->group_root = nullptr; t->group_node = nullptr; t->ngroups = 0; t->groups_G = 0;
     const int64_t N = t->ntot, M = t->mtot;
     int64_t *d_sys = nullptr, *d_node = nullptr;
     unsigned long long *cnt = nullptr;
     int2 *g0 = nullptr;
-    int *r0 = nullptr;
+    int *r0 = nullptr, *n0 = nullptr;
     TG_CUDA(tg::dev_malloc((void **)&g0, sizeof(int2) * N, st));
     TG_CUDA(tg::dev_malloc((void **)&r0, sizeof(int) * N, st));
+    TG_CUDA(tg::dev_malloc((void **)&n0, sizeof(int) * N, st));
     TG_CUDA(tg::dev_malloc((void **)&cnt, sizeof(unsigned long long), st));
     TG_CUDA(tg::dev_malloc((void **)&d_sys, sizeof(int64_t) * (t->nsys + 1), st));
     TG_CUDA(tg::dev_malloc((void **)&d_node, sizeof(int64_t) * (t->nsys + 1), st));
@@ -1053,7 +1103,7 @@ tg_status make_tree_groups(tg_tree_s *t, int G, int2 **groups, int **group_root,
     TG_CUDA(cudaMemcpyAsync(d_node, t->sys_node_off.data(), sizeof(int64_t) * (t->nsys + 1), cudaMemcpyHostToDevice,
                             st));
     { k_tree_groups<<<div_up(M, 256), 256, 0, st>>>(N, M, t->node_range, t->cell_center, t->size, t->coord, t->first,
-                                                  t->next, t->parent, G, d_sys, d_node, t->nsys, g0, r0, cnt); tg::note_launch(); }
+                                                  t->next, t->parent, G, d_sys, d_node, t->nsys, g0, r0, n0, cnt); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
     unsigned long long ng = 0;
     TG_CUDA(cudaMemcpyAsync(&ng, cnt, sizeof(ng), cudaMemcpyDeviceToHost, st));
@@ -1061,22 +1111,26 @@ tg_status make_tree_groups(tg_tree_s *t, int G, int2 **groups, int **group_root,
     // deterministic Morton order of the groups (their emission order depends on thread timing)
     uint64_t *keys = nullptr;
     uint32_t *vals = nullptr;
-    TG_CUDA(tg::dev_malloc((void **)&keys, sizeof(uint64_t) * ng, st));
-    TG_CUDA(tg::dev_malloc((void **)&vals, sizeof(uint32_t) * ng, st));
-    TG_CUDA(tg::dev_malloc((void **)groups, sizeof(int2) * std::max<unsigned long long>(ng, 1), st));
-    TG_CUDA(tg::dev_malloc((void **)group_root, sizeof(int) * std::max<unsigned long long>(ng, 1), st));
+    const unsigned long long ng1 = std::max<unsigned long long>(ng, 1);
+    TG_CUDA(tg::dev_malloc((void **)&keys, sizeof(uint64_t) * ng1, st));
+    TG_CUDA(tg::dev_malloc((void **)&vals, sizeof(uint32_t) * ng1, st));
+    TG_CUDA(tg::dev_malloc((void **)&t->groups, sizeof(int2) * ng1, st));
+    TG_CUDA(tg::dev_malloc((void **)&t->group_root, sizeof(int) * ng1, st));
+    TG_CUDA(tg::dev_malloc((void **)&t->group_node, sizeof(int) * ng1, st));
     { k_group_start_keys<<<div_up(ng, 256), 256, 0, st>>>(g0, ng, keys, vals); tg::note_launch(); }
     TG_TRY(radix_sort_pairs(keys, vals, ng, 32, st));
-    { k_permute_groups<<<div_up(ng, 256), 256, 0, st>>>(vals, ng, g0, r0, *groups, *group_root); tg::note_launch(); }
+    { k_permute_groups<<<div_up(ng, 256), 256, 0, st>>>(vals, ng, g0, r0, n0, t->groups, t->group_root, t->group_node); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
     TG_CUDA(cudaFreeAsync(keys, st));
     TG_CUDA(cudaFreeAsync(vals, st));
     TG_CUDA(cudaFreeAsync(g0, st));
     TG_CUDA(cudaFreeAsync(r0, st));
+    TG_CUDA(cudaFreeAsync(n0, st));
     TG_CUDA(cudaFreeAsync(cnt, st));
     TG_CUDA(cudaFreeAsync(d_sys, st));
     TG_CUDA(cudaFreeAsync(d_node, st));
-    *ngroups = (int64_t)ng;
+    t->ngroups = (int64_t)ng;
+    t->groups_G = G;
     return TG_OK;
 }
 

@@ -16,6 +16,11 @@ Differences a caller can see, all deliberate:
     pytreegrav's exactly; "tree" takes groups of at most ``group_size`` particles from the tree
     itself (self-gravity with a freshly built tree only), which never straddle a jump of the Morton
     curve and is the engine's fast path.
+  * ``learned`` / ``error_ratio`` (keywords, extension; Potential, Accel, TidalTensor, Field):
+    ``learned=True`` lets the packaged network set each group's acceptance test (a mass-aware
+    tolerance per group, trained on the GPU against brute force) instead of one global theta, for a
+    freshly built tree; ``error_ratio`` asks for that RMS force error relative to the plain walk at
+    theta = 0.7. See ``pytreegrav_gb300.theta``.
   * ``morton_order=False``/``radix=False`` in ConstructTree still build the radix tree (pytreegrav
     documents both builds as giving identical fields on generic data); ``vel`` (the velocity tree
     used only by the correlation functions) is not provided.
@@ -108,7 +113,7 @@ def ConstructTree(pos, m=None, softening=None, quadrupole=False, vel=None, compu
 
 
 def _self_field(key, pos, m, softening, G, theta, tree, return_tree, method, quadrupole, group_size, device,
-                precision, parallel_threshold, grouping="blocks"):
+                precision, parallel_threshold, grouping="blocks", learned=None, error_ratio=None):
     valueTestMethod(method)
     pos = np.atleast_2d(_f64(pos))
     m = np.atleast_1d(_f64(m))
@@ -130,8 +135,11 @@ def _self_field(key, pos, m, softening, G, theta, tree, return_tree, method, qua
             checkTreeQuadrupoles(tree, quadrupole)
             res = tree.fields(potential=key == "potential", accel=key == "accel", tidal=key == "tidal",
                               quadrupole=quadrupole, group_size=group_size, theta=theta, G=G, order="tree",
-                              precision=precision, grouping=grouping)[key]
+                              precision=precision, grouping=grouping, learned=learned,
+                              error_ratio=error_ratio)[key]
         else:
+            if learned:
+                raise ValueError("learned=True evaluates a freshly built tree (tree=None)")
             _check_tree(tree)
             checkTreeQuadrupoles(tree, quadrupole)
             # targets sorted by their own Morton order, not the tree's stored permutation
@@ -183,24 +191,26 @@ def _target_field(key, pos_target, pos_source, m_source, softening_target, softe
 
 def Potential(pos, m, softening=None, G=1.0, theta=0.7, tree=None, return_tree=False, parallel=False,
               method="adaptive", quadrupole=False, group_size=8, device="cpu", *, precision="fp32",
-              grouping="blocks"):
+              grouping="blocks", learned=None, error_ratio=None):
     """Gravitational potential of N particles at their own positions (frontend.py:145-293)."""
     return _self_field("potential", pos, m, softening, G, theta, tree, return_tree, method, quadrupole, group_size,
-                       device, precision, 4000 if parallel else 1000, grouping)
+                       device, precision, 4000 if parallel else 1000, grouping, learned, error_ratio)
 
 
 def Accel(pos, m, softening=None, G=1.0, theta=0.7, tree=None, return_tree=False, parallel=False,
-          method="adaptive", quadrupole=False, group_size=8, device="cpu", *, precision="fp32", grouping="blocks"):
+          method="adaptive", quadrupole=False, group_size=8, device="cpu", *, precision="fp32", grouping="blocks",
+          learned=None, error_ratio=None):
     """Gravitational acceleration of N particles at their own positions (frontend.py:421-560)."""
     return _self_field("accel", pos, m, softening, G, theta, tree, return_tree, method, quadrupole, group_size,
-                       device, precision, 4000 if parallel else 1000, grouping)
+                       device, precision, 4000 if parallel else 1000, grouping, learned, error_ratio)
 
 
 def TidalTensor(pos, m, softening=None, G=1.0, theta=0.7, tree=None, return_tree=False, parallel=False,
-                method="adaptive", quadrupole=False, group_size=8, *, precision="fp32", grouping="blocks"):
+                method="adaptive", quadrupole=False, group_size=8, *, precision="fp32", grouping="blocks",
+                learned=None, error_ratio=None):
     """Tidal tensor T_ij = dg_i/dx_j at the particle positions (frontend.py:688-789)."""
     return _self_field("tidal", pos, m, softening, G, theta, tree, return_tree, method, quadrupole, group_size,
-                       None, precision, 4000 if parallel else 1000, grouping)
+                       None, precision, 4000 if parallel else 1000, grouping, learned, error_ratio)
 
 
 def PotentialTarget(pos_target, pos_source, m_source, softening_target=None, softening_source=None, G=1.0,
@@ -232,7 +242,7 @@ class Field:
     potential/accel/tidal from a single traversal (frontend.py:904-1044)."""
 
     def __init__(self, pos, m, softening=None, G=1.0, theta=0.7, quadrupole=False, group_size=8, parallel=False, *,
-                 precision="fp32", grouping="blocks"):
+                 precision="fp32", grouping="blocks", learned=None, error_ratio=None):
         pos = np.atleast_2d(_f64(pos))
         m = np.atleast_1d(_f64(m))
         if softening is None:
@@ -245,6 +255,8 @@ class Field:
         self.parallel = parallel
         self.precision = precision
         self.grouping = grouping
+        self.learned = learned
+        self.error_ratio = error_ratio
         self.tree = ConstructTree(pos, m, softening, quadrupole=quadrupole)
 
     def __repr__(self):
@@ -262,7 +274,8 @@ class Field:
         kw = dict(potential=potential, accel=accel, tidal=tidal, quadrupole=self.quadrupole, group_size=group_size,
                   theta=theta, G=self.G, precision=precision)
         if pos_target is None:
-            return self.tree.fields(order="tree", grouping=self.grouping, **kw)
+            return self.tree.fields(order="tree", grouping=self.grouping, learned=self.learned,
+                                    error_ratio=self.error_ratio, **kw)
         pos_target = np.atleast_2d(_f64(pos_target))
         if softening_target is None:
             softening_target = zeros(len(pos_target))

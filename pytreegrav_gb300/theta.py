@@ -1,0 +1,484 @@
+"""Learned opening angle for the grouped walk (C entries in include/pytreegrav_gb300_theta.h).
+
+pytreegrav walks with one global theta (treewalk.py:22-25, grouped_treewalk.py:163-241). Here a small
+network gives every group of targets its own angle: groups whose error would be small open fewer
+nodes, groups whose error dominates the total open more, so the same RMS force error costs fewer
+interactions. Nothing here has a counterpart in pytreegrav.
+
+The pieces, all on the GPU through the library:
+
+* features: per group, from the tree (``tg_theta_features``);
+* training data (:func:`collect`): for every angle of a grid, the walk's per-group cost (from its
+  per-group counters) and the per-group force error against an FP32 Kahan-compensated brute-force
+  sum on a sample of groups -- errors the method itself produces;
+* :func:`train`: a 16-64-64-1 SiLU network fitted with the library's own FP32 forward, backward,
+  loss and Adam kernels. Per group it minimises cost(theta) + lambda * error(theta); lambda, the
+  price of error, is one of the inputs, so one network covers a range of accuracies;
+* :func:`calibrate`: the lambda at which the predicted angles reach a requested error relative to
+  the plain walk at theta = 0.7, from the training systems' tables;
+* inference: ``tg_theta_infer``, one fused BF16 tensor-core kernel, inside
+  ``tg_tree_fields_learned``; the plain global-theta walk is the fallback (no model, or a
+  non-finite angle).
+
+Cost and error are normalised per system so that, at the plain angle, the sampled groups' costs
+sum to 1 and their squared errors sum to 1; the error ratio sqrt(sum err) is then the RMS force
+error relative to the plain walk's.
+
+Train a model (GPU): ``python -m pytreegrav_gb300.theta --out model.npz``.
+"""
+
+import argparse
+import ctypes
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+from . import _lib
+
+GRID = np.round(np.arange(0.3, 1.0001, 0.1), 6)  # angles of the training walks (angle models)
+THETA_MIN, THETA_MAX = float(GRID[0]), float(GRID[-1])
+# log10 of the tolerance relative to the system's estimated RMS acceleration (tolerance models)
+TOL_GRID = np.round(np.arange(-3.5, 1.0001, 0.5), 6)
+THETA_CAP = 1.2  # angle cap of the mass-aware test
+GROUP_SIZE = 32  # targets per group of the tree grouping the models are trained and used with
+PLAIN_THETA = 0.7
+I_PLAIN = int(np.argmin(np.abs(GRID - PLAIN_THETA)))
+KINDS = {"angle": _lib.TG_THETA_KIND_ANGLE, "tolerance": _lib.TG_THETA_KIND_TOLERANCE}
+
+
+def grid_of(kind):
+    return GRID if kind == "angle" else TOL_GRID
+# cost of a group in relative warp time: point-mass entries, quadrupole entries, node tests; the
+# entries of a group of n targets take P/32 of a warp's time, P the power of two >= n that the walk
+# gives each slice of lanes
+COST_W = np.array([1.0, 1.7, 0.1])
+
+
+def group_cost(stats, count):
+    p = 2 ** np.ceil(np.log2(np.maximum(count, 1)))
+    return (stats[:, 0] * COST_W[0] + stats[:, 1] * COST_W[1]) * (p / 32.0) + stats[:, 2] * COST_W[2]
+LOG10_LAMBDA_RANGE = (-1.5, 2.5)
+NF = _lib.TG_THETA_NFEAT
+NP = _lib.TG_MLP_NPARAM
+H = _lib.TG_MLP_H
+OFF = dict(W1=0, b1=H * NF, W2=H * NF + H, b2=H * NF + H + H * H, W3=H * NF + 2 * H + H * H,
+           b3=H * NF + 3 * H + H * H)
+DEFAULT_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "models", "theta_mlp.npz")
+
+
+def _vp(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _check(rc, what):
+    _lib.check(rc, what)
+
+
+class ThetaModel:
+    """Network parameters (FP32), feature normalisation, output kind and range, the angle cap of a
+    tolerance model, and the calibrated lambda."""
+
+    def __init__(self, params, mean, std, log10_lambda=0.0, meta=None, kind="angle", theta_max=THETA_CAP):
+        self.params = np.ascontiguousarray(params, np.float32).reshape(NP)
+        self.mean = np.ascontiguousarray(mean, np.float32).reshape(NF)
+        self.std = np.ascontiguousarray(std, np.float32).reshape(NF)
+        self.log10_lambda = float(log10_lambda)
+        self.meta = dict(meta or {})
+        self.kind = kind
+        self.theta_max = float(theta_max)
+        self._handle = None
+
+    @property
+    def out_range(self):
+        g = grid_of(self.kind)
+        return float(g[0]), float(g[-1])
+
+    @staticmethod
+    def init_params(seed=0):
+        rng = np.random.default_rng(seed)
+        p = np.zeros(NP, np.float32)
+        p[OFF["W1"]:OFF["b1"]] = rng.normal(0, np.sqrt(2.0 / NF), H * NF)
+        p[OFF["W2"]:OFF["b2"]] = rng.normal(0, np.sqrt(2.0 / H), H * H)
+        p[OFF["W3"]:OFF["b3"]] = rng.normal(0, np.sqrt(1.0 / H), H)
+        return p
+
+    def save(self, path):
+        np.savez(path, params=self.params, mean=self.mean, std=self.std,
+                 log10_lambda=np.float64(self.log10_lambda), meta=json.dumps(self.meta), kind=self.kind,
+                 theta_max=np.float64(self.theta_max))
+
+    @classmethod
+    def load(cls, path=None):
+        z = np.load(path or DEFAULT_MODEL, allow_pickle=False)
+        return cls(z["params"], z["mean"], z["std"], float(z["log10_lambda"]), json.loads(str(z["meta"])),
+                   str(z["kind"]), float(z["theta_max"]))
+
+    def handle(self):
+        """The library's inference model (BF16 weights on the current device)."""
+        if self._handle is None:
+            L = _lib.load()
+            h = ctypes.c_void_p()
+            lo, hi = self.out_range
+            _check(L.tg_theta_model_create(_lib.ptr(self.params), _lib.ptr(self.mean), _lib.ptr(self.std),
+                                           KINDS[self.kind], lo, hi, self.theta_max, _lib.TG_MEM_HOST,
+                                           ctypes.byref(h)), "theta model")
+            self._handle = h
+        return self._handle
+
+    def close(self):
+        if self._handle is not None:
+            _lib.load().tg_theta_model_free(self._handle)
+            self._handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------------------------
+# Training data
+
+
+def _tree_device(torch, pos, m, h, quadrupole):
+    L = _lib.load()
+    dpos = torch.from_numpy(np.ascontiguousarray(pos, np.float64)).cuda()
+    dm = torch.from_numpy(np.ascontiguousarray(m, np.float64)).cuda()
+    dh = torch.from_numpy(np.ascontiguousarray(h, np.float64)).cuda()
+    tree = ctypes.c_void_p()
+    st = torch.cuda.current_stream().cuda_stream
+    _check(L.tg_tree_build(_vp(dpos), _vp(dm), _vp(dh), len(pos), int(quadrupole), 1, _lib.TG_MEM_DEVICE,
+                           ctypes.c_void_p(st), ctypes.byref(tree)), "build")
+    return tree, (dpos, dm, dh)
+
+
+def groups_of(tree, group_size):
+    """(first, count, node) of the tree grouping, host int32 arrays."""
+    L = _lib.load()
+    ng = ctypes.c_int64()
+    _check(L.tg_tree_groups(tree, group_size, ctypes.byref(ng), None), "groups")
+    first, count, node = (np.empty(ng.value, np.int32) for _ in range(3))
+    _check(L.tg_tree_groups_copy(tree, group_size, _lib.ptr(first), _lib.ptr(count), _lib.ptr(node),
+                                 _lib.TG_MEM_HOST, None), "groups copy")
+    return first, count, node
+
+
+def features(tree, group_size, quadrupole):
+    """Per-group features (ngroups x 16 float32, host)."""
+    import torch
+
+    L = _lib.load()
+    ng = ctypes.c_int64()
+    _check(L.tg_tree_groups(tree, group_size, ctypes.byref(ng), None), "groups")
+    f = torch.empty((max(ng.value, 1), NF), dtype=torch.float32, device="cuda")
+    _check(L.tg_theta_features(tree, group_size, int(quadrupole), _vp(f),
+                               ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), "features")
+    torch.cuda.synchronize()
+    return f[:ng.value].cpu().numpy()
+
+
+def collect(pos, m, h, quadrupole=True, group_size=GROUP_SIZE, sample=0.25, seed=0, G=1.0, label="", kind="tolerance",
+            theta_max=THETA_CAP):
+    """Training tables of one particle system (see the module docstring): for every value of the
+    kind's grid, each sampled group's cost and squared force error, both relative to the plain
+    walk at theta = 0.7 (summed over the sampled groups, the plain walk's are 1)."""
+    import torch
+
+    L = _lib.load()
+    n = len(pos)
+    pos = np.ascontiguousarray(pos, np.float64)
+    m = np.ascontiguousarray(m, np.float64)
+    h = np.ascontiguousarray(h, np.float64)
+    tree, keep = _tree_device(torch, pos, m, h, quadrupole)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    grid = grid_of(kind)
+    try:
+        first, count, node = groups_of(tree, group_size)
+        ng = len(first)
+        walk_idx = np.empty(n, np.int64)
+        _check(L.tg_tree_copy_out(tree, None, None, None, None, None, None, None, None, _lib.ptr(walk_idx), None),
+               "copy out")
+        feat = features(tree, group_size, quadrupole)
+        rng = np.random.default_rng(seed)
+        S = np.sort(rng.choice(ng, size=max(1, int(sample * ng)), replace=False))
+        seg = np.concatenate([[0], np.cumsum(count[S])])
+        targets = np.concatenate([np.arange(first[g], first[g] + count[g]) for g in S])
+        idx = walk_idx[targets]
+        # judge: FP32 Kahan-compensated direct sum over all sources
+        t0 = time.time()
+        dpt = torch.from_numpy(pos[idx]).cuda()
+        dht = torch.from_numpy(h[idx]).cuda()
+        aref = torch.empty((len(idx), 3), dtype=torch.float64, device="cuda")
+        _check(L.tg_bruteforce(_vp(dpt), _vp(dht), len(idx), _vp(keep[0]), _vp(keep[1]), _vp(keep[2]), n,
+                               _lib.TG_FIELD_ACCEL, 0, G, _lib.TG_FP32, _lib.TG_MEM_DEVICE, _vp(aref), st),
+               "brute force")
+        torch.cuda.synchronize()
+        t_bf = time.time() - t0
+        aref_h = aref.cpu().numpy()
+        rms2 = float(np.mean(np.sum(aref_h ** 2, axis=1)))
+        out = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+        didx = torch.from_numpy(idx).cuda()
+        stats = np.empty((ng, 3), np.uint32)
+        u = torch.empty(max(ng, 1), dtype=torch.float32, device="cuda")
+        tol = torch.empty(max(ng, 1), dtype=torch.float32, device="cuda")
+        _check(L.tg_tree_record_group_stats(tree, 1), "record")
+
+        def measure(angle, tol_dev=None):
+            if tol_dev is None:
+                _check(L.tg_tree_fields(tree, None, None, n, _lib.TG_FIELD_ACCEL, int(quadrupole), float(angle), G,
+                                        group_size, _lib.TG_GROUP_TREE, _lib.TG_ORDER_TREE, _lib.TG_FP32, None,
+                                        _lib.TG_MEM_DEVICE, _vp(out), st), "walk")
+            else:
+                _check(L.tg_tree_fields_grouped(tree, _lib.TG_FIELD_ACCEL, int(quadrupole), G, group_size,
+                                                float(angle), None, _vp(tol_dev), _lib.TG_MEM_DEVICE, _vp(out), st),
+                       "walk")
+            _check(L.tg_tree_last_group_stats(tree, _lib.ptr(stats), _lib.TG_MEM_HOST, st), "group stats")
+            a = out.index_select(0, didx).cpu().numpy()
+            d2 = np.sum((a - aref_h) ** 2, axis=1) / rms2
+            return group_cost(stats[S].astype(np.float64), count[S]), np.add.reduceat(d2, seg[:-1])
+
+        c_plain, e_plain = measure(PLAIN_THETA)
+        cost = np.empty((len(S), len(grid)))
+        err = np.empty((len(S), len(grid)))
+        for k, v in enumerate(grid):
+            if kind == "angle":
+                cost[:, k], err[:, k] = measure(v)
+            else:
+                u.fill_(float(v))
+                _check(L.tg_theta_tolerances(tree, group_size, int(quadrupole), _vp(u), _vp(tol), st), "tolerances")
+                cost[:, k], err[:, k] = measure(theta_max, tol)
+        _check(L.tg_tree_record_group_stats(tree, 0), "record")
+    finally:
+        L.tg_tree_free(tree)
+    c0, e0 = c_plain.sum(), e_plain.sum()
+    floor = 1e-6 / len(S)
+    return dict(label=label, kind=kind, n=n, ngroups=ng, sampled=len(S), features=feat[S],
+                log_cost=np.log(cost / c0).astype(np.float32), log_err=np.log(err / e0 + floor).astype(np.float32),
+                plain_rms_rel=float(np.sqrt(e0 / len(idx))), bf_seconds=t_bf, quadrupole=bool(quadrupole))
+
+
+# ---------------------------------------------------------------------------------------------
+# Training with the library's kernels
+
+
+def feature_stats(datasets):
+    X = np.concatenate([d["features"] for d in datasets])
+    mean = X.mean(axis=0)
+    std = X.std(axis=0)
+    lo, hi = LOG10_LAMBDA_RANGE
+    mean[_lib.TG_THETA_FEAT_LAMBDA] = 0.5 * (lo + hi)
+    std[_lib.TG_THETA_FEAT_LAMBDA] = (hi - lo) / np.sqrt(12.0)
+    std = np.where(std > 1e-6, std, 1.0)
+    return mean.astype(np.float32), std.astype(np.float32)
+
+
+def train(datasets, steps=3000, batch=8192, lr=2e-3, seed=0, log_every=500, verbose=True, theta_max=THETA_CAP):
+    """Fit the network to the datasets' tables; returns a ThetaModel (lambda not yet calibrated)."""
+    import torch
+
+    L = _lib.load()
+    kind = datasets[0]["kind"]
+    assert all(d["kind"] == kind for d in datasets)
+    grid = grid_of(kind)
+    mean, std = feature_stats(datasets)
+    X = np.concatenate([d["features"] for d in datasets]).astype(np.float32)
+    Xn = ((X - mean) / std).astype(np.float32)
+    LC = np.concatenate([d["log_cost"] for d in datasets]).astype(np.float32)
+    LE = np.concatenate([d["log_err"] for d in datasets]).astype(np.float32)
+    # each system weighs the same, whatever its number of sampled groups
+    w = np.concatenate([np.full(d["sampled"], 1.0 / d["sampled"]) for d in datasets])
+    w = w / w.sum()
+    dev = "cuda"
+    Xd, LCd, LEd = (torch.from_numpy(a).to(dev) for a in (Xn, LC, LE))
+    wd = torch.from_numpy(w).to(dev)
+    params = torch.from_numpy(ThetaModel.init_params(seed)).to(dev)
+    m1 = torch.zeros(NP, dtype=torch.float32, device=dev)
+    v1 = torch.zeros(NP, dtype=torch.float32, device=dev)
+    grad = torch.zeros(NP, dtype=torch.float32, device=dev)
+    B = min(batch, len(X))
+    y = torch.empty(B, dtype=torch.float32, device=dev)
+    dy = torch.empty(B, dtype=torch.float32, device=dev)
+    acts = torch.empty((B, 2 * H), dtype=torch.float32, device=dev)
+    work = torch.empty((B, 2 * H), dtype=torch.float32, device=dev)
+    loss = torch.zeros(1, dtype=torch.float32, device=dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    lo, hi = LOG10_LAMBDA_RANGE
+    li = _lib.TG_THETA_FEAT_LAMBDA
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    history = []
+    t0 = time.time()
+    for step in range(1, steps + 1):
+        rows = torch.multinomial(wd, B, replacement=True, generator=gen)
+        xb = Xd.index_select(0, rows).contiguous()
+        l10 = lo + (hi - lo) * torch.rand(B, device=dev, generator=gen)
+        xb[:, li] = (l10 - float(mean[li])) / float(std[li])
+        lam = torch.pow(10.0, l10).float().contiguous()
+        lcb = LCd.index_select(0, rows).contiguous()
+        leb = LEd.index_select(0, rows).contiguous()
+        loss.zero_()
+        _check(L.tg_mlp_forward(_vp(params), _vp(xb), B, _vp(acts), _vp(y), st), "forward")
+        _check(L.tg_theta_loss(_vp(y), _vp(lcb), _vp(leb), _vp(lam), B, len(grid), float(grid[0]),
+                               float(grid[1] - grid[0]), float(grid[0]), float(grid[-1]), _vp(dy), _vp(loss), st),
+               "loss")
+        _check(L.tg_mlp_backward(_vp(params), _vp(xb), _vp(acts), _vp(dy), B, _vp(work), _vp(grad), st), "backward")
+        rate = lr * (0.1 + 0.9 * 0.5 * (1 + np.cos(np.pi * step / steps)))  # cosine decay to lr/10
+        _check(L.tg_adam_step(_vp(params), _vp(grad), _vp(m1), _vp(v1), NP, float(rate), 0.9, 0.999, 1e-8, step, st),
+               "adam")
+        if step % log_every == 0 or step == steps:
+            history.append((step, float(loss.item())))
+            if verbose:
+                print(f"  step {step:5d}  loss {history[-1][1]:.5f}  ({time.time() - t0:.1f} s)", file=sys.stderr)
+    model = ThetaModel(params.cpu().numpy(), mean, std, 0.0,
+                       meta=dict(steps=steps, batch=B, lr=lr, history=history,
+                                 systems=[d["label"] for d in datasets]), kind=kind, theta_max=theta_max)
+    return model
+
+
+def predict(model, feats, log10_lambda):
+    """Network outputs (angles or log10 relative tolerances) from the BF16 inference kernel (host
+    arrays in and out)."""
+    import torch
+
+    L = _lib.load()
+    f = torch.from_numpy(np.ascontiguousarray(feats, np.float32)).cuda()
+    out = torch.empty(len(feats), dtype=torch.float32, device="cuda")
+    _check(L.tg_theta_infer(model.handle(), _vp(f), len(feats), float(log10_lambda), _vp(out),
+                            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), "infer")
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def table_at(log_tab, theta, grid=GRID):
+    """Per-row linear interpolation of a log table over `grid` at the values theta."""
+    u = (np.clip(theta, grid[0], grid[-1]) - grid[0]) / (grid[1] - grid[0])
+    k = np.clip(np.floor(u).astype(int), 0, len(grid) - 2)
+    w = u - k
+    r = np.arange(len(theta))
+    return np.exp(log_tab[r, k] * (1 - w) + log_tab[r, k + 1] * w)
+
+
+def predicted_ratios(model, d, log10_lambda):
+    """(error ratio, cost ratio) against the plain walk that the model's angles give on dataset d."""
+    th = predict(model, d["features"], log10_lambda)
+    g = grid_of(model.kind)
+    return float(np.sqrt(table_at(d["log_err"], th, g).sum())), float(table_at(d["log_cost"], th, g).sum())
+
+
+def calibrate(model, datasets, target_ratio=0.85, grid=None):
+    """Error-ratio curves of the training systems over a lambda grid, stored in the model; the
+    default lambda of each multipole order is the smallest (cheapest) one at which the median
+    error ratio of that order's systems is within target_ratio. Returns the per-system (error,
+    cost) ratios at the chosen lambdas."""
+    grid = np.arange(LOG10_LAMBDA_RANGE[0], LOG10_LAMBDA_RANGE[1] + 1e-9, 0.05) if grid is None else grid
+    curves = {d["label"]: dict(quadrupole=d["quadrupole"], error=[], cost=[]) for d in datasets}
+    for l10 in grid:
+        for d in datasets:
+            e, c = predicted_ratios(model, d, l10)
+            curves[d["label"]]["error"].append(e)
+            curves[d["label"]]["cost"].append(c)
+    model.meta["calibration"] = dict(grid=[float(g) for g in grid], target_ratio=target_ratio, systems=curves)
+    chosen = {}
+    for quad in (True, False):
+        l10 = lambda_for_ratio(model, target_ratio, quad)
+        if l10 is not None:
+            chosen[quad] = l10
+    model.log10_lambda = chosen.get(True, chosen.get(False, 0.0))
+    model.meta["log10_lambda_mono"] = chosen.get(False, model.log10_lambda)
+    out = []
+    for d in datasets:
+        out.append(predicted_ratios(model, d, chosen.get(d["quadrupole"], model.log10_lambda)))
+    return out
+
+
+def lambda_for_ratio(model, ratio, quadrupole):
+    """log10 lambda at which the median training system of this multipole order is predicted to
+    reach `ratio` times the plain walk's RMS force error (None without calibration curves)."""
+    cal = model.meta.get("calibration")
+    if not cal:
+        return None
+    sys_ = [v for v in cal["systems"].values() if v["quadrupole"] == bool(quadrupole)] or list(cal["systems"].values())
+    med = np.median(np.array([v["error"] for v in sys_]), axis=0)
+    grid = np.array(cal["grid"])
+    ok = np.nonzero(med <= ratio)[0]
+    return float(grid[ok[0]]) if len(ok) else float(grid[-1])
+
+
+def default_lambda(model, quadrupole):
+    return model.log10_lambda if quadrupole else float(model.meta.get("log10_lambda_mono", model.log10_lambda))
+
+
+# ---------------------------------------------------------------------------------------------
+# Training run
+
+
+def training_systems(scale=1.0):
+    """(label, positions, softening, quadrupole) of the synthetic training systems. The seeds are
+    not the benchmark's, so the benchmark system is held out."""
+    from . import synthetic as S
+
+    n0, n1, n2, n3 = (int(v * scale) for v in (2_000_000, 1_000_000, 500_000, 250_000))
+    return [
+        ("plummer_2e6_q", S.plummer(n0, 112), 0.005, True),
+        ("plummer_1e6_q", S.plummer(n1, 101), 0.005, True),
+        ("plummer_5e5_q", S.plummer(n2, 102), 0.005, True),
+        ("plummer_2.5e5_q", S.plummer(n3, 109), 0.005, True),
+        ("clustered_1e6_q", S.clustered(n1, 103), 0.002, True),
+        ("clustered_5e5_q", S.clustered(n2, 104), 0.002, True),
+        ("clustered_2.5e5_q", S.clustered(n3, 110), 0.002, True),
+        ("uniform_5e5_q", S.uniform(n2, 105), 0.01, True),
+        ("plummer_1e6_m", S.plummer(n1, 106), 0.005, False),
+        ("plummer_2.5e5_m", S.plummer(n3, 111), 0.005, False),
+        ("clustered_1e6_m", S.clustered(n1, 107), 0.002, False),
+        ("uniform_5e5_m", S.uniform(n2, 108), 0.01, False),
+    ]
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description="Train the learned opening-angle network on the GPU.")
+    ap.add_argument("--out", default=DEFAULT_MODEL)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--batch", type=int, default=8192)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--scale", type=float, default=1.0, help="system size factor (smaller for a quick run)")
+    ap.add_argument("--sample", type=float, default=0.25, help="fraction of groups judged by brute force")
+    ap.add_argument("--target-ratio", type=float, default=0.85,
+                    help="median training error relative to the plain walk at the default lambda")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--save-data", default=None, help="also save the training tables (.npz)")
+    ap.add_argument("--kind", choices=sorted(KINDS), default="tolerance")
+    ap.add_argument("--theta-max", type=float, default=THETA_CAP, help="angle cap of a tolerance model")
+    args = ap.parse_args(argv)
+    t0 = time.time()
+    datasets = []
+    for label, x, soft, quad in training_systems(args.scale):
+        n = len(x)
+        d = collect(x, np.full(n, 1.0 / n), np.full(n, soft), quadrupole=quad, sample=args.sample,
+                    seed=args.seed + len(datasets), label=label, kind=args.kind, theta_max=args.theta_max)
+        datasets.append(d)
+        print(f"{label}: {d['ngroups']} groups, {d['sampled']} judged, plain RMS rel error {d['plain_rms_rel']:.3e}, "
+              f"brute force {d['bf_seconds']:.2f} s", file=sys.stderr)
+    t1 = time.time()
+    if args.save_data:
+        np.savez(args.save_data, **{f"{d['label']}/{k}": d[k] for d in datasets
+                                    for k in ("features", "log_cost", "log_err")})
+    model = train(datasets, steps=args.steps, batch=args.batch, lr=args.lr, seed=args.seed,
+                  theta_max=args.theta_max)
+    t2 = time.time()
+    ratios = calibrate(model, datasets, target_ratio=args.target_ratio)
+    model.meta.update(collect_seconds=t1 - t0, train_seconds=t2 - t1, target_ratio=args.target_ratio)
+    os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
+    model.save(args.out)
+    summary = dict(out=args.out, kind=model.kind, theta_max=model.theta_max, log10_lambda=model.log10_lambda,
+                   ratios={d["label"]: dict(error=e, cost=c, speedup=1.0 / c) for d, (e, c) in zip(datasets, ratios)},
+                   collect_s=round(t1 - t0, 1), train_s=round(t2 - t1, 1))
+    print(json.dumps(summary))
+    return model
+
+
+if __name__ == "__main__":
+    main()

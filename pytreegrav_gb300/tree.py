@@ -107,15 +107,23 @@ class Octree:
     # -- evaluation ------------------------------------------------------------------------------
     def fields(self, pos=None, soft=None, potential=False, accel=False, tidal=False, quadrupole=False,
                group_size=8, theta=0.7, G=1.0, order="tree", precision="fp32", theta_per_group=None,
-               grouping="blocks"):
+               grouping="blocks", learned=None, error_ratio=None):
         """Any subset of {potential, accel, tidal} from one traversal (FieldsTarget_grouped).
 
         order="tree": the tree's own particles are the targets (pos/soft ignored); "morton": targets
         are Morton-sorted by their own bounding cube before grouping; "given": grouped as passed.
         grouping="blocks": group_size consecutive targets per group (pytreegrav's grouping);
         "tree": groups taken from the tree (order="tree" only).
+        learned (extension): True for the packaged opening-angle model, a path or a
+        theta.ThetaModel -- the acceptance test of each group then comes from the network
+        (order="tree", tree grouping of 32, FP32); error_ratio asks for that RMS force error
+        relative to the plain walk at theta = 0.7 (default: the model's calibrated lambda), and
+        `theta` is the fallback angle.
         Results come back in the caller's order (the tree's input order for order="tree").
         """
+        if learned is not None and learned is not False:
+            return self._fields_learned(potential, accel, tidal, quadrupole, theta, G, order, precision, learned,
+                                        error_ratio)
         fields = (_lib.TG_FIELD_POTENTIAL * bool(potential) + _lib.TG_FIELD_ACCEL * bool(accel)
                   + _lib.TG_FIELD_TIDAL * bool(tidal))
         if fields == 0:
@@ -144,6 +152,40 @@ class Octree:
                                         float(G), int(group_size), grp, ord_code, prec, tpg, _lib.TG_MEM_HOST,
                                         _lib.ptr(out), None)
         _lib.check(rc, "tree walk")
+        return _split(out, potential, accel, tidal)
+
+    def _fields_learned(self, potential, accel, tidal, quadrupole, theta, G, order, precision, learned, error_ratio):
+        from . import theta as th
+
+        if order != "tree":
+            raise ValueError("the learned opening test evaluates the tree's own particles (order='tree')")
+        if precision != "fp32":
+            raise ValueError("the learned opening test runs the FP32 walk")
+        fields = (_lib.TG_FIELD_POTENTIAL * bool(potential) + _lib.TG_FIELD_ACCEL * bool(accel)
+                  + _lib.TG_FIELD_TIDAL * bool(tidal))
+        if fields == 0:
+            raise ValueError("request at least one of potential=True, accel=True, tidal=True")
+        if quadrupole and not self.HasQuads:
+            _lib.check(_lib.TG_ERR_NO_QUADRUPOLES)
+        if isinstance(learned, th.ThetaModel):
+            model = learned
+        else:
+            model = self._models.get(learned) if hasattr(self, "_models") else None
+            if model is None:
+                model = th.ThetaModel.load(None if learned is True else learned)
+                if not hasattr(self, "_models"):
+                    self._models = {}
+                self._models[learned] = model
+        l10 = (th.default_lambda(model, quadrupole) if error_ratio is None
+               else th.lambda_for_ratio(model, float(error_ratio), quadrupole))
+        if l10 is None:
+            l10 = th.default_lambda(model, quadrupole)
+        W = int(bool(potential)) + 3 * int(bool(accel)) + 9 * int(bool(tidal))
+        out = np.empty((self.NumParticles, W))
+        rc = _lib.load().tg_tree_fields_learned(self._h, fields, int(bool(quadrupole)), float(G), th.GROUP_SIZE,
+                                                model.handle(), float(l10), float(theta), _lib.TG_MEM_HOST,
+                                                _lib.ptr(out), None)
+        _lib.check(rc, "learned tree walk")
         return _split(out, potential, accel, tidal)
 
     def last_walk_stats(self):

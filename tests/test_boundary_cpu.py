@@ -13,13 +13,22 @@ from pytreegrav_gb300 import _lib
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def header_symbols():
-    src = open(os.path.join(ROOT, "include", "pytreegrav_gb300.h")).read()
+def header_symbols(name="pytreegrav_gb300.h"):
+    src = open(os.path.join(ROOT, "include", name)).read()
     return sorted(set(re.findall(r"^(?:tg_status|const char \*)\s*(tg_\w+)\s*\(", src, re.M)))
 
 
 def test_header_and_binding_agree():
     assert header_symbols() == sorted(_lib.EXPORTS)
+    assert header_symbols("pytreegrav_gb300_theta.h") == sorted(_lib.THETA_EXPORTS)
+
+
+def test_theta_constants_agree_with_header():
+    src = open(os.path.join(ROOT, "include", "pytreegrav_gb300_theta.h")).read()
+    consts = dict(re.findall(r"^#define (TG_THETA_NFEAT|TG_MLP_H|TG_THETA_FEAT_LAMBDA) (\d+)", src, re.M))
+    assert int(consts["TG_THETA_NFEAT"]) == _lib.TG_THETA_NFEAT
+    assert int(consts["TG_MLP_H"]) == _lib.TG_MLP_H
+    assert int(consts["TG_THETA_FEAT_LAMBDA"]) == _lib.TG_THETA_FEAT_LAMBDA
 
 
 def test_library_builds_loads_and_exports_every_symbol():
@@ -27,7 +36,7 @@ def test_library_builds_loads_and_exports_every_symbol():
 
     path = build.build()
     L = ctypes.CDLL(path)
-    for name in header_symbols():
+    for name in header_symbols() + header_symbols("pytreegrav_gb300_theta.h"):
         assert hasattr(L, name), name
 
 

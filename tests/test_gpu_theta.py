@@ -1,0 +1,228 @@
+"""Learned opening angle on the GPU: the training kernels against the numpy checker, BF16 inference
+against the FP32 forward pass, features and per-group counters, and the learned walk."""
+
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+import mlp_ref as R
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def env():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    from pytreegrav_gb300 import _lib, theta
+
+    return torch, _lib, _lib.load(), theta
+
+
+def vp(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def dev(torch, a, dtype=None):
+    a = np.ascontiguousarray(a, dtype or np.float32)
+    return torch.from_numpy(a).cuda()
+
+
+def test_forward_and_backward_match_numpy(env):
+    torch, _lib, L, theta = env
+    rng = np.random.default_rng(0)
+    n = 333
+    p = (theta.ThetaModel.init_params(5) + rng.normal(0, 0.02, R.NP)).astype(np.float32)
+    x = rng.normal(size=(n, R.NF)).astype(np.float32)
+    dy = rng.normal(size=n).astype(np.float32)
+    P, X, DY = dev(torch, p), dev(torch, x), dev(torch, dy)
+    y = torch.empty(n, dtype=torch.float32, device="cuda")
+    acts = torch.empty((n, 128), dtype=torch.float32, device="cuda")
+    work = torch.empty((n, 128), dtype=torch.float32, device="cuda")
+    grad = torch.empty(R.NP, dtype=torch.float32, device="cuda")
+    assert L.tg_mlp_forward(vp(P), vp(X), n, vp(acts), vp(y), None) == 0
+    assert L.tg_mlp_backward(vp(P), vp(X), vp(acts), vp(DY), n, vp(work), vp(grad), None) == 0
+    torch.cuda.synchronize()
+    y_ref, z1, z2 = R.forward(p.astype(np.float64), x.astype(np.float64))
+    np.testing.assert_allclose(y.cpu().numpy(), y_ref, rtol=1e-4, atol=1e-4)
+    np.testing.assert_allclose(acts.cpu().numpy()[:, :64], z1, rtol=1e-4, atol=1e-4)
+    g_ref = R.backward(p.astype(np.float64), x.astype(np.float64), dy.astype(np.float64))
+    g = grad.cpu().numpy()
+    scale = np.abs(g_ref).max()
+    assert np.abs(g - g_ref).max() <= 1e-4 * scale, np.abs(g - g_ref).max() / scale
+
+
+def test_loss_and_adam_match_numpy(env):
+    torch, _lib, L, theta = env
+    rng = np.random.default_rng(1)
+    n, K = 1000, len(theta.GRID)
+    lc = np.cumsum(-rng.random((n, K)), axis=1).astype(np.float32)
+    le = (np.cumsum(rng.random((n, K)) * 2, axis=1) - 8).astype(np.float32)
+    lam = (10 ** rng.uniform(-1, 2, n)).astype(np.float32)
+    y = rng.normal(size=n).astype(np.float32)
+    Y, LC, LE, LAM = (dev(torch, a) for a in (y, lc, le, lam))
+    dy = torch.empty(n, dtype=torch.float32, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    t0, dt = float(theta.GRID[0]), float(theta.GRID[1] - theta.GRID[0])
+    assert L.tg_theta_loss(vp(Y), vp(LC), vp(LE), vp(LAM), n, K, t0, dt, theta.THETA_MIN, theta.THETA_MAX, vp(dy),
+                           vp(loss), None) == 0
+    torch.cuda.synchronize()
+    l_ref, dy_ref = R.theta_loss(y.astype(np.float64), lc.astype(np.float64), le.astype(np.float64),
+                                 lam.astype(np.float64), t0, dt, theta.THETA_MIN, theta.THETA_MAX)
+    assert float(loss.item()) == pytest.approx(l_ref, rel=1e-4)
+    np.testing.assert_allclose(dy.cpu().numpy(), dy_ref, rtol=1e-3, atol=1e-7 * np.abs(dy_ref).max())
+    p = rng.normal(size=R.NP).astype(np.float32)
+    g = rng.normal(size=R.NP).astype(np.float32)
+    m = rng.normal(size=R.NP).astype(np.float32) * 0.1
+    v = rng.random(R.NP).astype(np.float32) * 0.1
+    P, G_, M, V = (dev(torch, a) for a in (p, g, m, v))
+    assert L.tg_adam_step(vp(P), vp(G_), vp(M), vp(V), R.NP, 1e-3, 0.9, 0.999, 1e-8, 7, None) == 0
+    torch.cuda.synchronize()
+    p_ref, m_ref, v_ref = R.adam(p.astype(np.float64), g, m, v, 1e-3, 0.9, 0.999, 1e-8, 7)
+    np.testing.assert_allclose(P.cpu().numpy(), p_ref, rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(M.cpu().numpy(), m_ref, rtol=1e-5, atol=1e-7)
+
+
+def test_bf16_inference_matches_fp32_forward(env):
+    torch, _lib, L, theta = env
+    rng = np.random.default_rng(2)
+    n = 1000 + 7  # not a multiple of the 16-row tile
+    p = (theta.ThetaModel.init_params(9) + rng.normal(0, 0.02, R.NP)).astype(np.float32)
+    mean = rng.normal(size=R.NF).astype(np.float32)
+    std = (0.5 + rng.random(R.NF)).astype(np.float32)
+    feat = (mean + std * rng.normal(size=(n, R.NF))).astype(np.float32)
+    model = theta.ThetaModel(p, mean, std)
+    l10 = 0.4
+    th = theta.predict(model, feat, l10)
+    xn = (feat.astype(np.float64) - mean) / std
+    xn[:, _lib.TG_THETA_FEAT_LAMBDA] = (l10 - mean[_lib.TG_THETA_FEAT_LAMBDA]) / std[_lib.TG_THETA_FEAT_LAMBDA]
+    y, _, _ = R.forward(p.astype(np.float64), xn)
+    th_ref = theta.THETA_MIN + (theta.THETA_MAX - theta.THETA_MIN) * R.sigmoid(y)
+    err = np.abs(th - th_ref)
+    assert err.max() < 0.02 and err.mean() < 0.004, (err.max(), err.mean())
+    model.close()
+
+
+@pytest.fixture(scope="module")
+def plummer_tree(env):
+    torch, _lib, L, theta = env
+    from pytreegrav_gb300 import synthetic
+
+    n = 200_000
+    x = synthetic.plummer(n, 7)
+    tree, keep = theta._tree_device(torch, x, np.full(n, 1.0 / n), np.full(n, 0.005), True)
+    yield tree, keep, x
+    L.tg_tree_free(tree)
+
+
+def test_features_and_group_counters(env, plummer_tree):
+    torch, _lib, L, theta = env
+    tree, keep, x = plummer_tree
+    n = len(x)
+    first, count, node = theta.groups_of(tree, 32)
+    assert count.sum() == n and np.all(count >= 1) and np.all(count <= 32)
+    assert np.all(np.diff(first) > 0) and first[0] == 0
+    f = theta.features(tree, 32, True)
+    assert f.shape == (len(first), R.NF) and np.all(np.isfinite(f))
+    assert np.allclose(f[:, 0], np.log2(count))
+    assert np.all(f[:, _lib.TG_THETA_FEAT_LAMBDA] == 0) and np.all(f[:, 14] == 1)
+    out = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    assert L.tg_tree_record_group_stats(tree, 1) == 0
+    assert L.tg_tree_fields(tree, None, None, n, _lib.TG_FIELD_ACCEL, 1, 0.7, 1.0, 32, _lib.TG_GROUP_TREE,
+                            _lib.TG_ORDER_TREE, _lib.TG_FP32, None, _lib.TG_MEM_DEVICE, vp(out), None) == 0
+    stats = np.empty((len(first), 3), np.uint32)
+    assert L.tg_tree_last_group_stats(tree, _lib.ptr(stats), _lib.TG_MEM_HOST, None) == 0
+    assert L.tg_tree_record_group_stats(tree, 0) == 0
+    v = [ctypes.c_int64() for _ in range(4)]
+    L.tg_tree_last_walk_stats(tree, *[ctypes.byref(q) for q in v])
+    # the walk counts an interaction per (entry, target of the group)
+    total = int(((stats[:, 0].astype(np.int64) + stats[:, 1]) * count).sum())
+    assert total == v[0].value
+    assert int(stats[:, 2].astype(np.int64).sum()) >= len(first)
+
+
+def test_learned_walk_without_model_is_the_plain_walk(env, plummer_tree):
+    torch, _lib, L, theta = env
+    tree, keep, x = plummer_tree
+    n = len(x)
+    a = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    b = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    assert L.tg_tree_fields(tree, None, None, n, _lib.TG_FIELD_ACCEL, 1, 0.7, 1.0, 32, _lib.TG_GROUP_TREE,
+                            _lib.TG_ORDER_TREE, _lib.TG_FP32, None, _lib.TG_MEM_DEVICE, vp(a), None) == 0
+    assert L.tg_tree_fields_learned(tree, _lib.TG_FIELD_ACCEL, 1, 1.0, 32, None, 0.0, 0.7, _lib.TG_MEM_DEVICE, vp(b),
+                                    None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("quad", [1, 0])
+def test_shipped_model_beats_the_plain_walk_at_equal_error(env, quad):
+    """On a Plummer system outside the training set, the learned walk at the model's default
+    lambda keeps the plain theta = 0.7 walk's RMS force error (FP32 brute force judge) with far
+    fewer interactions."""
+    torch, _lib, L, theta = env
+    if not os.path.exists(theta.DEFAULT_MODEL):
+        pytest.skip("no trained model in the package")
+    from pytreegrav_gb300 import synthetic
+
+    model = theta.ThetaModel.load()
+    n = 300_000
+    x = synthetic.plummer(n, 11)
+    tree, keep = theta._tree_device(torch, x, np.full(n, 1.0 / n), np.full(n, 0.005), quad)
+    try:
+        idx = np.sort(np.random.default_rng(3).choice(n, 5000, replace=False))
+        pt = dev(torch, x[idx], np.float64)
+        ht = dev(torch, np.full(len(idx), 0.005), np.float64)
+        ref = torch.empty((len(idx), 3), dtype=torch.float64, device="cuda")
+        assert L.tg_bruteforce(vp(pt), vp(ht), len(idx), vp(keep[0]), vp(keep[1]), vp(keep[2]), n,
+                               _lib.TG_FIELD_ACCEL, 0, 1.0, _lib.TG_FP32, _lib.TG_MEM_DEVICE, vp(ref), None) == 0
+        ref = ref.cpu().numpy()
+        rms = np.sqrt(np.mean(np.sum(ref ** 2, 1)))
+        out = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+
+        def err_and_interactions():
+            torch.cuda.synchronize()
+            a = out.cpu().numpy()[idx]
+            v = [ctypes.c_int64() for _ in range(4)]
+            L.tg_tree_last_walk_stats(tree, *[ctypes.byref(q) for q in v])
+            return np.sqrt(np.mean(np.sum((a - ref) ** 2, 1))) / rms, v[0].value
+
+        assert L.tg_tree_fields(tree, None, None, n, _lib.TG_FIELD_ACCEL, quad, 0.7, 1.0, 32, _lib.TG_GROUP_TREE,
+                                _lib.TG_ORDER_TREE, _lib.TG_FP32, None, _lib.TG_MEM_DEVICE, vp(out), None) == 0
+        e_plain, i_plain = err_and_interactions()
+        assert L.tg_tree_fields_learned(tree, _lib.TG_FIELD_ACCEL, quad, 1.0, 32, model.handle(),
+                                        theta.default_lambda(model, quad), 0.7, _lib.TG_MEM_DEVICE, vp(out),
+                                        None) == 0
+        e_learned, i_learned = err_and_interactions()
+    finally:
+        L.tg_tree_free(tree)
+        model.close()
+    assert e_learned <= 1.15 * e_plain, (e_learned, e_plain)
+    assert i_learned <= 0.7 * i_plain, (i_learned, i_plain)
+
+
+def test_frontend_learned_keyword(env):
+    torch, _lib, L, theta = env
+    if not os.path.exists(theta.DEFAULT_MODEL):
+        pytest.skip("no trained model in the package")
+    import pytreegrav_gb300 as pg
+    from pytreegrav_gb300 import synthetic
+
+    n = 50_000
+    x = synthetic.plummer(n, 12)
+    m = np.full(n, 1.0 / n)
+    h = np.full(n, 0.005)
+    a_plain = pg.Accel(x, m, h, quadrupole=True, method="tree")
+    a_learn = pg.Accel(x, m, h, quadrupole=True, method="tree", learned=True)
+    a_tight = pg.Accel(x, m, h, quadrupole=True, method="tree", learned=True, error_ratio=0.3)
+    ref = pg.AccelTarget(x[:2000], x, m, h[:2000], h, method="bruteforce")
+    rms = np.sqrt(np.mean(np.sum(ref ** 2, 1)))
+    e = [np.sqrt(np.mean(np.sum((a[:2000] - ref) ** 2, 1))) / rms for a in (a_plain, a_learn, a_tight)]
+    assert e[1] < 2e-3 and e[2] < e[1]
+    f = pg.Field(x, m, h, quadrupole=True, learned=True)
+    assert np.allclose(f.accel(), a_learn, rtol=0, atol=0)
+    with pytest.raises(ValueError):
+        pg.Accel(x, m, h, quadrupole=True, method="tree", learned=True, tree=pg.ConstructTree(x, m, h, quadrupole=True))
