@@ -64,9 +64,10 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi sampling during the timed region (SM clock, throttle reasons)."""
+    """nvidia-smi sampling (every 20 ms, timestamped) around the timed region; only the samples
+    taken inside the region (or, for a region shorter than the interval, the nearest ones) count."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -74,19 +75,31 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.path = os.path.join("/tmp", f"tg_clocks_{os.getpid()}.csv")
+        self.t_begin = self.t_end = None
 
     def start(self):
+        """Start sampling; returns once it is underway."""
         try:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=self.fh, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+        time.sleep(0.5)
+
+    def begin(self):
+        self.t_begin = time.time()
+
+    def end(self):
+        self.t_end = time.time()
 
     def stop(self):
+        import datetime
+
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.1)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -96,17 +109,25 @@ class ClockSampler:
         rows = []
         for line in open(self.path):
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) >= 9:
-                rows.append(parts)
+            if len(parts) < 10:
+                continue
+            try:
+                t = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                continue
+            rows.append((t, parts[1:]))
         os.unlink(self.path)
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        inside = [r for t, r in rows if self.t_begin is None or self.t_begin <= t <= self.t_end]
+        if not inside:  # region shorter than the interval: the samples just before and after it
+            inside = [r for t, r in rows if t < self.t_begin][-1:] + [r for t, r in rows if t > self.t_end][:1]
+        sm = [float(r[1]) for r in inside if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in inside if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        reasons = sorted({names[i] for r in inside for i in range(4) if r[5 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(inside)}
 
 
 def read_traffic():
@@ -211,7 +232,7 @@ def run_ours(args):
     mh = model.handle()
     l10 = th.default_lambda(model, True)
 
-    def timed(step_fn, dest, count_launches=False):
+    def timed(step_fn, dest, sampler=None):
         for _ in range(args.warmup):
             step_fn(dest)
         torch.cuda.synchronize()
@@ -221,6 +242,8 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
         l0 = L.tg_launch_count()
+        if sampler:
+            sampler.begin()
         t0 = time.perf_counter()
         for k in range(args.steps):
             flush.zero_()  # evict the previous step's data from L2 (outside the step events)
@@ -229,6 +252,8 @@ def run_ours(args):
             ev[k][1].record()
         torch.cuda.synchronize()
         region = time.perf_counter() - t0
+        if sampler:
+            sampler.end()
         if dist:
             dist.barrier()
         ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
@@ -242,7 +267,7 @@ def run_ours(args):
     plain_step = lambda dest: gpu_step(L, _lib, dpos, dm, dh, dest, n, stream)
     clocks = ClockSampler(local)
     clocks.start()
-    ms, stats, t_region, launches = timed(learned_step, out)
+    ms, stats, t_region, launches = timed(learned_step, out, clocks)
     clk = clocks.stop()
     ms_plain, stats_plain, _, _ = timed(plain_step, out_plain)
     value = n * ws / (ms * 1e-3)
@@ -364,7 +389,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=N_DEFAULT)
