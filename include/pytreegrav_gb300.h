@@ -112,6 +112,26 @@ tg_status tg_tree_fields(tg_tree tree, const double *pos, const double *h, int64
                          int order, int precision, const float *theta_per_group, int mem,
                          double *out, void *stream);
 
+/* Launch shape of this tree's walks (no counterpart in pytreegrav): warps_per_block in {2, 4, 8}
+ * and the node stack a walk starts with: 1024 entries per warp (groups that overflow it are
+ * rewalked, on the device, with 4096) or 4096 (fewer resident warps, no second pass). Results do
+ * not depend on it; pytreegrav_gb300.autotune picks it by timing. Default: 4, 1024. */
+tg_status tg_tree_set_walk_config(tg_tree tree, int warps_per_block, int first_stack);
+
+/* A tree's walk (tg_tree_fields with TG_ORDER_TREE, FP32) captured in a CUDA graph, for calling
+ * many times on one tree -- typically a batched tree of many systems (no counterpart in
+ * pytreegrav). Creation makes the groups, the walk arena and the scratch, and synchronises; a
+ * launch replays the graph on `stream` (zeroing the counters, the walk, and the large-stack pass
+ * over the groups that overflowed the first stack) with no host synchronisation and writes `out`
+ * (device, ntot x W, the caller's order); status waits for `stream` and returns the last replay's
+ * status. The tree and `out` must outlive the graph; replays on one graph must not overlap. */
+typedef struct tg_walk_graph_s *tg_walk_graph;
+tg_status tg_walk_graph_create(tg_tree tree, int fields, int quadrupole, double theta, double G,
+                               int group_size, int grouping, double *out, tg_walk_graph *graph);
+tg_status tg_walk_graph_launch(tg_walk_graph graph, void *stream);
+tg_status tg_walk_graph_status(tg_walk_graph graph, void *stream);
+tg_status tg_walk_graph_free(tg_walk_graph graph);
+
 /* Interaction statistics of the last tg_tree_fields call on this tree: total interactions and
  * node tests, the deepest node stack seen, and the number of groups. */
 tg_status tg_tree_last_walk_stats(tg_tree tree, int64_t *interactions, int64_t *node_tests,

@@ -47,6 +47,11 @@ EXPORTS = [
     "tg_tree_free",
     "tg_tree_fields",
     "tg_tree_last_walk_stats",
+    "tg_tree_set_walk_config",
+    "tg_walk_graph_create",
+    "tg_walk_graph_launch",
+    "tg_walk_graph_status",
+    "tg_walk_graph_free",
     "tg_morton_order",
     "tg_morton_order_noalloc",
     "tg_bruteforce",
@@ -119,6 +124,11 @@ def _declare(L):
     L.tg_tree_free.argtypes = [vp]
     L.tg_tree_fields.argtypes = [vp, vp, vp, i64, ci, ci, dbl, dbl, ci, ci, ci, ci, vp, ci, vp, vp]
     L.tg_tree_last_walk_stats.argtypes = [vp, vp, vp, vp, vp]
+    L.tg_tree_set_walk_config.argtypes = [vp, ci, ci]
+    L.tg_walk_graph_create.argtypes = [vp, ci, ci, dbl, dbl, ci, ci, vp, ctypes.POINTER(vp)]
+    L.tg_walk_graph_launch.argtypes = [vp, vp]
+    L.tg_walk_graph_status.argtypes = [vp, vp]
+    L.tg_walk_graph_free.argtypes = [vp]
     L.tg_morton_order.argtypes = [vp, i64, ci, vp, vp]
     L.tg_morton_order_noalloc.argtypes = [vp, i64, vp, vp]
     L.tg_bruteforce.argtypes = [vp, vp, i64, vp, vp, vp, i64, ci, ci, dbl, ci, ci, vp, vp]

@@ -218,6 +218,15 @@ tg_status tg_tree_copy_out(tg_tree t, double *coord, double *mass, double *size,
     return TG_OK;
 }
 
+tg_status tg_tree_set_walk_config(tg_tree t, int warps_per_block, int first_stack) {
+    if (!t || (warps_per_block != 2 && warps_per_block != 4 && warps_per_block != 8) ||
+        (first_stack != 1024 && first_stack != 4096))
+        return TG_ERR_BAD_ARG;
+    t->walk_warps = warps_per_block;
+    t->walk_stack = first_stack;
+    return TG_OK;
+}
+
 tg_status tg_tree_free(tg_tree t) {
     destroy(t);
     return TG_OK;

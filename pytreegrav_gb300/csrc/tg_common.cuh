@@ -97,5 +97,9 @@ cudaError_t dev_malloc(void **p, size_t bytes, cudaStream_t s);
 
 // Counts kernel launches (every launch site calls it; read through tg_launch_count()).
 void note_launch();
+// Adjusts the count by delta: + the kernels of a replayed CUDA graph, - the launches recorded (not
+// run) while capturing one.
+void note_launches(int64_t delta);
+int64_t launches_so_far();
 
 }  // namespace tg

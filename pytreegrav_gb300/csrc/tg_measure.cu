@@ -8,6 +8,8 @@
 namespace tg {
 static std::atomic<int64_t> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void note_launches(int64_t delta) { g_launches.fetch_add(delta, std::memory_order_relaxed); }
+int64_t launches_so_far() { return g_launches.load(); }
 }  // namespace tg
 
 namespace {

@@ -89,4 +89,8 @@ struct tg_tree_s {
     int record_group_stats = 0;
     unsigned *gstats = nullptr;
     int64_t gstats_n = 0;
+    // Walk launch shape (tg_tree_set_walk_config): warps per block, and the node stack a walk starts
+    // with (1024: groups that overflow it are rewalked with 4096; 4096: every group starts there).
+    int walk_warps = 4;
+    int walk_stack = 1024;
 };

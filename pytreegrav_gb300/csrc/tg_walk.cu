@@ -17,13 +17,15 @@
 // within any target's softening length (checked once per source against the group box) take the
 // point-mass path; the rest take the full softened path. Each lane sums a batch in registers and
 // adds the batch total into a Kahan-compensated accumulator.
+#include <new>
 #include <type_traits>
+#include <vector>
 
 #include "tg_tree.cuh"
 
 namespace tg {
 
-constexpr int WALK_WARPS = 4;
+constexpr int MAX_WALK_WARPS = 8;  // block shapes of 2, 4 or 8 warps, chosen per tree
 constexpr int STACK_SMALL = 1024;  // per-warp node stack; a walk that overflows it is rerun with
 constexpr int STACK_LARGE = 4096;  // the large stack (fewer resident warps)
 constexpr int ILIST_CAP = 320;
@@ -255,6 +257,10 @@ struct WalkArgs {
     int *status;
     unsigned long long *stats;  // interactions, node tests, max stack, steps, quadrupole-node interactions
     unsigned *gstats;           // per group (3): point-mass entries, quadrupole entries, nodes tested; or null
+    // Small-stack pass: a group that overflows the stack is appended to retry (count in *retry_count)
+    // for the large-stack pass instead of failing. Null: overflow is an error.
+    int *retry, *retry_count;
+    const int *ngroups_dev;  // non-null: the number of groups is read here (the retry pass)
 };
 
 template <typename T, bool QUAD, int STACK>
@@ -423,19 +429,20 @@ __device__ __forceinline__ bool accept_exact(int64_t f, const double *tc, const 
 }
 
 template <typename T, int FIELDS, bool QUAD, int STACK>
-__global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2) k_walk(WalkArgs<T> a) {
+__global__ void __launch_bounds__(MAX_WALK_WARPS * 32, STACK == STACK_SMALL ? 3 : 1) k_walk(WalkArgs<T> a) {
     extern __shared__ unsigned char smem_raw[];
     WarpSmem<T, QUAD, STACK> &sm = reinterpret_cast<WarpSmem<T, QUAD, STACK> *>(smem_raw)[threadIdx.x >> 5];
     const int lane = lane_id();
     const unsigned lt = lanemask_lt();
     unsigned long long n_int = 0, n_tests = 0, n_steps = 0, n_qint = 0;
     int max_sp = 0;
+    const int64_t ngroups = a.ngroups_dev ? (int64_t)*a.ngroups_dev : a.ngroups;
 
     for (;;) {
         int g = 0;
         if (lane == 0) g = atomicAdd(a.queue, 1);
         g = __shfl_sync(FULL, g, 0);
-        if (g >= a.ngroups) break;
+        if (g >= ngroups) break;
         if (a.group_order) g = a.group_order[g];
         const int2 gr = a.groups[g];
         // lanes per target slot: the smallest power of two holding the group (at most a.gs); the
@@ -607,7 +614,7 @@ __global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2)
             n_qint += (unsigned long long)cnt * (unsigned long long)gr.y;
         };
 
-        unsigned g_mono = 0, g_quad = 0, g_tests = 0;  // this group's counters (warp-uniform)
+        unsigned g_mono = 0, g_quad = 0, g_tests = 0, g_steps = 0;  // this group's counters (warp-uniform)
         int sp = 1, ni = 0, nn = 0;
         if (lane == 0) sm.stack[0] = a.group_root[g];
         __syncwarp();
@@ -621,6 +628,7 @@ __global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2)
             }
             if (sp > 0) {
                 n_steps++;
+                g_steps++;
                 const int cnt = min(sp, 32);
                 g_tests += cnt;
                 const int node = lane < cnt ? sm.stack[sp - 1 - lane] : -1;
@@ -698,6 +706,19 @@ __global__ void __launch_bounds__(WALK_WARPS * 32, STACK == STACK_SMALL ? 6 : 2)
                 }
             }
             if (sp == 0) break;
+        }
+        if (overflow && a.retry) {
+            // handed to the large-stack pass; its counts so far are taken back so the statistics
+            // count the group once
+            if (lane == 0) {
+                a.retry[atomicAdd(a.retry_count, 1)] = g;
+                n_tests -= g_tests;
+            }
+            n_int -= (unsigned long long)(g_mono + g_quad) * (unsigned long long)gr.y;
+            n_qint -= (unsigned long long)g_quad * (unsigned long long)gr.y;
+            n_steps -= g_steps;
+            __syncwarp();
+            continue;
         }
         if (overflow || runaway) {
             if (lane == 0) atomicOr(a.status, 1 << (overflow ? TG_ERR_STACK_OVERFLOW : TG_ERR_ITER_LIMIT));
@@ -926,71 +947,96 @@ __global__ void k_prep_targets(const double *tpos, const double *th, int64_t n, 
     tlo[i] = vec4<T>{lx, ly, lz, T(0)};
 }
 
+// Persistent grid: as many blocks of `warps` warps as fit on the GPU (fewer when every group has a
+// warp anyway; all of them for the retry pass, whose group count is known only on the device).
 template <typename T, int FIELDS, bool QUAD, int STACK>
-static tg_status launch_walk(WalkArgs<T> &a, cudaStream_t st) {
-    size_t smem = sizeof(WarpSmem<T, QUAD, STACK>) * WALK_WARPS;
+static tg_status launch_walk(WalkArgs<T> &a, int warps, cudaStream_t st) {
+    size_t smem = sizeof(WarpSmem<T, QUAD, STACK>) * warps;
     auto kern = k_walk<T, FIELDS, QUAD, STACK>;
     TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    TG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WALK_WARPS * 32, smem));
+    TG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem));
     if (per_sm < 1) per_sm = 1;
     int64_t blocks = (int64_t)per_sm * num_sms();
-    int64_t need = (a.ngroups + WALK_WARPS - 1) / WALK_WARPS;
-    if (blocks > need) blocks = need;
+    if (!a.ngroups_dev) {
+        int64_t need = (a.ngroups + warps - 1) / warps;
+        if (blocks > need) blocks = need;
+    }
     if (blocks < 1) blocks = 1;
-    { kern<<<(unsigned)blocks, WALK_WARPS * 32, smem, st>>>(a); tg::note_launch(); }
+    { kern<<<(unsigned)blocks, warps * 32, smem, st>>>(a); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
     return TG_OK;
 }
 
 template <typename T, int STACK>
-static tg_status dispatch_walk(WalkArgs<T> &a, int fields, bool quad, cudaStream_t st) {
+static tg_status dispatch_walk(WalkArgs<T> &a, int fields, bool quad, int warps, cudaStream_t st) {
     // Fields computed: potential and/or acceleration alone, or everything when the tidal tensor is
     // wanted (its setup already contains the other two).
     int fc = (fields & F_TID) ? (F_POT | F_ACC | F_TID) : fields;
     if (quad) {
         switch (fc) {
-            case F_POT: return launch_walk<T, F_POT, true, STACK>(a, st);
-            case F_ACC: return launch_walk<T, F_ACC, true, STACK>(a, st);
-            case F_POT | F_ACC: return launch_walk<T, F_POT | F_ACC, true, STACK>(a, st);
-            default: return launch_walk<T, F_POT | F_ACC | F_TID, true, STACK>(a, st);
+            case F_POT: return launch_walk<T, F_POT, true, STACK>(a, warps, st);
+            case F_ACC: return launch_walk<T, F_ACC, true, STACK>(a, warps, st);
+            case F_POT | F_ACC: return launch_walk<T, F_POT | F_ACC, true, STACK>(a, warps, st);
+            default: return launch_walk<T, F_POT | F_ACC | F_TID, true, STACK>(a, warps, st);
         }
     }
     switch (fc) {
-        case F_POT: return launch_walk<T, F_POT, false, STACK>(a, st);
-        case F_ACC: return launch_walk<T, F_ACC, false, STACK>(a, st);
-        case F_POT | F_ACC: return launch_walk<T, F_POT | F_ACC, false, STACK>(a, st);
-        default: return launch_walk<T, F_POT | F_ACC | F_TID, false, STACK>(a, st);
+        case F_POT: return launch_walk<T, F_POT, false, STACK>(a, warps, st);
+        case F_ACC: return launch_walk<T, F_ACC, false, STACK>(a, warps, st);
+        case F_POT | F_ACC: return launch_walk<T, F_POT | F_ACC, false, STACK>(a, warps, st);
+        default: return launch_walk<T, F_POT | F_ACC | F_TID, false, STACK>(a, warps, st);
     }
 }
 
-// Run the walk with the small stack; if any group overflowed it, rerun everything with the large one.
+// Scratch of one walk, in ints: queue, status, retry count, retry queue, then the retry list.
+constexpr int WS_QUEUE = 0, WS_STATUS = 1, WS_RETRY_COUNT = 2, WS_RETRY_QUEUE = 3, WS_RETRY_LIST = 4;
+inline int64_t walk_scratch_ints(int64_t ngroups) { return WS_RETRY_LIST + std::max<int64_t>(ngroups, 1); }
+
+// Enqueue a whole walk on st (no host synchronisation, so it can be captured): with the small
+// first stack, the small-stack pass, then a large-stack pass over the groups that overflowed it
+// (an empty pass when none did); with the large first stack, one large-stack pass. scratch:
+// walk_scratch_ints(a.ngroups) ints, zeroed here.
 template <typename T>
-static tg_status walk_with_fallback(WalkArgs<T> &a, int fields, bool quad, int *scratch, cudaStream_t st,
-                                    int *status_out, float *kernel_ms) {
+static tg_status enqueue_walk(WalkArgs<T> a, int fields, bool quad, int warps, int first_stack, int *scratch,
+                              cudaStream_t st) {
+    TG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int) * WS_RETRY_LIST, st));
+    a.queue = scratch + WS_QUEUE;
+    a.status = scratch + WS_STATUS;
+    a.ngroups_dev = nullptr;
+    if (first_stack == STACK_LARGE) {
+        a.retry = a.retry_count = nullptr;
+        return dispatch_walk<T, STACK_LARGE>(a, fields, quad, warps, st);
+    }
+    a.retry = scratch + WS_RETRY_LIST;
+    a.retry_count = scratch + WS_RETRY_COUNT;
+    TG_TRY((dispatch_walk<T, STACK_SMALL>(a, fields, quad, warps, st)));
+    WalkArgs<T> b = a;
+    b.queue = scratch + WS_RETRY_QUEUE;
+    b.group_order = scratch + WS_RETRY_LIST;  // retry list entries are group indices
+    b.ngroups_dev = scratch + WS_RETRY_COUNT;
+    b.retry = b.retry_count = nullptr;
+    return dispatch_walk<T, STACK_LARGE>(b, fields, quad, warps, st);
+}
+
+// Run a walk and time it on the stream; *status_out receives the device status word.
+template <typename T>
+static tg_status walk_with_fallback(WalkArgs<T> &a, int fields, bool quad, int warps, int first_stack, int *scratch,
+                                    cudaStream_t st, int *status_out, float *kernel_ms) {
     cudaEvent_t e0, e1;
     TG_CUDA(cudaEventCreate(&e0));
     TG_CUDA(cudaEventCreate(&e1));
     TG_CUDA(cudaEventRecord(e0, st));
-    TG_TRY((dispatch_walk<T, STACK_SMALL>(a, fields, quad, st)));
+    tg_status rc = enqueue_walk<T>(a, fields, quad, warps, first_stack, scratch, st);
     TG_CUDA(cudaEventRecord(e1, st));
     int status = 0;
-    TG_CUDA(cudaMemcpyAsync(&status, scratch + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TG_CUDA(cudaMemcpyAsync(&status, scratch + WS_STATUS, sizeof(int), cudaMemcpyDeviceToHost, st));
     TG_CUDA(cudaStreamSynchronize(st));
-    if (status & (1 << TG_ERR_STACK_OVERFLOW)) {
-        TG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int) * 2, st));
-        if (a.stats) TG_CUDA(cudaMemsetAsync(a.stats, 0, sizeof(unsigned long long) * 8, st));
-        TG_CUDA(cudaEventRecord(e0, st));
-        TG_TRY((dispatch_walk<T, STACK_LARGE>(a, fields, quad, st)));
-        TG_CUDA(cudaEventRecord(e1, st));
-        TG_CUDA(cudaMemcpyAsync(&status, scratch + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-        TG_CUDA(cudaStreamSynchronize(st));
-    }
     TG_CUDA(cudaEventElapsedTime(kernel_ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *status_out = status;
-    return TG_OK;
+    return rc;
 }
 
 // Walk targets already in walk order (tpos/th on the device). groups/group_root describe the
@@ -1002,8 +1048,7 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
     int w = ((fields & F_POT) ? 1 : 0) + ((fields & F_ACC) ? 3 : 0) + ((fields & F_TID) ? 9 : 0);
     if (!t->stats_dev) TG_CUDA(tg::dev_malloc((void **)&t->stats_dev, sizeof(unsigned long long) * 8, st));
     int *scratch = nullptr;
-    TG_CUDA(tg::dev_malloc((void **)&scratch, sizeof(int) * 2, st));
-    TG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int) * 2, st));
+    TG_CUDA(tg::dev_malloc((void **)&scratch, sizeof(int) * walk_scratch_ints(ngroups), st));
     TG_CUDA(cudaMemsetAsync(t->stats_dev, 0, sizeof(unsigned long long) * 8, st));
     tg_status rc = TG_OK;
     int status = 0;
@@ -1030,7 +1075,7 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         a.group_order = group_order;
         a.ngroups = ngroups; a.theta = theta; a.theta_group = theta_group; a.tol_group = tol_group; a.G = G;
         a.out_fields = fields; a.out_w = w; a.out = out; a.gs = group_size;
-        a.queue = scratch; a.status = scratch + 1; a.stats = (unsigned long long *)t->stats_dev;
+        a.stats = (unsigned long long *)t->stats_dev;
         a.gstats = gstats;
         vec4<double> *thi = nullptr, *tlo = nullptr;
         TG_CUDA(tg::dev_malloc((void **)&thi, sizeof(vec4<double>) * std::max<int64_t>(ntargets, 1), st));
@@ -1038,7 +1083,8 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         { k_prep_targets<double><<<div_up(ntargets, 256), 256, 0, st>>>(tpos, th, ntargets, thi, tlo); tg::note_launch(); }
         a.thi = thi;
         a.tlo = tlo;
-        rc = walk_with_fallback<double>(a, fields, quadrupole != 0, scratch, st, &status, &kms);
+        rc = walk_with_fallback<double>(a, fields, quadrupole != 0, t->walk_warps, t->walk_stack, scratch, st, &status,
+                                        &kms);
         cudaFreeAsync(thi, st);
         cudaFreeAsync(tlo, st);
     } else {
@@ -1051,7 +1097,7 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         a.group_order = group_order;
         a.ngroups = ngroups; a.theta = theta; a.theta_group = theta_group; a.tol_group = tol_group; a.G = G;
         a.out_fields = fields; a.out_w = w; a.out = out; a.gs = group_size;
-        a.queue = scratch; a.status = scratch + 1; a.stats = (unsigned long long *)t->stats_dev;
+        a.stats = (unsigned long long *)t->stats_dev;
         a.gstats = gstats;
         vec4<float> *thi = nullptr, *tlo = nullptr;
         TG_CUDA(tg::dev_malloc((void **)&thi, sizeof(vec4<float>) * std::max<int64_t>(ntargets, 1), st));
@@ -1059,7 +1105,8 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         { k_prep_targets<float><<<div_up(ntargets, 256), 256, 0, st>>>(tpos, th, ntargets, thi, tlo); tg::note_launch(); }
         a.thi = thi;
         a.tlo = tlo;
-        rc = walk_with_fallback<float>(a, fields, quadrupole != 0, scratch, st, &status, &kms);
+        rc = walk_with_fallback<float>(a, fields, quadrupole != 0, t->walk_warps, t->walk_stack, scratch, st, &status,
+                                       &kms);
         cudaFreeAsync(thi, st);
         cudaFreeAsync(tlo, st);
     }
@@ -1177,3 +1224,149 @@ tg_status make_groups(tg_tree_s *t, const std::vector<int64_t> &sys_off_host, in
 }
 
 }  // namespace tg
+
+// ---------------------------------------------------------------------------------------------
+// A tree's walk captured in a CUDA graph (tg_walk_graph_*; declared in include/pytreegrav_gb300.h).
+// Everything that needs the host (groups, the arena, the targets' hi/lo split, scratch) is made
+// once at creation; the graph holds only stream work: zeroing the counters, the small-stack pass
+// and the large-stack pass over the groups that overflowed it. Replays run with no host
+// synchronisation; tg_walk_graph_status reads the last replay's status word.
+
+struct tg_walk_graph_s {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int *scratch = nullptr;
+    float4 *thi = nullptr, *tlo = nullptr;
+    int2 *groups = nullptr;  // owned when the grouping is not the tree's cached one
+    int *groot = nullptr, *gorder = nullptr;
+    int64_t kernels = 0;     // kernel nodes per replay
+};
+
+namespace {
+
+void graph_release(tg_walk_graph_s *g) {
+    if (!g) return;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    void *bufs[] = {g->scratch, g->thi, g->tlo, g->groups, g->groot, g->gorder};
+    for (void *b : bufs)
+        if (b) cudaFreeAsync(b, 0);
+    delete g;
+}
+
+}  // namespace
+
+extern "C" {
+
+tg_status tg_walk_graph_create(tg_tree t, int fields, int quadrupole, double theta, double G, int group_size,
+                               int grouping, double *out, tg_walk_graph *out_graph) {
+    using namespace tg;
+    if (!t || !out || !out_graph || (fields & 7) == 0 || (fields & ~7) || !(theta > 0)) return TG_ERR_BAD_ARG;
+    if (group_size != 1 && group_size != 2 && group_size != 4 && group_size != 8 && group_size != 16 &&
+        group_size != 32)
+        return TG_ERR_BAD_ARG;
+    if (grouping != TG_GROUP_BLOCKS && grouping != TG_GROUP_TREE) return TG_ERR_BAD_ARG;
+    if (quadrupole && !t->quad) return TG_ERR_NO_QUADRUPOLES;
+    *out_graph = nullptr;
+    tg_walk_graph_s *g = new (std::nothrow) tg_walk_graph_s();
+    if (!g) return TG_ERR_OOM;
+    cudaStream_t cs = nullptr;
+    tg_status rc = TG_OK;
+    auto fail = [&](tg_status r) {
+        if (cs) cudaStreamDestroy(cs);
+        graph_release(g);
+        return r;
+    };
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return fail(TG_ERR_CUDA);
+    const int2 *wg;
+    const int *wr;
+    int64_t ng;
+    if (grouping == TG_GROUP_TREE) {
+        if ((rc = tree_groups(t, group_size, cs)) != TG_OK) return fail(rc);
+        wg = t->groups;
+        wr = t->group_root;
+        ng = t->ngroups;
+    } else {
+        if ((rc = make_groups(t, t->sys_off, group_size, &g->groups, &g->groot, &ng, cs)) != TG_OK) return fail(rc);
+        if ((rc = make_cost_order(t->coord, g->groups, ng, &g->gorder, cs)) != TG_OK) return fail(rc);
+        wg = g->groups;
+        wr = g->groot;
+    }
+    if ((rc = build_arena(t, t->arena32, cs)) != TG_OK) return fail(rc);
+    const int64_t n = t->ntot;
+    if (!t->stats_dev && dev_malloc((void **)&t->stats_dev, sizeof(unsigned long long) * 8, cs) != cudaSuccess)
+        return fail(TG_ERR_OOM);
+    if (dev_malloc((void **)&g->thi, sizeof(float4) * std::max<int64_t>(n, 1), cs) != cudaSuccess ||
+        dev_malloc((void **)&g->tlo, sizeof(float4) * std::max<int64_t>(n, 1), cs) != cudaSuccess ||
+        dev_malloc((void **)&g->scratch, sizeof(int) * walk_scratch_ints(ng), cs) != cudaSuccess)
+        return fail(TG_ERR_OOM);
+    { k_prep_targets<float><<<div_up(n, 256), 256, 0, cs>>>(t->coord, t->soft, n, g->thi, g->tlo); note_launch(); }
+    if (cudaStreamSynchronize(cs) != cudaSuccess) return fail(TG_ERR_CUDA);
+
+    WalkArgs<float> a;
+    a.ar = t->arena32;
+    a.ntot = t->ntot;
+    a.tc = t->coord; a.ts = t->soft; a.tsize = t->size; a.tdelta = t->delta;
+    a.tpos = t->coord; a.th = t->soft; a.scatter = t->walk_idx; a.groups = wg; a.group_root = wr;
+    a.group_order = g->gorder;
+    a.ngroups = ng; a.theta = theta; a.theta_group = nullptr; a.tol_group = nullptr; a.G = G;
+    a.out_fields = fields;
+    a.out_w = ((fields & F_POT) ? 1 : 0) + ((fields & F_ACC) ? 3 : 0) + ((fields & F_TID) ? 9 : 0);
+    a.out = out; a.gs = group_size;
+    a.stats = (unsigned long long *)t->stats_dev;
+    a.gstats = nullptr;
+    a.thi = g->thi;
+    a.tlo = g->tlo;
+    const int64_t launches0 = launches_so_far();
+    if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed) != cudaSuccess) return fail(TG_ERR_CUDA);
+    rc = TG_OK;
+    if (cudaMemsetAsync(t->stats_dev, 0, sizeof(unsigned long long) * 8, cs) != cudaSuccess) rc = TG_ERR_CUDA;
+    if (rc == TG_OK) rc = enqueue_walk<float>(a, fields, quadrupole != 0, t->walk_warps, t->walk_stack, g->scratch, cs);
+    cudaError_t ce = cudaStreamEndCapture(cs, &g->graph);
+    note_launches(launches0 - launches_so_far());  // recorded, not run
+    if (rc != TG_OK) return fail(rc);
+    if (ce != cudaSuccess) {
+        set_last_error("cudaStreamEndCapture", ce);
+        return fail(TG_ERR_CUDA);
+    }
+    if ((ce = cudaGraphInstantiate(&g->exec, g->graph, 0)) != cudaSuccess) {
+        set_last_error("cudaGraphInstantiate", ce);
+        return fail(TG_ERR_CUDA);
+    }
+    size_t nn = 0;
+    cudaGraphGetNodes(g->graph, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (nn) cudaGraphGetNodes(g->graph, nodes.data(), &nn);
+    for (auto nd : nodes) {
+        cudaGraphNodeType ty;
+        if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) g->kernels++;
+    }
+    cudaStreamDestroy(cs);
+    *out_graph = g;
+    return TG_OK;
+}
+
+tg_status tg_walk_graph_launch(tg_walk_graph g, void *stream) {
+    if (!g) return TG_ERR_BAD_ARG;
+    TG_CUDA(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+    tg::note_launches(g->kernels);
+    return TG_OK;
+}
+
+tg_status tg_walk_graph_status(tg_walk_graph g, void *stream) {
+    if (!g) return TG_ERR_BAD_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    int status = 0;
+    TG_CUDA(cudaMemcpyAsync(&status, g->scratch + tg::WS_STATUS, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TG_CUDA(cudaStreamSynchronize(st));
+    if (status & (1 << TG_ERR_STACK_OVERFLOW)) return TG_ERR_STACK_OVERFLOW;
+    if (status & (1 << TG_ERR_ITER_LIMIT)) return TG_ERR_ITER_LIMIT;
+    return TG_OK;
+}
+
+tg_status tg_walk_graph_free(tg_walk_graph g) {
+    graph_release(g);
+    return TG_OK;
+}
+
+}  // extern "C"

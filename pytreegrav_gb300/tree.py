@@ -65,6 +65,35 @@ class Octree:
         self.HasCoincidentPoints = bool(info.has_coincident)
         return self
 
+    @classmethod
+    def batched(cls, pos, m, softening, offsets, quadrupole=False):
+        """Independent systems stored back to back (system s owns rows offsets[s]:offsets[s+1]) in
+        one tree arena from one segmented build (no counterpart in pytreegrav)."""
+        L = _lib.load()
+        pos = _as_f64(pos, (-1, 3))
+        n = len(pos)
+        m = _as_f64(m, (n,))
+        softening = np.zeros(n) if softening is None else _as_f64(softening, (n,))
+        offsets = np.ascontiguousarray(offsets, np.int64)
+        handle = ctypes.c_void_p()
+        rc = L.tg_tree_build_batched(_lib.ptr(pos), _lib.ptr(m), _lib.ptr(softening), _lib.ptr(offsets),
+                                     len(offsets) - 1, int(bool(quadrupole)), _lib.TG_MEM_HOST, None,
+                                     ctypes.byref(handle))
+        _lib.check(rc, "batched build")
+        return cls._from_handle(handle, quadrupole)
+
+    def set_walk_config(self, warps_per_block=4, first_stack=1024):
+        """Launch shape of this tree's walks (see tg_tree_set_walk_config); results do not depend on it."""
+        _lib.check(_lib.load().tg_tree_set_walk_config(self._h, int(warps_per_block), int(first_stack)),
+                   "walk config")
+
+    def walk_graph(self, out, potential=False, accel=False, tidal=False, quadrupole=False, group_size=32,
+                   theta=0.7, G=1.0, grouping="tree"):
+        """The walk of this tree's own particles captured in a CUDA graph (tg_walk_graph_*), writing
+        to `out`, a device array of NumParticles x W float64 (an integer address or an object with
+        data_ptr()) that must outlive the graph."""
+        return WalkGraph(self, out, potential, accel, tidal, quadrupole, group_size, theta, G, grouping)
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h is not None and h.value:
@@ -193,6 +222,43 @@ class Octree:
         v = [ctypes.c_int64() for _ in range(4)]
         _lib.check(_lib.load().tg_tree_last_walk_stats(self._h, *[ctypes.byref(x) for x in v]))
         return tuple(int(x.value) for x in v)
+
+
+class WalkGraph:
+    """A captured walk (see Octree.walk_graph): launch() replays it on a stream, status() waits and
+    raises if the last replay failed."""
+
+    def __init__(self, tree, out, potential, accel, tidal, quadrupole, group_size, theta, G, grouping):
+        fields = (_lib.TG_FIELD_POTENTIAL * bool(potential) + _lib.TG_FIELD_ACCEL * bool(accel)
+                  + _lib.TG_FIELD_TIDAL * bool(tidal))
+        if fields == 0:
+            raise ValueError("request at least one of potential=True, accel=True, tidal=True")
+        self.tree = tree  # the graph reads the tree's arrays
+        self.out = out
+        addr = out.data_ptr() if hasattr(out, "data_ptr") else int(out)
+        grp = {"blocks": _lib.TG_GROUP_BLOCKS, "tree": _lib.TG_GROUP_TREE}[grouping]
+        self._g = ctypes.c_void_p()
+        _lib.check(_lib.load().tg_walk_graph_create(tree._h, fields, int(bool(quadrupole)), float(theta), float(G),
+                                                    int(group_size), grp, ctypes.c_void_p(addr),
+                                                    ctypes.byref(self._g)), "walk graph")
+
+    def launch(self, stream=None):
+        _lib.check(_lib.load().tg_walk_graph_launch(self._g, stream), "walk graph launch")
+
+    def status(self, stream=None):
+        _lib.check(_lib.load().tg_walk_graph_status(self._g, stream), "walk graph")
+
+    def close(self):
+        g = getattr(self, "_g", None)
+        if g is not None and g.value:
+            _lib.load().tg_walk_graph_free(g)
+            self._g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def _split(out, potential, accel, tidal):
