@@ -272,6 +272,7 @@ struct WarpSmem {
     vec4<T> snear[32];  // offsets + mass of the near sources, swept with softening
     T sh[32];
     vec4<T> sq[QUAD ? 64 : 1];   // quadrupole records of the staged nodes
+    double xbox[8];  // the exact test's FP64 group box: min (3), max (3), max softening, theta
 };
 
 template <typename T>
@@ -474,10 +475,12 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32, STACK == STACK_SMALL ? 3 
             }
             hmax_g = fmax(hmax_g, __shfl_xor_sync(FULL, hmax_g, o));
         }
-        // FP64 box for the exact acceptance test, computed on first need
+        // FP64 box for the exact acceptance test, computed on first need and kept in the warp's
+        // shared memory (with theta), not in registers through the whole traversal
         bool have_box_d = false;
-        double bmin[3], bmax[3], hmax_d = 0.0;
+        if (lane == 0) sm.xbox[7] = theta;
         auto box_d = [&]() {
+            double bmin[3], bmax[3], hmax_d;
             double px = a.tpos[3 * t], py = a.tpos[3 * t + 1], pz = a.tpos[3 * t + 2];
             bmin[0] = bmax[0] = px;
             bmin[1] = bmax[1] = py;
@@ -492,6 +495,14 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32, STACK == STACK_SMALL ? 3 
                 }
                 hmax_d = fmax(hmax_d, __shfl_xor_sync(FULL, hmax_d, o));
             }
+            if (lane == 0) {
+                for (int k = 0; k < 3; k++) {
+                    sm.xbox[k] = bmin[k];
+                    sm.xbox[3 + k] = bmax[k];
+                }
+                sm.xbox[6] = hmax_d;
+            }
+            __syncwarp();
             have_box_d = true;
         };
         const T gscale = fabs(abmin[0]) + fabs(abmin[1]) + fabs(abmin[2]) + fabs(abmax[0]) + fabs(abmax[1]) +
@@ -664,7 +675,8 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32, STACK == STACK_SMALL ? 3 
                 if (__any_sync(FULL, unsure)) {
                     if (!have_box_d) box_d();
                     if (unsure)
-                        acc = accept_exact(a.ntot + node, a.tc, a.ts, a.tsize, a.tdelta, bmin, bmax, hmax_d, theta);
+                        acc = accept_exact(a.ntot + node, a.tc, a.ts, a.tsize, a.tdelta, sm.xbox, sm.xbox + 3,
+                                           sm.xbox[6], sm.xbox[7]);
                 }
                 const bool opn = node >= 0 && !acc;
                 const int cbits = opn ? bits_int(r1.z) : 0, lbits = opn ? bits_int(r1.w) : 0;
