@@ -1489,6 +1489,7 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     dfree(lvl, st); dfree(lvl_list, st); dfree(fdepth, st);
     dfree(sys_off, st); dfree(mn, st); dfree(mx, st); dfree(center, st); dfree(size, st);
     TG_CUDA(cudaStreamSynchronize(st));
+    TG_TRY(sort_error_check());
     if (links_bad) {
         set_last_error_msg("internal error: octree links out of range");
         return TG_ERR_CUDA;
@@ -1528,7 +1529,7 @@ tg_status morton_order_device(const double *pos, int64_t n, uint32_t *perm, cuda
     dfree(sys_off, st); dfree(mn, st); dfree(mx, st); dfree(center, st); dfree(size, st); dfree(keys, st);
     // the host vector `off` must outlive the copy
     TG_CUDA(cudaStreamSynchronize(st));
-    return TG_OK;
+    return sort_error_check();
 }
 
 }  // namespace tg

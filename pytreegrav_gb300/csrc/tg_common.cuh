@@ -82,6 +82,9 @@ tg_status exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n, cudaStr
 // Stable LSD radix sort of (key, value) pairs on the low `bits` bits of the keys. keys/vals are
 // sorted in place (scratch buffers are allocated stream-ordered and freed before return).
 tg_status radix_sort_pairs(uint64_t *keys, uint32_t *vals, int64_t n, int bits, cudaStream_t s);
+// After a synchronisation: TG_ERR_QUEUE_TIMEOUT (and the flag cleared) if a sort's look-back ran
+// out of its bound since the last check.
+tg_status sort_error_check();
 
 int num_sms();
 

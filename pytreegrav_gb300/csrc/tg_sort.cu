@@ -4,6 +4,7 @@
 // yields the same permutation, which is what makes the GPU order bit-identical to the reference:
 // 8-bit digits, one tile of 4096 keys per CTA, ranks made stable by processing each warp's slice
 // in order with __match_any_sync, and per-(digit, tile) offsets from a digit-major scan.
+#include <algorithm>
 #include <cstdio>
 #include <mutex>
 
@@ -174,13 +175,14 @@ constexpr int RS_WARP_KEYS = RS_ROUNDS * 32;       // 512 consecutive keys per w
 constexpr int RS_TILE = RS_WARPS * RS_WARP_KEYS;   // 4096 keys per CTA
 constexpr int RS_BINS = 256;
 
-// Per-warp stable ranking of the warp's 512 keys; leaves per-warp digit counts in wcount.
+// Per-warp stable ranking of the warp's ROUNDS * 32 keys; leaves per-warp digit counts in wcount.
+template <int ROUNDS = RS_ROUNDS>
 __device__ __forceinline__ void rank_warp_slice(const uint64_t *keys, int64_t n, int64_t wbase, int shift,
                                                 int *wcount, int *digit, int *rank) {
     const int lane = lane_id();
     const unsigned lt = lanemask_lt();
 #pragma unroll
-    for (int r = 0; r < RS_ROUNDS; r++) {
+    for (int r = 0; r < ROUNDS; r++) {
         int64_t i = wbase + r * 32 + lane;
         int d = RS_BINS;  // sentinel for keys past the end
         if (i < n) d = (int)((keys[i] >> shift) & (RS_BINS - 1));
@@ -246,22 +248,145 @@ __global__ void __launch_bounds__(RS_THREADS) radix_scatter(const uint64_t *keys
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// One-sweep passes (decoupled look-back). All digit histograms come from one read of the keys;
+// then each pass is one kernel: a CTA takes the next tile from an atomic counter (so every earlier
+// tile belongs to a CTA that is already running), ranks its keys stably as above, publishes its
+// per-digit count, looks back over earlier tiles' published words for its exclusive prefix, and
+// scatters. A look-back spin is bounded; running out sets g_sort_error (checked by sort_error_check)
+// instead of hanging.
+
+constexpr int MAX_PASSES = 8;
+constexpr int OS_ROUNDS = 4;                        // keys per thread in a one-sweep pass
+constexpr int OS_WARP_KEYS = OS_ROUNDS * 32;
+constexpr int OS_TILE = RS_WARPS * OS_WARP_KEYS;   // 1024 keys per CTA: many CTAs per SM
+constexpr unsigned long long ST_AGG = 1ull << 62, ST_INC = 2ull << 62, ST_VAL = (1ull << 62) - 1;
+constexpr long long SPIN_LIMIT = 1ll << 22;
+__device__ int g_sort_error;
+
+__global__ void __launch_bounds__(256) k_sort_hist_all(const uint64_t *keys, int64_t n, int npass, int *hist) {
+    __shared__ int h[MAX_PASSES * RS_BINS];
+    for (int i = threadIdx.x; i < npass * RS_BINS; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = keys[i];
+        for (int p = 0; p < npass; p++) atomicAdd(&h[p * RS_BINS + (int)((k >> (8 * p)) & (RS_BINS - 1))], 1);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < npass * RS_BINS; i += blockDim.x)
+        if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+// Exclusive scan of each pass's 256 digit counts, in place. One block of 256 threads.
+__global__ void k_sort_digit_offsets(int *hist, int npass) {
+    __shared__ int tot;
+    for (int p = 0; p < npass; p++) {
+        int v = hist[p * RS_BINS + threadIdx.x];
+        int ex = block_exclusive_scan(v, &tot);
+        hist[p * RS_BINS + threadIdx.x] = ex;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_onesweep(const uint64_t *keys, const uint32_t *vals, int64_t n,
+                                                         int shift, const int *digit_off,
+                                                         unsigned long long *status, int *tile_counter,
+                                                         uint64_t *keys_out, uint32_t *vals_out) {
+    __shared__ int wcount[RS_WARPS][RS_BINS];
+    __shared__ int prefix[RS_BINS];
+    __shared__ int tile_s;
+    if (threadIdx.x == 0) tile_s = atomicAdd(tile_counter, 1);
+    for (int i = threadIdx.x; i < RS_WARPS * RS_BINS; i += RS_THREADS) (&wcount[0][0])[i] = 0;
+    __syncthreads();
+    const int t = tile_s;
+    const int w = threadIdx.x >> 5;
+    const int64_t wbase = (int64_t)t * OS_TILE + (int64_t)w * OS_WARP_KEYS;
+    int digit[OS_ROUNDS], rank[OS_ROUNDS];
+    rank_warp_slice<OS_ROUNDS>(keys, n, wbase, shift, wcount[w], digit, rank);
+    __syncthreads();
+    {  // one thread per digit: offsets of the warps within the tile, then the tile's prefix
+        const int d = threadIdx.x;
+        int run = 0;
+#pragma unroll
+        for (int ww = 0; ww < RS_WARPS; ww++) {
+            int c = wcount[ww][d];
+            wcount[ww][d] = run;
+            run += c;
+        }
+        volatile unsigned long long *st = status + (int64_t)t * RS_BINS + d;
+        long long acc = 0;
+        if (t == 0) {
+            *st = ST_INC | (unsigned long long)run;
+        } else {
+            *st = ST_AGG | (unsigned long long)run;
+            // earlier tiles publish their aggregate without waiting on anyone, so each wait ends
+            // once that tile's CTA (already running: it took its tile before this one) has ranked
+            for (int64_t j = t - 1; j >= 0; j--) {
+                const volatile unsigned long long *src = status + j * RS_BINS + d;
+                unsigned long long wd = *src;
+                for (long long spins = 0; !(wd & ~ST_VAL) && spins < SPIN_LIMIT; spins++) wd = *src;
+                if (!(wd & ~ST_VAL)) {
+                    atomicExch(&g_sort_error, 1);
+                    break;
+                }
+                acc += (long long)(wd & ST_VAL);
+                if ((wd & ~ST_VAL) == ST_INC) break;
+            }
+            *st = ST_INC | (unsigned long long)(acc + run);
+        }
+        prefix[d] = digit_off[d] + (int)acc;
+    }
+    __syncthreads();
+    const int lane = lane_id();
+#pragma unroll
+    for (int r = 0; r < OS_ROUNDS; r++) {
+        int64_t i = wbase + r * 32 + lane;
+        if (i < n) {
+            int pos = prefix[digit[r]] + wcount[w][digit[r]] + rank[r];
+            keys_out[pos] = keys[i];
+            vals_out[pos] = vals[i];
+        }
+    }
+}
+
+tg_status sort_error_check() {
+    int e = 0;
+    TG_CUDA(cudaMemcpyFromSymbol(&e, g_sort_error, sizeof(int)));
+    if (e) {
+        int z = 0;
+        cudaMemcpyToSymbol(g_sort_error, &z, sizeof(int));
+        set_last_error_msg("radix sort: a tile's look-back did not complete within its bound");
+        return TG_ERR_QUEUE_TIMEOUT;
+    }
+    return TG_OK;
+}
+
 tg_status radix_sort_pairs(uint64_t *keys, uint32_t *vals, int64_t n, int bits, cudaStream_t s) {
     if (n <= 1 || bits <= 0) return TG_OK;
     if (n > (int64_t)0x7fffffff) return TG_ERR_BAD_ARG;
-    int ntiles = div_up(n, RS_TILE);
+    const int ntiles = div_up(n, OS_TILE);
+    const int npass = std::min((bits + 7) / 8, MAX_PASSES);
     uint64_t *k2 = nullptr;
     uint32_t *v2 = nullptr;
-    int *hist = nullptr;
+    unsigned char *scr = nullptr;
+    const size_t st_bytes = sizeof(unsigned long long) * (size_t)ntiles * RS_BINS;
+    const size_t hist_bytes = sizeof(int) * MAX_PASSES * RS_BINS;
     TG_CUDA(tg::dev_malloc((void **)&k2, sizeof(uint64_t) * n, s));
     TG_CUDA(tg::dev_malloc((void **)&v2, sizeof(uint32_t) * n, s));
-    TG_CUDA(tg::dev_malloc((void **)&hist, sizeof(int) * (int64_t)RS_BINS * ntiles, s));
+    TG_CUDA(tg::dev_malloc((void **)&scr, st_bytes + hist_bytes + sizeof(int) * MAX_PASSES, s));
+    unsigned long long *status = (unsigned long long *)scr;
+    int *hist = (int *)(scr + st_bytes);
+    int *counters = hist + MAX_PASSES * RS_BINS;
+    TG_CUDA(cudaMemsetAsync(hist, 0, hist_bytes + sizeof(int) * MAX_PASSES, s));
+    const int hblocks = (int)std::min<int64_t>(div_up(n, 256 * 16), (int64_t)num_sms() * 4);
+    { k_sort_hist_all<<<hblocks, 256, 0, s>>>(keys, n, npass, hist); tg::note_launch(); }
+    { k_sort_digit_offsets<<<1, RS_BINS, 0, s>>>(hist, npass); tg::note_launch(); }
     uint64_t *kin = keys, *kout = k2;
     uint32_t *vin = vals, *vout = v2;
-    for (int shift = 0; shift < bits; shift += 8) {
-        { radix_hist<<<ntiles, RS_THREADS, 0, s>>>(kin, n, shift, ntiles, hist); tg::note_launch(); }
-        TG_TRY(exclusive_scan_i32(hist, hist, (int64_t)RS_BINS * ntiles, s));
-        { radix_scatter<<<ntiles, RS_THREADS, 0, s>>>(kin, vin, n, shift, ntiles, hist, kout, vout); tg::note_launch(); }
+    for (int p = 0; p < npass; p++) {
+        TG_CUDA(cudaMemsetAsync(status, 0, st_bytes, s));
+        { k_onesweep<<<ntiles, RS_THREADS, 0, s>>>(kin, vin, n, 8 * p, hist + p * RS_BINS, status, counters + p, kout,
+                                                   vout); tg::note_launch(); }
         TG_CUDA(cudaGetLastError());
         uint64_t *tk = kin; kin = kout; kout = tk;
         uint32_t *tv = vin; vin = vout; vout = tv;
@@ -272,7 +397,7 @@ tg_status radix_sort_pairs(uint64_t *keys, uint32_t *vals, int64_t n, int bits, 
     }
     TG_CUDA(cudaFreeAsync(k2, s));
     TG_CUDA(cudaFreeAsync(v2, s));
-    TG_CUDA(cudaFreeAsync(hist, s));
+    TG_CUDA(cudaFreeAsync(scr, s));
     return TG_OK;
 }
 

@@ -1134,6 +1134,7 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
     t->last_stats.steps = (int64_t)stats[3];
     t->last_stats.quad_interactions = (int64_t)stats[4];
     t->last_stats.kernel_ms = kms;
+    TG_TRY(sort_error_check());  // the grouping's sorts
     if (status & (1 << TG_ERR_STACK_OVERFLOW)) return TG_ERR_STACK_OVERFLOW;
     if (status & (1 << TG_ERR_ITER_LIMIT)) return TG_ERR_ITER_LIMIT;
     return TG_OK;
