@@ -683,6 +683,29 @@ __global__ void k_write_particles(int64_t ntot, const int64_t *p_parent, const i
     delta[i] = 0.0;
 }
 
+// Children of every node in the order the moment sums take them (octree.py:199-292): particle
+// children in chain order, then node children in reverse chain order. An entry >= 0 is a particle
+// index, an entry < 0 the node ~entry; nk holds the count (at most 8, as the chain walks in the
+// moment kernels allow). A second walk over the chain (whose lines the first one brought into L1)
+// places the node children from the back, so no local array is needed.
+__global__ void k_kids(int64_t ntot, int64_t mtot, const int64_t *first, const int64_t *next, int32_t *kids,
+                       int8_t *nk) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= mtot) return;
+    const int64_t f = ntot + j, stop = next[f], ne = ntot + mtot;
+    int32_t *out = kids + 8 * j;
+    int np = 0, nn = 0;
+    for (int64_t c = first[f]; c != stop && c >= 0 && c < ne && np + nn < 8; c = next[c]) {
+        if (c < ntot) out[np++] = (int32_t)c;
+        else nn++;
+    }
+    int w = np + nn;
+    int s = 0;
+    for (int64_t c = first[f]; c != stop && c >= 0 && c < ne && s < 8; c = next[c], s++)
+        if (c >= ntot) out[--w] = ~(int32_t)(c - ntot);
+    nk[j] = (int8_t)(np + nn);
+}
+
 // Capacity bookkeeping for a bucket (octree.py:930-933): new_node_idx when the bucket is reached
 // plus the worst-case chain; new_node_idx there is 1 + the number of nodes the split allocated
 // earlier, i.e. the sorted position of the bucket's first allocation.
@@ -843,10 +866,114 @@ __device__ void node_moments(const MomentArgs &a, int64_t f) {
 
 // Level by level, deepest first: one launch per depth over that depth's node list, so every lane
 // of a warp works on a node (FP64 throughput is scarce on this GPU, and a warp instruction costs
-// the same with one lane active as with 32). Children are finished by the previous launch.
-__global__ void k_moments_level(MomentArgs a, const int32_t *list, int count) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < count) node_moments(a, a.ntot + list[i]);
+// the same with one lane active as with 32). Children are finished by the previous launch, so the
+// level kernels read them through L1.
+// node_moments over the child list k_kids made. Every child takes the same instructions: a
+// particle adds (m, m x, softening) and a node (m, its mass-weighted coordinate sum times 1.0,
+// which is exact, softening); a zero-mass node adds -0.0, the exact identity of a sum, and leaves
+// the softening maximum alone, which is the reference's skipping it. A warp's lanes thus part only
+// on the node children's quadrupole term, and a warp of nodes with equal child counts (see
+// k_moments_sorted) runs with every lane busy.
+__device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j, const int32_t *kids, int n) {
+    const int4 k0 = *reinterpret_cast<const int4 *>(kids + 8 * j);
+    const int4 k1 = *reinterpret_cast<const int4 *>(kids + 8 * j + 4);
+    const int32_t ch[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+    const int64_t N = a.ntot;
+    double m = 0.0, ax = 0.0, ay = 0.0, az = 0.0, h = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        if (q < n) {
+            const int32_t c = ch[q];
+            const bool part = c >= 0;
+            const int64_t g = part ? (int64_t)c : N + (int64_t)(~c);
+            const double mc = a.mass[g];
+            const double *src = part ? a.coord + 3 * g : a.acc + 3 * (int64_t)(~c);
+            const double w = part ? mc : 1.0;
+            const bool use = part || mc != 0.0;
+            const double hc = a.soft[g];
+            m = dadd(m, use ? mc : -0.0);
+            ax = dadd(ax, use ? dmul(w, src[0]) : -0.0);
+            ay = dadd(ay, use ? dmul(w, src[1]) : -0.0);
+            az = dadd(az, use ? dmul(w, src[2]) : -0.0);
+            h = use ? pymax(h, hc) : h;
+        }
+    }
+    const int64_t f = N + j;
+    a.mass[f] = m;
+    a.soft[f] = h;
+    a.acc[3 * j] = ax;
+    a.acc[3 * j + 1] = ay;
+    a.acc[3 * j + 2] = az;
+    double com[3] = {a.coord[3 * f], a.coord[3 * f + 1], a.coord[3 * f + 2]};
+    if (m != 0.0) {
+        double inv = ddiv(1.0, m);
+        double accs[3] = {ax, ay, az};
+        double d2 = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            double cm = dmul(accs[k], inv);
+            double dx = dsub(cm, com[k]);
+            d2 = dadd(d2, dmul(dx, dx));
+            com[k] = cm;
+            a.coord[3 * f + k] = cm;
+        }
+        a.delta[f] = __dsqrt_rn(d2);
+    }
+    if (a.quads) {
+        double Q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            if (q < n) {
+                const int32_t c = ch[q];
+                const bool part = c >= 0;
+                const int64_t g = part ? (int64_t)c : N + (int64_t)(~c);
+                const double mc = a.mass[g];
+                if (part || mc != 0.0) {
+                    if (!part) {
+#pragma unroll
+                        for (int k = 0; k < 9; k++) Q[k] = dadd(Q[k], a.quad[9 * (int64_t)(~c) + k]);
+                    }
+                    shift_quad(Q, mc, dsub(a.coord[3 * g], com[0]), dsub(a.coord[3 * g + 1], com[1]),
+                               dsub(a.coord[3 * g + 2], com[2]));
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 9; k++) a.quad[9 * j + k] = Q[k];
+    }
+}
+
+// Large levels (FP64-throughput-bound): one thread per node, the block's nodes first ordered by
+// child count (a counting sort in shared memory, most children first) so that a warp's lanes run
+// the same number of child steps. Which thread takes which node does not change any result.
+constexpr int MOM_BLOCK = 256;
+__global__ void __launch_bounds__(MOM_BLOCK) k_moments_sorted(MomentArgs a, const int32_t *list, int count,
+                                                              const int32_t *kids, const int8_t *nk) {
+    __shared__ int bin[9];
+    __shared__ int order[MOM_BLOCK];
+    const int t = threadIdx.x;
+    const int i = blockIdx.x * MOM_BLOCK + t;
+    const int j0 = i < count ? list[i] : -1;
+    int k0 = j0 >= 0 ? (int)nk[j0] : 0;
+    k0 = k0 < 0 ? 0 : (k0 > 8 ? 8 : k0);
+    if (t < 9) bin[t] = 0;
+    __syncthreads();
+    const int r = atomicAdd(&bin[k0], 1);
+    __syncthreads();
+    if (t == 0) {
+        int run = 0;
+        for (int b = 8; b >= 0; b--) {
+            const int c = bin[b];
+            bin[b] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    order[bin[k0] + r] = j0;
+    __syncthreads();
+    const int j = order[t];
+    if (j < 0) return;
+    node_moments_kids(a, j, kids, nk[j]);
 }
 
 // One quadrupole entry e = 3a + b of shift_quad's update for a child of mass m at offset r.
@@ -862,42 +989,39 @@ __device__ __forceinline__ double quad_term(int e, double m, double r0, double r
 }
 
 // Small levels (latency-bound: too few nodes to hide a thread's long FP64 chain): 16 lanes per
-// node. Lanes 0-4 each carry one of the mass pass's sums (mass, three mass-weighted coordinates,
-// softening max) and lanes 0-8 one quadrupole entry each; every sum takes its terms in the same
-// order as node_moments, so the results are identical.
-__global__ void k_moments_level_coop(MomentArgs a, const int32_t *list, int count) {
+// node over k_kids's child list. Lanes 0-4 each carry one of the mass pass's sums (mass, three
+// mass-weighted coordinates, softening max) and lanes 0-8 one quadrupole entry each; every sum
+// takes its terms in the same order as node_moments, so the results are identical.
+__global__ void k_moments_level_coop(MomentArgs a, const int32_t *list, int count, const int32_t *kids,
+                                     const int8_t *nk) {
     const int lane = threadIdx.x & 31, sub = lane & 15, half = lane >> 4;
     const int node = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 4);
     if (node >= count) return;  // whole half-warps leave together
     const unsigned hmask = 0xFFFFu << (16 * half);
-    const int64_t f = a.ntot + list[node];
-    const int64_t stop = a.next[f];
-    const int64_t ne = a.ntot + a.mtot;
-    int64_t ch[8];
-    int n = 0;
-    for (int64_t c = a.first[f]; c != stop && c >= 0 && c < ne && n < 8; c = a.next[c]) ch[n++] = c;
+    const int64_t N = a.ntot;
+    const int64_t j = list[node];
+    const int64_t f = N + j;
+    const int n = nk[j];
+    const int4 k0 = *reinterpret_cast<const int4 *>(kids + 8 * j);
+    const int4 k1 = *reinterpret_cast<const int4 *>(kids + 8 * j + 4);
+    const int32_t ch[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
     double v = 0.0;
     if (sub < 5) {
 #pragma unroll
         for (int q = 0; q < 8; q++) {
-            if (q < n && ch[q] < a.ntot) {
-                const int64_t c = ch[q];
-                double mi = __ldcg(a.mass + c);
-                if (sub == 0) v = dadd(v, mi);
-                else if (sub < 4) v = dadd(v, dmul(mi, __ldcg(a.coord + 3 * c + sub - 1)));
-                else v = pymax(v, __ldcg(a.soft + c));
-            }
-        }
-#pragma unroll
-        for (int q = 7; q >= 0; q--) {
-            if (q < n && ch[q] >= a.ntot) {
-                const int64_t c = ch[q];
-                double mc = __ldcg(a.mass + c);
-                if (mc != 0.0) {
-                    const int64_t cj = c - a.ntot;
-                    if (sub == 0) v = dadd(v, mc);
-                    else if (sub < 4) v = dadd(v, __ldcg(a.acc + 3 * cj + sub - 1));
-                    else v = pymax(v, __ldcg(a.soft + c));
+            if (q < n) {
+                const int32_t c = ch[q];
+                const bool part = c >= 0;
+                const int64_t g = part ? (int64_t)c : N + (int64_t)(~c);
+                const double mc = a.mass[g];
+                const bool use = part || mc != 0.0;
+                if (sub == 0) {
+                    v = dadd(v, use ? mc : -0.0);
+                } else if (sub < 4) {
+                    const double x = part ? a.coord[3 * g + sub - 1] : a.acc[3 * (int64_t)(~c) + sub - 1];
+                    v = dadd(v, use ? dmul(part ? mc : 1.0, x) : -0.0);
+                } else if (use) {
+                    v = pymax(v, a.soft[g]);
                 }
             }
         }
@@ -905,7 +1029,6 @@ __global__ void k_moments_level_coop(MomentArgs a, const int32_t *list, int coun
     const double m = __shfl_sync(hmask, v, 0, 16);
     const double ax = __shfl_sync(hmask, v, 1, 16), ay = __shfl_sync(hmask, v, 2, 16);
     const double az = __shfl_sync(hmask, v, 3, 16), h = __shfl_sync(hmask, v, 4, 16);
-    const int64_t j = f - a.ntot;
     double com0 = 0.0, com1 = 0.0, com2 = 0.0;
     if (sub == 0) {
         a.mass[f] = m;
@@ -937,21 +1060,15 @@ __global__ void k_moments_level_coop(MomentArgs a, const int32_t *list, int coun
         double Q = 0.0;
 #pragma unroll
         for (int q = 0; q < 8; q++) {
-            if (q < n && ch[q] < a.ntot) {
-                const int64_t c = ch[q];
-                Q = dadd(Q, quad_term(sub, __ldcg(a.mass + c), dsub(__ldcg(a.coord + 3 * c), com0),
-                                      dsub(__ldcg(a.coord + 3 * c + 1), com1), dsub(__ldcg(a.coord + 3 * c + 2), com2)));
-            }
-        }
-#pragma unroll
-        for (int q = 7; q >= 0; q--) {
-            if (q < n && ch[q] >= a.ntot) {
-                const int64_t c = ch[q];
-                double mc = __ldcg(a.mass + c);
-                if (mc != 0.0) {
-                    Q = dadd(Q, __ldcg(a.quad + 9 * (c - a.ntot) + sub));
-                    Q = dadd(Q, quad_term(sub, mc, dsub(__ldcg(a.coord + 3 * c), com0),
-                                          dsub(__ldcg(a.coord + 3 * c + 1), com1), dsub(__ldcg(a.coord + 3 * c + 2), com2)));
+            if (q < n) {
+                const int32_t c = ch[q];
+                const bool part = c >= 0;
+                const int64_t g = part ? (int64_t)c : N + (int64_t)(~c);
+                const double mc = a.mass[g];
+                if (part || mc != 0.0) {
+                    if (!part) Q = dadd(Q, a.quad[9 * (int64_t)(~c) + sub]);
+                    Q = dadd(Q, quad_term(sub, mc, dsub(a.coord[3 * g], com0), dsub(a.coord[3 * g + 1], com1),
+                                          dsub(a.coord[3 * g + 2], com2)));
                 }
             }
         }
@@ -1461,16 +1578,28 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
             { k_count_node_children<<<LAUNCH(M)>>>(N, M, T->parent, a.nchild); tg::note_launch(); }
             { k_moments_deep<<<div_up(ndeep, 128), 128, 0, st>>>(a, lvl_list + off[DEPTH_CAP], ndeep, fdepth); tg::note_launch(); }
         }
+        // every node's children once, in summation order, for the level passes
+        int32_t *kids = nullptr;
+        int8_t *nk = nullptr;
+        TG_TRY(dalloc(&kids, 8 * M, st));
+        TG_TRY(dalloc(&nk, M, st));
+        { k_kids<<<LAUNCH(M)>>>(N, M, T->first, T->next, kids, nk); tg::note_launch(); }
         // a level with few nodes is latency-bound: 16 lanes per node there; one thread per node
         // on the large levels, which are FP64-throughput-bound
         const int few = 128 * num_sms();
         for (int d = DEPTH_CAP - 1; d >= 0; d--) {
             const int c = hs.depth_hist[d];
             if (c <= 0) continue;
-            if (c < few) { k_moments_level_coop<<<div_up((int64_t)c * 16, 128), 128, 0, st>>>(a, lvl_list + off[d], c); tg::note_launch(); }
-            else { k_moments_level<<<div_up(c, 128), 128, 0, st>>>(a, lvl_list + off[d], c); tg::note_launch(); }
+            if (c < few) {
+                k_moments_level_coop<<<div_up((int64_t)c * 16, 128), 128, 0, st>>>(a, lvl_list + off[d], c, kids, nk);
+                tg::note_launch();
+            } else {
+                k_moments_sorted<<<div_up(c, MOM_BLOCK), MOM_BLOCK, 0, st>>>(a, lvl_list + off[d], c, kids, nk);
+                tg::note_launch();
+            }
         }
         TG_CUDA(cudaGetLastError());
+        dfree(kids, st); dfree(nk, st);
         dfree(a.acc, st); dfree(a.nchild, st); dfree(a.arrived, st);
     } else {
         { k_fold_only<<<LAUNCH(M)>>>(a); tg::note_launch(); }
