@@ -163,6 +163,24 @@ tg_status tg_bruteforce(const double *pos_t, const double *h_t, int64_t nt, cons
                         const double *m_s, const double *h_s, int64_t ns, int fields, int mutual,
                         double G, int precision, int mem, double *out, void *stream);
 
+/* Number of visible CUDA devices (0, not an error, when there is no driver or device); the check
+ * behind pytreegrav.cuda.is_available (cuda.py:70-80). */
+tg_status tg_device_count(int *count);
+
+/* A source set uploaded once and summed against new targets on every call: the device side of the
+ * numba-cuda CudaPotentialBruteforce / CudaAccelBruteforce contexts (cuda.py:737-796).
+ * tg_sources_create copies pos (n, 3), m (n,) and h (n,) (h NULL: zeros) from host or device memory
+ * (mem). tg_sources_bruteforce writes fields (W columns) for nt targets; pos_t NULL takes the sources
+ * themselves as the targets, with their softenings (nt ignored). Pairs at r == 0 are skipped in
+ * either case (the target form, bruteforce.py:7-50), so a target coinciding with a source drops
+ * that source, as in the reference contexts. */
+typedef struct tg_sources_s *tg_sources;
+tg_status tg_sources_create(const double *pos, const double *m, const double *h, int64_t n, int mem, void *stream,
+                            tg_sources *out);
+tg_status tg_sources_bruteforce(tg_sources s, const double *pos_t, const double *h_t, int64_t nt, int fields,
+                                double G, int precision, int mem, double *out, void *stream);
+tg_status tg_sources_free(tg_sources s);
+
 #ifdef __cplusplus
 }
 #endif

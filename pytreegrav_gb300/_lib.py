@@ -55,6 +55,10 @@ EXPORTS = [
     "tg_morton_order",
     "tg_morton_order_noalloc",
     "tg_bruteforce",
+    "tg_device_count",
+    "tg_sources_create",
+    "tg_sources_bruteforce",
+    "tg_sources_free",
 ]
 
 # every extern "C" symbol declared in include/pytreegrav_gb300_theta.h
@@ -132,6 +136,10 @@ def _declare(L):
     L.tg_morton_order.argtypes = [vp, i64, ci, vp, vp]
     L.tg_morton_order_noalloc.argtypes = [vp, i64, vp, vp]
     L.tg_bruteforce.argtypes = [vp, vp, i64, vp, vp, vp, i64, ci, ci, dbl, ci, ci, vp, vp]
+    L.tg_device_count.argtypes = [ctypes.POINTER(ci)]
+    L.tg_sources_create.argtypes = [vp, vp, vp, i64, ci, vp, ctypes.POINTER(vp)]
+    L.tg_sources_bruteforce.argtypes = [vp, vp, vp, i64, ci, dbl, ci, ci, vp, vp]
+    L.tg_sources_free.argtypes = [vp]
     for name in EXPORTS[1:]:
         getattr(L, name).restype = ci
     flt = ctypes.c_float

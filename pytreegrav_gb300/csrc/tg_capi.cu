@@ -114,6 +114,12 @@ bool valid_group_size(int gs) { return gs == 1 || gs == 2 || gs == 4 || gs == 8 
 
 using namespace tg;
 
+// A source set kept on the device between direct-sum calls.
+struct tg_sources_s {
+    double *pos = nullptr, *m = nullptr, *h = nullptr;
+    int64_t n = 0;
+};
+
 extern "C" {
 
 const char *tg_last_error(void) { return tg::last_error(); }
@@ -415,6 +421,108 @@ tg_status tg_bruteforce(const double *pos_t, const double *h_t, int64_t nt, cons
     if (zs) cudaFreeAsync(zs, st);
     TG_CUDA(cudaStreamSynchronize(st));
     return rc;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Device-resident source sets (the numba-cuda brute-force contexts, cuda.py:737-796).           */
+
+tg_status tg_device_count(int *count) {
+    if (!count) return TG_ERR_BAD_ARG;
+    *count = 0;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+        cudaGetLastError();  // no driver or no device: report zero devices, not an error
+        return TG_OK;
+    }
+    *count = n;
+    return TG_OK;
+}
+
+tg_status tg_sources_create(const double *pos, const double *m, const double *h, int64_t n, int mem, void *stream,
+                            tg_sources *out) {
+    if (!out) return TG_ERR_BAD_ARG;
+    *out = nullptr;
+    if (n < 0 || (n > 0 && (!pos || !m))) return TG_ERR_BAD_ARG;
+    if (mem != TG_MEM_HOST && mem != TG_MEM_DEVICE) return TG_ERR_BAD_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    tg_sources_s *S = new (std::nothrow) tg_sources_s();
+    if (!S) return TG_ERR_OOM;
+    S->n = n;
+    const int64_t cnt = std::max<int64_t>(n, 1);
+    const cudaMemcpyKind kind = mem == TG_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    auto fail = [&](tg_status r) {
+        tg_sources_free(S);
+        return r;
+    };
+    if (cudaMalloc((void **)&S->pos, sizeof(double) * 3 * cnt) != cudaSuccess ||
+        cudaMalloc((void **)&S->m, sizeof(double) * cnt) != cudaSuccess ||
+        cudaMalloc((void **)&S->h, sizeof(double) * cnt) != cudaSuccess) {
+        cudaGetLastError();
+        set_last_error_msg("out of device memory for the source set");
+        return fail(TG_ERR_OOM);
+    }
+    if (n > 0) {
+        if (cudaMemcpyAsync(S->pos, pos, sizeof(double) * 3 * n, kind, st) != cudaSuccess ||
+            cudaMemcpyAsync(S->m, m, sizeof(double) * n, kind, st) != cudaSuccess ||
+            (h ? cudaMemcpyAsync(S->h, h, sizeof(double) * n, kind, st)
+               : cudaMemsetAsync(S->h, 0, sizeof(double) * n, st)) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
+            tg::set_last_error("tg_sources_create", cudaGetLastError());
+            return fail(TG_ERR_CUDA);
+        }
+    }
+    *out = S;
+    return TG_OK;
+}
+
+tg_status tg_sources_bruteforce(tg_sources S, const double *pos_t, const double *h_t, int64_t nt, int fields,
+                                double G, int precision, int mem, double *out, void *stream) {
+    if (!S || !out || (fields & 7) == 0 || (fields & ~7)) return TG_ERR_BAD_ARG;
+    if (precision != TG_FP32 && precision != TG_FP64) return TG_ERR_BAD_ARG;
+    if (mem != TG_MEM_HOST && mem != TG_MEM_DEVICE) return TG_ERR_BAD_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    DevBuf dpt, dht;
+    if (!pos_t) {  // the sources themselves, in the target form: r == 0 pairs are skipped
+        nt = S->n;
+        dpt.ptr = S->pos;
+        dht.ptr = S->h;
+    } else {
+        if (nt < 0) return TG_ERR_BAD_ARG;
+        TG_TRY(stage_in(pos_t, 3 * nt, mem, st, dpt));
+        TG_TRY(stage_in(h_t, nt, mem, st, dht));
+    }
+    if (nt == 0) return TG_OK;
+    double *zt = nullptr;
+    if (!dht.ptr) {
+        TG_CUDA(tg::dev_malloc((void **)&zt, sizeof(double) * nt, st));
+        TG_CUDA(cudaMemsetAsync(zt, 0, sizeof(double) * nt, st));
+        dht.ptr = zt;
+    }
+    const int W = field_width(fields);
+    double *dout = out;
+    if (mem == TG_MEM_HOST) TG_CUDA(tg::dev_malloc((void **)&dout, sizeof(double) * nt * W, st));
+    tg_status rc = TG_OK;
+    if (S->n > 0) {
+        rc = run_bruteforce(dpt.ptr, dht.ptr, nt, S->pos, S->m, S->h, S->n, fields, 0, G, precision, dout, st);
+    } else {
+        TG_CUDA(cudaMemsetAsync(dout, 0, sizeof(double) * nt * W, st));
+    }
+    if (rc == TG_OK && mem == TG_MEM_HOST)
+        TG_CUDA(cudaMemcpyAsync(out, dout, sizeof(double) * nt * W, cudaMemcpyDeviceToHost, st));
+    if (mem == TG_MEM_HOST) cudaFreeAsync(dout, st);
+    if (zt) cudaFreeAsync(zt, st);
+    TG_CUDA(cudaStreamSynchronize(st));
+    return rc;
+}
+
+tg_status tg_sources_free(tg_sources S) {
+    if (!S) return TG_OK;
+    if (S->pos) cudaFree(S->pos);
+    if (S->m) cudaFree(S->m);
+    if (S->h) cudaFree(S->h);
+    delete S;
+    return TG_OK;
 }
 
 }  // extern "C"
