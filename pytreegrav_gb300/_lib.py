@@ -178,6 +178,14 @@ def load(path=None):
     return _lib
 
 
+NONFINITE_MSG = "Invalid input detected - aborting treebuild to avoid going into an infinite loop!"
+
+
+class NonFiniteInput(RuntimeError):
+    """TG_ERR_NONFINITE: a position, mass or softening is NaN or infinite (ConstructTree's error,
+    frontend.py:123-125)."""
+
+
 def check(rc, what=""):
     if rc == TG_OK:
         return
@@ -186,7 +194,7 @@ def check(rc, what=""):
     if rc == TG_ERR_BAD_ARG:
         raise ValueError(msg + "invalid argument")
     if rc == TG_ERR_NONFINITE:
-        raise RuntimeError(msg + "Invalid input detected - aborting treebuild to avoid going into an infinite loop!")
+        raise NonFiniteInput(msg + NONFINITE_MSG)
     if rc == TG_ERR_OOM:
         raise MemoryError(msg + "device allocation failed")
     if rc == TG_ERR_NO_QUADRUPOLES:

@@ -31,6 +31,7 @@ import warnings
 import numpy as np
 from numpy import zeros
 
+from . import _lib
 from .tree import Octree, bruteforce, morton_order
 
 SYMMETRIC_NMIN = 1000
@@ -103,11 +104,13 @@ def ConstructTree(pos, m=None, softening=None, quadrupole=False, vel=None, compu
     if softening is None:
         softening = zeros(len(pos))
     softening = np.atleast_1d(_f64(softening))
-    finite = np.all(np.isfinite(pos)) and np.all(np.isfinite(softening)) and (m is None or np.all(np.isfinite(m)))
-    if not finite:
-        print("Invalid input detected - aborting treebuild to avoid going into an infinite loop!")
-        raise RuntimeError("Invalid input detected - aborting treebuild to avoid going into an infinite loop!")
-    tree = Octree(pos, m, softening, quadrupole=quadrupole, compute_moments=compute_moments)
+    # non-finite positions, masses or softenings are found by the library's device-side check
+    # (TG_ERR_NONFINITE), which frontend.py:123-125's print-and-raise then reports
+    try:
+        tree = Octree(pos, m, softening, quadrupole=quadrupole, compute_moments=compute_moments)
+    except _lib.NonFiniteInput:
+        print(_lib.NONFINITE_MSG)
+        raise RuntimeError(_lib.NONFINITE_MSG) from None
     warn_if_coincident_positions(tree, softening)
     return tree
 

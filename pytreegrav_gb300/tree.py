@@ -22,6 +22,9 @@ def _as_f64(a, shape=None):
     return a
 
 
+_MODELS = {}  # learned opening-test models by the `learned` argument that named them
+
+
 class Octree:
     """An octree built on the GPU by ConstructTree.
 
@@ -199,12 +202,10 @@ class Octree:
         if isinstance(learned, th.ThetaModel):
             model = learned
         else:
-            model = self._models.get(learned) if hasattr(self, "_models") else None
-            if model is None:
+            model = _MODELS.get(learned)
+            if model is None:  # loaded and uploaded once per process, shared by every tree
                 model = th.ThetaModel.load(None if learned is True else learned)
-                if not hasattr(self, "_models"):
-                    self._models = {}
-                self._models[learned] = model
+                _MODELS[learned] = model
         l10 = (th.default_lambda(model, quadrupole) if error_ratio is None
                else th.lambda_for_ratio(model, float(error_ratio), quadrupole))
         if l10 is None:

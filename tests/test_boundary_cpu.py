@@ -88,13 +88,21 @@ def test_frontend_rejects_bad_device_combinations(fn):
         getattr(tg, fn)(x, m, device="cuda", quadrupole=True)
 
 
-def test_nonfinite_input_raises_before_the_gpu():
+def test_nonfinite_status_prints_and_raises_like_construct_tree(monkeypatch, capsys):
+    """The library's device-side check reports TG_ERR_NONFINITE; ConstructTree then prints and raises
+    as frontend.py:123-125 does. The device call is replaced by its status here (no GPU)."""
     import pytreegrav_gb300 as tg
+    from pytreegrav_gb300 import frontend
 
+    def fake_octree(*a, **k):
+        _lib.check(_lib.TG_ERR_NONFINITE, "ConstructTree")
+
+    monkeypatch.setattr(frontend, "Octree", fake_octree)
     x = np.random.default_rng(0).random((100, 3))
     x[3, 1] = np.nan
-    with pytest.raises(RuntimeError, match="Invalid input"):
+    with pytest.raises(RuntimeError, match="^Invalid input detected - aborting treebuild"):
         tg.ConstructTree(x, np.ones(100))
+    assert "Invalid input detected" in capsys.readouterr().out
 
 
 def test_quadrupole_guard():

@@ -146,3 +146,21 @@ def test_root_quadrupole_matches_analytic(tg):
         r = x - com
         Qref = 3.0 * np.einsum("i,ik,il->kl", m, r, r) - np.eye(3) * np.sum(m * np.sum(r**2, 1))
         assert np.max(np.abs(t.Quadrupoles[root] - Qref)) / np.max(np.abs(Qref)) < 1e-10
+
+
+@pytest.mark.parametrize("where", ["pos", "m", "softening"])
+@pytest.mark.parametrize("bad", [np.nan, np.inf, -np.inf])
+def test_nonfinite_input_raises_like_construct_tree(tg, capsys, where, bad):
+    """A NaN or infinity in any input array is found by the device-side check and reported as
+    pytreegrav's ConstructTree reports it: the message printed, then RuntimeError (frontend.py:123-125)."""
+    rng = np.random.default_rng(5)
+    x, m, h = rng.random((300, 3)), np.ones(300), np.full(300, 0.01)
+    {"pos": x[:, 2], "m": m, "softening": h}[where][117] = bad
+    with pytest.raises(RuntimeError, match="^Invalid input detected - aborting treebuild"):
+        tg.ConstructTree(x, m, h)
+    assert "Invalid input detected" in capsys.readouterr().out
+    with pytest.raises(RuntimeError, match="Invalid input detected"):
+        tg.Accel(x, m, h, method="tree")
+    # the library is usable right after a rejected call
+    x2 = rng.random((300, 3))
+    assert np.all(np.isfinite(tg.Accel(x2, np.ones(300), np.full(300, 0.01), method="tree")))
