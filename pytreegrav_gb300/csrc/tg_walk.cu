@@ -809,105 +809,209 @@ __global__ void k_make_groups(const int64_t *sys_off, int nsys, int gs, const in
 // with more than G particles breaks the run (it emits its own children), and a child joins the run
 // only if the run's bounding box stays clear of every such large sibling's cell -- a group whose
 // box reached into a dense sibling would open that sibling down to its particles.
-__global__ void k_tree_groups(int64_t ntot, int64_t mtot, const int2 *node_range, const double *cell,
-                              const double *size, const double *coord, const int64_t *first, const int64_t *next,
-                              const int64_t *parent, int G, const int64_t *sys_off, const int64_t *sys_node_off,
-                              int nsys, int2 *groups, int *group_root, int *group_node, unsigned long long *count) {
-    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= mtot) return;
-    const int2 r = node_range[j];
-    const int64_t f = ntot + j;
-    int s = 0;
-    if (nsys > 1) {
-        int lo = 0, hi = nsys;
-        while (hi - lo > 1) {
-            int mid = (lo + hi) >> 1;
-            if (sys_off[mid] <= r.x) lo = mid;
-            else hi = mid;
+// A node with more than G particles, queued by k_tree_groups_mark with its children in chain order.
+struct LargeNode {
+    int64_t child[8];
+    int64_t node;  // node index j (arena element ntot + j)
+    int root;      // its system's root node
+    int nch;
+};
+
+// One thread per node: a system root with at most G particles is one group; a node with more than
+// G particles is queued, children gathered here (their chain is walked once, by every such node's
+// thread at the same time), for k_tree_groups_large.
+__global__ void k_tree_groups_mark(int64_t ntot, int64_t mtot, const int2 *node_range, const int64_t *first,
+                                   const int64_t *next, const int64_t *parent, int G, const int64_t *sys_off,
+                                   const int64_t *sys_node_off, int nsys, int2 *groups, int *group_root,
+                                   int *group_node, unsigned long long *count, LargeNode *large, int *nlarge) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = j < mtot;
+    int2 r = make_int2(0, 0);
+    int root = 0;
+    if (valid) {
+        r = node_range[j];
+        int s = 0;
+        if (nsys > 1) {
+            int lo = 0, hi = nsys;
+            while (hi - lo > 1) {
+                int mid = (lo + hi) >> 1;
+                if (sys_off[mid] <= r.x) lo = mid;
+                else hi = mid;
+            }
+            s = lo;
         }
-        s = lo;
+        root = (int)sys_node_off[s];
+        if (r.y - r.x <= G && parent[ntot + j] < 0) {
+            unsigned long long q = atomicAdd(count, 1ull);
+            groups[q] = make_int2(r.x, r.y - r.x);
+            group_root[q] = root;
+            group_node[q] = (int)j;
+        }
     }
-    const int root = (int)sys_node_off[s];
-    auto emit = [&](int lo, int cnt) {  // a group inside node j's subtree
-        unsigned long long q = atomicAdd(count, 1ull);
-        groups[q] = make_int2(lo, cnt);
-        group_root[q] = root;
-        group_node[q] = (int)j;
-    };
-    if (r.y - r.x <= G) {
-        if (parent[f] < 0) emit(r.x, r.y - r.x);
-        return;
-    }
-    // children (at most 8) and the cells of the large ones
-    int clo[8], chi[8], nch = 0;
-    double bmin[8][3], bmax[8][3];
-    int nbig = 0;
-    for (int64_t c = first[f]; c != next[f] && c >= 0 && nch < 8; c = next[c]) {
-        if (c < ntot) {
-            clo[nch] = (int)c;
-            chi[nch] = (int)c + 1;
-        } else {
-            int2 cr = node_range[c - ntot];
-            clo[nch] = cr.x;
-            chi[nch] = cr.y;
-            if (cr.y - cr.x > G) {
-                double hs = 0.5 * size[c];
-                for (int k = 0; k < 3; k++) {
-                    bmin[nbig][k] = cell[3 * (c - ntot) + k] - hs;
-                    bmax[nbig][k] = cell[3 * (c - ntot) + k] + hs;
-                }
-                nbig++;
+    const bool big = valid && r.y - r.x > G;
+    const unsigned bm = __ballot_sync(FULL, big);
+    if (!big) return;
+    const int leader = __ffs(bm) - 1;
+    int base = 0;
+    if (lane_id() == leader) base = atomicAdd(nlarge, __popc(bm));
+    base = __shfl_sync(bm, base, leader);
+    LargeNode &e = large[base + __popc(bm & lanemask_lt())];
+    const int64_t f = ntot + j, stop = next[f];
+    int nch = 0;
+    for (int64_t c = first[f]; c != stop && c >= 0 && nch < 8; c = next[c]) e.child[nch++] = c;
+    e.node = j;
+    e.root = root;
+    e.nch = nch;
+}
+
+// Order-preserving integer image of a double (not NaN): u(a) <= u(b) exactly when a <= b, with -0.0
+// taken as +0.0 (the two compare equal). Boxes are reduced and compared in this form, on the
+// integer units: FP64 min/max/compare run on GB300's narrow FP64 pipe.
+__device__ __forceinline__ unsigned long long order_key(double x) {
+    long long b = __double_as_longlong(x);
+    if (b == (long long)0x8000000000000000ull) b = 0;
+    b ^= (b >> 63) & 0x7fffffffffffffffll;
+    return (unsigned long long)b ^ 0x8000000000000000ull;
+}
+__device__ __forceinline__ unsigned long long warp_min_key(unsigned long long u) {
+    const unsigned hi = __reduce_min_sync(FULL, (unsigned)(u >> 32));
+    const unsigned lo = __reduce_min_sync(FULL, (unsigned)(u >> 32) == hi ? (unsigned)u : 0xffffffffu);
+    return ((unsigned long long)hi << 32) | lo;
+}
+__device__ __forceinline__ unsigned long long warp_max_key(unsigned long long u) {
+    const unsigned hi = __reduce_max_sync(FULL, (unsigned)(u >> 32));
+    const unsigned lo = __reduce_max_sync(FULL, (unsigned)(u >> 32) == hi ? (unsigned)u : 0u);
+    return ((unsigned long long)hi << 32) | lo;
+}
+
+// The groups inside one queued node, one warp per node (a persistent grid over the queue): every
+// lane holds the same decisions; lane q keeps child q, and each small child's particle box is a
+// warp reduction (lane p loads the child's particle p, all children's loads issued together).
+// Boxes and cells are compared as order keys, which decides exactly as the FP64 comparisons do.
+__global__ void k_tree_groups_large(int64_t ntot, const int2 *node_range, const double *cell, const double *size,
+                                    const double *coord, int G, const LargeNode *large, const int *nlarge,
+                                    int2 *groups, int *group_root, int *group_node, unsigned long long *count) {
+    typedef unsigned long long u64;
+    const int lane = lane_id();
+    const int n = *nlarge;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n; w += nwarps) {
+        const LargeNode &e = large[w];
+        const int64_t j = e.node;
+        const int root = e.root;
+        const int nch = e.nch;
+        // this node's groups, collected on lanes 0.. and written with one atomic
+        int nemit = 0, my_glo = 0, my_gcnt = 0;
+        auto emit = [&](int lo, int cnt) {
+            if (lane == nemit) {
+                my_glo = lo;
+                my_gcnt = cnt;
+            }
+            nemit++;
+        };
+        int my_lo = 0, my_hi = 0;
+        int64_t my_c = -1;
+        if (lane < nch) {
+            my_c = e.child[lane];
+            if (my_c < ntot) {
+                my_lo = (int)my_c;
+                my_hi = (int)my_c + 1;
+            } else {
+                const int2 cr = node_range[my_c - ntot];
+                my_lo = cr.x;
+                my_hi = cr.y;
             }
         }
-        nch++;
-    }
-    int run_lo = -1, run_cnt = 0;
-    double rlo[3], rhi[3];
-    for (int q = 0; q < nch; q++) {
-        int sz = chi[q] - clo[q];
-        if (sz > G) {
-            if (run_cnt) emit(run_lo, run_cnt);
-            run_cnt = 0;
-            continue;
-        }
-        double lo3[3], hi3[3];
-        for (int k = 0; k < 3; k++) lo3[k] = hi3[k] = coord[3 * (int64_t)clo[q] + k];
-        for (int p = clo[q] + 1; p < chi[q]; p++)
+        const bool my_big = lane < nch && my_hi - my_lo > G;
+        u64 cbmin[3] = {0, 0, 0}, cbmax[3] = {0, 0, 0};  // large child's cell (lane q)
+        if (my_big) {  // a large child is a node
+            const double hs = 0.5 * size[my_c];
             for (int k = 0; k < 3; k++) {
-                double v = coord[3 * (int64_t)p + k];
-                lo3[k] = fmin(lo3[k], v);
-                hi3[k] = fmax(hi3[k], v);
+                cbmin[k] = order_key(cell[3 * (my_c - ntot) + k] - hs);
+                cbmax[k] = order_key(cell[3 * (my_c - ntot) + k] + hs);
             }
-        if (run_cnt) {
-            double nlo[3], nhi[3];
+        }
+        const unsigned bigmask = __ballot_sync(FULL, my_big);
+        // this lane's particle of every small child (a large or missing child repeats a valid load)
+        double v[8][3];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int lo = __shfl_sync(FULL, my_lo, q), hi = __shfl_sync(FULL, my_hi, q);
+            const int64_t p = (int64_t)lo + lane;
+            const int64_t src = (q < nch && hi - lo <= G && p < hi) ? p : (q < nch ? (int64_t)lo : 0);
+#pragma unroll
+            for (int k = 0; k < 3; k++) v[q][k] = coord[3 * src + k];
+        }
+        u64 pbmin[3] = {0, 0, 0}, pbmax[3] = {0, 0, 0};  // small child's particle box (lane q)
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            if (q >= nch) break;
+            if ((bigmask >> q) & 1u) continue;  // warp-uniform
+#pragma unroll
             for (int k = 0; k < 3; k++) {
-                nlo[k] = fmin(rlo[k], lo3[k]);
-                nhi[k] = fmax(rhi[k], hi3[k]);
-            }
-            bool hits = false;
-            for (int b = 0; b < nbig && !hits; b++) {
-                bool overlap = true;
-                for (int k = 0; k < 3; k++) overlap = overlap && nlo[k] <= bmax[b][k] && nhi[k] >= bmin[b][k];
-                hits = overlap;
-            }
-            if (run_cnt + sz <= G && !hits) {
-                run_cnt += sz;
-                for (int k = 0; k < 3; k++) {
-                    rlo[k] = nlo[k];
-                    rhi[k] = nhi[k];
+                const u64 key = order_key(v[q][k]);
+                const u64 mn = warp_min_key(key), mx = warp_max_key(key);
+                if (lane == q) {
+                    pbmin[k] = mn;
+                    pbmax[k] = mx;
                 }
+            }
+        }
+        // greedy runs in chain order
+        int run_lo = -1, run_cnt = 0;
+        u64 rlo[3] = {0, 0, 0}, rhi[3] = {0, 0, 0};
+        for (int q = 0; q < nch; q++) {
+            const int lo = __shfl_sync(FULL, my_lo, q), hi = __shfl_sync(FULL, my_hi, q);
+            const int sz = hi - lo;
+            if (sz > G) {
+                if (run_cnt) emit(run_lo, run_cnt);
+                run_cnt = 0;
                 continue;
             }
-            emit(run_lo, run_cnt);
+            u64 lo3[3], hi3[3];
+            for (int k = 0; k < 3; k++) {
+                lo3[k] = __shfl_sync(FULL, pbmin[k], q);
+                hi3[k] = __shfl_sync(FULL, pbmax[k], q);
+            }
+            if (run_cnt) {
+                u64 nlo[3], nhi[3];
+                for (int k = 0; k < 3; k++) {
+                    nlo[k] = rlo[k] < lo3[k] ? rlo[k] : lo3[k];
+                    nhi[k] = rhi[k] > hi3[k] ? rhi[k] : hi3[k];
+                }
+                // does the grown box reach into a large sibling's cell? (lane b tests sibling b)
+                bool overlap = my_big;
+                for (int k = 0; k < 3; k++) overlap = overlap && nlo[k] <= cbmax[k] && nhi[k] >= cbmin[k];
+                const bool hits = __any_sync(FULL, overlap);
+                if (run_cnt + sz <= G && !hits) {
+                    run_cnt += sz;
+                    for (int k = 0; k < 3; k++) {
+                        rlo[k] = nlo[k];
+                        rhi[k] = nhi[k];
+                    }
+                    continue;
+                }
+                emit(run_lo, run_cnt);
+            }
+            run_lo = lo;
+            run_cnt = sz;
+            for (int k = 0; k < 3; k++) {
+                rlo[k] = lo3[k];
+                rhi[k] = hi3[k];
+            }
         }
-        run_lo = clo[q];
-        run_cnt = sz;
-        for (int k = 0; k < 3; k++) {
-            rlo[k] = lo3[k];
-            rhi[k] = hi3[k];
+        if (run_cnt) emit(run_lo, run_cnt);
+        if (nemit > 0) {  // at most one group per child, so nemit <= 8 lanes hold them
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(count, (unsigned long long)nemit);
+            base = __shfl_sync(FULL, base, 0);
+            if (lane < nemit) {
+                groups[base + lane] = make_int2(my_glo, my_gcnt);
+                group_root[base + lane] = root;
+                group_node[base + lane] = (int)j;
+            }
         }
     }
-    if (run_cnt) emit(run_lo, run_cnt);
 }
 
 // Queue key for reference grouping: the group's bounding-box diagonal, largest first (as float
@@ -1162,8 +1266,15 @@ tg_status tree_groups(tg_tree_s *t, int G, cudaStream_t st) {
     TG_CUDA(cudaMemcpyAsync(d_sys, t->sys_off.data(), sizeof(int64_t) * (t->nsys + 1), cudaMemcpyHostToDevice, st));
     TG_CUDA(cudaMemcpyAsync(d_node, t->sys_node_off.data(), sizeof(int64_t) * (t->nsys + 1), cudaMemcpyHostToDevice,
                             st));
-    { k_tree_groups<<<div_up(M, 256), 256, 0, st>>>(N, M, t->node_range, t->cell_center, t->size, t->coord, t->first,
-                                                  t->next, t->parent, G, d_sys, d_node, t->nsys, g0, r0, n0, cnt); tg::note_launch(); }
+    LargeNode *large = nullptr;
+    int *nlarge = nullptr;
+    TG_CUDA(tg::dev_malloc((void **)&large, sizeof(LargeNode) * std::max<int64_t>(M, 1), st));
+    TG_CUDA(tg::dev_malloc((void **)&nlarge, sizeof(int), st));
+    TG_CUDA(cudaMemsetAsync(nlarge, 0, sizeof(int), st));
+    { k_tree_groups_mark<<<div_up(M, 256), 256, 0, st>>>(N, M, t->node_range, t->first, t->next, t->parent, G, d_sys,
+                                                       d_node, t->nsys, g0, r0, n0, cnt, large, nlarge); tg::note_launch(); }
+    { k_tree_groups_large<<<num_sms() * 8, 256, 0, st>>>(N, t->node_range, t->cell_center, t->size, t->coord, G, large,
+                                                       nlarge, g0, r0, n0, cnt); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
     unsigned long long ng = 0;
     TG_CUDA(cudaMemcpyAsync(&ng, cnt, sizeof(ng), cudaMemcpyDeviceToHost, st));
@@ -1187,6 +1298,8 @@ tg_status tree_groups(tg_tree_s *t, int G, cudaStream_t st) {
     TG_CUDA(cudaFreeAsync(r0, st));
     TG_CUDA(cudaFreeAsync(n0, st));
     TG_CUDA(cudaFreeAsync(cnt, st));
+    TG_CUDA(cudaFreeAsync(large, st));
+    TG_CUDA(cudaFreeAsync(nlarge, st));
     TG_CUDA(cudaFreeAsync(d_sys, st));
     TG_CUDA(cudaFreeAsync(d_node, st));
     t->ngroups = (int64_t)ng;
