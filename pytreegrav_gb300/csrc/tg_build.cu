@@ -216,6 +216,7 @@ struct Nodes {  // node slots in discovery order
     int64_t *lo = nullptr, *hi = nullptr, *parent = nullptr, *first = nullptr, *next = nullptr;
     int64_t *aparent = nullptr, *rank = nullptr;  // allocating parent slot, sibling order key
     int32_t *depth = nullptr, *sys = nullptr;
+    int32_t *seg = nullptr;  // segment of the round that made the slot (for k_node_centers)
     int8_t *level = nullptr;
     double *center = nullptr, *size = nullptr;
 };
@@ -336,23 +337,11 @@ __global__ void k_nodes(RoundView v, int64_t E, const int8_t *L, const int64_t *
     if (i == seg_lo && v.seg_root[s] >= 0) {
         root_first[s] = (1 <= L[e]) ? node_ref(slot_base + nstart[e]) : i;
     }
-    // geometric centres: the digits are applied from the segment cell down (octree.py:974-978);
-    // the element's nodes are consecutive levels, so one pass over the digits serves them all
-    double c0 = v.seg_center[3 * s], c1 = v.seg_center[3 * s + 1], c2 = v.seg_center[3 * s + 2];
-    double sz = v.seg_size[s];
-    int at = 0;  // level the running centre belongs to
     const int64_t nc = cnt[e];
     const int64_t slot0 = slot_base + nstart[e];
     for (int64_t j = 0; j < nc; j++) {
         int k = l0 + (int)j;
         int64_t slot = slot0 + j;
-        for (; at < k; at++) {
-            int d = (int)((key >> (63 - 3 * (at + 1))) & 7);
-            c0 = dadd(c0, dmul(sz, c_octant[d][0]));
-            c1 = dadd(c1, dmul(sz, c_octant[d][1]));
-            c2 = dadd(c2, dmul(sz, c_octant[d][2]));
-            sz = dmul(sz, 0.5);
-        }
         nd.lo[slot] = i;
         nd.level[slot] = (int8_t)k;
         nd.depth[slot] = v.seg_depth0[s] + k;
@@ -363,10 +352,7 @@ __global__ void k_nodes(RoundView v, int64_t E, const int8_t *L, const int64_t *
         nd.parent[slot] = par;
         nd.aparent[slot] = par;
         nd.rank[slot] = i;
-        nd.center[3 * slot] = c0;
-        nd.center[3 * slot + 1] = c1;
-        nd.center[3 * slot + 2] = c2;
-        nd.size[slot] = sz;
+        nd.seg[slot] = s;
         if (k == MAX_LEVEL) {
             nd.first[slot] = -1;  // set by the re-key round or the bucket
             unsigned long long q = atomicAdd(n_exhausted, 1ull);
@@ -385,6 +371,41 @@ __global__ void k_nodes(RoundView v, int64_t E, const int8_t *L, const int64_t *
         nd.hi[slot] = hi;
         nd.next[slot] = next_after(v, L, nstart, slot_base, s, hi);
     }
+}
+
+// x * 2^-q for q in {1, 2}, exactly: an exponent decrement when x and the result are normal
+// numbers (the common case, on the integer units), else the FP64 multiply, which is then exact too.
+__device__ __forceinline__ double scale_down(double x, int q) {
+    const long long b = __double_as_longlong(x);
+    const int ex = (int)((b >> 52) & 0x7ff);
+    if (ex > q && ex < 0x7ff) return __longlong_as_double(b - ((long long)q << 52));
+    return dmul(x, q == 1 ? 0.5 : 0.25);
+}
+
+// Geometric centre and size of every node slot of a round: the octant digits of the slot's key
+// applied from its segment's cell down to the slot's level (octree.py:974-978), in the reference's
+// order: centre += size * (+-1/4) per axis, then size *= 1/2. The products are powers-of-two
+// scalings (exact), so only the additions round, each once, as there.
+__global__ void k_node_centers(RoundView v, Nodes nd, int64_t slot_base, int64_t count, const uint64_t *keys) {
+    const int64_t slot = slot_base + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= slot_base + count || slot >= nd.cap) return;
+    const int s = nd.seg[slot];
+    const int k = nd.level[slot];
+    const uint64_t key = keys[nd.lo[slot]];
+    double c0 = v.seg_center[3 * s], c1 = v.seg_center[3 * s + 1], c2 = v.seg_center[3 * s + 2];
+    double sz = v.seg_size[s];
+    for (int at = 0; at < k; at++) {
+        const int d = (int)((key >> (63 - 3 * (at + 1))) & 7);
+        const double q = scale_down(sz, 2);  // size / 4
+        c0 = dadd(c0, (d & 1) ? q : -q);
+        c1 = dadd(c1, (d & 2) ? q : -q);
+        c2 = dadd(c2, (d & 4) ? q : -q);
+        sz = scale_down(sz, 1);
+    }
+    nd.center[3 * slot] = c0;
+    nd.center[3 * slot + 1] = c1;
+    nd.center[3 * slot + 2] = c2;
+    nd.size[slot] = sz;
 }
 
 __global__ void k_particles(RoundView v, int64_t E, const int8_t *L, const int64_t *nstart, int64_t slot_base,
@@ -1184,6 +1205,7 @@ static tg_status nodes_reserve(Nodes &nd, int64_t need, cudaStream_t s) {
     TG_TRY(grow_copy(&nd.rank, nd.count, nc, 1, s));
     TG_TRY(grow_copy(&nd.depth, nd.count, nc, 1, s));
     TG_TRY(grow_copy(&nd.sys, nd.count, nc, 1, s));
+    TG_TRY(grow_copy(&nd.seg, nd.count, nc, 1, s));
     TG_TRY(grow_copy(&nd.level, nd.count, nc, 1, s));
     TG_TRY(grow_copy(&nd.center, nd.count, nc, 3, s));
     TG_TRY(grow_copy(&nd.size, nd.count, nc, 1, s));
@@ -1192,7 +1214,8 @@ static tg_status nodes_reserve(Nodes &nd, int64_t need, cudaStream_t s) {
 }
 static void nodes_free(Nodes &nd, cudaStream_t s) {
     dfree(nd.lo, s); dfree(nd.hi, s); dfree(nd.parent, s); dfree(nd.first, s); dfree(nd.next, s);
-    dfree(nd.aparent, s); dfree(nd.rank, s); dfree(nd.depth, s); dfree(nd.sys, s); dfree(nd.level, s);
+    dfree(nd.aparent, s); dfree(nd.rank, s); dfree(nd.depth, s); dfree(nd.sys, s); dfree(nd.seg, s);
+    dfree(nd.level, s);
     dfree(nd.center, s); dfree(nd.size, s);
 }
 
@@ -1410,6 +1433,7 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
             TG_TRY(run_round());
         }
         nd.count = slot_base + Mr;
+        if (Mr > 0) { k_node_centers<<<LAUNCH(Mr)>>>(v, nd, slot_base, Mr, keys_sorted); tg::note_launch(); }
         n_exh = (int)hs.n_exh;
         dfree(L, st); dfree(cnt, st); dfree(nstart, st);
         if (n_exh == 0) {
