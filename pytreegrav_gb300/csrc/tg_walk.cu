@@ -87,6 +87,38 @@ __device__ __forceinline__ double rsqrt_t(double x) { return rsqrt(x); }
 __device__ __forceinline__ float sqrt_t(float x) { return sqrtf(x); }
 __device__ __forceinline__ double sqrt_t(double x) { return sqrt(x); }
 
+// Two FP32 values in one 64-bit register and the paired (f32x2) arithmetic of this GPU: one issued
+// instruction computes both halves, leaving issue slots to other warps' traversal work.
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 f2_pack(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f2 v, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b) {
+    f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b) {
+    f2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_rsqrt(f2 x) {
+    float a, b;
+    f2_unpack(x, a, b);
+    return f2_pack(rsqrt_t(a), rsqrt_t(b));
+}
+
 // ---------------------------------------------------------------------------------------------
 // Arena packing.
 __device__ __forceinline__ void split_hi_lo(double x, float &hi, float &lo) {
@@ -555,14 +587,48 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32, STACK == STACK_SMALL ? 3 
                     st = vec4<T>{sx, sy, sz, p.w};
                 }
             }
-            sm.spos[lane] = st;
+            // acceleration with groups of 2 or more targets: sources staged as pairs [x x y y] [z z m m]
+            // for the paired sweep; otherwise one 16-byte word per source
+            bool paired = false;
+            if constexpr (sizeof(T) == 4 && FIELDS == F_ACC) paired = GS >= 2;
+            if (paired) {
+                float *o = reinterpret_cast<float *>(sm.spos) + 8 * (lane >> 1) + (lane & 1);
+                o[0] = (float)st.x;
+                o[2] = (float)st.y;
+                o[4] = (float)st.z;
+                o[6] = (float)st.w;
+            } else {
+                sm.spos[lane] = st;
+            }
             const unsigned slowmask = __ballot_sync(FULL, slow);
             __syncwarp();
             Acc<T> b;
 #pragma unroll
             for (int c = 0; c < 10; c++) b.v[c] = T(0);
             const vec4<T> *chunk = sm.spos + slice * GS;
-            if (GS == 32) {
+            if (paired) {
+                const f2 TX = f2_pack((float)tx, (float)tx), TY = f2_pack((float)ty, (float)ty);
+                const f2 TZ = f2_pack((float)tz, (float)tz);
+                f2 ax = 0, ay = 0, az = 0;  // even and odd sources summed apart (bit pattern 0 is +0.0f)
+                const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(sm.spos) + 2 * ((slice * GS) >> 1);
+#pragma unroll 4
+                for (int i = 0; i < (GS >> 1); i++) {
+                    const ulonglong2 w0 = src[2 * i], w1 = src[2 * i + 1];
+                    const f2 dx = f2_sub(w0.x, TX), dy = f2_sub(w0.y, TY), dz = f2_sub(w1.x, TZ);
+                    const f2 rinv = f2_rsqrt(f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx))));
+                    const f2 mr3 = f2_mul(f2_mul(w1.y, rinv), f2_mul(rinv, rinv));
+                    ax = f2_fma(mr3, dx, ax);
+                    ay = f2_fma(mr3, dy, ay);
+                    az = f2_fma(mr3, dz, az);
+                }
+                float h0, h1;
+                f2_unpack(ax, h0, h1);
+                b.v[1] = (T)(h0 + h1);
+                f2_unpack(ay, h0, h1);
+                b.v[2] = (T)(h0 + h1);
+                f2_unpack(az, h0, h1);
+                b.v[3] = (T)(h0 + h1);
+            } else if (GS == 32) {
 #pragma unroll 16
                 for (int i = 0; i < 32; i++) {
                     vec4<T> s = chunk[i];
@@ -588,7 +654,75 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32, STACK == STACK_SMALL ? 3 
             kahan_add<T, FIELDS>(S, C, b);
             n_int += (unsigned long long)cnt * (unsigned long long)gr.y;
         };
+        // Quadrupole acceleration sweep with paired arithmetic (FP32, groups of 2 or more targets).
+        // Sources are staged as pairs (2p, 2p + 1), each 16-byte word holding one quantity of both:
+        // [x x y y] [z z m m] [q0 q0 q1 q1] [q2 q2 q3 q3] [q4 q4 q5 q5], the quadrupole negated. Per pair:
+        // a += r^-5 (t dx - Q dx) with t = m r^2 + 2.5 A r^-2 and A = dx.Q.dx, the same expansion as
+        // acc_mono_quad rearranged. The two halves sum the even and the odd sources separately.
+        auto eval_nodes_paired = [&](const int *list, int cnt) {
+            float *buf = reinterpret_cast<float *>(sm.spos);
+            {
+                float v[10] = {(float)FAR, (float)FAR, (float)FAR, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                if (lane < cnt) {
+                    const int e = list[lane];
+                    const vec4<T> p = a.ar.n_pos[e], q = a.ar.n_lo[e];
+                    const vec4<T> qa = a.ar.n_quad[2 * e], qb = a.ar.n_quad[2 * e + 1];
+                    v[0] = (p.x - gcx) + q.x;
+                    v[1] = (p.y - gcy) + q.y;
+                    v[2] = (p.z - gcz) + q.z;
+                    v[3] = p.w;
+                    v[4] = -qa.x; v[5] = -qa.y; v[6] = -qa.z; v[7] = -qa.w; v[8] = -qb.x; v[9] = -qb.y;
+                }
+                float *o = buf + 20 * (lane >> 1) + (lane & 1);
+#pragma unroll
+                for (int k = 0; k < 10; k++) o[2 * k] = v[k];
+            }
+            __syncwarp();
+            const f2 TX = f2_pack(tx, tx), TY = f2_pack(ty, ty), TZ = f2_pack(tz, tz);
+            const f2 C25 = f2_pack(-2.5f, -2.5f);
+            f2 ax = 0, ay = 0, az = 0;  // two partial sums each (bit pattern 0 is +0.0f, +0.0f)
+            const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(buf) + 5 * ((slice * GS) >> 1);
+#pragma unroll 2
+            for (int i = 0; i < (GS >> 1); i++) {
+                const ulonglong2 w0 = src[5 * i], w1 = src[5 * i + 1], w2 = src[5 * i + 2], w3 = src[5 * i + 3],
+                                 w4 = src[5 * i + 4];
+                const f2 dx = f2_sub(w0.x, TX), dy = f2_sub(w0.y, TY), dz = f2_sub(w1.x, TZ);
+                const f2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+                const f2 rinv = f2_rsqrt(r2);
+                const f2 u = f2_mul(rinv, rinv);
+                const f2 r5 = f2_mul(f2_mul(rinv, u), u);
+                // n = -Q dx from the negated quadrupole; A' = dx.n = -A
+                const f2 nx = f2_fma(w3.x, dz, f2_fma(w2.y, dy, f2_mul(w2.x, dx)));
+                const f2 ny = f2_fma(w4.x, dz, f2_fma(w3.y, dy, f2_mul(w2.y, dx)));
+                const f2 nz = f2_fma(w4.y, dz, f2_fma(w4.x, dy, f2_mul(w3.x, dx)));
+                const f2 A = f2_fma(dz, nz, f2_fma(dy, ny, f2_mul(dx, nx)));
+                const f2 t = f2_fma(f2_mul(A, C25), u, f2_mul(w1.y, r2));
+                ax = f2_fma(r5, f2_fma(t, dx, nx), ax);
+                ay = f2_fma(r5, f2_fma(t, dy, ny), ay);
+                az = f2_fma(r5, f2_fma(t, dz, nz), az);
+            }
+            __syncwarp();
+            Acc<T> b;
+#pragma unroll
+            for (int c = 0; c < 10; c++) b.v[c] = T(0);
+            float h0, h1;
+            f2_unpack(ax, h0, h1);
+            b.v[1] = h0 + h1;
+            f2_unpack(ay, h0, h1);
+            b.v[2] = h0 + h1;
+            f2_unpack(az, h0, h1);
+            b.v[3] = h0 + h1;
+            kahan_add<T, FIELDS>(S, C, b);
+            n_int += (unsigned long long)cnt * (unsigned long long)gr.y;
+            n_qint += (unsigned long long)cnt * (unsigned long long)gr.y;
+        };
         auto eval_nodes = [&](const int *list, int cnt) {
+            if constexpr (sizeof(T) == 4 && FIELDS == F_ACC) {
+                if (GS >= 2) {
+                    eval_nodes_paired(list, cnt);
+                    return;
+                }
+            }
             vec4<T> st = vec4<T>{FAR, FAR, FAR, T(0)}, q0 = vec4<T>{T(0), T(0), T(0), T(0)}, q1 = q0;
             if (lane < cnt) {
                 int e = list[lane];
