@@ -37,6 +37,12 @@ tg_status tg_tree_record_group_stats(tg_tree tree, int enable);
 /* Counters of the last walk, ngroups x 3 uint32 (host or device per mem). */
 tg_status tg_tree_last_group_stats(tg_tree tree, uint32_t *out, int mem, void *stream);
 
+/* Each group's estimated relative truncation error in the last walk with per-group tolerances
+ * (recorded while tg_tree_record_group_stats is on), ngroups float32: the sum, over the nodes the
+ * group accepted, of M s^p / (r - delta)^(p+2) (p = 3 with quadrupoles, 2 without; r the node's
+ * distance from the group box), divided by the RMS acceleration of the group's targets. */
+tg_status tg_tree_last_group_error(tg_tree tree, float *out, int mem, void *stream);
+
 /* Per-group features, ngroups x TG_THETA_NFEAT float32 (device): group size and extent, the
  * mass, size and density of the node holding the group, its distance from the system centre, the
  * field of the tree's top three levels at the group (sum of m/r^2, |sum of m r/r^3|, sum of m/r,
@@ -88,6 +94,11 @@ tg_status tg_theta_model_create(const float *params, const float *feat_mean, con
                                 float out_min, float out_max, float theta_max, int mem, tg_theta_model *out);
 tg_status tg_theta_model_free(tg_theta_model model);
 
+/* Error budget of a tolerance model (default 0, no check): in tg_tree_fields_learned, a group whose
+ * estimated relative truncation error (tg_tree_last_group_error's quantity) exceeds it is walked
+ * again at theta_fallback, the global opening angle, and its rows rewritten. */
+tg_status tg_theta_model_set_error_budget(tg_theta_model model, float budget);
+
 /* Network output per sample from features (n x 16; feature TG_THETA_FEAT_LAMBDA replaced by
  * log10_lambda): a fused BF16 tensor-core forward pass with FP32 accumulation. */
 tg_status tg_theta_infer(tg_theta_model model, const float *features, int64_t n, float log10_lambda, float *out,
@@ -106,7 +117,8 @@ tg_status tg_tree_fields_grouped(tg_tree tree, int fields, int quadrupole, doubl
 /* tg_tree_fields (TG_ORDER_TREE, TG_GROUP_TREE, FP32) with the acceptance test of every group set
  * by the model at weight log10_lambda: its opening angle, or its mass-aware tolerance under the
  * model's angle cap. With model NULL this is the plain walk at theta_fallback, and a group whose
- * output is not finite falls back to it. */
+ * output is not finite falls back to it. With a tolerance model whose error budget is set
+ * (tg_theta_model_set_error_budget), groups over the budget are walked again at theta_fallback. */
 tg_status tg_tree_fields_learned(tg_tree tree, int fields, int quadrupole, double G, int group_size,
                                  tg_theta_model model, float log10_lambda, double theta_fallback, int mem,
                                  double *out, void *stream);

@@ -67,6 +67,7 @@ THETA_EXPORTS = [
     "tg_tree_groups_copy",
     "tg_tree_record_group_stats",
     "tg_tree_last_group_stats",
+    "tg_tree_last_group_error",
     "tg_theta_features",
     "tg_mlp_forward",
     "tg_mlp_backward",
@@ -75,6 +76,7 @@ THETA_EXPORTS = [
     "tg_theta_tolerances",
     "tg_theta_model_create",
     "tg_theta_model_free",
+    "tg_theta_model_set_error_budget",
     "tg_theta_infer",
     "tg_tree_fields_grouped",
     "tg_tree_fields_learned",
@@ -155,6 +157,8 @@ def _declare(L):
     L.tg_theta_tolerances.argtypes = [vp, ci, ci, vp, vp, vp]
     L.tg_theta_model_create.argtypes = [vp, vp, vp, ci, flt, flt, flt, ci, ctypes.POINTER(vp)]
     L.tg_theta_model_free.argtypes = [vp]
+    L.tg_theta_model_set_error_budget.argtypes = [vp, flt]
+    L.tg_tree_last_group_error.argtypes = [vp, vp, ci, vp]
     L.tg_theta_infer.argtypes = [vp, vp, i64, flt, vp, vp]
     L.tg_tree_fields_grouped.argtypes = [vp, ci, ci, dbl, ci, dbl, vp, vp, ci, vp, vp]
     L.tg_tree_fields_learned.argtypes = [vp, ci, ci, dbl, ci, vp, flt, dbl, ci, vp, vp]

@@ -99,7 +99,7 @@ void destroy(tg_tree_s *t) {
     free_arena(t->arena32, st);
     free_arena(t->arena64, st);
     if (t->stats_dev) cudaFreeAsync(t->stats_dev, st);
-    f(t->groups); f(t->group_root); f(t->group_node); f(t->gstats);
+    f(t->groups); f(t->group_root); f(t->group_node); f(t->gstats); f(t->gerr);
     delete t;
 }
 

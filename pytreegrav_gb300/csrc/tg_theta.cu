@@ -482,6 +482,7 @@ struct tg_theta_model_s {
     int kind = TG_THETA_KIND_ANGLE;
     float tmin = 0.f, tmax = 0.f;  // output range
     float theta_max = 0.f;         // angle cap of a tolerance model
+    float err_budget = 0.f;        // per-group relative error budget (0: no rewalk)
 };
 
 namespace {
@@ -590,6 +591,21 @@ tg_status tg_tree_groups_copy(tg_tree t, int group_size, int32_t *first, int32_t
 tg_status tg_tree_record_group_stats(tg_tree t, int enable) {
     if (!t) return TG_ERR_BAD_ARG;
     t->record_group_stats = enable ? 1 : 0;
+    return TG_OK;
+}
+
+tg_status tg_theta_model_set_error_budget(tg_theta_model m, float budget) {
+    if (!m || !(budget >= 0.f)) return TG_ERR_BAD_ARG;
+    m->err_budget = budget;
+    return TG_OK;
+}
+
+tg_status tg_tree_last_group_error(tg_tree t, float *out, int mem, void *stream) {
+    if (!t || !out || !t->gerr) return TG_ERR_BAD_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    TG_CUDA(cudaMemcpyAsync(out, t->gerr, sizeof(float) * t->ngroups,
+                            mem == TG_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
+    TG_CUDA(cudaStreamSynchronize(st));
     return TG_OK;
 }
 
@@ -806,8 +822,11 @@ tg_status tg_tree_fields_learned(tg_tree t, int fields, int quadrupole, double G
     const int W = field_width_of(fields);
     double *dout = out;
     if (mem == TG_MEM_HOST) TG_CUDA(dev_malloc((void **)&dout, sizeof(double) * nt * W, st));
+    t->err_budget = (m && tol) ? m->err_budget : 0.f;
+    t->rewalk_theta = theta_fallback;
     tg_status rc = run_walk(t, t->coord, t->soft, nt, t->groups, t->group_root, nullptr, ng, t->walk_idx, fields,
                             quadrupole, theta, G, group_size, TG_FP32, tg_theta, tol, dout, st);
+    t->err_budget = 0.f;
     if (feat) cudaFreeAsync(feat, st);
     if (tg_theta) cudaFreeAsync(tg_theta, st);
     if (tol) cudaFreeAsync(tol, st);

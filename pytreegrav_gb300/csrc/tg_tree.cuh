@@ -89,6 +89,12 @@ struct tg_tree_s {
     int record_group_stats = 0;
     unsigned *gstats = nullptr;
     int64_t gstats_n = 0;
+    // Walks with per-group tolerances: each group's estimated relative truncation error (recorded
+    // with the counters above), and the budget above which a group is walked again at the global
+    // theta (0: no check); set by the learned entry from its model for the duration of its walk.
+    float *gerr = nullptr;
+    float err_budget = 0.f;
+    double rewalk_theta = 0.7;
     // Walk launch shape (tg_tree_set_walk_config): warps per block, and the node stack a walk starts
     // with (1024: groups that overflow it are rewalked with 4096; 4096: every group starts there).
     int walk_warps = 4;

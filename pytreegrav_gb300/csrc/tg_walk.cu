@@ -293,6 +293,14 @@ struct WalkArgs {
     // for the large-stack pass instead of failing. Null: overflow is an error.
     int *retry, *retry_count;
     const int *ngroups_dev;  // non-null: the number of groups is read here (the retry pass)
+    // Groups walked with a tolerance: each sums, over the nodes it accepts, the first neglected
+    // multipole term M s^p / (r - delta)^(p+2) (r the node's distance from the group box), and divides
+    // by its targets' RMS acceleration. gerr (or null) receives that estimate per group; a group whose
+    // estimate exceeds err_budget (> 0) is appended to rewalk, for a pass at the global theta.
+    float err_budget = 0.f;
+    float *gerr = nullptr;
+    int *rewalk = nullptr, *rewalk_count = nullptr;
+    double rewalk_theta = 0.0;  // the global theta of the rewalk pass
 };
 
 template <typename T, bool QUAD, int STACK>
@@ -542,6 +550,8 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32, STACK == STACK_SMALL ? 3 
         const T inv_theta = (T)(1.0 / theta);
         const float tolg = a.tol_group ? a.tol_group[g] : 0.f;
         const bool mass_aware = tolg > 0.f;  // warp-uniform
+        const bool track_err = mass_aware && (FIELDS & F_ACC) && (a.gerr || a.rewalk);
+        float err_est = 0.f;  // this lane's share of the group's truncation estimate
         const T inv_tol = mass_aware ? (T)(1.0 / (double)tolg) : T(0);
         const T rel_eps = sizeof(T) == 4 ? T(1e-5) : T(0);
         const T abs_eps = sizeof(T) == 4 ? T(1e-6) : T(0);
@@ -790,8 +800,10 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32, STACK == STACK_SMALL ? 3 
                     T r2 = dx * dx + dy * dy + dz * dz;
                     T h = r1.y > hmax_g ? r1.y : hmax_g;
                     T c1 = p.w * inv_theta + r1.x, c2 = h + T(0.6) * p.w + r1.x;
+                    T msp = T(0);  // M s^p of the node (tolerance test only)
                     if (mass_aware) {
-                        const T q = a.ar.n_pos[node].w * (QUAD ? p.w * p.w * p.w : p.w * p.w) * inv_tol;
+                        msp = a.ar.n_pos[node].w * (QUAD ? p.w * p.w * p.w : p.w * p.w);
+                        const T q = msp * inv_tol;
                         const T rc = QUAD ? pow_fifth(q) : sqrt(sqrt(q));
                         c1 = fmax(p.w * inv_theta, rc) + r1.x;
                     }
@@ -800,7 +812,13 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32, STACK == STACK_SMALL ? 3 
                     // the origin, so the relative term covers their rounding
                     T tol = rel_eps * crit + abs_eps * gscale;
                     T hiq = crit + tol, loq = crit - tol;
-                    if (mass_aware) acc = r2 > crit * crit;  // no pytreegrav decision to reproduce
+                    if (mass_aware) {  // no pytreegrav decision to reproduce
+                        acc = r2 > crit * crit;
+                        if (acc && track_err) {  // r - delta > rc >= 0 here
+                            const T d = sqrt(r2) - r1.x, d2 = d * d;
+                            err_est += (float)(msp / (QUAD ? d2 * d2 * d : d2 * d2));
+                        }
+                    }
                     else if (sizeof(T) == 8) unsure = true;
                     else if (r2 > hiq * hiq) acc = true;
                     else if (loq > T(0) && r2 < loq * loq) acc = false;
@@ -888,6 +906,24 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32, STACK == STACK_SMALL ? 3 
             for (int o = GS; o < 32; o <<= 1) {
                 S.v[c] += __shfl_xor_sync(FULL, S.v[c], o);
                 C.v[c] += __shfl_xor_sync(FULL, C.v[c], o);
+            }
+        }
+        if (track_err) {  // warp-uniform
+            float e = err_est, a2 = 0.f;
+            if (slice == 0 && valid) {
+                const float ax = (float)(S.v[1] - C.v[1]), ay = (float)(S.v[2] - C.v[2]), az = (float)(S.v[3] - C.v[3]);
+                a2 = ax * ax + ay * ay + az * az;
+            }
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                e += __shfl_xor_sync(FULL, e, o);
+                a2 += __shfl_xor_sync(FULL, a2, o);
+            }
+            const float rms = sqrtf(a2 / (float)gr.y);
+            const float eta = rms > 0.f ? e / rms : (e > 0.f ? INFINITY : 0.f);
+            if (lane == 0) {
+                if (a.gerr) a.gerr[g] = eta;
+                if (a.rewalk && a.err_budget > 0.f && !(eta <= a.err_budget)) a.rewalk[atomicAdd(a.rewalk_count, 1)] = g;
             }
         }
         if (slice == 0 && valid) {
@@ -1240,8 +1276,9 @@ static tg_status dispatch_walk(WalkArgs<T> &a, int fields, bool quad, int warps,
 }
 
 // Scratch of one walk, in ints: queue, status, retry count, retry queue, then the retry list.
-constexpr int WS_QUEUE = 0, WS_STATUS = 1, WS_RETRY_COUNT = 2, WS_RETRY_QUEUE = 3, WS_RETRY_LIST = 4;
-inline int64_t walk_scratch_ints(int64_t ngroups) { return WS_RETRY_LIST + std::max<int64_t>(ngroups, 1); }
+constexpr int WS_QUEUE = 0, WS_STATUS = 1, WS_RETRY_COUNT = 2, WS_RETRY_QUEUE = 3, WS_REWALK_COUNT = 4,
+              WS_REWALK_QUEUE = 5, WS_RETRY_LIST = 6;  // then the retry list, then the rewalk list
+inline int64_t walk_scratch_ints(int64_t ngroups) { return WS_RETRY_LIST + 2 * std::max<int64_t>(ngroups, 1); }
 
 // Enqueue a whole walk on st (no host synchronisation, so it can be captured): with the small
 // first stack, the small-stack pass, then a large-stack pass over the groups that overflowed it
@@ -1251,22 +1288,40 @@ template <typename T>
 static tg_status enqueue_walk(WalkArgs<T> a, int fields, bool quad, int warps, int first_stack, int *scratch,
                               cudaStream_t st) {
     TG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int) * WS_RETRY_LIST, st));
+    const int64_t ng1 = std::max<int64_t>(a.ngroups, 1);
     a.queue = scratch + WS_QUEUE;
     a.status = scratch + WS_STATUS;
     a.ngroups_dev = nullptr;
+    const bool budget = a.tol_group && a.err_budget > 0.f;
+    a.rewalk = budget ? scratch + WS_RETRY_LIST + ng1 : nullptr;
+    a.rewalk_count = budget ? scratch + WS_REWALK_COUNT : nullptr;
     if (first_stack == STACK_LARGE) {
         a.retry = a.retry_count = nullptr;
-        return dispatch_walk<T, STACK_LARGE>(a, fields, quad, warps, st);
+        TG_TRY((dispatch_walk<T, STACK_LARGE>(a, fields, quad, warps, st)));
+    } else {
+        a.retry = scratch + WS_RETRY_LIST;
+        a.retry_count = scratch + WS_RETRY_COUNT;
+        TG_TRY((dispatch_walk<T, STACK_SMALL>(a, fields, quad, warps, st)));
+        WalkArgs<T> b = a;
+        b.queue = scratch + WS_RETRY_QUEUE;
+        b.group_order = scratch + WS_RETRY_LIST;  // retry list entries are group indices
+        b.ngroups_dev = scratch + WS_RETRY_COUNT;
+        b.retry = b.retry_count = nullptr;
+        TG_TRY((dispatch_walk<T, STACK_LARGE>(b, fields, quad, warps, st)));
     }
-    a.retry = scratch + WS_RETRY_LIST;
-    a.retry_count = scratch + WS_RETRY_COUNT;
-    TG_TRY((dispatch_walk<T, STACK_SMALL>(a, fields, quad, warps, st)));
-    WalkArgs<T> b = a;
-    b.queue = scratch + WS_RETRY_QUEUE;
-    b.group_order = scratch + WS_RETRY_LIST;  // retry list entries are group indices
-    b.ngroups_dev = scratch + WS_RETRY_COUNT;
-    b.retry = b.retry_count = nullptr;
-    return dispatch_walk<T, STACK_LARGE>(b, fields, quad, warps, st);
+    if (!budget) return TG_OK;
+    // groups over their error budget, walked again with the global theta (their rows rewritten)
+    WalkArgs<T> r = a;
+    r.queue = scratch + WS_REWALK_QUEUE;
+    r.group_order = scratch + WS_RETRY_LIST + ng1;
+    r.ngroups_dev = scratch + WS_REWALK_COUNT;
+    r.retry = r.retry_count = nullptr;
+    r.rewalk = r.rewalk_count = nullptr;
+    r.tol_group = nullptr;
+    r.theta_group = nullptr;
+    r.gerr = nullptr;
+    r.theta = a.rewalk_theta > 0.0 ? a.rewalk_theta : a.theta;
+    return dispatch_walk<T, STACK_LARGE>(r, fields, quad, warps, st);
 }
 
 // Run a walk and time it on the stream; *status_out receives the device status word.
@@ -1315,6 +1370,14 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         TG_CUDA(cudaMemsetAsync(t->gstats, 0, sizeof(unsigned) * 3 * std::max<int64_t>(ngroups, 1), st));
         gstats = t->gstats;
     }
+    float *gerr = nullptr;
+    if (t->record_group_stats && tol_group) {
+        if (t->gerr) cudaFreeAsync(t->gerr, st);
+        t->gerr = nullptr;
+        TG_CUDA(tg::dev_malloc((void **)&t->gerr, sizeof(float) * std::max<int64_t>(ngroups, 1), st));
+        TG_CUDA(cudaMemsetAsync(t->gerr, 0, sizeof(float) * std::max<int64_t>(ngroups, 1), st));
+        gerr = t->gerr;
+    }
     if (precision == TG_FP64) {
         TG_TRY(build_arena(t, t->arena64, st));
         WalkArgs<double> a;
@@ -1324,6 +1387,9 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         a.tpos = tpos; a.th = th; a.scatter = scatter; a.groups = groups; a.group_root = group_root;
         a.group_order = group_order;
         a.ngroups = ngroups; a.theta = theta; a.theta_group = theta_group; a.tol_group = tol_group; a.G = G;
+        a.err_budget = tol_group ? t->err_budget : 0.f;
+        a.gerr = gerr;
+        a.rewalk_theta = t->rewalk_theta;
         a.out_fields = fields; a.out_w = w; a.out = out; a.gs = group_size;
         a.stats = (unsigned long long *)t->stats_dev;
         a.gstats = gstats;
@@ -1346,6 +1412,9 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         a.tpos = tpos; a.th = th; a.scatter = scatter; a.groups = groups; a.group_root = group_root;
         a.group_order = group_order;
         a.ngroups = ngroups; a.theta = theta; a.theta_group = theta_group; a.tol_group = tol_group; a.G = G;
+        a.err_budget = tol_group ? t->err_budget : 0.f;
+        a.gerr = gerr;
+        a.rewalk_theta = t->rewalk_theta;
         a.out_fields = fields; a.out_w = w; a.out = out; a.gs = group_size;
         a.stats = (unsigned long long *)t->stats_dev;
         a.gstats = gstats;

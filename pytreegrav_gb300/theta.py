@@ -92,6 +92,18 @@ class ThetaModel:
         self._handle = None
 
     @property
+    def error_budget(self):
+        """Per-group relative error budget of a tolerance model (tg_theta_model_set_error_budget; 0:
+        no rewalk), kept in the model file's metadata."""
+        return float(self.meta.get("error_budget", 0.0))
+
+    @error_budget.setter
+    def error_budget(self, value):
+        self.meta["error_budget"] = float(value)
+        if self._handle is not None:
+            _check(_lib.load().tg_theta_model_set_error_budget(self._handle, float(value)), "error budget")
+
+    @property
     def out_range(self):
         g = grid_of(self.kind)
         return float(g[0]), float(g[-1])
@@ -126,6 +138,8 @@ class ThetaModel:
                                            KINDS[self.kind], lo, hi, self.theta_max, _lib.TG_MEM_HOST,
                                            ctypes.byref(h)), "theta model")
             self._handle = h
+            if self.error_budget > 0:
+                _check(L.tg_theta_model_set_error_budget(h, self.error_budget), "error budget")
         return self._handle
 
     def close(self):
@@ -438,6 +452,44 @@ def training_systems(scale=1.0):
     ]
 
 
+def group_errors(model, pos, h, quadrupole, log10_lambda=None, G=1.0):
+    """Per-group estimated relative truncation errors (tg_tree_last_group_error) of the learned walk of
+    one system (m = 1/N, softening h), taken with the budget check off."""
+    import torch
+
+    n = len(pos)
+    L = _lib.load()
+    tree, keep = _tree_device(torch, pos, np.full(n, 1.0 / n), np.full(n, h), quadrupole)
+    handle = model.handle()
+    try:
+        _check(L.tg_tree_record_group_stats(tree, 1), "group stats")
+        _check(L.tg_theta_model_set_error_budget(handle, 0.0), "error budget")
+        l10 = default_lambda(model, quadrupole) if log10_lambda is None else float(log10_lambda)
+        out = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+        st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        _check(L.tg_tree_fields_learned(tree, _lib.TG_FIELD_ACCEL, int(quadrupole), float(G), GROUP_SIZE, handle,
+                                        float(l10), 0.7, _lib.TG_MEM_DEVICE, _vp(out), st), "learned walk")
+        first, _, _ = groups_of(tree, GROUP_SIZE)
+        eta = np.empty(len(first), np.float32)
+        _check(L.tg_tree_last_group_error(tree, _lib.ptr(eta), _lib.TG_MEM_HOST, st), "group error")
+    finally:
+        _check(L.tg_theta_model_set_error_budget(handle, model.error_budget), "error budget")
+        L.tg_tree_free(tree)
+    return eta
+
+
+def calibrate_error_budget(model, systems, factor=2.0):
+    """The error budget: `factor` times the largest per-group estimate seen on the training systems at
+    the model's calibrated lambda, so that only groups outside anything met in training (a network
+    asked about inputs unlike its data) are walked again at the global theta. Sets and returns it."""
+    worst = 0.0
+    for _, x, soft, quad in systems:
+        eta = group_errors(model, x, soft, quad)
+        worst = max(worst, float(np.max(eta)) if len(eta) else 0.0)
+    model.error_budget = factor * worst
+    return model.error_budget
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description="Train the learned opening-angle network on the GPU.")
     ap.add_argument("--out", default=DEFAULT_MODEL)
@@ -452,7 +504,15 @@ def main(argv=None):
     ap.add_argument("--save-data", default=None, help="also save the training tables (.npz)")
     ap.add_argument("--kind", choices=sorted(KINDS), default="tolerance")
     ap.add_argument("--theta-max", type=float, default=THETA_CAP, help="angle cap of a tolerance model")
+    ap.add_argument("--budget-only", action="store_true",
+                    help="only calibrate the error budget of the model at --out (no training)")
     args = ap.parse_args(argv)
+    if args.budget_only:
+        model = ThetaModel.load(args.out)
+        budget = calibrate_error_budget(model, training_systems(args.scale))
+        model.save(args.out)
+        print(json.dumps(dict(out=args.out, error_budget=budget)))
+        return model
     t0 = time.time()
     datasets = []
     for label, x, soft, quad in training_systems(args.scale):
@@ -470,10 +530,12 @@ def main(argv=None):
                   theta_max=args.theta_max)
     t2 = time.time()
     ratios = calibrate(model, datasets, target_ratio=args.target_ratio)
+    budget = calibrate_error_budget(model, training_systems(args.scale)) if model.kind == "tolerance" else 0.0
     model.meta.update(collect_seconds=t1 - t0, train_seconds=t2 - t1, target_ratio=args.target_ratio)
     os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
     model.save(args.out)
     summary = dict(out=args.out, kind=model.kind, theta_max=model.theta_max, log10_lambda=model.log10_lambda,
+                   error_budget=budget,
                    ratios={d["label"]: dict(error=e, cost=c, speedup=1.0 / c) for d, (e, c) in zip(datasets, ratios)},
                    collect_s=round(t1 - t0, 1), train_s=round(t2 - t1, 1))
     print(json.dumps(summary))

@@ -158,6 +158,54 @@ def test_learned_walk_without_model_is_the_plain_walk(env, plummer_tree):
     assert torch.equal(a, b)
 
 
+def test_groups_over_the_error_budget_are_rewalked_at_the_global_theta(env, plummer_tree):
+    """A budget below every group's estimate sends every group back through the walk at the
+    global theta: the result is then the plain walk's, bit for bit. Budget 0 (off) leaves the
+    learned result alone; the per-group estimates are finite and non-negative."""
+    torch, _lib, L, theta = env
+    tree, keep, x = plummer_tree
+    n = len(x)
+    model = theta.ThetaModel.load()
+    l10 = theta.default_lambda(model, True)
+    plain = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    learned = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    rewalked = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    assert L.tg_tree_fields(tree, None, None, n, _lib.TG_FIELD_ACCEL, 1, 0.7, 1.0, 32, _lib.TG_GROUP_TREE,
+                            _lib.TG_ORDER_TREE, _lib.TG_FP32, None, _lib.TG_MEM_DEVICE, vp(plain), None) == 0
+    h = model.handle()
+    try:
+        assert L.tg_theta_model_set_error_budget(h, 0.0) == 0
+        assert L.tg_tree_record_group_stats(tree, 1) == 0
+        assert L.tg_tree_fields_learned(tree, _lib.TG_FIELD_ACCEL, 1, 1.0, 32, h, l10, 0.7, _lib.TG_MEM_DEVICE,
+                                        vp(learned), None) == 0
+        first, _, _ = theta.groups_of(tree, 32)
+        eta = np.empty(len(first), np.float32)
+        assert L.tg_tree_last_group_error(tree, _lib.ptr(eta), _lib.TG_MEM_HOST, None) == 0
+        assert L.tg_tree_record_group_stats(tree, 0) == 0
+        assert np.all(np.isfinite(eta)) and np.all(eta >= 0) and eta.max() > 0
+        assert L.tg_theta_model_set_error_budget(h, float(eta[eta > 0].min()) * 1e-3) == 0
+        assert L.tg_tree_fields_learned(tree, _lib.TG_FIELD_ACCEL, 1, 1.0, 32, h, l10, 0.7, _lib.TG_MEM_DEVICE,
+                                        vp(rewalked), None) == 0
+        torch.cuda.synchronize()
+        assert torch.equal(rewalked, plain)
+        assert not torch.equal(learned, plain)
+    finally:
+        model.close()
+
+
+def test_shipped_model_error_budget_rewalks_few_groups(env, plummer_tree):
+    """The shipped budget (twice the worst estimate over the training systems) leaves a held-out
+    Plummer system's groups alone, or nearly so."""
+    torch, _lib, L, theta = env
+    tree, keep, x = plummer_tree
+    model = theta.ThetaModel.load()
+    if model.error_budget <= 0:
+        pytest.skip("the shipped model has no error budget")
+    eta = theta.group_errors(model, x, 0.005, True)
+    assert np.mean(eta > model.error_budget) < 0.01
+    model.close()
+
+
 @pytest.mark.parametrize("quad", [1, 0])
 def test_shipped_model_beats_the_plain_walk_at_equal_error(env, quad):
     """On a Plummer system outside the training set, the learned walk at the model's default
