@@ -33,11 +33,14 @@ SOFT = 0.005
 GROUP = 32
 SEED = 20261203
 
-# FP32 flops per interaction, counted from the walk kernel's arithmetic with add/sub/mul = 1,
-# FMA = 2, rsqrt = 1 (pytreegrav_gb300/csrc/tg_walk.cu, point_mass and quad_terms):
+# FP32 flops per interaction: the algorithmic count of the interaction as the monopole and
+# quadrupole terms are written (pytreegrav_gb300/csrc/tg_walk.cu, point_mass and quad_terms, which
+# the walk evaluates for potential and tidal fields), with add/sub/mul = 1, FMA = 2, rsqrt = 1:
 #   monopole acceleration: 3 sub + r^2 (1 mul + 2 fma) + rsqrt + rinv^2, m*rinv, *rinv^2 (3 mul)
 #   + 3 fma = 18; quadrupole node, acceleration: +38 (Q.dx 15, A 5, r^-5 and r^-7 4, 2.5*A*r^-7 2,
 #   three components of qf*dx - qdx*r^-5 accumulated, 12).
+# The fused FP32 acceleration sweep computes the same quantities in fewer operations (48 for a
+# quadrupole node); the fixed algorithmic count keeps rates comparable across kernel versions.
 FLOPS_MONO_ACC = 18
 FLOPS_QUAD_ACC = 18 + 38
 

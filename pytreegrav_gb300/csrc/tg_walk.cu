@@ -692,7 +692,7 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32, STACK == STACK_SMALL ? 3 
             const f2 C25 = f2_pack(-2.5f, -2.5f);
             f2 ax = 0, ay = 0, az = 0;  // two partial sums each (bit pattern 0 is +0.0f, +0.0f)
             const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(buf) + 5 * ((slice * GS) >> 1);
-#pragma unroll 2
+#pragma unroll 4
             for (int i = 0; i < (GS >> 1); i++) {
                 const ulonglong2 w0 = src[5 * i], w1 = src[5 * i + 1], w2 = src[5 * i + 2], w3 = src[5 * i + 3],
                                  w4 = src[5 * i + 4];
@@ -814,9 +814,9 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32, STACK == STACK_SMALL ? 3 
                     T hiq = crit + tol, loq = crit - tol;
                     if (mass_aware) {  // no pytreegrav decision to reproduce
                         acc = r2 > crit * crit;
-                        if (acc && track_err) {  // r - delta > rc >= 0 here
-                            const T d = sqrt(r2) - r1.x, d2 = d * d;
-                            err_est += (float)(msp / (QUAD ? d2 * d2 * d : d2 * d2));
+                        if (acc && track_err) {  // r - delta > rc >= 0 here; an estimate: approximate ops
+                            const float d = (float)r2 * rsqrt_t((float)r2) - (float)r1.x, d2 = d * d;
+                            err_est += __fdividef((float)msp, QUAD ? d2 * d2 * d : d2 * d2);
                         }
                     }
                     else if (sizeof(T) == 8) unsure = true;
