@@ -469,8 +469,18 @@ __device__ __forceinline__ bool accept_exact(int64_t f, const double *tc, const 
     return r_min > crit;
 }
 
+// Register caps (registers are granted 8 per thread at a time): the FP32 quadrupole acceleration
+// walk with the small stack runs at 72, which with its shared memory lets 7 blocks of 4 warps share
+// an SM (6 at 80); the other small-stack walks at 80 (6 blocks of 4 warps, 3 of 8; 81 would round
+// to 88 and leave 5 or 2); large-stack walks uncapped.
 template <typename T, int FIELDS, bool QUAD, int STACK>
-__global__ void __launch_bounds__(MAX_WALK_WARPS * 32, STACK == STACK_SMALL ? 3 : 1) k_walk(WalkArgs<T> a) {
+constexpr int walk_reg_cap() {
+    if (STACK != STACK_SMALL) return 255;
+    return (sizeof(T) == 4 && FIELDS == F_ACC && QUAD) ? 72 : 80;
+}
+template <typename T, int FIELDS, bool QUAD, int STACK>
+__global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap<T, FIELDS, QUAD, STACK>()))
+    k_walk(WalkArgs<T> a) {
     extern __shared__ unsigned char smem_raw[];
     WarpSmem<T, QUAD, STACK> &sm = reinterpret_cast<WarpSmem<T, QUAD, STACK> *>(smem_raw)[threadIdx.x >> 5];
     const int lane = lane_id();
@@ -1240,6 +1250,11 @@ static tg_status launch_walk(WalkArgs<T> &a, int warps, cudaStream_t st) {
     size_t smem = sizeof(WarpSmem<T, QUAD, STACK>) * warps;
     auto kern = k_walk<T, FIELDS, QUAD, STACK>;
     TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // the 72-register walk reaches 7 blocks per SM only with the largest shared-memory carveout; the
+    // others keep the driver's choice, which leaves them more L1
+    if (sizeof(T) == 4 && FIELDS == F_ACC && QUAD && STACK == STACK_SMALL)
+        TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     cudaSharedmemCarveoutMaxShared));
     int per_sm = 0;
     TG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem));
     if (per_sm < 1) per_sm = 1;
