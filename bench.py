@@ -489,6 +489,100 @@ def run_batched(args):
             "accuracy_rms_rel_vs_fp64_bruteforce_sampled_systems": errs, "gpu_launches": int(launches)}
 
 
+def run_column(args):
+    """Ray-traced column density, 1e6 Plummer particles as uniform spheres of radius 0.01, the six axis
+    rays from every particle: a step is the tree build plus the FP64 walk of all N x 6 (target, ray)
+    pairs, inputs resident in HBM. e2e is the public ColumnDensity call from host arrays."""
+    import torch
+
+    import pytreegrav_gb300 as tg
+    from oracle import oracle as O
+    from pytreegrav_gb300 import _lib
+    from pytreegrav_gb300.tree import Octree
+
+    L = _bind(_lib.load())
+    n = args.n
+    x = plummer(n, SEED)
+    m = np.full(n, 1.0 / n)
+    h = np.full(n, 0.01)
+    rays = np.vstack([np.eye(3), -np.eye(3)])
+    dpos, dm, dh, dr = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (x, m, h, rays))
+    out = torch.empty((n, 6), dtype=torch.float64, device="cuda")
+    vp = ctypes.c_void_p
+    st = vp(torch.cuda.current_stream().cuda_stream)
+
+    def step():
+        t = vp()
+        _lib.check(L.tg_tree_build(vp(dpos.data_ptr()), vp(dm.data_ptr()), vp(dh.data_ptr()), n, 0, 1,
+                                   _lib.TG_MEM_DEVICE, st, ctypes.byref(t)), "build")
+        tree = Octree._from_handle(t, False)
+        info = _lib.TreeInfo()
+        _lib.check(L.tg_tree_info_get(t, ctypes.byref(info)), "tree info")
+        e = torch.cuda.Event(enable_timing=True)
+        e.record()
+        # targets: the tree's own particles, which its first N coordinate rows hold in Morton order
+        _lib.check(L.tg_tree_column_density(t, vp(info.coord), n, vp(dr.data_ptr()), 6, 0, 0, 0.0,
+                                            _lib.TG_MEM_DEVICE, vp(out.data_ptr()), st), "column density")
+        return tree, e
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    steps = max(3, min(args.steps, 10))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    walk = []
+    l0 = L.tg_launch_count()
+    for k in range(steps):
+        ev[k][0].record()
+        tree, e = step()
+        ev[k][1].record()
+        walk.append((e, ev[k][1]))
+    torch.cuda.synchronize()
+    launches = L.tg_launch_count() - l0
+    ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    walk_ms = statistics.mean(a.elapsed_time(b) for a, b in walk)
+    # parity on a sample of targets against the oracle (FP64, same order of operations: equal)
+    got = out.cpu().numpy()
+    ot = O.OracleTree(x, m, h)
+    sample = np.arange(0, n, max(1, n // 500))
+    ref = O.column_rays(ot, x[ot.TreewalkIndices][sample], rays)
+    mismatches = int(np.count_nonzero(got[sample] != ref))
+    # end to end through the public call
+    tg.ColumnDensity(x, m, h, rays=6)
+    e2e_t = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tg.ColumnDensity(x, m, h, rays=6)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = statistics.median(e2e_t)
+    # CPU baseline: the oracle (the reference's walk in C, FP64, OpenMP on all host cores), full build
+    # and every 64th target, extrapolated
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ot2 = O.OracleTree(x, m, h)
+    t1 = time.perf_counter()
+    sub = x[ot2.TreewalkIndices][::64]
+    O.column_rays(ot2, sub, rays, nthreads=cores)
+    t2 = time.perf_counter()
+    cpu_s = (t1 - t0) + (t2 - t1) * 64
+    return {"metric": "ColumnDensity rays/s, 1e6 Plummer, six axis rays per particle", "value": round(6 * n / (ms * 1e-3), 1),
+            "unit": "rays/s", "n_gpus": 1, "steps": steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded Plummer sphere, a=1, r<50)",
+            "config": {"workload": f"ColumnDensity, N={n} Plummer, m=1/N, radii 0.01, rays=6 (the axis grid), "
+                                   "ray-traced walk of every particle",
+                       "step": "tree build + FP64 column walk of N x 6 (target, ray) pairs, inputs resident in HBM"},
+            "walk_ms": round(walk_ms, 3), "walk_rays_per_s": round(6 * n / (walk_ms * 1e-3), 1),
+            "parity": {"sample_targets": int(len(sample)), "mismatches_vs_oracle": mismatches},
+            "e2e": {"value": round(6 * n / e2e_s, 1), "unit": "rays/s", "h2d_bytes_per_step": int(x.nbytes + m.nbytes + h.nbytes),
+                    "d2h_bytes_per_step": int(8 * 6 * n), "api": "pytreegrav_gb300.ColumnDensity(pos, m, radii, rays=6)",
+                    "ms_per_step": round(1e3 * e2e_s, 3)},
+            "cpu_baseline": {"value": round(6 * n / cpu_s, 1), "unit": "rays/s", "cores": cores, "kind": "port",
+                             "sample": "oracle build of all N + the ray-traced walk (C, FP64, OpenMP) of every 64th "
+                                       f"target, extrapolated; {cpu_s:.2f} s per step"},
+            "gpu_launches": int(launches)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -496,12 +590,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=N_DEFAULT)
-    ap.add_argument("--config", choices=["plummer", "batched"], default="plummer",
-                    help="batched: the 4096-system configuration (its own JSON line)")
+    ap.add_argument("--config", choices=["plummer", "batched", "column"], default="plummer",
+                    help="batched: the 4096-system configuration; column: ray-traced column density "
+                         "(each its own JSON line)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.config == "batched" and args.impl == "ours":
         res = run_batched(args)
+    elif args.config == "column" and args.impl == "ours":
+        res = run_column(args)
     else:
         res = run_reference(args) if args.impl == "reference" else run_ours(args)
     if res is not None:

@@ -62,6 +62,8 @@ def lib():
         L.tgo_radix_argsort.argtypes = [_ip, _i64, _ip]
         L.tgo_morton_order.argtypes = [_dp, _i64, _ip]
         L.tgo_bounding_cube.argtypes = [_dp, _i64, _dp, _dp]
+        L.tgo_column_rays.argtypes = [ctypes.POINTER(_Tree), _dp, _i64, _dp, _i64, _i64, _dp, ctypes.c_int]
+        L.tgo_column_binned.argtypes = [ctypes.POINTER(_Tree), _dp, _i64, ctypes.c_double, _dp, ctypes.c_int]
         for k in ("tgo_force_kernel", "tgo_potential_kernel", "tgo_tidal_kernel"):
             getattr(L, k).argtypes = [ctypes.c_double, ctypes.c_double]
             getattr(L, k).restype = ctypes.c_double
@@ -339,6 +341,27 @@ def target_fields(pos_t, h_t, pos_s, m_s, h_s, potential=False, accel=False, tid
         o[ts] = v
         out[k] = o
     return out, tree
+
+
+def column_rays(tree, pos, rays, per_target=False, nthreads=0):
+    """Ray-traced column density (treewalk.py:904-973) of every (target, ray): rays (nrays, 3) shared
+    by all targets, or (n, nrays, 3) with per_target. Returns (n, nrays)."""
+    pos = _f64c(pos, (-1, 3))
+    n = len(pos)
+    rays = np.ascontiguousarray(rays, np.float64)
+    nrays = rays.shape[-2] if rays.ndim == 3 else rays.shape[0]
+    stride = 3 * nrays if per_target else 0
+    out = np.zeros((n, nrays))
+    lib().tgo_column_rays(ctypes.byref(tree._t), _d(pos), n, _d(rays), nrays, stride, _d(out), int(nthreads))
+    return out
+
+
+def column_binned(tree, pos, theta=0.5, nthreads=0):
+    """Angle-binned column density (treewalk.py:976-1030), (n, 6)."""
+    pos = _f64c(pos, (-1, 3))
+    out = np.zeros((len(pos), 6))
+    lib().tgo_column_binned(ctypes.byref(tree._t), _d(pos), len(pos), float(theta), _d(out), int(nthreads))
+    return out
 
 
 def force_kernel(r, h):

@@ -876,3 +876,120 @@ int tgo_bruteforce(const double *pt, const double *ht, int64_t nt, const double 
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------------------------------ */
+/* Column density.                                                                             */
+#ifndef M_PI
+#define M_PI 3.14159265358979323846 /* numpy.pi */
+#endif
+
+/* ColumnDensityWalk_singleray (treewalk.py:904-973), in its order of operations: the column from
+ * pos to infinity along ray of the uniform spheres (mass, radius = softening) in the tree. */
+static double column_singleray(const tgo_tree *t, const double *pos, const double *ray) {
+    const int64_t N = t->npart;
+    const double fac_density = 3.0 / (4.0 * M_PI);
+    double column = 0.0;
+    int64_t no = N;
+    const int64_t stop = t->next[N];
+    while (no > -1 && no != stop) {
+        double dx[3], r2 = 0.0;
+        for (int k = 0; k < 3; k++) {
+            dx[k] = t->coord[3 * no + k] - pos[k];
+            r2 += dx[k] * dx[k];
+        }
+        const double r = sqrt(r2);
+        const double z = ray[0] * dx[0] + ray[1] * dx[1] + ray[2] * dx[2];
+        if (r2 - z * z < 0) {
+            no = t->next[no];
+            continue;
+        }
+        const double h_no = t->soft[no];
+        if (no < N) {
+            if (h_no > 0) {
+                const double h_inv = 1.0 / h_no;
+                const double fac = fac_density * t->mass[no] * h_inv * h_inv;
+                const double r_proj = sqrt(r2 - z * z);
+                const double q = r_proj * h_inv;
+                if (r_proj < h_no) {
+                    if (r > h_no) {
+                        if (z > 0) column += fac * 2 * sqrt(1 - q * q);
+                    } else {
+                        const double dz = z * h_inv;
+                        column += fac * (dz + sqrt(1 - q * q));
+                    }
+                }
+            }
+            no = t->next[no];
+        } else {
+            const double R_eff = t->size[no] * 0.8660254037844386 + t->delta[no];
+            int open = 0;
+            if (r < h_no + R_eff) open = 1;
+            else if (z > 0 && (r2 - z * z) < (t->soft[no] + R_eff) * (t->soft[no] + R_eff)) open = 1;
+            no = open ? t->first[no] : t->next[no];
+        }
+    }
+    return column;
+}
+
+void tgo_column_rays(const tgo_tree *t, const double *pos, int64_t n, const double *rays, int64_t nrays,
+                     int64_t ray_stride, double *out, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+    for (int64_t i = 0; i < n; i++)
+        for (int64_t j = 0; j < nrays; j++)
+            out[i * nrays + j] = column_singleray(t, pos + 3 * i, rays + i * ray_stride + 3 * j);
+}
+
+/* angular_bin (treewalk.py:49-70): the axis of the largest |component|, sign first */
+static int angular_bin(const double dx[3]) {
+    if (fabs(dx[0]) > fabs(dx[1]) && fabs(dx[0]) > fabs(dx[2])) return dx[0] > 0 ? 0 : 1;
+    if (fabs(dx[1]) > fabs(dx[2])) return dx[1] > 0 ? 2 : 3;
+    return dx[2] > 0 ? 4 : 5;
+}
+
+/* ColumnDensityWalk_binned (treewalk.py:976-1030) */
+static void column_binned(const tgo_tree *t, const double *pos, double theta, double *column) {
+    const int64_t N = t->npart;
+    const double angular_bin_size = (4 * M_PI) / 6;
+    for (int k = 0; k < 6; k++) column[k] = 0.0;
+    int64_t no = N;
+    const int64_t stop = t->next[N];
+    while (no > -1 && no != stop) {
+        double dx[3], r2 = 0.0;
+        for (int k = 0; k < 3; k++) {
+            dx[k] = t->coord[3 * no + k] - pos[k];
+            r2 += dx[k] * dx[k];
+        }
+        const double h = t->soft[no];
+        if (no < N) {
+            const int bin = angular_bin(dx);
+            if (r2 > h * h) {
+                column[bin] += t->mass[no] / r2 / angular_bin_size;
+            } else if (h > 0) {
+                const double col0 = t->mass[no] * (3 / (4 * M_PI * h * h));
+                const double fac = sqrt(r2) / h;
+                const double col_iso = (1 - fac) * col0;
+                for (int k = 0; k < 6; k++) column[k] += col_iso;
+                column[bin] += col0 * fac * 2;
+            }
+            no = t->next[no];
+        } else {
+            if (accept(sqrt(r2), h, t->size[no], t->delta[no], theta)) {
+                column[angular_bin(dx)] += t->mass[no] / r2 / angular_bin_size;
+                no = t->next[no];
+            } else {
+                no = t->first[no];
+            }
+        }
+    }
+}
+
+void tgo_column_binned(const tgo_tree *t, const double *pos, int64_t n, double theta, double *out, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+    for (int64_t i = 0; i < n; i++) column_binned(t, pos + 3 * i, theta, out + 6 * i);
+}

@@ -66,6 +66,14 @@ int tgo_walk_counts_groups(const tgo_tree *t, const double *pos, const double *s
                            const int64_t *count, int64_t ngroups, double theta, int64_t *n_interactions,
                            int64_t *n_opened, int nthreads);
 
+/* Column density (treewalk.py:904-1030). tgo_column_rays: the single-ray walk (904-973) of every
+ * (target, ray) pair; rays (nrays, 3) unit vectors, shared by all targets when ray_stride == 0, else
+ * target i's rays start at rays + i * ray_stride. out (n, nrays). tgo_column_binned: the
+ * angle-binned walk (976-1030) with opening angle theta; out (n, 6). */
+void tgo_column_rays(const tgo_tree *t, const double *pos, int64_t n, const double *rays, int64_t nrays,
+                     int64_t ray_stride, double *out, int nthreads);
+void tgo_column_binned(const tgo_tree *t, const double *pos, int64_t n, double theta, double *out, int nthreads);
+
 /* Brute force.  mode 0: target form (r == 0 pairs skipped, bruteforce.py:7-50, 209-256, 353-386);
  * mode 1: mutual form (self excluded by index, bruteforce.py:86-116, 164-206, 319-350).
  * out is (nt, W) like tgo_fields. */

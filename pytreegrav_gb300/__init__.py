@@ -7,12 +7,13 @@ The compute path is libpytreegrav_gb300.so (hand-written CUDA, C ABI in include/
 built in-tree by ``python -m pytreegrav_gb300.build``.
 """
 
-from .frontend import (Accel, AccelTarget, ConstructTree, Field, Potential, PotentialTarget, TidalTensor,
-                       TidalTensorTarget, checkTreeQuadrupoles, valueTestMethod, warn_if_coincident_positions)
+from .frontend import (Accel, AccelTarget, ColumnDensity, ConstructTree, Field, Potential, PotentialTarget,
+                       TidalTensor, TidalTensorTarget, checkTreeQuadrupoles, valueTestMethod,
+                       warn_if_coincident_positions)
 from .tree import Octree, bruteforce, morton_order
 
 __all__ = [
-    "Accel", "AccelTarget", "ConstructTree", "Field", "Potential", "PotentialTarget", "TidalTensor",
+    "Accel", "AccelTarget", "ColumnDensity", "ConstructTree", "Field", "Potential", "PotentialTarget", "TidalTensor",
     "TidalTensorTarget", "checkTreeQuadrupoles", "valueTestMethod", "warn_if_coincident_positions", "Octree",
     "bruteforce", "morton_order",
 ]

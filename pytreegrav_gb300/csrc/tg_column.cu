@@ -1,0 +1,226 @@
+// Column density through the octree: pytreegrav's ray-traced and angle-binned walks
+// (treewalk.py:904-1030, frontend.py:1321-1458) over the tree's FP64 arrays, in the reference's order
+// of operations with every operation rounded once (explicit _rn intrinsics, no FMA contraction).
+//
+// The ray-traced walk has no truncation: a node opens whenever its bounding sphere, inflated by its
+// largest particle radius, can meet the ray, and only particles contribute, each as a uniform sphere
+// of its mass and radius (the softening). One thread walks one (target, ray) pair; lanes of a warp
+// take consecutive targets (Morton order) for the same ray, so their walks stay together.
+#include "tg_tree.cuh"
+
+namespace tg {
+namespace {
+
+constexpr double FAC_DENSITY = 3.0 / (4.0 * 3.141592653589793);  // 3 / (4 pi), as numpy evaluates it
+constexpr double FOUR_PI = 4.0 * 3.141592653589793;
+constexpr double BIN_SOLID_ANGLE = (4.0 * 3.141592653589793) / 6.0;  // angular_bin_size
+
+struct ColumnTree {
+    const double *coord, *mass, *soft, *size, *delta;
+    const int64_t *first, *next;
+    int64_t npart, nelem;
+};
+
+// ColumnDensityWalk_singleray (treewalk.py:904-973). *runaway is set if the walk does not end
+// within one visit per element (a malformed tree).
+__device__ double column_singleray(const ColumnTree &t, double px, double py, double pz, double r0, double r1,
+                                   double r2d, int *runaway) {
+    const int64_t N = t.npart;
+    double column = 0.0;
+    int64_t no = N;
+    const int64_t stop = t.next[N];
+    for (int64_t guard = 0; no > -1 && no != stop; guard++) {
+        if (guard > t.nelem || no >= t.nelem) {
+            atomicOr(runaway, 1);
+            return column;
+        }
+        const double dx = dsub(t.coord[3 * no], px), dy = dsub(t.coord[3 * no + 1], py);
+        const double dz = dsub(t.coord[3 * no + 2], pz);
+        const double r2 = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
+        const double r = __dsqrt_rn(r2);
+        const double z = dadd(dadd(dmul(r0, dx), dmul(r1, dy)), dmul(r2d, dz));
+        const double b2 = dsub(r2, dmul(z, z));
+        if (b2 < 0.0) {
+            no = t.next[no];
+            continue;
+        }
+        const double h_no = t.soft[no];
+        if (no < N) {
+            if (h_no > 0.0) {
+                const double h_inv = ddiv(1.0, h_no);
+                const double fac = dmul(dmul(dmul(FAC_DENSITY, t.mass[no]), h_inv), h_inv);
+                const double r_proj = __dsqrt_rn(b2);
+                const double q = dmul(r_proj, h_inv);
+                if (r_proj < h_no) {
+                    if (r > h_no) {
+                        if (z > 0.0) column = dadd(column, dmul(dmul(fac, 2.0), __dsqrt_rn(dsub(1.0, dmul(q, q)))));
+                    } else {
+                        const double dzh = dmul(z, h_inv);
+                        column = dadd(column, dmul(fac, dadd(dzh, __dsqrt_rn(dsub(1.0, dmul(q, q))))));
+                    }
+                }
+            }
+            no = t.next[no];
+        } else {
+            const double R_eff = dadd(dmul(t.size[no], 0.8660254037844386), t.delta[no]);
+            bool open = false;
+            if (r < dadd(h_no, R_eff)) {
+                open = true;
+            } else if (z > 0.0) {
+                const double reach = dadd(t.soft[no], R_eff);
+                open = b2 < dmul(reach, reach);
+            }
+            no = open ? t.first[no] : t.next[no];
+        }
+    }
+    return column;
+}
+
+// rays shared by all targets (ray_stride 0) or per target (ray_stride 3 * nrays): pair p is
+// target p % n on ray p / n
+__global__ void k_column_rays(ColumnTree t, const double *pos, int64_t n, const double *rays, int64_t nrays,
+                              int64_t ray_stride, double *out, int *runaway) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n * nrays) return;
+    const int64_t i = p % n, j = p / n;
+    const double *ray = rays + i * ray_stride + 3 * j;
+    out[i * nrays + j] = column_singleray(t, pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], ray[0], ray[1], ray[2],
+                                          runaway);
+}
+
+// angular_bin (treewalk.py:49-70)
+__device__ __forceinline__ int angular_bin(double dx, double dy, double dz) {
+    if (fabs(dx) > fabs(dy) && fabs(dx) > fabs(dz)) return dx > 0.0 ? 0 : 1;
+    if (fabs(dy) > fabs(dz)) return dy > 0.0 ? 2 : 3;
+    return dz > 0.0 ? 4 : 5;
+}
+
+// ColumnDensityWalk_binned (treewalk.py:976-1030): one thread per target, six sky bins.
+__global__ void k_column_binned(ColumnTree t, const double *pos, int64_t n, double theta, double *out,
+                                int *runaway) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
+    double col[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    const int64_t N = t.npart;
+    int64_t no = N;
+    const int64_t stop = t.next[N];
+    for (int64_t guard = 0; no > -1 && no != stop; guard++) {
+        if (guard > t.nelem || no >= t.nelem) {
+            atomicOr(runaway, 1);
+            break;
+        }
+        const double dx = dsub(t.coord[3 * no], px), dy = dsub(t.coord[3 * no + 1], py);
+        const double dz = dsub(t.coord[3 * no + 2], pz);
+        const double r2 = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
+        const double h = t.soft[no];
+        if (no < N) {
+            const int bin = angular_bin(dx, dy, dz);
+            if (r2 > dmul(h, h)) {
+                const double c = ddiv(ddiv(t.mass[no], r2), BIN_SOLID_ANGLE);
+#pragma unroll
+                for (int k = 0; k < 6; k++)
+                    if (k == bin) col[k] = dadd(col[k], c);
+            } else if (h > 0.0) {
+                const double col0 = dmul(t.mass[no], ddiv(3.0, dmul(dmul(FOUR_PI, h), h)));
+                const double fac = ddiv(__dsqrt_rn(r2), h);
+                const double iso = dmul(dsub(1.0, fac), col0);
+                const double peak = dmul(dmul(col0, fac), 2.0);
+#pragma unroll
+                for (int k = 0; k < 6; k++) {
+                    col[k] = dadd(col[k], iso);
+                    if (k == bin) col[k] = dadd(col[k], peak);
+                }
+            }
+            no = t.next[no];
+        } else {
+            const double size = t.size[no], delta = t.delta[no];
+            const double crit = pymax(dadd(ddiv(size, theta), delta), dadd(dadd(h, dmul(size, 0.6)), delta));
+            if (__dsqrt_rn(r2) > crit) {
+                const double c = ddiv(ddiv(t.mass[no], r2), BIN_SOLID_ANGLE);
+                const int bin = angular_bin(dx, dy, dz);
+#pragma unroll
+                for (int k = 0; k < 6; k++)
+                    if (k == bin) col[k] = dadd(col[k], c);
+                no = t.next[no];
+            } else {
+                no = t.first[no];
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; k++) out[6 * i + k] = col[k];
+}
+
+}  // namespace
+}  // namespace tg
+
+using namespace tg;
+
+extern "C" {
+
+tg_status tg_tree_column_density(tg_tree t, const double *pos, int64_t n, const double *rays, int64_t nrays,
+                                 int64_t ray_stride, int binned, double theta, int mem, double *out, void *stream) {
+    if (!t || !out || n < 0 || (n > 0 && !pos)) return TG_ERR_BAD_ARG;
+    if (mem != TG_MEM_HOST && mem != TG_MEM_DEVICE) return TG_ERR_BAD_ARG;
+    if (binned) {
+        if (!(theta > 0)) return TG_ERR_BAD_ARG;
+        nrays = 6;
+        ray_stride = 0;
+    } else if (!rays || nrays < 1 || (ray_stride != 0 && ray_stride != 3 * nrays)) {
+        return TG_ERR_BAD_ARG;
+    }
+    if (t->nsys != 1) {
+        set_last_error_msg("column density needs a tree of one particle system");
+        return TG_ERR_BAD_ARG;
+    }
+    if (n == 0) return TG_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    ColumnTree ct;
+    ct.coord = t->coord; ct.mass = t->mass; ct.soft = t->soft; ct.size = t->size; ct.delta = t->delta;
+    ct.first = t->first; ct.next = t->next;
+    ct.npart = t->ntot;
+    ct.nelem = t->ntot + t->mtot;
+    const int64_t nray_vals = binned ? 0 : (ray_stride ? n * ray_stride : 3 * nrays);
+    const double *dpos = pos, *drays = rays;
+    double *dout = out, *owned = nullptr;
+    int *flag = nullptr;
+    // one allocation: flag, positions, rays and output when they come from or go to the host
+    size_t bytes = 16;
+    if (mem == TG_MEM_HOST) bytes += sizeof(double) * (3 * n + nray_vals + n * nrays);
+    TG_CUDA(dev_malloc((void **)&owned, bytes, st));
+    flag = (int *)owned;
+    TG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    if (mem == TG_MEM_HOST) {
+        double *p = owned + 2;
+        TG_CUDA(cudaMemcpyAsync(p, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+        dpos = p;
+        p += 3 * n;
+        if (nray_vals) {
+            TG_CUDA(cudaMemcpyAsync(p, rays, sizeof(double) * nray_vals, cudaMemcpyHostToDevice, st));
+            drays = p;
+            p += nray_vals;
+        }
+        dout = p;
+    }
+    if (binned) {
+        k_column_binned<<<div_up(n, 128), 128, 0, st>>>(ct, dpos, n, theta, dout, flag);
+    } else {
+        k_column_rays<<<div_up(n * nrays, 128), 128, 0, st>>>(ct, dpos, n, drays, nrays, ray_stride, dout, flag);
+    }
+    note_launch();
+    TG_CUDA(cudaGetLastError());
+    int hflag = 0;
+    if (mem == TG_MEM_HOST)
+        TG_CUDA(cudaMemcpyAsync(out, dout, sizeof(double) * n * nrays, cudaMemcpyDeviceToHost, st));
+    TG_CUDA(cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TG_CUDA(cudaFreeAsync(owned, st));
+    TG_CUDA(cudaStreamSynchronize(st));
+    if (hflag) {
+        set_last_error_msg("column density walk did not end within one visit per element");
+        return TG_ERR_ITER_LIMIT;
+    }
+    return TG_OK;
+}
+
+}  // extern "C"

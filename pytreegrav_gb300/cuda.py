@@ -213,3 +213,30 @@ class CudaAccelBruteforce(_CudaBruteforce):
 
     def __call__(self, pos=None, softening=None, G=1.0):
         return self._run(pos, softening, G)
+
+
+class CudaColumnDensity:
+    """Ray-traced column density on the GPU against one uploaded tree (cuda.py:240-296): the tree
+    stays on the device, each call walks it for new targets and rays. float32 results, shape
+    (len(pos), len(rays)); the walk itself is FP64 (tg_tree_column_density)."""
+
+    def __init__(self, tree, threads_x=THREADS_X):
+        _require_device()
+        if isinstance(tree, Octree):
+            self._tree = tree
+        else:  # any object with pytreegrav's Octree attributes
+            n = int(tree.NumParticles)
+            self._tree = Octree(np.ascontiguousarray(tree.Coordinates[:n], dtype=np.float64),
+                                np.ascontiguousarray(tree.Masses[:n], dtype=np.float64),
+                                np.ascontiguousarray(tree.Softenings[:n], dtype=np.float64))
+        self.npart = int(self._tree.NumParticles)
+        self.threads_x = int(threads_x)
+        nodes = int(self._tree.node_hi) - self.npart
+        self.device_bytes = (self.npart + nodes) * (3 * 8 + 4 * 8 + 2 * 8)
+
+    def __call__(self, pos, rays):
+        """Column densities, shape (len(pos), len(rays)), float32; rays are normalised here."""
+        pos = np.ascontiguousarray(np.atleast_2d(np.asarray(pos, dtype=np.float64)))
+        rays = np.atleast_2d(np.asarray(rays, dtype=np.float64))
+        rays = np.ascontiguousarray(rays / np.linalg.norm(rays, axis=1)[:, None])
+        return self._tree.column_density(pos, rays).astype(np.float32)

@@ -293,3 +293,80 @@ class Field:
 
     def tidal(self, pos_target=None, **kwargs):
         return self.evaluate(tidal=True, pos_target=pos_target, **kwargs)["tidal"]
+
+
+def ColumnDensity(pos, m, radii, rays=None, randomize_rays=False, healpix=False, tree=None, theta=0.5,
+                  return_tree=False, parallel=False, group_size=16, device="cpu"):
+    """Column density from each particle integrated to infinity, the particles being uniform spheres
+    of mass m and radius radii (frontend.py:1321-1458): ray-traced along the given rays (int 6: the
+    six axis rays; other ints: that many random directions; (N_rays, 3) array: normalised), or
+    averaged over six bins on the sky with rays=None (opening angle theta). randomize_rays rotates
+    the ray grid per particle by random_rotation(i) of its position i in Morton order. Returns
+    (N, N_rays) or (N, 6) in the caller's order.
+
+    The walks run on the GPU in FP64 (device and parallel are accepted; device keeps pytreegrav's
+    checks). The ray-traced columns equal pytreegrav's at any group_size (its grouped walk is
+    bit-identical to the per-target one). The binned estimator is the per-target walk, which is
+    pytreegrav's result at group_size=1. Its default grouped walk, used from 1000 targets, opens a
+    superset of nodes and shifts the binned answer slightly.
+    """
+    from .misc import random_rotation
+
+    if np.any(np.asarray(radii) <= 0):
+        warnings.warn("Some particle radii are <= 0; these particles are point-like and contribute no column "
+                      "density. Supply a nonzero radius if their mass should be included.")
+    pos = np.atleast_2d(_f64(pos))
+    if tree is None:
+        tree = ConstructTree(pos, _f64(m), _f64(radii))
+        idx = tree.TreewalkIndices
+    else:
+        _check_tree(tree)
+        idx = morton_order(pos)
+    pos_sorted = np.ascontiguousarray(pos[idx])
+
+    if type(rays) == int:
+        if rays == 6:
+            rays = np.vstack([np.eye(3), -np.eye(3)])
+        else:
+            rays = np.random.normal(size=(rays, 3))
+    elif type(rays) == np.ndarray:
+        if not len(rays.shape) == 2:
+            raise Exception("rays array argument must be 2D.")
+        elif rays.shape[1] != 3:
+            raise Exception("rays array argument is not an array of 3D vectors.")
+        rays = np.array(rays, dtype=np.float64)
+    elif rays is not None:
+        raise Exception("rays argument type is not supported")
+    if healpix:
+        try:
+            import healpy as hp
+        except ImportError as e:
+            raise ImportError("healpix=... needs healpy: pip install healpy") from e
+        nside = healpix
+        rays = np.array(hp.pix2vec(nside, np.arange(hp.nside2npix(nside)))).T
+    if rays is not None:
+        rays /= np.sqrt((rays * rays).sum(1))[:, None]
+
+    if device not in ("cpu", "cuda"):
+        raise ValueError(f"device must be 'cpu' or 'cuda', got {device!r}")
+    if device == "cuda" and (rays is None or randomize_rays):
+        raise ValueError("device='cuda' supports only the ray-traced path: pass rays, and not randomize_rays")
+
+    if rays is None:
+        columns = tree.column_density(pos_sorted, None, theta)
+    elif randomize_rays:
+        per = np.empty((len(pos_sorted),) + rays.shape)
+        for i in range(len(pos_sorted)):
+            per[i] = rays @ random_rotation(i)
+        columns = tree.column_density(pos_sorted, per)
+    else:
+        columns = tree.column_density(pos_sorted, rays)
+    if device == "cuda":  # pytreegrav's device path returns float32
+        columns = columns.astype(np.float32)
+    if np.any(np.isnan(columns)):
+        print("WARNING some column densities are NaN!")
+    unsorted = np.empty_like(columns)
+    unsorted[idx] = columns
+    if return_tree:
+        return unsorted, tree
+    return unsorted

@@ -38,3 +38,8 @@ def golden_bruteforce():
 @pytest.fixture(scope="session")
 def golden_bigtree():
     return load_golden("golden_bigtree.npz")
+
+
+@pytest.fixture(scope="session")
+def golden_column():
+    return load_golden("golden_column.npz")

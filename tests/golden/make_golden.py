@@ -6,7 +6,8 @@ pytreegrav's unmodified algorithm runs as plain Python (IEEE double, no FMA cont
 
 Run from the repository root, with the pytreegrav checkout's src/ directory as the argument:
 
-    python tests/golden/make_golden.py /path/to/pytreegrav/src
+    python tests/golden/make_golden.py /path/to/pytreegrav/src            (all fixtures)
+    python tests/golden/make_golden.py /path/to/pytreegrav/src column     (golden_column.npz only)
 
 Writes tests/golden/golden_*.npz. Small cases store full arrays; large cases store SHA-256 digests of
 each array, so the fixtures stay a few hundred KB. Seeds are fixed; rerunning reproduces the files.
@@ -214,7 +215,39 @@ def main(src):
     print("wrote", sorted(f for f in os.listdir(OUT) if f.endswith(".npz")))
 
 
+def column(src):
+    """golden_column.npz: pytreegrav's column-density walks (treewalk.py:904-1030) and its
+    random_rotation (misc.py:7-55) on a small cloud of uniform spheres."""
+    sys.path.insert(0, os.path.join(HERE, "_numba_shim"))
+    sys.path.insert(0, src)
+    from pytreegrav import ConstructTree
+    from pytreegrav.misc import random_rotation
+    from pytreegrav.treewalk import ColumnDensityWalk_binned, ColumnDensityWalk_singleray
+
+    rng = np.random.default_rng(17)
+    n = 300
+    x = rng.normal(size=(n, 3))
+    m = rng.random(n) / n
+    h = rng.uniform(0.05, 0.5, n)
+    h[7] = 0.0  # a point-like particle: no cross-section
+    tree = ConstructTree(x, m, h)
+    xt = np.vstack([x[:24], rng.normal(size=(16, 3)) * 1.5, [[0.0, 0.0, 0.0], [5.0, 0.0, 0.0]]])
+    rays = np.vstack([np.eye(3), -np.eye(3), rng.normal(size=(3, 3))])
+    rays /= np.sqrt((rays * rays).sum(1))[:, None]
+    col = {"src/pos": x, "src/m": m, "src/h": h, "tgt/pos": xt, "rays": rays}
+    col["rays_out"] = np.array([[ColumnDensityWalk_singleray(p, r, tree) for r in rays] for p in xt])
+    for theta in (0.5, 0.8):
+        col[f"binned_theta{theta}"] = np.array([ColumnDensityWalk_binned(p, tree, theta) for p in xt])
+    col["rotations"] = np.array([random_rotation(i) for i in range(12)])
+    np.savez_compressed(os.path.join(OUT, "golden_column.npz"), **col)
+    print("wrote golden_column.npz")
+
+
 if __name__ == "__main__":
-    if len(sys.argv) != 2:
+    if len(sys.argv) == 3 and sys.argv[2] == "column":
+        column(sys.argv[1])
+    elif len(sys.argv) != 2:
         sys.exit(__doc__)
-    main(sys.argv[1])
+    else:
+        main(sys.argv[1])
+        column(sys.argv[1])

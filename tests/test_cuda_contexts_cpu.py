@@ -9,7 +9,7 @@ from pytreegrav_gb300 import cuda
 
 def test_names_of_pytreegrav_cuda():
     for name in ("is_available", "pack_tree_gravity", "CudaPotential", "CudaAccel", "CudaPotentialBruteforce",
-                 "CudaAccelBruteforce", "THREADS_X", "GRAV_ROW"):
+                 "CudaAccelBruteforce", "CudaColumnDensity", "THREADS_X", "GRAV_ROW"):
         assert hasattr(cuda, name), name
 
 

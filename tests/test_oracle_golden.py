@@ -132,3 +132,17 @@ def test_oracle_thread_count_independence(golden_walk):
     b = t.fields(xs, hs, True, True, False, True, 8, 0.5, nthreads=4)
     for k in a:
         assert np.array_equal(a[k], b[k])
+
+
+def test_column_density_walks_bit_exact(golden_column):
+    """The oracle's ray-traced and angle-binned column-density walks against pytreegrav's own
+    (treewalk.py:904-1030), run on the same tree: identical to the last bit."""
+    g = golden_column
+    t = O.OracleTree(g["src/pos"], g["src/m"], g["src/h"])
+    got = O.column_rays(t, g["tgt/pos"], g["rays"])
+    assert np.array_equal(got, g["rays_out"])
+    for theta in (0.5, 0.8):
+        assert np.array_equal(O.column_binned(t, g["tgt/pos"], theta), g[f"binned_theta{theta}"])
+    # per-target ray sets: the same rays repeated per target give the same columns
+    per = np.broadcast_to(g["rays"], (len(g["tgt/pos"]),) + g["rays"].shape)
+    assert np.array_equal(O.column_rays(t, g["tgt/pos"], per, per_target=True), g["rays_out"])
