@@ -19,13 +19,46 @@ struct ColumnTree {
     const double *coord, *mass, *soft, *size, *delta;
     const int64_t *first, *next;
     int64_t npart, nelem;
+    // FP32 copy for the screen: coordinates split hi + lo, with the radius (hi.w) and, for nodes,
+    // size * sqrt(3)/2 + delta (lo.w)
+    const float4 *fhi, *flo;
 };
 
-// ColumnDensityWalk_singleray (treewalk.py:904-973). *runaway is set if the walk does not end
-// within one visit per element (a malformed tree).
+__device__ __forceinline__ void split_f(double v, float &hi, float &lo) {
+    hi = __double2float_rn(v);
+    lo = __double2float_rn(v - (double)hi);
+}
+
+__global__ void k_column_prep(ColumnTree t, float4 *fhi, float4 *flo) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= t.nelem) return;
+    float4 a, b;
+    split_f(t.coord[3 * e], a.x, b.x);
+    split_f(t.coord[3 * e + 1], a.y, b.y);
+    split_f(t.coord[3 * e + 2], a.z, b.z);
+    a.w = (float)t.soft[e];
+    b.w = e < t.npart ? 0.f : (float)(t.size[e] * 0.8660254037844386 + t.delta[e]);
+    fhi[e] = a;
+    flo[e] = b;
+}
+
+// ColumnDensityWalk_singleray (treewalk.py:904-973). Each visited element is first screened in FP32
+// from its FP64 offset: distance r, along-ray coordinate z and impact parameter b (from |d x n|,
+// which does not cancel). Their FP32 errors are a few 1e-7 of r, so with a margin of 4e-6 r the
+// screen's "certainly" answers are the FP64 decisions. The element is evaluated in FP64, in the
+// reference's order, only when its particle may contribute or a decision is within the margin,
+// including the reference's skip of elements whose r^2 - z^2 rounds below zero. *runaway is set if
+// the walk does not end within one visit per element (a malformed tree).
 __device__ double column_singleray(const ColumnTree &t, double px, double py, double pz, double r0, double r1,
                                    double r2d, int *runaway) {
     const int64_t N = t.npart;
+    const float n0 = (float)r0, n1 = (float)r1, n2 = (float)r2d;
+    float phx, phy, phz, plx, ply, plz;
+    split_f(px, phx, plx);
+    split_f(py, phy, ply);
+    split_f(pz, phz, plz);
+    // absolute part of the margin: the lo parts' own rounding
+    const float m_abs = 1e-13f * (fabsf(phx) + fabsf(phy) + fabsf(phz)) + 1e-30f;
     double column = 0.0;
     int64_t no = N;
     const int64_t stop = t.next[N];
@@ -34,8 +67,54 @@ __device__ double column_singleray(const ColumnTree &t, double px, double py, do
             atomicOr(runaway, 1);
             return column;
         }
+        // FP32 screen
+        {
+            const float4 ah = t.fhi[no], al = t.flo[no];
+            const float fx = (ah.x - phx) + (al.x - plx), fy = (ah.y - phy) + (al.y - ply);
+            const float fz = (ah.z - phz) + (al.z - plz), hf = ah.w;
+            const float rf = sqrtf(fx * fx + fy * fy + fz * fz);
+            const float zf = n0 * fx + n1 * fy + n2 * fz;
+            const float cx = n1 * fz - n2 * fy, cy = n2 * fx - n0 * fz, cz = n0 * fy - n1 * fx;
+            const float bf = sqrtf(cx * cx + cy * cy + cz * cz);
+            const float m = 4e-6f * rf + m_abs;  // error margin of r, z and b
+            bool decided = false;
+            int64_t nxt = -1;
+            if (no < N) {
+                // no contribution: a point-like particle, or one the ray certainly misses (which also
+                // makes r^2 - z^2 certainly positive)
+                if (!(hf > 0.f) && !(t.soft[no] > 0.0)) {  // no cross-section
+                    decided = true;
+                    nxt = t.next[no];
+                } else if (bf - m > hf * 1.000001f) {
+                    decided = true;
+                    nxt = t.next[no];
+                }
+            } else if (bf > m) {  // r^2 - z^2 certainly positive: the node test decides
+                const float Rf = al.w;
+                const float near = hf + Rf;
+                if (rf + m < near * 0.999999f) {  // contains the target's neighbourhood: open
+                    decided = true;
+                    nxt = t.first[no];
+                } else if (rf - m > near * 1.000001f) {
+                    const float reach = near;  // Softenings[no] + R_eff
+                    if (zf < -m || bf - m > reach * 1.000001f) {  // behind the target or missed: skip
+                        decided = true;
+                        nxt = t.next[no];
+                    } else if (zf > m && bf + m < reach * 0.999999f) {  // ahead and hit: open
+                        decided = true;
+                        nxt = t.first[no];
+                    }
+                }
+            }
+            if (decided) {
+                no = nxt;
+                continue;
+            }
+        }
+        // FP64, the reference's expression
         const double dx = dsub(t.coord[3 * no], px), dy = dsub(t.coord[3 * no + 1], py);
         const double dz = dsub(t.coord[3 * no + 2], pz);
+        const double h_no = t.soft[no];
         const double r2 = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
         const double r = __dsqrt_rn(r2);
         const double z = dadd(dadd(dmul(r0, dx), dmul(r1, dy)), dmul(r2d, dz));
@@ -44,7 +123,6 @@ __device__ double column_singleray(const ColumnTree &t, double px, double py, do
             no = t.next[no];
             continue;
         }
-        const double h_no = t.soft[no];
         if (no < N) {
             if (h_no > 0.0) {
                 const double h_inv = ddiv(1.0, h_no);
@@ -203,18 +281,27 @@ tg_status tg_tree_column_density(tg_tree t, const double *pos, int64_t n, const 
         }
         dout = p;
     }
+    float4 *fcopy = nullptr;
+    ct.fhi = ct.flo = nullptr;
     if (binned) {
         k_column_binned<<<div_up(n, 128), 128, 0, st>>>(ct, dpos, n, theta, dout, flag);
+        note_launch();
     } else {
+        TG_CUDA(dev_malloc((void **)&fcopy, sizeof(float4) * 2 * ct.nelem, st));
+        ct.fhi = fcopy;
+        ct.flo = fcopy + ct.nelem;
+        k_column_prep<<<div_up(ct.nelem, 256), 256, 0, st>>>(ct, fcopy, fcopy + ct.nelem);
+        note_launch();
         k_column_rays<<<div_up(n * nrays, 128), 128, 0, st>>>(ct, dpos, n, drays, nrays, ray_stride, dout, flag);
+        note_launch();
     }
-    note_launch();
     TG_CUDA(cudaGetLastError());
     int hflag = 0;
     if (mem == TG_MEM_HOST)
         TG_CUDA(cudaMemcpyAsync(out, dout, sizeof(double) * n * nrays, cudaMemcpyDeviceToHost, st));
     TG_CUDA(cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
     TG_CUDA(cudaFreeAsync(owned, st));
+    if (fcopy) TG_CUDA(cudaFreeAsync(fcopy, st));
     TG_CUDA(cudaStreamSynchronize(st));
     if (hflag) {
         set_last_error_msg("column density walk did not end within one visit per element");
