@@ -521,7 +521,7 @@ def run_column(args):
         e = torch.cuda.Event(enable_timing=True)
         e.record()
         # targets: the tree's own particles, which its first N coordinate rows hold in Morton order
-        _lib.check(L.tg_tree_column_density(t, vp(info.coord), n, vp(dr.data_ptr()), 6, 0, 0, 0.0,
+        _lib.check(L.tg_tree_column_density(t, vp(info.coord), n, vp(dr.data_ptr()), 6, 0, 0, 0.0, 0,
                                             _lib.TG_MEM_DEVICE, vp(out.data_ptr()), st), "column density")
         return tree, e
 

@@ -167,11 +167,14 @@ tg_status tg_bruteforce(const double *pos_t, const double *h_t, int64_t nt, cons
  * infinity (frontend.py:1321-1458). binned = 0: pytreegrav's ray-traced walk (treewalk.py:904-973) for
  * every (target, ray); rays are unit vectors, (nrays, 3) shared by all targets (ray_stride 0) or
  * target i's own set at rays + i * ray_stride (ray_stride 3 * nrays); out is (n, nrays).
- * binned = 1: the six-bin angular estimator with opening angle theta (treewalk.py:976-1030); rays
- * ignored; out is (n, 6). FP64 in the reference's order of operations. Trees of one system only.
- * TG_ERR_ITER_LIMIT if a walk does not end within one visit per element. */
+ * binned = 1: the six-bin angular estimator with opening angle theta; rays ignored; out is (n, 6):
+ * group_size 0 gives the per-target walk (treewalk.py:976-1030), group_size 1..32 the grouped walk
+ * of that many consecutive targets (treewalk.py:1197-1294), pytreegrav's choice from 1000 targets.
+ * FP64 in the reference's order of operations. Trees of one system only. TG_ERR_ITER_LIMIT if a walk
+ * does not end within one visit per element. */
 tg_status tg_tree_column_density(tg_tree tree, const double *pos, int64_t n, const double *rays, int64_t nrays,
-                                 int64_t ray_stride, int binned, double theta, int mem, double *out, void *stream);
+                                 int64_t ray_stride, int binned, double theta, int group_size, int mem, double *out,
+                                 void *stream);
 
 /* Number of visible CUDA devices (0, not an error, when there is no driver or device); the check
  * behind pytreegrav.cuda.is_available (cuda.py:70-80). */

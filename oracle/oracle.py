@@ -64,6 +64,8 @@ def lib():
         L.tgo_bounding_cube.argtypes = [_dp, _i64, _dp, _dp]
         L.tgo_column_rays.argtypes = [ctypes.POINTER(_Tree), _dp, _i64, _dp, _i64, _i64, _dp, ctypes.c_int]
         L.tgo_column_binned.argtypes = [ctypes.POINTER(_Tree), _dp, _i64, ctypes.c_double, _dp, ctypes.c_int]
+        L.tgo_column_binned_grouped.argtypes = [ctypes.POINTER(_Tree), _dp, _i64, ctypes.c_double, _i64, _dp,
+                                                ctypes.c_int]
         for k in ("tgo_force_kernel", "tgo_potential_kernel", "tgo_tidal_kernel"):
             getattr(L, k).argtypes = [ctypes.c_double, ctypes.c_double]
             getattr(L, k).restype = ctypes.c_double
@@ -361,6 +363,15 @@ def column_binned(tree, pos, theta=0.5, nthreads=0):
     pos = _f64c(pos, (-1, 3))
     out = np.zeros((len(pos), 6))
     lib().tgo_column_binned(ctypes.byref(tree._t), _d(pos), len(pos), float(theta), _d(out), int(nthreads))
+    return out
+
+
+def column_binned_grouped(tree, pos, theta=0.5, group_size=16, nthreads=0):
+    """ColumnDensityBinned_grouped (treewalk.py:1197-1294): targets in the order to be grouped, (n, 6)."""
+    pos = _f64c(pos, (-1, 3))
+    out = np.zeros((len(pos), 6))
+    lib().tgo_column_binned_grouped(ctypes.byref(tree._t), _d(pos), len(pos), float(theta), int(group_size),
+                                    _d(out), int(nthreads))
     return out
 
 

@@ -993,3 +993,70 @@ void tgo_column_binned(const tgo_tree *t, const double *pos, int64_t n, double t
 #endif
     for (int64_t i = 0; i < n; i++) column_binned(t, pos + 3 * i, theta, out + 6 * i);
 }
+
+/* angular_bin_scalar (treewalk.py:38-45) is angular_bin on the three components */
+void tgo_column_binned_grouped(const tgo_tree *t, const double *pos, int64_t n, double theta, int64_t group_size,
+                               double *out, int nthreads) {
+    const int64_t N = t->npart;
+    const double angular_bin_size = (4 * M_PI) / 6;
+    const int64_t ngroups = (n + group_size - 1) / group_size;
+    for (int64_t i = 0; i < 6 * n; i++) out[i] = 0.0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 4)
+#endif
+    for (int64_t gi = 0; gi < ngroups; gi++) {
+        const int64_t a = gi * group_size, b = a + group_size < n ? a + group_size : n;
+        double bmin[3], bmax[3];
+        for (int k = 0; k < 3; k++) bmin[k] = bmax[k] = pos[3 * a + k];
+        for (int64_t tt = a + 1; tt < b; tt++)
+            for (int k = 0; k < 3; k++) {
+                const double v = pos[3 * tt + k];
+                if (v < bmin[k]) bmin[k] = v;
+                else if (v > bmax[k]) bmax[k] = v;
+            }
+        int64_t no = N;
+        const int64_t stop = t->next[N];
+        while (no > -1 && no != stop) {
+            const double c[3] = {t->coord[3 * no], t->coord[3 * no + 1], t->coord[3 * no + 2]};
+            const double h_no = t->soft[no], M = t->mass[no];
+            if (no < N) {
+                const double hh = h_no * h_no;
+                for (int64_t tt = a; tt < b; tt++) {
+                    const double d[3] = {c[0] - pos[3 * tt], c[1] - pos[3 * tt + 1], c[2] - pos[3 * tt + 2]};
+                    const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                    const int bin = angular_bin(d);
+                    double *o = out + 6 * tt;
+                    if (r2 > hh) {
+                        o[bin] += M / r2 / angular_bin_size;
+                    } else if (h_no > 0) {
+                        const double col0 = M * (3 / (4 * M_PI * hh));
+                        const double fac = sqrt(r2) / h_no;
+                        const double col_iso = (1 - fac) * col0;
+                        for (int k = 0; k < 6; k++) o[k] += col_iso;
+                        o[bin] += col0 * fac * 2;
+                    }
+                }
+                no = t->next[no];
+            } else {
+                double dm[3];
+                for (int k = 0; k < 3; k++) {
+                    dm[k] = 0.0;
+                    if (c[k] < bmin[k]) dm[k] = bmin[k] - c[k];
+                    else if (c[k] > bmax[k]) dm[k] = c[k] - bmax[k];
+                }
+                const double r_min = sqrt(dm[0] * dm[0] + dm[1] * dm[1] + dm[2] * dm[2]);
+                if (accept(r_min, h_no, t->size[no], t->delta[no], theta)) {
+                    for (int64_t tt = a; tt < b; tt++) {
+                        const double d[3] = {c[0] - pos[3 * tt], c[1] - pos[3 * tt + 1], c[2] - pos[3 * tt + 2]};
+                        const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                        out[6 * tt + angular_bin(d)] += M / r2 / angular_bin_size;
+                    }
+                    no = t->next[no];
+                } else {
+                    no = t->first[no];
+                }
+            }
+        }
+    }
+}

@@ -73,6 +73,10 @@ int tgo_walk_counts_groups(const tgo_tree *t, const double *pos, const double *s
 void tgo_column_rays(const tgo_tree *t, const double *pos, int64_t n, const double *rays, int64_t nrays,
                      int64_t ray_stride, double *out, int nthreads);
 void tgo_column_binned(const tgo_tree *t, const double *pos, int64_t n, double theta, double *out, int nthreads);
+/* ColumnDensityBinned_grouped (treewalk.py:1197-1294): groups of group_size consecutive targets share
+ * one walk, accepting a node on its distance r_min from the group's bounding box; out (n, 6). */
+void tgo_column_binned_grouped(const tgo_tree *t, const double *pos, int64_t n, double theta, int64_t group_size,
+                               double *out, int nthreads);
 
 /* Brute force.  mode 0: target form (r == 0 pairs skipped, bruteforce.py:7-50, 209-256, 353-386);
  * mode 1: mutual form (self excluded by index, bruteforce.py:86-116, 164-206, 319-350).

@@ -139,7 +139,7 @@ def _declare(L):
     L.tg_morton_order.argtypes = [vp, i64, ci, vp, vp]
     L.tg_morton_order_noalloc.argtypes = [vp, i64, vp, vp]
     L.tg_bruteforce.argtypes = [vp, vp, i64, vp, vp, vp, i64, ci, ci, dbl, ci, ci, vp, vp]
-    L.tg_tree_column_density.argtypes = [vp, vp, i64, vp, i64, i64, ci, dbl, ci, vp, vp]
+    L.tg_tree_column_density.argtypes = [vp, vp, i64, vp, i64, i64, ci, dbl, ci, ci, vp, vp]
     L.tg_device_count.argtypes = [ctypes.POINTER(ci)]
     L.tg_sources_create.argtypes = [vp, vp, vp, i64, ci, vp, ctypes.POINTER(vp)]
     L.tg_sources_bruteforce.argtypes = [vp, vp, vp, i64, ci, dbl, ci, ci, vp, vp]

@@ -230,6 +230,91 @@ __global__ void k_column_binned(ColumnTree t, const double *pos, int64_t n, doub
     for (int k = 0; k < 6; k++) out[6 * i + k] = col[k];
 }
 
+// ColumnDensityBinned_grouped (treewalk.py:1197-1294): one warp per group of gsz (<= 32)
+// consecutive targets, lane k holding target k. The group's bounding box decides every node for all
+// its targets, so the warp walks one path; each lane adds its own target's share of every accepted
+// node and particle, in the walk's order.
+__global__ void k_column_binned_grouped(ColumnTree t, const double *pos, int64_t n, double theta, int gsz,
+                                        double *out, int *runaway) {
+    const int64_t a = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * gsz;
+    const int lane = threadIdx.x & 31;
+    if (a >= n) return;  // whole warps leave together
+    const int cnt = (int)(n - a < (int64_t)gsz ? n - a : (int64_t)gsz);
+    const bool mine = lane < cnt;
+    const int64_t ti = a + (mine ? lane : 0);
+    const double px = pos[3 * ti], py = pos[3 * ti + 1], pz = pos[3 * ti + 2];
+    double bmin[3] = {px, py, pz}, bmax[3] = {px, py, pz};
+#pragma unroll
+    for (int o = 16; o; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            bmin[k] = fmin(bmin[k], __shfl_xor_sync(FULL, bmin[k], o));
+            bmax[k] = fmax(bmax[k], __shfl_xor_sync(FULL, bmax[k], o));
+        }
+    double col[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    const int64_t N = t.npart;
+    int64_t no = N;
+    const int64_t stop = t.next[N];
+    for (int64_t guard = 0; no > -1 && no != stop; guard++) {
+        if (guard > t.nelem || no >= t.nelem) {
+            if (lane == 0) atomicOr(runaway, 1);
+            break;
+        }
+        const double cx = t.coord[3 * no], cy = t.coord[3 * no + 1], cz = t.coord[3 * no + 2];
+        const double h_no = t.soft[no], M = t.mass[no];
+        if (no < N) {
+            const double hh = dmul(h_no, h_no);
+            const double d0 = dsub(cx, px), d1 = dsub(cy, py), d2 = dsub(cz, pz);
+            const double r2 = dadd(dadd(dmul(d0, d0), dmul(d1, d1)), dmul(d2, d2));
+            const int bin = angular_bin(d0, d1, d2);
+            if (r2 > hh) {
+                const double c = ddiv(ddiv(M, r2), BIN_SOLID_ANGLE);
+#pragma unroll
+                for (int k = 0; k < 6; k++)
+                    if (k == bin) col[k] = dadd(col[k], c);
+            } else if (h_no > 0.0) {
+                const double col0 = dmul(M, ddiv(3.0, dmul(FOUR_PI, hh)));
+                const double fac = ddiv(__dsqrt_rn(r2), h_no);
+                const double iso = dmul(dsub(1.0, fac), col0);
+                const double peak = dmul(dmul(col0, fac), 2.0);
+#pragma unroll
+                for (int k = 0; k < 6; k++) {
+                    col[k] = dadd(col[k], iso);
+                    if (k == bin) col[k] = dadd(col[k], peak);
+                }
+            }
+            no = t.next[no];
+        } else {
+            const double c3[3] = {cx, cy, cz};
+            double dm[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                dm[k] = 0.0;
+                if (c3[k] < bmin[k]) dm[k] = dsub(bmin[k], c3[k]);
+                else if (c3[k] > bmax[k]) dm[k] = dsub(c3[k], bmax[k]);
+            }
+            const double r_min = __dsqrt_rn(dadd(dadd(dmul(dm[0], dm[0]), dmul(dm[1], dm[1])), dmul(dm[2], dm[2])));
+            const double size = t.size[no], delta = t.delta[no];
+            const double crit = pymax(dadd(ddiv(size, theta), delta), dadd(dadd(h_no, dmul(size, 0.6)), delta));
+            if (r_min > crit) {  // the same answer on every lane
+                const double d0 = dsub(cx, px), d1 = dsub(cy, py), d2 = dsub(cz, pz);
+                const double r2 = dadd(dadd(dmul(d0, d0), dmul(d1, d1)), dmul(d2, d2));
+                const double c = ddiv(ddiv(M, r2), BIN_SOLID_ANGLE);
+                const int bin = angular_bin(d0, d1, d2);
+#pragma unroll
+                for (int k = 0; k < 6; k++)
+                    if (k == bin) col[k] = dadd(col[k], c);
+                no = t.next[no];
+            } else {
+                no = t.first[no];
+            }
+        }
+    }
+    if (mine)
+#pragma unroll
+        for (int k = 0; k < 6; k++) out[6 * ti + k] = col[k];
+}
+
 }  // namespace
 }  // namespace tg
 
@@ -238,8 +323,10 @@ using namespace tg;
 extern "C" {
 
 tg_status tg_tree_column_density(tg_tree t, const double *pos, int64_t n, const double *rays, int64_t nrays,
-                                 int64_t ray_stride, int binned, double theta, int mem, double *out, void *stream) {
+                                 int64_t ray_stride, int binned, double theta, int group_size, int mem, double *out,
+                                 void *stream) {
     if (!t || !out || n < 0 || (n > 0 && !pos)) return TG_ERR_BAD_ARG;
+    if (binned && (group_size < 0 || group_size > 32)) return TG_ERR_BAD_ARG;
     if (mem != TG_MEM_HOST && mem != TG_MEM_DEVICE) return TG_ERR_BAD_ARG;
     if (binned) {
         if (!(theta > 0)) return TG_ERR_BAD_ARG;
@@ -283,7 +370,11 @@ tg_status tg_tree_column_density(tg_tree t, const double *pos, int64_t n, const 
     }
     float4 *fcopy = nullptr;
     ct.fhi = ct.flo = nullptr;
-    if (binned) {
+    if (binned && group_size >= 1) {
+        const int64_t ngroups = (n + group_size - 1) / group_size;
+        k_column_binned_grouped<<<div_up(ngroups * 32, 128), 128, 0, st>>>(ct, dpos, n, theta, group_size, dout, flag);
+        note_launch();
+    } else if (binned) {
         k_column_binned<<<div_up(n, 128), 128, 0, st>>>(ct, dpos, n, theta, dout, flag);
         note_launch();
     } else {

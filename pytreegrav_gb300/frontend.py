@@ -295,6 +295,9 @@ class Field:
         return self.evaluate(tidal=True, pos_target=pos_target, **kwargs)["tidal"]
 
 
+COLUMN_GROUP_MIN_TARGETS = 1000  # treewalk.py:16-19: from this many targets the binned walk is grouped
+
+
 def ColumnDensity(pos, m, radii, rays=None, randomize_rays=False, healpix=False, tree=None, theta=0.5,
                   return_tree=False, parallel=False, group_size=16, device="cpu"):
     """Column density from each particle integrated to infinity, the particles being uniform spheres
@@ -304,11 +307,11 @@ def ColumnDensity(pos, m, radii, rays=None, randomize_rays=False, healpix=False,
     the ray grid per particle by random_rotation(i) of its position i in Morton order. Returns
     (N, N_rays) or (N, 6) in the caller's order.
 
-    The walks run on the GPU in FP64 (device and parallel are accepted; device keeps pytreegrav's
-    checks). The ray-traced columns equal pytreegrav's at any group_size (its grouped walk is
-    bit-identical to the per-target one). The binned estimator is the per-target walk, which is
-    pytreegrav's result at group_size=1. Its default grouped walk, used from 1000 targets, opens a
-    superset of nodes and shifts the binned answer slightly.
+    The walks run on the GPU in FP64 in pytreegrav's order of operations (device and parallel are
+    accepted; device keeps pytreegrav's checks), and the dispatch is pytreegrav's: the binned estimator
+    walks per target below COLUMN_GROUP_MIN_TARGETS targets and by groups of group_size (at most 32
+    here) from there on. The ray-traced walk does not depend on group_size (pytreegrav's grouped ray
+    walk is bit-identical to its per-target one).
     """
     from .misc import random_rotation
 
@@ -352,8 +355,11 @@ def ColumnDensity(pos, m, radii, rays=None, randomize_rays=False, healpix=False,
     if device == "cuda" and (rays is None or randomize_rays):
         raise ValueError("device='cuda' supports only the ray-traced path: pass rays, and not randomize_rays")
 
-    if rays is None:
-        columns = tree.column_density(pos_sorted, None, theta)
+    if rays is None:  # pytreegrav groups the binned walk from COLUMN_GROUP_MIN_TARGETS targets on
+        grouped = len(pos_sorted) >= COLUMN_GROUP_MIN_TARGETS
+        if grouped and not 1 <= group_size <= 32:
+            raise ValueError("group_size must be between 1 and 32 for the grouped binned walk")
+        columns = tree.column_density(pos_sorted, None, theta, group_size if grouped else 0)
     elif randomize_rays:
         per = np.empty((len(pos_sorted),) + rays.shape)
         for i in range(len(pos_sorted)):

@@ -218,17 +218,18 @@ class Octree:
         _lib.check(rc, "learned tree walk")
         return _split(out, potential, accel, tidal)
 
-    def column_density(self, pos, rays=None, theta=0.5):
+    def column_density(self, pos, rays=None, theta=0.5, group_size=0):
         """Column density of this tree's particles (uniform spheres, radius = softening) from each
         target to infinity (tg_tree_column_density). rays: (nrays, 3) unit vectors shared by all
         targets, or (n, nrays, 3) per target, -> (n, nrays) from the ray-traced walk; None -> (n, 6)
-        from the angle-binned walk at opening angle theta. Targets are taken in the order given."""
+        from the angle-binned walk at opening angle theta, per target (group_size 0) or grouped by
+        group_size consecutive targets. Targets are taken in the order given."""
         pos = _as_f64(pos, (-1, 3))
         n = len(pos)
         if rays is None:
             out = np.empty((n, 6))
             rc = _lib.load().tg_tree_column_density(self._h, _lib.ptr(pos), n, None, 0, 0, 1, float(theta),
-                                                    _lib.TG_MEM_HOST, _lib.ptr(out), None)
+                                                    int(group_size), _lib.TG_MEM_HOST, _lib.ptr(out), None)
         else:
             rays = np.ascontiguousarray(rays, np.float64)
             per_target = rays.ndim == 3
@@ -237,7 +238,7 @@ class Octree:
                 raise ValueError("rays must be (nrays, 3), or (n, nrays, 3) for per-target rays")
             out = np.empty((n, nrays))
             rc = _lib.load().tg_tree_column_density(self._h, _lib.ptr(pos), n, _lib.ptr(rays), nrays,
-                                                    3 * nrays if per_target else 0, 0, 0.0, _lib.TG_MEM_HOST,
+                                                    3 * nrays if per_target else 0, 0, 0.0, 0, _lib.TG_MEM_HOST,
                                                     _lib.ptr(out), None)
         _lib.check(rc, "column density")
         return out

@@ -239,6 +239,13 @@ def column(src):
     for theta in (0.5, 0.8):
         col[f"binned_theta{theta}"] = np.array([ColumnDensityWalk_binned(p, tree, theta) for p in xt])
     col["rotations"] = np.array([random_rotation(i) for i in range(12)])
+    from pytreegrav.grouped_treewalk import _morton_order
+    from pytreegrav.treewalk import ColumnDensityBinned_grouped
+
+    xs = x[_morton_order(x)]  # targets in Morton order, as the frontend passes them
+    col["grouped/pos"] = xs
+    for gs in (1, 7, 16):
+        col[f"binned_grouped_gs{gs}"] = ColumnDensityBinned_grouped(xs, tree, 0.5, gs)
     np.savez_compressed(os.path.join(OUT, "golden_column.npz"), **col)
     print("wrote golden_column.npz")
 

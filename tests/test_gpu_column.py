@@ -63,6 +63,8 @@ def test_walks_equal_pytreegrav_and_oracle(tg, golden_column):
         assert np.array_equal(t.column_density(g["tgt/pos"], None, theta), g[f"binned_theta{theta}"])
     per = np.ascontiguousarray(np.broadcast_to(g["rays"], (len(g["tgt/pos"]),) + g["rays"].shape))
     assert np.array_equal(t.column_density(g["tgt/pos"], per), g["rays_out"])
+    for gs in (1, 7, 16):  # the grouped binned walk
+        assert np.array_equal(t.column_density(g["grouped/pos"], None, 0.5, gs), g[f"binned_grouped_gs{gs}"]), gs
 
 
 @pytest.mark.parametrize("n", [500, 4000])
@@ -105,10 +107,15 @@ def test_frontend_matches_the_oracle_in_the_callers_order(tg):
     ref[idx] = ref_sorted
     cols, tree = tg.ColumnDensity(x, m, h, rays=6, return_tree=True)
     assert np.array_equal(cols, ref)
-    binned_sorted = O.column_binned(ot, x[idx], 0.5)
+    # 3000 targets: pytreegrav groups the binned walk (16 consecutive Morton targets by default)
+    binned_sorted = O.column_binned_grouped(ot, x[idx], 0.5, 16)
     binned = np.empty_like(binned_sorted)
     binned[idx] = binned_sorted
     assert np.array_equal(tg.ColumnDensity(x, m, h), binned)
+    small = O.column_binned(ot, x[idx][:500], 0.5)  # below 1000 targets: the per-target walk
+    assert np.array_equal(tg.ColumnDensity(x[idx][:500], m[:500], h[:500], tree=tree), small)
+    with pytest.raises(ValueError, match="group_size"):
+        tg.ColumnDensity(x, m, h, group_size=64)
     assert np.array_equal(tg.ColumnDensity(x, m, h, tree=tree, rays=6), ref)
 
 

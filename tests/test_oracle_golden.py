@@ -146,3 +146,10 @@ def test_column_density_walks_bit_exact(golden_column):
     # per-target ray sets: the same rays repeated per target give the same columns
     per = np.broadcast_to(g["rays"], (len(g["tgt/pos"]),) + g["rays"].shape)
     assert np.array_equal(O.column_rays(t, g["tgt/pos"], per, per_target=True), g["rays_out"])
+
+
+def test_grouped_binned_column_density_bit_exact(golden_column):
+    g = golden_column
+    t = O.OracleTree(g["src/pos"], g["src/m"], g["src/h"])
+    for gs in (1, 7, 16):
+        assert np.array_equal(O.column_binned_grouped(t, g["grouped/pos"], 0.5, gs), g[f"binned_grouped_gs{gs}"]), gs
