@@ -572,8 +572,9 @@ struct BuildSummary {
     unsigned long long nodes;  // node slots made by the round (its scan total)
     unsigned long long n_exh;  // key-exhausted runs found by the round
     int bad;                   // invalid references (bit flags)
-    int pad;
+    int nonfinite;             // the input check's flag, copied in before the read-back
     int depth_hist[DEPTH_CAP + 1];
+    int sort_error;  // the radix sorts' look-back flag, taken with the final read-back
 };
 
 // Slot validation (as above) plus the depth histogram, over the slots [0, M) with
@@ -1260,7 +1261,8 @@ __global__ void k_init_root_segs(Segs g, const int64_t *sys_off, const double *c
 
 // Build the whole arena. pos/m/h are device pointers (m/h may be null).
 tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const double *h,
-                     const std::vector<int64_t> &sys_off_host, int quadrupole, int compute_moments, cudaStream_t st) {
+                     const std::vector<int64_t> &sys_off_host, int quadrupole, int compute_moments,
+                     const int *nonfinite, cudaStream_t st) {
     const int nsys = (int)sys_off_host.size() - 1;
     const int64_t N = sys_off_host.back();
     if (N < 1 || nsys < 1) return TG_ERR_BAD_ARG;
@@ -1345,6 +1347,9 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     BuildSummary hs;
     memset(&hs, 0, sizeof(hs));
     bool summary_final = false;
+    // Non-finite input is reported once the build has run to its end and freed its memory: every
+    // kernel stays in bounds on such input (keys of NaN quantize to 0, every link is checked).
+    bool nonfinite_seen = false;
 
     for (int round = 0; round <= MORTON_MAX_ROUNDS; round++) {
         // element offsets of the segments; round 0's segments are the systems
@@ -1417,8 +1422,10 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
             { k_summarize_slots<<<LAUNCH(std::max<int64_t>(nd.cap, N))>>>(nd, slot_base, &sum->nodes, p_parent, p_next,
                                                                        N, sum); tg::note_launch(); }
             TG_CUDA(cudaGetLastError());
+            if (nonfinite) TG_CUDA(cudaMemcpyAsync(&sum->nonfinite, nonfinite, sizeof(int), cudaMemcpyDeviceToDevice, st));
             TG_CUDA(cudaMemcpyAsync(&hs, sum, sizeof(BuildSummary), cudaMemcpyDeviceToHost, st));
             TG_CUDA(cudaStreamSynchronize(st));
+            if (hs.nonfinite) nonfinite_seen = true;
             return TG_OK;
         };
         TG_TRY(run_round());
@@ -1482,6 +1489,7 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
         TG_CUDA(cudaStreamSynchronize(st));
     }
     if (hs.bad) {
+        if (nonfinite_seen) return TG_ERR_NONFINITE;
         set_last_error_msg("internal error: octree build produced an invalid node reference");
         return TG_ERR_CUDA;
     }
@@ -1631,8 +1639,10 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     }
 
     // 9. the one closing synchronisation: link check, per-system node offsets, bucket reservations
-    int links_bad = 0;
+    int links_bad = 0, sort_bad = 0;
     std::vector<unsigned long long> rq(nsys, 0);
+    TG_TRY(sort_error_take(&sum->sort_error, st));
+    TG_CUDA(cudaMemcpyAsync(&sort_bad, &sum->sort_error, sizeof(int), cudaMemcpyDeviceToHost, st));
     TG_CUDA(cudaMemcpyAsync(&links_bad, &sum->bad, sizeof(int), cudaMemcpyDeviceToHost, st));
     if (nsys > 1)
         TG_CUDA(cudaMemcpyAsync(T->sys_node_off.data(), sys_node_off, sizeof(int64_t) * (nsys + 1),
@@ -1642,7 +1652,11 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     dfree(lvl, st); dfree(lvl_list, st); dfree(fdepth, st);
     dfree(sys_off, st); dfree(mn, st); dfree(mx, st); dfree(center, st); dfree(size, st);
     TG_CUDA(cudaStreamSynchronize(st));
-    TG_TRY(sort_error_check());
+    if (nonfinite_seen) return TG_ERR_NONFINITE;
+    if (sort_bad) {
+        set_last_error_msg("radix sort: a tile's look-back did not complete within its bound");
+        return TG_ERR_QUEUE_TIMEOUT;
+    }
     if (links_bad) {
         set_last_error_msg("internal error: octree links out of range");
         return TG_ERR_CUDA;

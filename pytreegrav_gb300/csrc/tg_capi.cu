@@ -8,7 +8,8 @@
 
 namespace tg {
 tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const double *h,
-                     const std::vector<int64_t> &sys_off_host, int quadrupole, int compute_moments, cudaStream_t st);
+                     const std::vector<int64_t> &sys_off_host, int quadrupole, int compute_moments,
+                     const int *nonfinite, cudaStream_t st);
 tg_status morton_order_device(const double *pos, int64_t n, uint32_t *perm, cudaStream_t st);
 template <typename T>
 tg_status build_arena(tg_tree_s *t, Arena<T> &ar, cudaStream_t st);
@@ -31,6 +32,14 @@ namespace {
 __global__ void k_nonfinite(const double *a, int64_t n, int *flag) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n && !isfinite(a[i])) atomicOr(flag, 1);
+}
+
+// Any non-finite value among positions (3n), masses (n, may be NULL) and softenings (n, may be NULL).
+__global__ void k_nonfinite3(const double *pos, const double *m, const double *h, int64_t n, int *flag) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 5 * n) return;
+    const double v = i < 3 * n ? pos[i] : (i < 4 * n ? (m ? m[i - 3 * n] : 0.0) : (h ? h[i - 4 * n] : 0.0));
+    if (!isfinite(v)) atomicOr(flag, 1);
 }
 
 __global__ void k_u32_to_i64(const uint32_t *a, int64_t n, int64_t *b) {
@@ -136,12 +145,20 @@ static tg_status build_common(const double *pos, const double *m, const double *
     TG_TRY(stage_in(pos, 3 * n, mem, st, dp));
     TG_TRY(stage_in(m, n, mem, st, dm));
     TG_TRY(stage_in(h, n, mem, st, dh));
-    const double *arrs[3] = {dp.ptr, dm.ptr, dh.ptr};
-    int64_t counts[3] = {3 * n, n, n};
-    TG_TRY(check_finite(arrs, counts, 3, st));
+    // the input check runs ahead of the build on the stream; the build reads its flag back with
+    // its first summary and reports non-finite input at its end
+    int *flag = nullptr;
+    TG_CUDA(tg::dev_malloc((void **)&flag, sizeof(int), st));
+    TG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    { k_nonfinite3<<<div_up(5 * n, 256), 256, 0, st>>>(dp.ptr, dm.ptr, dh.ptr, n, flag); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
     tg_tree_s *t = new (std::nothrow) tg_tree_s();
-    if (!t) return TG_ERR_OOM;
-    tg_status rc = build_tree(t, dp.ptr, dm.ptr, dh.ptr, off, quadrupole, compute_moments, st);
+    if (!t) {
+        cudaFreeAsync(flag, st);
+        return TG_ERR_OOM;
+    }
+    tg_status rc = build_tree(t, dp.ptr, dm.ptr, dh.ptr, off, quadrupole, compute_moments, flag, st);
+    cudaFreeAsync(flag, st);
     if (rc != TG_OK) {
         destroy(t);
         return rc;

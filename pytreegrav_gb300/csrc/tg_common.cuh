@@ -85,6 +85,8 @@ tg_status radix_sort_pairs(uint64_t *keys, uint32_t *vals, int64_t n, int bits, 
 // After a synchronisation: TG_ERR_QUEUE_TIMEOUT (and the flag cleared) if a sort's look-back ran
 // out of its bound since the last check.
 tg_status sort_error_check();
+// The same flag taken into *dst (device) on `st` and cleared, without a synchronisation.
+tg_status sort_error_take(int *dst, cudaStream_t st);
 
 int num_sms();
 

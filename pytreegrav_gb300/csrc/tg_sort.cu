@@ -349,6 +349,19 @@ __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const uint64_t *keys, c
     }
 }
 
+__global__ void k_take_sort_error(int *dst) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) dst[0] = atomicExch(&g_sort_error, 0);
+}
+
+// Stream-ordered: *dst (device) receives the flag and the flag is cleared, for a caller that reads
+// it back with its own results instead of synchronising for it.
+tg_status sort_error_take(int *dst, cudaStream_t st) {
+    k_take_sort_error<<<1, 32, 0, st>>>(dst);
+    note_launch();
+    TG_CUDA(cudaGetLastError());
+    return TG_OK;
+}
+
 tg_status sort_error_check() {
     int e = 0;
     TG_CUDA(cudaMemcpyFromSymbol(&e, g_sort_error, sizeof(int)));
