@@ -27,6 +27,12 @@ int64_t tg_launch_count(void);
  * and the kernel's duration. */
 int tg_measure_fp32_fma(double *tflops, double *ms, void *stream);
 
+/* Self-check of the library's integer binary64 -> binary32 conversions (used where kernels repack
+ * FP64 tree data as FP32) against the GPU's own conversion: for each of the n doubles at x (device
+ * memory, finite or not) float(x), and the split hi = float(x), lo = float(x - hi), are compared bit
+ * for bit (NaN results: NaN on both sides). *mismatches receives the count of differing values. */
+int tg_check_f32_conversion(const double *x, int64_t n, int64_t *mismatches, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

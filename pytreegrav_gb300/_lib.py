@@ -82,6 +82,15 @@ THETA_EXPORTS = [
     "tg_tree_fields_grouped",
     "tg_tree_fields_learned",
 ]
+# every extern "C" symbol declared in include/pytreegrav_gb300_measure.h (measurement and self-checks)
+MEASURE_EXPORTS = [
+    "tg_tree_last_walk_steps",
+    "tg_tree_last_walk_quad_interactions",
+    "tg_tree_last_walk_kernel_ms",
+    "tg_launch_count",
+    "tg_measure_fp32_fma",
+    "tg_check_f32_conversion",
+]
 TG_THETA_NFEAT = 16
 TG_MLP_H = 64
 TG_MLP_NPARAM = TG_MLP_H * TG_THETA_NFEAT + TG_MLP_H + TG_MLP_H * TG_MLP_H + TG_MLP_H + TG_MLP_H + 1

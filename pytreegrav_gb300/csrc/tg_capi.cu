@@ -22,6 +22,7 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
 tg_status make_groups(tg_tree_s *t, const std::vector<int64_t> &sys_off_host, int gs, int2 **groups,
                       int **group_root, int64_t *ngroups, cudaStream_t st);
 tg_status tree_groups(tg_tree_s *t, int G, cudaStream_t st);
+tg_status tree_groups_with_arena(tg_tree_s *t, int G, bool fp64, cudaStream_t st);
 tg_status make_cost_order(const double *tpos, const int2 *groups, int64_t ngroups, int **order, cudaStream_t st);
 tg_status run_bruteforce(const double *pt, const double *ht, int64_t nt, const double *ps, const double *ms,
                          const double *hs, int64_t ns, int fields, int mutual, double G, int precision, double *out,
@@ -109,6 +110,9 @@ void destroy(tg_tree_s *t) {
     free_arena(t->arena64, st);
     if (t->stats_dev) cudaFreeAsync(t->stats_dev, st);
     f(t->groups); f(t->group_root); f(t->group_node); f(t->gstats); f(t->gerr);
+    if (t->side) cudaStreamDestroy(t->side);  // released once its work is done
+    if (t->ev_fork) cudaEventDestroy(t->ev_fork);
+    if (t->ev_join) cudaEventDestroy(t->ev_join);
     delete t;
 }
 
@@ -278,7 +282,7 @@ tg_status tg_tree_fields(tg_tree t, const double *pos, const double *h, int64_t 
         const int2 *wg = nullptr;
         const int *wr = nullptr;
         if (grouping == TG_GROUP_TREE) {  // kept on the tree, not freed here
-            TG_TRY(tree_groups(t, group_size, st));
+            TG_TRY(tree_groups_with_arena(t, group_size, precision == TG_FP64, st));
             wg = t->groups;
             wr = t->group_root;
             ngroups = t->ngroups;

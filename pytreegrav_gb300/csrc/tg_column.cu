@@ -24,10 +24,7 @@ struct ColumnTree {
     const float4 *fhi, *flo;
 };
 
-__device__ __forceinline__ void split_f(double v, float &hi, float &lo) {
-    hi = __double2float_rn(v);
-    lo = __double2float_rn(v - (double)hi);
-}
+__device__ __forceinline__ void split_f(double v, float &hi, float &lo) { d2f_split(v, hi, lo); }
 
 __global__ void k_column_prep(ColumnTree t, float4 *fhi, float4 *flo) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -36,7 +33,7 @@ __global__ void k_column_prep(ColumnTree t, float4 *fhi, float4 *flo) {
     split_f(t.coord[3 * e], a.x, b.x);
     split_f(t.coord[3 * e + 1], a.y, b.y);
     split_f(t.coord[3 * e + 2], a.z, b.z);
-    a.w = (float)t.soft[e];
+    a.w = d2f(t.soft[e]);
     b.w = e < t.npart ? 0.f : (float)(t.size[e] * 0.8660254037844386 + t.delta[e]);
     fhi[e] = a;
     flo[e] = b;

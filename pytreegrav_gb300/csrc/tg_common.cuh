@@ -55,6 +55,117 @@ __device__ __forceinline__ double ordered_to_dbl(unsigned long long u) {
     return __longlong_as_double((long long)u);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Binary64 -> binary32 conversion in integer arithmetic, round to nearest, ties to even (IEEE 754
+// convertFormat), with float subnormals and overflow to infinity. GB300 executes FP64
+// instructions, conversions from double included, at a small fraction of its integer rate, so
+// kernels that only repack FP64 data as FP32 convert with these. Each result is bit-identical to
+// a hardware conversion without flush-to-zero.
+
+// Bits of the binary32 nearest to mag * 2^e2 (mag < 2^62), with the given sign bit. *r and *shift
+// receive the rounded significand before renormalisation and the count of low bits of mag it
+// dropped (r * 2^(e2 + shift) is the result's magnitude; shift <= 0: exact).
+__device__ __forceinline__ uint32_t f32_rne(uint64_t mag, int e2, uint32_t sign, uint64_t *r_out = nullptr,
+                                            int *shift_out = nullptr) {
+    if (mag == 0) {
+        if (r_out) *r_out = 0, *shift_out = 0;
+        return sign;
+    }
+    const int top = e2 + 63 - __clzll((long long)mag);  // mag * 2^e2 lies in [2^top, 2^(top+1))
+    const int q = max(top - 23, -149);                    // exponent of the result's last bit
+    const int shift = q - e2;
+    uint64_t r;
+    if (shift <= 0) r = mag << (-shift);  // exact: at most 24 significant bits
+    else if (shift >= 63) r = 0;          // below half the smallest subnormal
+    else {
+        r = mag >> shift;
+        const uint64_t rem = mag & ((1ull << shift) - 1), half = 1ull << (shift - 1);
+        if (rem > half || (rem == half && (r & 1))) r++;
+    }
+    if (r_out) *r_out = r, *shift_out = shift;
+    if (r == 0) return sign;
+    int qq = q;
+    if (r >> 24) r >>= 1, qq++;  // rounding carried into a new bit
+    if (r >> 23) {               // normal
+        const int ef = qq + 150;
+        return ef >= 255 ? (sign | 0x7f800000u) : (sign | ((uint32_t)ef << 23) | (uint32_t)(r & 0x7fffffu));
+    }
+    return sign | (uint32_t)r;  // subnormal (q == -149)
+}
+
+// Infinity or quiet NaN (payload's top bits kept) for a double with the all-ones exponent.
+__device__ __forceinline__ uint32_t f32_special(uint64_t u) {
+    const uint32_t sign = (uint32_t)(u >> 32) & 0x80000000u;
+    const uint64_t m = u & 0xfffffffffffffull;
+    return m ? (sign | 0x7fc00000u | (uint32_t)(m >> 29)) : (sign | 0x7f800000u);
+}
+
+// Generic path: any double (zeros, subnormal and overflowing results, infinities, NaN).
+static __device__ __noinline__ void d2f_split_slow(uint64_t u, float &hi, float &lo) {
+    const int E = (int)((u >> 52) & 0x7ff);
+    if (E == 0x7ff) {  // x - x is NaN for an infinity and a NaN alike
+        hi = __uint_as_float(f32_special(u));
+        lo = __uint_as_float(0x7fffffffu);
+        return;
+    }
+    const uint32_t sign = (uint32_t)(u >> 32) & 0x80000000u;
+    const uint64_t mag = E ? ((u & 0xfffffffffffffull) | (1ull << 52)) : (u & 0xfffffffffffffull);
+    const int e2 = (E ? E : 1) - 1075;
+    uint64_t r;
+    int shift;
+    const uint32_t hb = f32_rne(mag, e2, sign, &r, &shift);
+    hi = __uint_as_float(hb);
+    if ((hb & 0x7fffffffu) == 0x7f800000u) {  // overflow: x - inf
+        lo = -hi;
+        return;
+    }
+    const int64_t d = shift <= 0 ? 0 : (int64_t)mag - (int64_t)(r == 0 || shift >= 63 ? 0 : (r << shift));
+    lo = d == 0 ? 0.f : __uint_as_float(f32_rne((uint64_t)(d < 0 ? -d : d), e2, sign ^ (d < 0 ? 0x80000000u : 0u)));
+}
+
+// hi = float(x), lo = float(x - (double)hi) (the FP64 difference is exact). Fast path for
+// 2^-74 <= |x| < 2^127, where hi and a nonzero lo are both normal floats: hi keeps the top 23
+// fraction bits, rounded on the 29 dropped ones; lo is those dropped bits less the rounding step,
+// a signed integer below 2^28 in magnitude, converted exactly by two magic-number additions and
+// one rounding FP32 add, then scaled by a power of two.
+__device__ __forceinline__ void d2f_split(double x, float &hi, float &lo) {
+    const uint64_t u = (uint64_t)__double_as_longlong(x);
+    const uint32_t uh = (uint32_t)(u >> 32), ul = (uint32_t)u;
+    const uint32_t E = (uh >> 20) & 0x7ffu;
+    if (E - 949u > 1149u - 949u) {
+        d2f_split_slow(u, hi, lo);
+        return;
+    }
+    const uint32_t sign = uh & 0x80000000u;
+    const uint32_t rest = ul & 0x1fffffffu;  // the 29 dropped fraction bits
+    uint32_t b = (((uh & 0xfffffu) << 3) | (ul >> 29)) + ((E - 896u) << 23);
+    const uint32_t up = (rest > 0x10000000u || (rest == 0x10000000u && (b & 1u))) ? 1u : 0u;
+    b += up;  // a carry out of the fraction moves into the exponent
+    hi = __uint_as_float(sign | b);
+    const int32_t d = (int32_t)rest - (int32_t)(up << 29);  // (x - hi) / 2^(e - 52)
+    const uint32_t ad = (uint32_t)(d < 0 ? -d : d);
+    const float fa = (__uint_as_float(0x4b000000u | (ad >> 6)) - 8388608.f) * 64.f;  // exact
+    const float fb = __uint_as_float(0x4b000000u | (ad & 63u)) - 8388608.f;          // exact
+    const float f = __fadd_rn(fa, fb) * __uint_as_float((E - 948u) << 23);             // RNE(|d|) * 2^(e-52)
+    lo = d == 0 ? 0.f : __uint_as_float(__float_as_uint(f) | (sign ^ (d < 0 ? 0x80000000u : 0u)));
+}
+
+// float(x) (the hi part of d2f_split).
+__device__ __forceinline__ float d2f(double x) {
+    const uint64_t u = (uint64_t)__double_as_longlong(x);
+    const uint32_t uh = (uint32_t)(u >> 32), ul = (uint32_t)u;
+    const uint32_t E = (uh >> 20) & 0x7ffu;
+    if (E - 949u > 1149u - 949u) {
+        float hi, lo;
+        d2f_split_slow(u, hi, lo);
+        return hi;
+    }
+    const uint32_t rest = ul & 0x1fffffffu;
+    uint32_t b = (((uh & 0xfffffu) << 3) | (ul >> 29)) + ((E - 896u) << 23);
+    b += (rest > 0x10000000u || (rest == 0x10000000u && (b & 1u))) ? 1u : 0u;
+    return __uint_as_float((uh & 0x80000000u) | b);
+}
+
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 __device__ __forceinline__ unsigned lanemask_lt() {
     unsigned m;

@@ -29,6 +29,19 @@ __global__ void __launch_bounds__(256) k_fma_probe(float *sink, float a, float b
     for (int c = 0; c < FMA_CHAINS; c++) s += v[c];
     if (s == 1234.5f) sink[0] = s;  // never true in practice; keeps the chains live
 }
+
+__global__ void k_check_conversion(const double *x, int64_t n, unsigned long long *bad) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = x[i];
+    const float hw = __double2float_rn(v), hwlo = __double2float_rn(v - (double)hw);
+    float hi, lo;
+    tg::d2f_split(v, hi, lo);
+    const float one = tg::d2f(v);
+    // equal bits, or NaN where the hardware gives NaN (its payload is not specified)
+    auto same = [](float a, float b) { return __float_as_uint(a) == __float_as_uint(b) || (b != b && a != a); };
+    if (!same(one, hw) || !same(hi, hw) || !same(lo, hwlo)) atomicAdd(bad, 1ull);
+}
 }  // namespace
 
 extern "C" {
@@ -61,6 +74,24 @@ int tg_measure_fp32_fma(double *tflops, double *ms, void *stream) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(sink);
+    return TG_OK;
+}
+
+int tg_check_f32_conversion(const double *x, int64_t n, int64_t *mismatches, void *stream) {
+    if (!mismatches || n < 0 || (n > 0 && !x)) return TG_ERR_BAD_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned long long *bad = nullptr;
+    TG_CUDA(tg::dev_malloc((void **)&bad, sizeof(unsigned long long), st));
+    TG_CUDA(cudaMemsetAsync(bad, 0, sizeof(unsigned long long), st));
+    if (n > 0) {
+        k_check_conversion<<<tg::div_up(n, 256), 256, 0, st>>>(x, n, bad);
+        tg::note_launch();
+    }
+    unsigned long long h = 0;
+    TG_CUDA(cudaMemcpyAsync(&h, bad, sizeof(h), cudaMemcpyDeviceToHost, st));
+    TG_CUDA(cudaFreeAsync(bad, st));
+    TG_CUDA(cudaStreamSynchronize(st));
+    *mismatches = (int64_t)h;
     return TG_OK;
 }
 

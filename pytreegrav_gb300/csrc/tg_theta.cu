@@ -19,6 +19,7 @@
 namespace tg {
 
 tg_status tree_groups(tg_tree_s *t, int G, cudaStream_t st);
+tg_status tree_groups_with_arena(tg_tree_s *t, int G, bool fp64, cudaStream_t st);
 template <typename T>
 tg_status build_arena(tg_tree_s *t, Arena<T> &ar, cudaStream_t st);
 tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t ntargets, const int2 *groups,
@@ -56,6 +57,10 @@ __global__ void k_copy_groups(const int2 *groups, const int *node, int64_t ng, i
 __global__ void k_top_nodes(Arena<float> ar, int *top, int *ntop) {
     __shared__ int cur[TOP_MAX], nxt[TOP_MAX];
     __shared__ int ncur, nnxt, nout;
+    if (ar.bad && *ar.bad) {  // the arena is invalid (the walk reports it): no frontier
+        if (threadIdx.x == 0) *ntop = 0;
+        return;
+    }
     if (threadIdx.x == 0) {
         cur[0] = 0;
         ncur = 1;
@@ -123,9 +128,13 @@ __global__ void k_features(int64_t ntot, const double *coord, const double *mass
     float lo[3], hi[3], hm;
     {
         const int64_t t = gr.x + (lane < gr.y ? lane : 0);
-        const double o[3] = {(double)o4.x, (double)o4.y, (double)o4.z};
-        for (int k = 0; k < 3; k++) lo[k] = hi[k] = (float)(coord[3 * t + k] - o[k]);
-        hm = (float)soft[t];
+        const float o[3] = {o4.x, o4.y, o4.z};
+        for (int k = 0; k < 3; k++) {  // (hi - o) + lo: the offset from the origin to ~1 float ulp
+            float ch, cl;
+            d2f_split(coord[3 * t + k], ch, cl);
+            lo[k] = hi[k] = (ch - o[k]) + cl;
+        }
+        hm = d2f(soft[t]);
     }
 #pragma unroll
     for (int s = 16; s; s >>= 1) {
@@ -168,11 +177,13 @@ __global__ void k_features(int64_t ntot, const double *coord, const double *mass
     }
     if (lane != 0) return;
     const int64_t R = ntot, P = ntot + group_node[g];  // system root (node 0) and the group's node
-    const float S = size[R] > 0 ? (float)size[R] : 1.f, Mt = mass[R] > 0 ? (float)mass[R] : 1.f;
+    // FP64 compares and conversions as integer work (finite inputs: x > 0 iff its bits are a positive int64)
+    auto pos = [](double x) { return __double_as_longlong(x) > 0; };
+    const float S = pos(size[R]) ? d2f(size[R]) : 1.f, Mt = pos(mass[R]) ? d2f(mass[R]) : 1.f;
     const float tiny = 1e-9f * S;
     const float emax = fmaxf(ext[0], fmaxf(ext[1], ext[2])), emin = fminf(ext[0], fminf(ext[1], ext[2]));
     const float dcen = sqrtf(gc[0] * gc[0] + gc[1] * gc[1] + gc[2] * gc[2]);
-    const float sP = size[P] > 0 ? (float)size[P] : tiny, mP = (float)mass[P];
+    const float sP = pos(size[P]) ? d2f(size[P]) : tiny, mP = d2f(mass[P]);
     const float fa = s1 * S * S / Mt, fv = sqrtf(vx * vx + vy * vy + vz * vz) * S * S / Mt, fp = s3 * S / Mt;
     const float lmP = logf(mP / Mt + 1e-30f), lsP = logf(sP / S);
     float *o = feat + g * NF;
@@ -195,8 +206,10 @@ __global__ void k_features(int64_t ntot, const double *coord, const double *mass
     // group-size weighted sum of the field's square (units M / S^2, fixed point 2^-32: integer
     // sums do not depend on the order of the atomics) and of the weights, for the tolerance unit
     // of tg_theta_tolerances
-    const double q = fmin((double)gr.y * (double)fv * (double)fv, 1e8) * 4294967296.0;
-    atomicAdd(field_sums, (unsigned long long)q);
+    const uint32_t qb = __float_as_uint(fminf((float)gr.y * fv * fv, 1e8f) * 4294967296.f) & 0x7fffffffu;
+    const int qe = (int)(qb >> 23) - 150;  // truncation to an integer, without a 64-bit conversion
+    const unsigned long long qm = (qb & 0x7fffffu) | 0x800000u;
+    atomicAdd(field_sums, qb < 0x3f800000u ? 0ull : (qe >= 0 ? qm << qe : qm >> -qe));
     atomicAdd(field_sums + 1, (unsigned long long)gr.y);
 }
 
@@ -797,7 +810,7 @@ tg_status tg_tree_fields_learned(tg_tree t, int fields, int quadrupole, double G
         return TG_ERR_BAD_ARG;
     if (quadrupole && !t->quad) return TG_ERR_NO_QUADRUPOLES;
     cudaStream_t st = (cudaStream_t)stream;
-    TG_TRY(tree_groups(t, group_size, st));
+    TG_TRY(tree_groups_with_arena(t, group_size, false, st));
     const int64_t ng = t->ngroups, nt = t->ntot;
     float *tg_theta = nullptr, *feat = nullptr, *tol = nullptr;
     double theta = theta_fallback;

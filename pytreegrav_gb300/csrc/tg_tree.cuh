@@ -34,6 +34,7 @@ struct Arena {
     // per leaf
     vec4<T> *l_pos = nullptr;  // hi.xyz, m
     vec4<T> *l_lo = nullptr;   // lo.xyz, h
+    int *bad = nullptr;        // device: nonzero if the tree's links did not make a valid arena
     bool built = false;
     bool has_quad = false;
 };
@@ -99,4 +100,8 @@ struct tg_tree_s {
     // with (1024: groups that overflow it are rewalked with 4096; 4096: every group starts there).
     int walk_warps = 4;
     int walk_stack = 1024;
+    // Side stream (non-blocking, made on first use) on which the walk arena is packed while the
+    // grouping runs on the caller's stream, and the two events that order it.
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };

@@ -121,14 +121,14 @@ __device__ __forceinline__ f2 f2_rsqrt(f2 x) {
 
 // ---------------------------------------------------------------------------------------------
 // Arena packing.
-__device__ __forceinline__ void split_hi_lo(double x, float &hi, float &lo) {
-    hi = __double2float_rn(x);
-    lo = __double2float_rn(x - (double)hi);
-}
+__device__ __forceinline__ void split_hi_lo(double x, float &hi, float &lo) { d2f_split(x, hi, lo); }
 __device__ __forceinline__ void split_hi_lo(double x, double &hi, double &lo) {
     hi = x;
     lo = 0.0;
 }
+// FP64 value in the walk precision (integer conversion for FP32).
+__device__ __forceinline__ float narrow(double x, float) { return d2f(x); }
+__device__ __forceinline__ double narrow(double x, double) { return x; }
 
 __global__ void k_arena_links(int64_t ntot, int64_t mtot, const int64_t *first, const int64_t *next, int4 *link,
                               int64_t *nleaf, int *bad) {
@@ -168,16 +168,20 @@ __global__ void k_arena_fill(int64_t ntot, int64_t mtot, const int64_t *first, c
     split_hi_lo(coord[3 * f], hx, lx);
     split_hi_lo(coord[3 * f + 1], hy, ly);
     split_hi_lo(coord[3 * f + 2], hz, lz);
-    T hm = (T)soft[f];
-    ar.n_pos[j] = vec4<T>{hx, hy, hz, (T)mass[f]};
+    T hm = narrow(soft[f], T(0));
+    ar.n_pos[j] = vec4<T>{hx, hy, hz, narrow(mass[f], T(0))};
     ar.n_lo[j] = vec4<T>{lx, ly, lz, hm};
     const int fc = lk.y > 0 ? lk.x : 0;
-    ar.n_trav[2 * j] = vec4<T>{hx, hy, hz, (T)size[f]};
-    ar.n_trav[2 * j + 1] = vec4<T>{(T)delta[f], hm, int_bits((fc << 4) | lk.y, T(0)), int_bits(((int)ls << 4) | lk.w, T(0))};
+    ar.n_trav[2 * j] = vec4<T>{hx, hy, hz, narrow(size[f], T(0))};
+    ar.n_trav[2 * j + 1] = vec4<T>{narrow(delta[f], T(0)), hm, int_bits((fc << 4) | lk.y, T(0)), int_bits(((int)ls << 4) | lk.w, T(0))};
     if (ar.n_quad) {
         const double *Q = quad + 9 * j;
-        ar.n_quad[2 * j] = vec4<T>{(T)Q[0], (T)Q[1], (T)Q[2], (T)Q[4]};
-        ar.n_quad[2 * j + 1] = vec4<T>{(T)Q[5], (T)Q[8], T(0), T(0)};
+        ar.n_quad[2 * j] = vec4<T>{narrow(Q[0], T(0)), narrow(Q[1], T(0)), narrow(Q[2], T(0)), narrow(Q[4], T(0))};
+        ar.n_quad[2 * j + 1] = vec4<T>{narrow(Q[5], T(0)), narrow(Q[8], T(0)), T(0), T(0)};
+    }
+    if (ls < 0 || ls + lk.w > ar.n_leaves) {  // leaf ranges from invalid links: nothing written
+        atomicOr(ar.bad, 16);
+        return;
     }
     int64_t k = ls;
     const int64_t kend = ls + lk.w;
@@ -186,11 +190,16 @@ __global__ void k_arena_fill(int64_t ntot, int64_t mtot, const int64_t *first, c
             split_hi_lo(coord[3 * c], hx, lx);
             split_hi_lo(coord[3 * c + 1], hy, ly);
             split_hi_lo(coord[3 * c + 2], hz, lz);
-            ar.l_pos[k] = vec4<T>{hx, hy, hz, (T)mass[c]};
-            ar.l_lo[k] = vec4<T>{lx, ly, lz, (T)soft[c]};
+            ar.l_pos[k] = vec4<T>{hx, hy, hz, narrow(mass[c], T(0))};
+            ar.l_lo[k] = vec4<T>{lx, ly, lz, narrow(soft[c], T(0))};
             k++;
         }
     }
+}
+
+// Every particle must be exactly one node's leaf.
+__global__ void k_arena_total(const int64_t *ltot, int64_t ntot, int *bad) {
+    if (threadIdx.x == 0 && *ltot != ntot) atomicOr(bad, 8);
 }
 
 template <typename T>
@@ -212,27 +221,17 @@ tg_status build_arena(tg_tree_s *t, Arena<T> &ar, cudaStream_t st) {
     TG_CUDA(tg::dev_malloc((void **)&ar.l_pos, sizeof(vec4<T>) * N, st));
     TG_CUDA(tg::dev_malloc((void **)&ar.l_lo, sizeof(vec4<T>) * N, st));
     int64_t *nleaf = nullptr, *lstart = nullptr, *ltot = nullptr;
-    int *bad = nullptr;
     TG_CUDA(tg::dev_malloc((void **)&nleaf, sizeof(int64_t) * M, st));
     TG_CUDA(tg::dev_malloc((void **)&lstart, sizeof(int64_t) * M, st));
     TG_CUDA(tg::dev_malloc((void **)&ltot, sizeof(int64_t), st));
-    TG_CUDA(tg::dev_malloc((void **)&bad, sizeof(int), st));
-    TG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
-    { k_arena_links<<<div_up(M, 256), 256, 0, st>>>(N, M, t->first, t->next, ar.n_link, nleaf, bad); tg::note_launch(); }
+    TG_CUDA(tg::dev_malloc((void **)&ar.bad, sizeof(int), st));
+    TG_CUDA(cudaMemsetAsync(ar.bad, 0, sizeof(int), st));
+    // validated on the device: the fill writes only in-range leaf ranges, and every walk checks the
+    // flag before it reads the arena (no host synchronisation here)
+    { k_arena_links<<<div_up(M, 256), 256, 0, st>>>(N, M, t->first, t->next, ar.n_link, nleaf, ar.bad); tg::note_launch(); }
     TG_TRY(exclusive_scan_i64(nleaf, lstart, M, ltot, st));
-    int hbad = 0;
-    int64_t htot = 0;
-    TG_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
-    TG_CUDA(cudaMemcpyAsync(&htot, ltot, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-    TG_CUDA(cudaStreamSynchronize(st));
-    TG_CUDA(cudaFreeAsync(bad, st));
+    { k_arena_total<<<1, 32, 0, st>>>(ltot, N, ar.bad); tg::note_launch(); }
     TG_CUDA(cudaFreeAsync(ltot, st));
-    if (hbad || htot != N) {
-        cudaFreeAsync(nleaf, st);
-        cudaFreeAsync(lstart, st);
-        set_last_error_msg("internal error: tree links do not form a valid octree for the walk arena");
-        return TG_ERR_CUDA;
-    }
     { k_arena_fill<T><<<div_up(M, 256), 256, 0, st>>>(N, M, t->first, t->next, t->coord, t->mass, t->soft, t->size,
                                                      t->delta, t->quad, lstart, ar); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
@@ -251,6 +250,7 @@ void free_arena(Arena<T> &ar, cudaStream_t st) {
     if (ar.n_quad) cudaFreeAsync(ar.n_quad, st);
     if (ar.l_pos) cudaFreeAsync(ar.l_pos, st);
     if (ar.l_lo) cudaFreeAsync(ar.l_lo, st);
+    if (ar.bad) cudaFreeAsync(ar.bad, st);
     ar = Arena<T>();
 }
 template tg_status build_arena<float>(tg_tree_s *, Arena<float> &, cudaStream_t);
@@ -488,6 +488,10 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
     unsigned long long n_int = 0, n_tests = 0, n_steps = 0, n_qint = 0;
     int max_sp = 0;
     const int64_t ngroups = a.ngroups_dev ? (int64_t)*a.ngroups_dev : a.ngroups;
+    if (a.ar.bad && *a.ar.bad) {  // the tree's links did not make a valid arena: read nothing
+        if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(a.status, 1 << TG_ERR_CUDA);
+        return;
+    }
 
     for (;;) {
         int g = 0;
@@ -1239,7 +1243,7 @@ __global__ void k_prep_targets(const double *tpos, const double *th, int64_t n, 
     split_hi_lo(tpos[3 * i], hx, lx);
     split_hi_lo(tpos[3 * i + 1], hy, ly);
     split_hi_lo(tpos[3 * i + 2], hz, lz);
-    thi[i] = vec4<T>{hx, hy, hz, (T)th[i]};
+    thi[i] = vec4<T>{hx, hy, hz, narrow(th[i], T(0))};
     tlo[i] = vec4<T>{lx, ly, lz, T(0)};
 }
 
@@ -1457,6 +1461,10 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
     t->last_stats.quad_interactions = (int64_t)stats[4];
     t->last_stats.kernel_ms = kms;
     TG_TRY(sort_error_check());  // the grouping's sorts
+    if (status & (1 << TG_ERR_CUDA)) {
+        set_last_error_msg("internal error: tree links do not form a valid octree for the walk arena");
+        return TG_ERR_CUDA;
+    }
     if (status & (1 << TG_ERR_STACK_OVERFLOW)) return TG_ERR_STACK_OVERFLOW;
     if (status & (1 << TG_ERR_ITER_LIMIT)) return TG_ERR_ITER_LIMIT;
     return TG_OK;
@@ -1523,6 +1531,32 @@ tg_status tree_groups(tg_tree_s *t, int G, cudaStream_t st) {
     t->ngroups = (int64_t)ng;
     t->groups_G = G;
     return TG_OK;
+}
+
+// Tree groups at size G and the walk arena of the given precision. An arena not yet built is packed
+// on the tree's side stream while the grouping (which reads its group count back to the host) runs
+// on st; st waits for the arena before this returns, also on error.
+tg_status tree_groups_with_arena(tg_tree_s *t, int G, bool fp64, cudaStream_t st) {
+    const bool need = fp64 ? !t->arena64.built : !t->arena32.built;
+    if (!need) return tree_groups(t, G, st);
+    if (!t->side) {
+        TG_CUDA(cudaStreamCreateWithFlags(&t->side, cudaStreamNonBlocking));
+        TG_CUDA(cudaEventCreateWithFlags(&t->ev_fork, cudaEventDisableTiming));
+        TG_CUDA(cudaEventCreateWithFlags(&t->ev_join, cudaEventDisableTiming));
+    }
+    TG_CUDA(cudaEventRecord(t->ev_fork, st));
+    TG_CUDA(cudaStreamWaitEvent(t->side, t->ev_fork, 0));
+    const tg_status ra = fp64 ? build_arena(t, t->arena64, t->side) : build_arena(t, t->arena32, t->side);
+    const cudaError_t ej = cudaEventRecord(t->ev_join, t->side);
+    const tg_status rg = tree_groups(t, G, st);
+    if (ej == cudaSuccess) TG_CUDA(cudaStreamWaitEvent(st, t->ev_join, 0));
+    else {  // the join could not be recorded: wait for the side stream from the host
+        cudaStreamSynchronize(t->side);
+        set_last_error_msg("could not record the walk arena's completion event");
+        return TG_ERR_CUDA;
+    }
+    TG_TRY(ra);
+    return rg;
 }
 
 // Largest-first queue order of consecutive-block groups (see k_group_cost_keys).
@@ -1703,6 +1737,10 @@ tg_status tg_walk_graph_status(tg_walk_graph g, void *stream) {
     int status = 0;
     TG_CUDA(cudaMemcpyAsync(&status, g->scratch + tg::WS_STATUS, sizeof(int), cudaMemcpyDeviceToHost, st));
     TG_CUDA(cudaStreamSynchronize(st));
+    if (status & (1 << TG_ERR_CUDA)) {
+        tg::set_last_error_msg("internal error: tree links do not form a valid octree for the walk arena");
+        return TG_ERR_CUDA;
+    }
     if (status & (1 << TG_ERR_STACK_OVERFLOW)) return TG_ERR_STACK_OVERFLOW;
     if (status & (1 << TG_ERR_ITER_LIMIT)) return TG_ERR_ITER_LIMIT;
     return TG_OK;

@@ -15,12 +15,13 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def header_symbols(name="pytreegrav_gb300.h"):
     src = open(os.path.join(ROOT, "include", name)).read()
-    return sorted(set(re.findall(r"^(?:tg_status|const char \*)\s*(tg_\w+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^(?:tg_status|const char \*|int64_t|double|int)\s*(tg_\w+)\s*\(", src, re.M)))
 
 
 def test_header_and_binding_agree():
     assert header_symbols() == sorted(_lib.EXPORTS)
     assert header_symbols("pytreegrav_gb300_theta.h") == sorted(_lib.THETA_EXPORTS)
+    assert header_symbols("pytreegrav_gb300_measure.h") == sorted(_lib.MEASURE_EXPORTS)
 
 
 def test_theta_constants_agree_with_header():
@@ -36,7 +37,8 @@ def test_library_builds_loads_and_exports_every_symbol():
 
     path = build.build()
     L = ctypes.CDLL(path)
-    for name in header_symbols() + header_symbols("pytreegrav_gb300_theta.h"):
+    for name in (header_symbols() + header_symbols("pytreegrav_gb300_theta.h")
+                 + header_symbols("pytreegrav_gb300_measure.h")):
         assert hasattr(L, name), name
 
 
