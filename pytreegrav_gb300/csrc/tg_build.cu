@@ -146,30 +146,58 @@ __device__ __forceinline__ uint64_t spread_bits(uint64_t x) {
     return x;
 }
 
-// int() truncation toward zero, then the clamp to [0, 2^21 - 1] (octree.py:85-96).
-__device__ __forceinline__ uint64_t quantize(double v) {
-    if (v >= 2097152.0) return (1u << MORTON_BITS) - 1;
-    if (!(v > -1.0)) return 0;
-    long long q = __double2ll_rz(v);
-    return q < 0 ? 0 : (uint64_t)q;
+// A key cell as the key formula uses it: the corner (centre - size/2) and 1/size.
+struct KeyCell {
+    double o0, o1, o2, inv;
+};
+__device__ __forceinline__ KeyCell key_cell(const double *c, double size) {
+    KeyCell k;
+    k.inv = size > 0 ? ddiv(1.0, size) : 0.0;
+    const double h = dmul(0.5, size);
+    k.o0 = dsub(c[0], h);
+    k.o1 = dsub(c[1], h);
+    k.o2 = dsub(c[2], h);
+    return k;
 }
 
-__device__ __forceinline__ uint64_t morton_key(double x, double y, double z, const double *c, double size) {
-    double inv = size > 0 ? ddiv(1.0, size) : 0.0;
-    double h = dmul(0.5, size);
-    double c0 = dsub(c[0], h), c1 = dsub(c[1], h), c2 = dsub(c[2], h);
-    uint64_t qx = quantize(dmul(dmul(dsub(x, c0), inv), 2097152.0));
-    uint64_t qy = quantize(dmul(dmul(dsub(y, c1), inv), 2097152.0));
-    uint64_t qz = quantize(dmul(dmul(dsub(z, c2), inv), 2097152.0));
+// int(t * 2^21) truncated toward zero, then clamped to [0, 2^21 - 1] (octree.py:85-96), read off the
+// bits of t on the integer units. The product by 2^21 is exact unless it overflows (t >= 2^1003:
+// clamped to the top either way) or underflows (t < 2^-1001: zero either way), so t decides alone:
+// NaN, negative or below 2^-21 gives 0; 1 or more gives the top; else the top 21 + e bits of the
+// significand, e = exponent(t) + 21.
+__device__ __forceinline__ uint64_t quantize21(double t) {
+    const long long b = __double_as_longlong(t);
+    if (b <= 0) return 0;  // +0, and every value with the sign bit set
+    const int E = (int)(b >> 52);
+    if (E >= 1023) return (E == 2047 && (b & 0xfffffffffffffll)) ? 0 : (1u << MORTON_BITS) - 1;
+    const int ev = E - 1023 + MORTON_BITS;
+    if (ev < 0) return 0;
+    return (uint64_t)(((b & 0xfffffffffffffll) | (1ll << 52)) >> (52 - ev));
+}
+
+// Per axis (x - corner) * (1/size), each FP64 operation rounded once, then quantize21.
+__device__ __forceinline__ uint64_t morton_key(double x, double y, double z, const KeyCell &k) {
+    const uint64_t qx = quantize21(dmul(dsub(x, k.o0), k.inv));
+    const uint64_t qy = quantize21(dmul(dsub(y, k.o1), k.inv));
+    const uint64_t qz = quantize21(dmul(dsub(z, k.o2), k.inv));
     return spread_bits(qx) | (spread_bits(qy) << 1) | (spread_bits(qz) << 2);
+}
+__device__ __forceinline__ uint64_t morton_key(double x, double y, double z, const double *c, double size) {
+    return morton_key(x, y, z, key_cell(c, size));
 }
 
 __global__ void k_keys(const double *pos, int64_t n, const int64_t *sys_off, int nsys, const double *center,
                        const double *size, uint64_t *keys, uint64_t *keys_copy, uint32_t *vals) {
+    __shared__ KeyCell one;  // one system: its cell (with the division) formed once per block
+    if (nsys == 1) {
+        if (threadIdx.x == 0) one = key_cell(center, size[0]);
+        __syncthreads();
+    }
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int s = nsys > 1 ? (int)find_seg(sys_off, nsys, i) : 0;
-    uint64_t k = morton_key(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], center + 3 * s, size[s]);
+    const KeyCell kc = nsys == 1 ? one : key_cell(center + 3 * s, size[s]);
+    uint64_t k = morton_key(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], kc);
     keys[i] = k;
     if (keys_copy) keys_copy[i] = k;
     vals[i] = (uint32_t)i;

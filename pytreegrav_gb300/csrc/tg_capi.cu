@@ -30,17 +30,22 @@ tg_status run_bruteforce(const double *pt, const double *ht, int64_t nt, const d
 
 namespace {
 
+// Infinity or NaN: the all-ones exponent, tested on the bits (integer units, not the FP64 pipe).
+__device__ __forceinline__ bool nonfinite_bits(const double *p) {
+    return (~(unsigned long long)__ldg((const long long *)p) & 0x7ff0000000000000ull) == 0;
+}
+
 __global__ void k_nonfinite(const double *a, int64_t n, int *flag) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n && !isfinite(a[i])) atomicOr(flag, 1);
+    if (i < n && nonfinite_bits(a + i)) atomicOr(flag, 1);
 }
 
 // Any non-finite value among positions (3n), masses (n, may be NULL) and softenings (n, may be NULL).
 __global__ void k_nonfinite3(const double *pos, const double *m, const double *h, int64_t n, int *flag) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 5 * n) return;
-    const double v = i < 3 * n ? pos[i] : (i < 4 * n ? (m ? m[i - 3 * n] : 0.0) : (h ? h[i - 4 * n] : 0.0));
-    if (!isfinite(v)) atomicOr(flag, 1);
+    const double *p = i < 3 * n ? pos + i : (i < 4 * n ? (m ? m + (i - 3 * n) : nullptr) : (h ? h + (i - 4 * n) : nullptr));
+    if (p && nonfinite_bits(p)) atomicOr(flag, 1);
 }
 
 __global__ void k_u32_to_i64(const uint32_t *a, int64_t n, int64_t *b) {

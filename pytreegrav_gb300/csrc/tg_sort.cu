@@ -181,11 +181,17 @@ __device__ __forceinline__ void rank_warp_slice(const uint64_t *keys, int64_t n,
                                                 int *wcount, int *digit, int *rank) {
     const int lane = lane_id();
     const unsigned lt = lanemask_lt();
+    uint64_t kv[ROUNDS];  // every round's key loaded up front: one memory round trip per slice
+#pragma unroll
+    for (int r = 0; r < ROUNDS; r++) {
+        const int64_t i = wbase + r * 32 + lane;
+        kv[r] = i < n ? __ldg(keys + i) : 0ull;
+    }
 #pragma unroll
     for (int r = 0; r < ROUNDS; r++) {
         int64_t i = wbase + r * 32 + lane;
         int d = RS_BINS;  // sentinel for keys past the end
-        if (i < n) d = (int)((keys[i] >> shift) & (RS_BINS - 1));
+        if (i < n) d = (int)((kv[r] >> shift) & (RS_BINS - 1));
         unsigned peers = __match_any_sync(FULL, d);
         int base = (d < RS_BINS) ? wcount[d] : 0;
         __syncwarp();
@@ -262,6 +268,7 @@ constexpr int OS_WARP_KEYS = OS_ROUNDS * 32;
 constexpr int OS_TILE = RS_WARPS * OS_WARP_KEYS;   // 1024 keys per CTA: many CTAs per SM
 constexpr unsigned long long ST_AGG = 1ull << 62, ST_INC = 2ull << 62, ST_VAL = (1ull << 62) - 1;
 constexpr long long SPIN_LIMIT = 1ll << 22;
+constexpr int LB = 4;  // predecessors read per look-back round trip
 __device__ int g_sort_error;
 
 __global__ void __launch_bounds__(256) k_sort_hist_all(const uint64_t *keys, int64_t n, int npass, int *hist) {
@@ -320,17 +327,29 @@ __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const uint64_t *keys, c
         } else {
             *st = ST_AGG | (unsigned long long)run;
             // earlier tiles publish their aggregate without waiting on anyone, so each wait ends
-            // once that tile's CTA (already running: it took its tile before this one) has ranked
-            for (int64_t j = t - 1; j >= 0; j--) {
-                const volatile unsigned long long *src = status + j * RS_BINS + d;
-                unsigned long long wd = *src;
-                for (long long spins = 0; !(wd & ~ST_VAL) && spins < SPIN_LIMIT; spins++) wd = *src;
-                if (!(wd & ~ST_VAL)) {
-                    atomicExch(&g_sort_error, 1);
-                    break;
+            // once that tile's CTA (already running: it took its tile before this one) has ranked.
+            // The words of LB predecessors are read together (independent loads, one round trip),
+            // then summed in order up to the first inclusive one.
+            bool done = false;
+            for (int64_t j = t - 1; j >= 0 && !done; j -= LB) {
+                unsigned long long w[LB];
+#pragma unroll
+                for (int k = 0; k < LB; k++)
+                    w[k] = j - k >= 0 ? ((const volatile unsigned long long *)status)[(j - k) * RS_BINS + d] : 0ull;
+#pragma unroll
+                for (int k = 0; k < LB; k++) {
+                    if (done || j - k < 0) break;
+                    unsigned long long wd = w[k];
+                    const volatile unsigned long long *src = status + (j - k) * RS_BINS + d;
+                    for (long long spins = 0; !(wd & ~ST_VAL) && spins < SPIN_LIMIT; spins++) wd = *src;
+                    if (!(wd & ~ST_VAL)) {
+                        atomicExch(&g_sort_error, 1);
+                        done = true;
+                        break;
+                    }
+                    acc += (long long)(wd & ST_VAL);
+                    if ((wd & ~ST_VAL) == ST_INC) done = true;
                 }
-                acc += (long long)(wd & ST_VAL);
-                if ((wd & ~ST_VAL) == ST_INC) break;
             }
             *st = ST_INC | (unsigned long long)(acc + run);
         }
