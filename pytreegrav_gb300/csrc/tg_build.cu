@@ -414,9 +414,36 @@ __device__ __forceinline__ double scale_down(double x, int q) {
 // applied from its segment's cell down to the slot's level (octree.py:974-978), in the reference's
 // order: centre += size * (+-1/4) per axis, then size *= 1/2. The products are powers-of-two
 // scalings (exact), so only the additions round, each once, as there.
-__global__ void k_node_centers(RoundView v, Nodes nd, int64_t slot_base, int64_t count, const uint64_t *keys) {
-    const int64_t slot = slot_base + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= slot_base + count || slot >= nd.cap) return;
+// FP64 instructions cost a warp the same with any number of active lanes, so the block's slots are
+// first ordered by level (a counting sort in shared memory, deepest first): a warp's lanes then run
+// equal numbers of steps. Which thread takes which slot does not change any result.
+constexpr int CENTER_BLOCK = 256;
+__global__ void __launch_bounds__(CENTER_BLOCK) k_node_centers(RoundView v, Nodes nd, int64_t slot_base,
+                                                               int64_t count, const uint64_t *keys) {
+    __shared__ int bin[MAX_LEVEL + 1];
+    __shared__ int64_t order[CENTER_BLOCK];
+    const int t = threadIdx.x;
+    const int64_t mine = slot_base + (int64_t)blockIdx.x * CENTER_BLOCK + t;
+    const bool valid = mine < slot_base + count && mine < nd.cap;
+    int lv = valid ? (int)nd.level[mine] : 0;
+    lv = lv < 0 ? 0 : (lv > MAX_LEVEL ? MAX_LEVEL : lv);
+    if (t <= MAX_LEVEL) bin[t] = 0;
+    __syncthreads();
+    const int r = atomicAdd(&bin[lv], 1);
+    __syncthreads();
+    if (t == 0) {
+        int run = 0;
+        for (int b = MAX_LEVEL; b >= 0; b--) {
+            const int c = bin[b];
+            bin[b] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    order[bin[lv] + r] = valid ? mine : -1;
+    __syncthreads();
+    const int64_t slot = order[t];
+    if (slot < 0) return;
     const int s = nd.seg[slot];
     const int k = nd.level[slot];
     const uint64_t key = keys[nd.lo[slot]];
@@ -1287,10 +1314,12 @@ __global__ void k_init_root_segs(Segs g, const int64_t *sys_off, const double *c
 
 #define LAUNCH(n) div_up((n), 256), 256, 0, st
 
-// Build the whole arena. pos/m/h are device pointers (m/h may be null).
+// Build the whole arena. pos/m/h are device pointers (m/h may be null). m_h_ready (may be null):
+// an event after which m and h may be read; the build waits for it only where it first reads them
+// (the gather into Morton order), so their upload overlaps the bounding cube, keys and sort.
 tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const double *h,
                      const std::vector<int64_t> &sys_off_host, int quadrupole, int compute_moments,
-                     const int *nonfinite, cudaStream_t st) {
+                     const int *nonfinite, cudaStream_t st, cudaEvent_t m_h_ready) {
     const int nsys = (int)sys_off_host.size() - 1;
     const int64_t N = sys_off_host.back();
     if (N < 1 || nsys < 1) return TG_ERR_BAD_ARG;
@@ -1350,6 +1379,7 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     TG_TRY(dalloc(&pm, N, st));
     TG_TRY(dalloc(&ps, N, st));
     uint64_t *keys_sorted = keys;  // reuse
+    if (m_h_ready) TG_CUDA(cudaStreamWaitEvent(st, m_h_ready, 0));
     { k_gather<<<LAUNCH(N)>>>(perm, N, pos, m, h, keys_orig, pc, pm, ps, keys_sorted, T->walk_idx); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
     dfree(keys_orig, st);
@@ -1468,7 +1498,7 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
             TG_TRY(run_round());
         }
         nd.count = slot_base + Mr;
-        if (Mr > 0) { k_node_centers<<<LAUNCH(Mr)>>>(v, nd, slot_base, Mr, keys_sorted); tg::note_launch(); }
+        if (Mr > 0) { k_node_centers<<<div_up(Mr, CENTER_BLOCK), CENTER_BLOCK, 0, st>>>(v, nd, slot_base, Mr, keys_sorted); tg::note_launch(); }
         n_exh = (int)hs.n_exh;
         dfree(L, st); dfree(cnt, st); dfree(nstart, st);
         if (n_exh == 0) {

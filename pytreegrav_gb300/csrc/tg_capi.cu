@@ -9,7 +9,8 @@
 namespace tg {
 tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const double *h,
                      const std::vector<int64_t> &sys_off_host, int quadrupole, int compute_moments,
-                     const int *nonfinite, cudaStream_t st);
+                     const int *nonfinite, cudaStream_t st, cudaEvent_t m_h_ready);
+tg_status tree_side_stream(tg_tree_s *t);
 tg_status morton_order_device(const double *pos, int64_t n, uint32_t *perm, cudaStream_t st);
 template <typename T>
 tg_status build_arena(tg_tree_s *t, Arena<T> &ar, cudaStream_t st);
@@ -150,24 +151,47 @@ static tg_status build_common(const double *pos, const double *m, const double *
     const int64_t n = off.back();
     if (n < 1) return TG_ERR_BAD_ARG;
     if (!m) compute_moments = 0;
-    DevBuf dp, dm, dh;
-    TG_TRY(stage_in(pos, 3 * n, mem, st, dp));
-    TG_TRY(stage_in(m, n, mem, st, dm));
-    TG_TRY(stage_in(h, n, mem, st, dh));
-    // the input check runs ahead of the build on the stream; the build reads its flag back with
-    // its first summary and reports non-finite input at its end
-    int *flag = nullptr;
-    TG_CUDA(tg::dev_malloc((void **)&flag, sizeof(int), st));
-    TG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
-    { k_nonfinite3<<<div_up(5 * n, 256), 256, 0, st>>>(dp.ptr, dm.ptr, dh.ptr, n, flag); tg::note_launch(); }
-    TG_CUDA(cudaGetLastError());
     tg_tree_s *t = new (std::nothrow) tg_tree_s();
-    if (!t) {
-        cudaFreeAsync(flag, st);
-        return TG_ERR_OOM;
+    if (!t) return TG_ERR_OOM;
+    tg_status rc = TG_OK;
+    {
+        DevBuf dp, dm, dh;
+        int *flag = nullptr;
+        cudaEvent_t m_h_ready = nullptr;
+        auto stage = [&]() -> tg_status {
+            TG_TRY(stage_in(pos, 3 * n, mem, st, dp));
+            // the input check runs ahead of the build on the stream; the build reads its flag back
+            // with its first summary and reports non-finite input at its end
+            TG_CUDA(tg::dev_malloc((void **)&flag, sizeof(int), st));
+            TG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+            if (mem == TG_MEM_HOST && (m || h)) {
+                { k_nonfinite<<<div_up(3 * n, 256), 256, 0, st>>>(dp.ptr, 3 * n, flag); tg::note_launch(); }
+                // masses and softenings are uploaded (and checked) on the tree's side stream while
+                // the build sorts the positions; the build waits for them where it first reads them
+                TG_TRY(tree_side_stream(t));
+                TG_CUDA(cudaEventRecord(t->ev_fork, st));
+                TG_CUDA(cudaStreamWaitEvent(t->side, t->ev_fork, 0));
+                TG_TRY(stage_in(m, n, mem, t->side, dm));
+                TG_TRY(stage_in(h, n, mem, t->side, dh));
+                dm.st = dh.st = st;  // freed on st, after the build's last read
+                if (dm.ptr) { k_nonfinite<<<div_up(n, 256), 256, 0, t->side>>>(dm.ptr, n, flag); tg::note_launch(); }
+                if (dh.ptr) { k_nonfinite<<<div_up(n, 256), 256, 0, t->side>>>(dh.ptr, n, flag); tg::note_launch(); }
+                TG_CUDA(cudaEventRecord(t->ev_join, t->side));
+                m_h_ready = t->ev_join;
+            } else {
+                TG_TRY(stage_in(m, n, mem, st, dm));
+                TG_TRY(stage_in(h, n, mem, st, dh));
+                { k_nonfinite3<<<div_up(5 * n, 256), 256, 0, st>>>(dp.ptr, dm.ptr, dh.ptr, n, flag); tg::note_launch(); }
+            }
+            TG_CUDA(cudaGetLastError());
+            return TG_OK;
+        };
+        rc = stage();
+        if (rc == TG_OK) rc = build_tree(t, dp.ptr, dm.ptr, dh.ptr, off, quadrupole, compute_moments, flag, st, m_h_ready);
+        // st is ordered after the side stream's uploads before anything staged is freed
+        if (m_h_ready) cudaStreamWaitEvent(st, m_h_ready, 0);
+        if (flag) cudaFreeAsync(flag, st);
     }
-    tg_status rc = build_tree(t, dp.ptr, dm.ptr, dh.ptr, off, quadrupole, compute_moments, flag, st);
-    cudaFreeAsync(flag, st);
     if (rc != TG_OK) {
         destroy(t);
         return rc;

@@ -1536,14 +1536,20 @@ tg_status tree_groups(tg_tree_s *t, int G, cudaStream_t st) {
 // Tree groups at size G and the walk arena of the given precision. An arena not yet built is packed
 // on the tree's side stream while the grouping (which reads its group count back to the host) runs
 // on st; st waits for the arena before this returns, also on error.
-tg_status tree_groups_with_arena(tg_tree_s *t, int G, bool fp64, cudaStream_t st) {
-    const bool need = fp64 ? !t->arena64.built : !t->arena32.built;
-    if (!need) return tree_groups(t, G, st);
+// The tree's side stream and its two events, made on first use.
+tg_status tree_side_stream(tg_tree_s *t) {
     if (!t->side) {
         TG_CUDA(cudaStreamCreateWithFlags(&t->side, cudaStreamNonBlocking));
         TG_CUDA(cudaEventCreateWithFlags(&t->ev_fork, cudaEventDisableTiming));
         TG_CUDA(cudaEventCreateWithFlags(&t->ev_join, cudaEventDisableTiming));
     }
+    return TG_OK;
+}
+
+tg_status tree_groups_with_arena(tg_tree_s *t, int G, bool fp64, cudaStream_t st) {
+    const bool need = fp64 ? !t->arena64.built : !t->arena32.built;
+    if (!need) return tree_groups(t, G, st);
+    TG_TRY(tree_side_stream(t));
     TG_CUDA(cudaEventRecord(t->ev_fork, st));
     TG_CUDA(cudaStreamWaitEvent(t->side, t->ev_fork, 0));
     const tg_status ra = fp64 ? build_arena(t, t->arena64, t->side) : build_arena(t, t->arena32, t->side);
