@@ -72,7 +72,11 @@ const char *tg_last_error(void);
 /* ConstructTree(pos, m, softening, quadrupole, compute_moments) on the radix path
  * (frontend.py:73-142 -> octree.py:664-723, 817-1091, 199-292).
  * m == NULL: zero masses and compute_moments forced off (frontend.py:115-117).
- * h == NULL: zero softenings. Synchronises `stream` (the node count is data dependent). */
+ * h == NULL: zero softenings. Synchronises `stream` once (the node count is data dependent), before
+ * the moment pass, and returns with that pass (node masses, centres of mass, Deltas, softenings,
+ * quadrupoles) still running on `stream`. Every entry point taking the tree orders its own stream
+ * after it; a caller reading the device arrays of tg_tree_info directly does so on `stream`, or after
+ * synchronising it. */
 tg_status tg_tree_build(const double *pos, const double *m, const double *h, int64_t n,
                         int quadrupole, int compute_moments, int mem, void *stream, tg_tree *out);
 
@@ -83,6 +87,8 @@ tg_status tg_tree_build_batched(const double *pos, const double *m, const double
                                 const int64_t *offsets, int32_t n_systems, int quadrupole,
                                 int mem, void *stream, tg_tree *out);
 
+/* Sizes and flags of a tree, and its device arrays (complete once the build's stream has passed the
+ * build; see tg_tree_build). */
 tg_status tg_tree_info_get(tg_tree tree, tg_tree_info *info);
 
 /* Copy the Octree arrays to host buffers sized for info.num_nodes rows (rows past node_hi are

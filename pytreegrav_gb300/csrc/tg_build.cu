@@ -1635,8 +1635,45 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     dfree(p_parent, st); dfree(p_next, st); dfree(nkeys, st); dfree(nvals, st); dfree(root_slot, st);
     dfree(final_of_slot, st); dfree(nonroot, st); dfree(keys, st); dfree(perm, st);
 
-    // 8. moments: nodes deeper than DEPTH_CAP by climbing, then one launch per depth, deepest first
-    // (the moment kernels bound every link they follow, so they may run before the link check is read)
+    // 8. the one closing synchronisation, ahead of the moment pass (nothing the host needs comes from
+    // it): link check, per-system node offsets, bucket reservations. The moment pass is then enqueued
+    // and the build returns while it runs; ev_topo marks the topology and geometry final, ev_built
+    // the end of the moment pass.
+    if (!T->ev_topo) {
+        TG_CUDA(cudaEventCreateWithFlags(&T->ev_topo, cudaEventDisableTiming));
+        TG_CUDA(cudaEventCreateWithFlags(&T->ev_built, cudaEventDisableTiming));
+    }
+    TG_CUDA(cudaEventRecord(T->ev_topo, st));
+    int links_bad = 0, sort_bad = 0;
+    std::vector<unsigned long long> rq(nsys, 0);
+    TG_TRY(sort_error_take(&sum->sort_error, st));
+    TG_CUDA(cudaMemcpyAsync(&sort_bad, &sum->sort_error, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TG_CUDA(cudaMemcpyAsync(&links_bad, &sum->bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (nsys > 1)
+        TG_CUDA(cudaMemcpyAsync(T->sys_node_off.data(), sys_node_off, sizeof(int64_t) * (nsys + 1),
+                                cudaMemcpyDeviceToHost, st));
+    if (req) TG_CUDA(cudaMemcpyAsync(rq.data(), req, sizeof(unsigned long long) * nsys, cudaMemcpyDeviceToHost, st));
+    dfree(req, st); dfree(sum, st); dfree(sys_node_off, st);
+    dfree(sys_off, st); dfree(mn, st); dfree(mx, st); dfree(center, st); dfree(size, st);
+    TG_CUDA(cudaStreamSynchronize(st));
+    if (nonfinite_seen || sort_bad || links_bad) {
+        dfree(lvl, st); dfree(lvl_list, st); dfree(fdepth, st);
+        if (nonfinite_seen) return TG_ERR_NONFINITE;
+        if (sort_bad) {
+            set_last_error_msg("radix sort: a tile's look-back did not complete within its bound");
+            return TG_ERR_QUEUE_TIMEOUT;
+        }
+        set_last_error_msg("internal error: octree links out of range");
+        return TG_ERR_CUDA;
+    }
+    T->sys_capacity.resize(nsys);
+    for (int s = 0; s < nsys; s++) {
+        int64_t np = sys_off_host[s + 1] - sys_off_host[s];
+        int64_t node_hi = np + (T->sys_node_off[s + 1] - T->sys_node_off[s]);
+        T->sys_capacity[s] = reference_capacity(np, std::max<int64_t>(node_hi, (int64_t)rq[s]));
+    }
+    // 9. moments: nodes deeper than DEPTH_CAP by climbing, then one launch per depth, deepest first
+    // (the moment kernels bound every link they follow)
     MomentArgs a;
     a.ntot = N;
     a.mtot = M;
@@ -1696,35 +1733,8 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
         TG_CUDA(cudaGetLastError());
     }
 
-    // 9. the one closing synchronisation: link check, per-system node offsets, bucket reservations
-    int links_bad = 0, sort_bad = 0;
-    std::vector<unsigned long long> rq(nsys, 0);
-    TG_TRY(sort_error_take(&sum->sort_error, st));
-    TG_CUDA(cudaMemcpyAsync(&sort_bad, &sum->sort_error, sizeof(int), cudaMemcpyDeviceToHost, st));
-    TG_CUDA(cudaMemcpyAsync(&links_bad, &sum->bad, sizeof(int), cudaMemcpyDeviceToHost, st));
-    if (nsys > 1)
-        TG_CUDA(cudaMemcpyAsync(T->sys_node_off.data(), sys_node_off, sizeof(int64_t) * (nsys + 1),
-                                cudaMemcpyDeviceToHost, st));
-    if (req) TG_CUDA(cudaMemcpyAsync(rq.data(), req, sizeof(unsigned long long) * nsys, cudaMemcpyDeviceToHost, st));
-    dfree(req, st); dfree(sum, st); dfree(sys_node_off, st);
     dfree(lvl, st); dfree(lvl_list, st); dfree(fdepth, st);
-    dfree(sys_off, st); dfree(mn, st); dfree(mx, st); dfree(center, st); dfree(size, st);
-    TG_CUDA(cudaStreamSynchronize(st));
-    if (nonfinite_seen) return TG_ERR_NONFINITE;
-    if (sort_bad) {
-        set_last_error_msg("radix sort: a tile's look-back did not complete within its bound");
-        return TG_ERR_QUEUE_TIMEOUT;
-    }
-    if (links_bad) {
-        set_last_error_msg("internal error: octree links out of range");
-        return TG_ERR_CUDA;
-    }
-    T->sys_capacity.resize(nsys);
-    for (int s = 0; s < nsys; s++) {
-        int64_t np = sys_off_host[s + 1] - sys_off_host[s];
-        int64_t node_hi = np + (T->sys_node_off[s + 1] - T->sys_node_off[s]);
-        T->sys_capacity[s] = reference_capacity(np, std::max<int64_t>(node_hi, (int64_t)rq[s]));
-    }
+    TG_CUDA(cudaEventRecord(T->ev_built, st));
     return TG_OK;
 }
 

@@ -119,6 +119,8 @@ void destroy(tg_tree_s *t) {
     if (t->side) cudaStreamDestroy(t->side);  // released once its work is done
     if (t->ev_fork) cudaEventDestroy(t->ev_fork);
     if (t->ev_join) cudaEventDestroy(t->ev_join);
+    if (t->ev_topo) cudaEventDestroy(t->ev_topo);
+    if (t->ev_built) cudaEventDestroy(t->ev_built);
     delete t;
 }
 
@@ -241,6 +243,7 @@ tg_status tg_tree_copy_out(tg_tree t, double *coord, double *mass, double *size,
                            double *quad, int64_t *first, int64_t *next, int64_t *walk_idx, void *stream) {
     if (!t) return TG_ERR_BAD_ARG;
     cudaStream_t st = (cudaStream_t)stream;
+    tree_wait_built(t, st);
     const int64_t NE = t->ntot + t->mtot;
     const int64_t cap = t->nsys == 1 ? t->sys_capacity[0] : NE;
     const int64_t pad = cap - NE;
@@ -299,6 +302,7 @@ tg_status tg_tree_fields(tg_tree t, const double *pos, const double *h, int64_t 
     if (precision != TG_FP32 && precision != TG_FP64) return TG_ERR_BAD_ARG;
     if (quadrupole && !t->quad) return TG_ERR_NO_QUADRUPOLES;
     cudaStream_t st = (cudaStream_t)stream;
+    tree_wait_built(t, st);
     const int W = field_width(fields);
     int2 *groups = nullptr;
     int *groot = nullptr, *gorder = nullptr;

@@ -338,6 +338,7 @@ tg_status tg_tree_column_density(tg_tree t, const double *pos, int64_t n, const 
     }
     if (n == 0) return TG_OK;
     cudaStream_t st = (cudaStream_t)stream;
+    tree_wait_built(t, st);
     ColumnTree ct;
     ct.coord = t->coord; ct.mass = t->mass; ct.soft = t->soft; ct.size = t->size; ct.delta = t->delta;
     ct.first = t->first; ct.next = t->next;

@@ -571,6 +571,7 @@ extern "C" {
 
 tg_status tg_tree_groups(tg_tree t, int group_size, int64_t *ngroups, void *stream) {
     if (!t || !ngroups || !valid_gs(group_size)) return TG_ERR_BAD_ARG;
+    tree_wait_built(t, (cudaStream_t)stream);
     TG_TRY(tree_groups(t, group_size, (cudaStream_t)stream));
     *ngroups = t->ngroups;
     return TG_OK;
@@ -580,6 +581,7 @@ tg_status tg_tree_groups_copy(tg_tree t, int group_size, int32_t *first, int32_t
                               void *stream) {
     if (!t || !valid_gs(group_size)) return TG_ERR_BAD_ARG;
     cudaStream_t st = (cudaStream_t)stream;
+    tree_wait_built(t, st);
     TG_TRY(tree_groups(t, group_size, st));
     const int64_t ng = t->ngroups;
     if (ng == 0) return TG_OK;
@@ -634,6 +636,7 @@ tg_status tg_tree_last_group_stats(tg_tree t, uint32_t *out, int mem, void *stre
 
 tg_status tg_theta_features(tg_tree t, int group_size, int quadrupole, float *features, void *stream) {
     if (!t || !features || !valid_gs(group_size)) return TG_ERR_BAD_ARG;
+    tree_wait_built(t, (cudaStream_t)stream);
     return features_device(t, group_size, quadrupole, features, (cudaStream_t)stream);
 }
 
@@ -771,6 +774,7 @@ tg_status tg_theta_infer(tg_theta_model m, const float *features, int64_t n, flo
 tg_status tg_theta_tolerances(tg_tree t, int group_size, int quadrupole, const float *u, float *tol, void *stream) {
     if (!t || !u || !tol || !valid_gs(group_size)) return TG_ERR_BAD_ARG;
     cudaStream_t st = (cudaStream_t)stream;
+    tree_wait_built(t, st);
     TG_TRY(tree_groups(t, group_size, st));
     float *feat = nullptr;
     const int64_t nfeat = NF * std::max<int64_t>(t->ngroups, 1);
@@ -789,6 +793,7 @@ tg_status tg_tree_fields_grouped(tg_tree t, int fields, int quadrupole, double G
         return TG_ERR_BAD_ARG;
     if (quadrupole && !t->quad) return TG_ERR_NO_QUADRUPOLES;
     cudaStream_t st = (cudaStream_t)stream;
+    tree_wait_built(t, st);
     TG_TRY(tree_groups(t, group_size, st));
     const int64_t nt = t->ntot;
     const int W = field_width_of(fields);
@@ -810,6 +815,7 @@ tg_status tg_tree_fields_learned(tg_tree t, int fields, int quadrupole, double G
         return TG_ERR_BAD_ARG;
     if (quadrupole && !t->quad) return TG_ERR_NO_QUADRUPOLES;
     cudaStream_t st = (cudaStream_t)stream;
+    tree_wait_built(t, st);
     TG_TRY(tree_groups_with_arena(t, group_size, false, st));
     const int64_t ng = t->ngroups, nt = t->ntot;
     float *tg_theta = nullptr, *feat = nullptr, *tol = nullptr;

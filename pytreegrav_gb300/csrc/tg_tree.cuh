@@ -104,4 +104,17 @@ struct tg_tree_s {
     // grouping runs on the caller's stream, and the two events that order it.
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // Recorded on the build's stream: ev_topo once the topology and geometry (links, ranges, cells,
+    // particle data) are final, before the moment pass; ev_built after it. A build returns once the
+    // host-visible results are known, with the moment pass still running on its stream: every entry
+    // point orders its own stream after ev_built, and tree grouping, which needs no moments, starts
+    // from ev_topo on the side stream.
+    cudaEvent_t ev_topo = nullptr, ev_built = nullptr;
 };
+
+namespace tg {
+// Orders work on s after the tree's build (a no-op when s is the build's stream).
+inline void tree_wait_built(const tg_tree_s *t, cudaStream_t s) {
+    if (t && t->ev_built) cudaStreamWaitEvent(s, t->ev_built, 0);
+}
+}  // namespace tg

@@ -1533,9 +1533,6 @@ tg_status tree_groups(tg_tree_s *t, int G, cudaStream_t st) {
     return TG_OK;
 }
 
-// Tree groups at size G and the walk arena of the given precision. An arena not yet built is packed
-// on the tree's side stream while the grouping (which reads its group count back to the host) runs
-// on st; st waits for the arena before this returns, also on error.
 // The tree's side stream and its two events, made on first use.
 tg_status tree_side_stream(tg_tree_s *t) {
     if (!t->side) {
@@ -1546,23 +1543,32 @@ tg_status tree_side_stream(tg_tree_s *t) {
     return TG_OK;
 }
 
+// Tree groups at size G and the walk arena of the given precision. Grouping reads only the topology
+// and the geometry, so a first grouping runs on the tree's side stream from the build's ev_topo, in
+// parallel with the moment pass still running on the build's stream (and its one host read-back of
+// the group count waits for the grouping alone). The arena needs the moments and is packed on st.
+// st waits for the grouping before this returns, also on error.
 tg_status tree_groups_with_arena(tg_tree_s *t, int G, bool fp64, cudaStream_t st) {
-    const bool need = fp64 ? !t->arena64.built : !t->arena32.built;
-    if (!need) return tree_groups(t, G, st);
-    TG_TRY(tree_side_stream(t));
-    TG_CUDA(cudaEventRecord(t->ev_fork, st));
-    TG_CUDA(cudaStreamWaitEvent(t->side, t->ev_fork, 0));
-    const tg_status ra = fp64 ? build_arena(t, t->arena64, t->side) : build_arena(t, t->arena32, t->side);
-    const cudaError_t ej = cudaEventRecord(t->ev_join, t->side);
-    const tg_status rg = tree_groups(t, G, st);
-    if (ej == cudaSuccess) TG_CUDA(cudaStreamWaitEvent(st, t->ev_join, 0));
-    else {  // the join could not be recorded: wait for the side stream from the host
-        cudaStreamSynchronize(t->side);
-        set_last_error_msg("could not record the walk arena's completion event");
-        return TG_ERR_CUDA;
+    const bool need_arena = fp64 ? !t->arena64.built : !t->arena32.built;
+    const bool need_groups = !(t->groups && t->groups_G == G);
+    tg_status rg = TG_OK;
+    if (need_groups && !t->groups && t->ev_topo) {  // a first grouping: off the build's critical path
+        TG_TRY(tree_side_stream(t));
+        TG_CUDA(cudaStreamWaitEvent(t->side, t->ev_topo, 0));
+        rg = tree_groups(t, G, t->side);
+        const cudaError_t ej = cudaEventRecord(t->ev_join, t->side);
+        if (ej != cudaSuccess) {  // the join could not be recorded: wait for the side stream from the host
+            cudaStreamSynchronize(t->side);
+            set_last_error_msg("could not record the tree grouping's completion event");
+            return TG_ERR_CUDA;
+        }
+        TG_CUDA(cudaStreamWaitEvent(st, t->ev_join, 0));
+    } else if (need_groups) {
+        rg = tree_groups(t, G, st);
     }
-    TG_TRY(ra);
-    return rg;
+    TG_TRY(rg);
+    if (need_arena) TG_TRY(fp64 ? build_arena(t, t->arena64, st) : build_arena(t, t->arena32, st));
+    return TG_OK;
 }
 
 // Largest-first queue order of consecutive-block groups (see k_group_cost_keys).
@@ -1662,6 +1668,7 @@ tg_status tg_walk_graph_create(tg_tree t, int fields, int quadrupole, double the
         return r;
     };
     if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return fail(TG_ERR_CUDA);
+    tree_wait_built(t, cs);
     const int2 *wg;
     const int *wr;
     int64_t ng;
