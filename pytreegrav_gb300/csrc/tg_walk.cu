@@ -153,10 +153,13 @@ __global__ void k_arena_links(int64_t ntot, int64_t mtot, const int64_t *first, 
     nleaf[j] = nl;
 }
 
+// Leaf ranges: each node's particle children, in chain order, copied to its range of the leaf
+// arrays; the range start also goes into the node's link. Reads particle data only, which is final
+// before the moment pass.
 template <typename T>
-__global__ void k_arena_fill(int64_t ntot, int64_t mtot, const int64_t *first, const int64_t *next,
-                             const double *coord, const double *mass, const double *soft, const double *size,
-                             const double *delta, const double *quad, const int64_t *leaf_start, Arena<T> ar) {
+__global__ void k_arena_leaves(int64_t ntot, int64_t mtot, const int64_t *first, const int64_t *next,
+                               const double *coord, const double *mass, const double *soft,
+                               const int64_t *leaf_start, Arena<T> ar) {
     int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= mtot) return;
     int64_t f = ntot + j, stop = next[f];
@@ -164,27 +167,13 @@ __global__ void k_arena_fill(int64_t ntot, int64_t mtot, const int64_t *first, c
     int4 lk = ar.n_link[j];
     lk.z = (int)ls;
     ar.n_link[j] = lk;
-    T hx, hy, hz, lx, ly, lz;
-    split_hi_lo(coord[3 * f], hx, lx);
-    split_hi_lo(coord[3 * f + 1], hy, ly);
-    split_hi_lo(coord[3 * f + 2], hz, lz);
-    T hm = narrow(soft[f], T(0));
-    ar.n_pos[j] = vec4<T>{hx, hy, hz, narrow(mass[f], T(0))};
-    ar.n_lo[j] = vec4<T>{lx, ly, lz, hm};
-    const int fc = lk.y > 0 ? lk.x : 0;
-    ar.n_trav[2 * j] = vec4<T>{hx, hy, hz, narrow(size[f], T(0))};
-    ar.n_trav[2 * j + 1] = vec4<T>{narrow(delta[f], T(0)), hm, int_bits((fc << 4) | lk.y, T(0)), int_bits(((int)ls << 4) | lk.w, T(0))};
-    if (ar.n_quad) {
-        const double *Q = quad + 9 * j;
-        ar.n_quad[2 * j] = vec4<T>{narrow(Q[0], T(0)), narrow(Q[1], T(0)), narrow(Q[2], T(0)), narrow(Q[4], T(0))};
-        ar.n_quad[2 * j + 1] = vec4<T>{narrow(Q[5], T(0)), narrow(Q[8], T(0)), T(0), T(0)};
-    }
     if (ls < 0 || ls + lk.w > ar.n_leaves) {  // leaf ranges from invalid links: nothing written
         atomicOr(ar.bad, 16);
         return;
     }
     int64_t k = ls;
     const int64_t kend = ls + lk.w;
+    T hx, hy, hz, lx, ly, lz;
     for (int64_t c = first[f]; c != stop && c >= 0 && k < kend; c = next[c]) {
         if (c < ntot) {
             split_hi_lo(coord[3 * c], hx, lx);
@@ -197,14 +186,42 @@ __global__ void k_arena_fill(int64_t ntot, int64_t mtot, const int64_t *first, c
     }
 }
 
+// Node records (centre of mass, mass, h_max, size, Delta, links, quadrupole): after the moment pass.
+template <typename T>
+__global__ void k_arena_nodes(int64_t ntot, int64_t mtot, const double *coord, const double *mass,
+                              const double *soft, const double *size, const double *delta, const double *quad,
+                              Arena<T> ar) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= mtot) return;
+    const int64_t f = ntot + j;
+    const int4 lk = ar.n_link[j];
+    T hx, hy, hz, lx, ly, lz;
+    split_hi_lo(coord[3 * f], hx, lx);
+    split_hi_lo(coord[3 * f + 1], hy, ly);
+    split_hi_lo(coord[3 * f + 2], hz, lz);
+    T hm = narrow(soft[f], T(0));
+    ar.n_pos[j] = vec4<T>{hx, hy, hz, narrow(mass[f], T(0))};
+    ar.n_lo[j] = vec4<T>{lx, ly, lz, hm};
+    const int fc = lk.y > 0 ? lk.x : 0;
+    ar.n_trav[2 * j] = vec4<T>{hx, hy, hz, narrow(size[f], T(0))};
+    ar.n_trav[2 * j + 1] = vec4<T>{narrow(delta[f], T(0)), hm, int_bits((fc << 4) | lk.y, T(0)),
+                                   int_bits((lk.z << 4) | lk.w, T(0))};
+    if (ar.n_quad) {
+        const double *Q = quad + 9 * j;
+        ar.n_quad[2 * j] = vec4<T>{narrow(Q[0], T(0)), narrow(Q[1], T(0)), narrow(Q[2], T(0)), narrow(Q[4], T(0))};
+        ar.n_quad[2 * j + 1] = vec4<T>{narrow(Q[5], T(0)), narrow(Q[8], T(0)), T(0), T(0)};
+    }
+}
+
 // Every particle must be exactly one node's leaf.
 __global__ void k_arena_total(const int64_t *ltot, int64_t ntot, int *bad) {
     if (threadIdx.x == 0 && *ltot != ntot) atomicOr(bad, 8);
 }
 
+// The arena's topology part: allocation, node links, leaf ranges (validated on the device, see
+// k_arena_total) and the leaf records. Needs no moments.
 template <typename T>
-tg_status build_arena(tg_tree_s *t, Arena<T> &ar, cudaStream_t st) {
-    if (ar.built) return TG_OK;
+tg_status build_arena_topology(tg_tree_s *t, Arena<T> &ar, cudaStream_t st) {
     const int64_t M = t->mtot, N = t->ntot;
     ar.n_nodes = M;
     ar.n_leaves = N;
@@ -232,13 +249,30 @@ tg_status build_arena(tg_tree_s *t, Arena<T> &ar, cudaStream_t st) {
     TG_TRY(exclusive_scan_i64(nleaf, lstart, M, ltot, st));
     { k_arena_total<<<1, 32, 0, st>>>(ltot, N, ar.bad); tg::note_launch(); }
     TG_CUDA(cudaFreeAsync(ltot, st));
-    { k_arena_fill<T><<<div_up(M, 256), 256, 0, st>>>(N, M, t->first, t->next, t->coord, t->mass, t->soft, t->size,
-                                                     t->delta, t->quad, lstart, ar); tg::note_launch(); }
+    { k_arena_leaves<T><<<div_up(M, 256), 256, 0, st>>>(N, M, t->first, t->next, t->coord, t->mass, t->soft, lstart,
+                                                       ar); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
     TG_CUDA(cudaFreeAsync(nleaf, st));
     TG_CUDA(cudaFreeAsync(lstart, st));
+    return TG_OK;
+}
+
+// The node records, after the moment pass; completes the arena.
+template <typename T>
+tg_status build_arena_nodes(tg_tree_s *t, Arena<T> &ar, cudaStream_t st) {
+    const int64_t M = t->mtot, N = t->ntot;
+    { k_arena_nodes<T><<<div_up(M, 256), 256, 0, st>>>(N, M, t->coord, t->mass, t->soft, t->size, t->delta, t->quad,
+                                                      ar); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
     ar.built = true;
     return TG_OK;
+}
+
+template <typename T>
+tg_status build_arena(tg_tree_s *t, Arena<T> &ar, cudaStream_t st) {
+    if (ar.built) return TG_OK;
+    TG_TRY(build_arena_topology(t, ar, st));
+    return build_arena_nodes(t, ar, st);
 }
 
 template <typename T>
@@ -1543,19 +1577,21 @@ tg_status tree_side_stream(tg_tree_s *t) {
     return TG_OK;
 }
 
-// Tree groups at size G and the walk arena of the given precision. Grouping reads only the topology
-// and the geometry, so a first grouping runs on the tree's side stream from the build's ev_topo, in
-// parallel with the moment pass still running on the build's stream (and its one host read-back of
-// the group count waits for the grouping alone). The arena needs the moments and is packed on st.
-// st waits for the grouping before this returns, also on error.
+// Tree groups at size G and the walk arena of the given precision. Grouping and the arena's topology
+// part (links, leaf ranges, leaf records) read only the tree's topology and particle data, so for a
+// first grouping they run on the tree's side stream from the build's ev_topo, in parallel with the
+// moment pass still running on the build's stream (and the grouping's one host read-back of its
+// group count waits for the side stream alone). The arena's node records need the moments: st.
+// st waits for the side stream before this returns, also on error.
 tg_status tree_groups_with_arena(tg_tree_s *t, int G, bool fp64, cudaStream_t st) {
     const bool need_arena = fp64 ? !t->arena64.built : !t->arena32.built;
     const bool need_groups = !(t->groups && t->groups_G == G);
-    tg_status rg = TG_OK;
     if (need_groups && !t->groups && t->ev_topo) {  // a first grouping: off the build's critical path
         TG_TRY(tree_side_stream(t));
         TG_CUDA(cudaStreamWaitEvent(t->side, t->ev_topo, 0));
-        rg = tree_groups(t, G, t->side);
+        tg_status r = tree_groups(t, G, t->side);
+        const bool topo = r == TG_OK && need_arena;
+        if (topo) r = fp64 ? build_arena_topology(t, t->arena64, t->side) : build_arena_topology(t, t->arena32, t->side);
         const cudaError_t ej = cudaEventRecord(t->ev_join, t->side);
         if (ej != cudaSuccess) {  // the join could not be recorded: wait for the side stream from the host
             cudaStreamSynchronize(t->side);
@@ -1563,10 +1599,11 @@ tg_status tree_groups_with_arena(tg_tree_s *t, int G, bool fp64, cudaStream_t st
             return TG_ERR_CUDA;
         }
         TG_CUDA(cudaStreamWaitEvent(st, t->ev_join, 0));
-    } else if (need_groups) {
-        rg = tree_groups(t, G, st);
+        TG_TRY(r);
+        if (topo) TG_TRY(fp64 ? build_arena_nodes(t, t->arena64, st) : build_arena_nodes(t, t->arena32, st));
+        return TG_OK;
     }
-    TG_TRY(rg);
+    if (need_groups) TG_TRY(tree_groups(t, G, st));
     if (need_arena) TG_TRY(fp64 ? build_arena(t, t->arena64, st) : build_arena(t, t->arena32, st));
     return TG_OK;
 }
