@@ -108,6 +108,11 @@ __device__ __forceinline__ f2 f2_mul(f2 a, f2 b) {
     asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
     return d;
 }
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b) {
+    f2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
 __device__ __forceinline__ f2 f2_sub(f2 a, f2 b) {
     f2 d;
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
@@ -645,10 +650,12 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
                     st = vec4<T>{sx, sy, sz, p.w};
                 }
             }
-            // acceleration with groups of 2 or more targets: sources staged as pairs [x x y y] [z z m m]
-            // for the paired sweep; otherwise one 16-byte word per source
+            // potential and/or acceleration with groups of 2 or more targets: sources staged as pairs
+            // [x x y y] [z z m m] for the paired sweep; otherwise one 16-byte word per source. (The
+            // monopole walk of both fields together measured 2% slower paired: it stays unpaired.)
             bool paired = false;
-            if constexpr (sizeof(T) == 4 && FIELDS == F_ACC) paired = GS >= 2;
+            if constexpr (sizeof(T) == 4 && (FIELDS & F_TID) == 0 && (QUAD || FIELDS != (F_POT | F_ACC)))
+                paired = GS >= 2;
             if (paired) {
                 float *o = reinterpret_cast<float *>(sm.spos) + 8 * (lane >> 1) + (lane & 1);
                 o[0] = (float)st.x;
@@ -667,25 +674,36 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
             if (paired) {
                 const f2 TX = f2_pack((float)tx, (float)tx), TY = f2_pack((float)ty, (float)ty);
                 const f2 TZ = f2_pack((float)tz, (float)tz);
-                f2 ax = 0, ay = 0, az = 0;  // even and odd sources summed apart (bit pattern 0 is +0.0f)
+                // even and odd sources summed apart (bit pattern 0 is +0.0f); ph sums m/r
+                f2 ax = 0, ay = 0, az = 0, ph = 0;
                 const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(sm.spos) + 2 * ((slice * GS) >> 1);
 #pragma unroll 4
                 for (int i = 0; i < (GS >> 1); i++) {
                     const ulonglong2 w0 = src[2 * i], w1 = src[2 * i + 1];
                     const f2 dx = f2_sub(w0.x, TX), dy = f2_sub(w0.y, TY), dz = f2_sub(w1.x, TZ);
                     const f2 rinv = f2_rsqrt(f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx))));
-                    const f2 mr3 = f2_mul(f2_mul(w1.y, rinv), f2_mul(rinv, rinv));
-                    ax = f2_fma(mr3, dx, ax);
-                    ay = f2_fma(mr3, dy, ay);
-                    az = f2_fma(mr3, dz, az);
+                    const f2 mr = f2_mul(w1.y, rinv);
+                    if constexpr ((FIELDS & F_POT) != 0) ph = f2_add(ph, mr);
+                    if constexpr ((FIELDS & F_ACC) != 0) {
+                        const f2 mr3 = f2_mul(mr, f2_mul(rinv, rinv));
+                        ax = f2_fma(mr3, dx, ax);
+                        ay = f2_fma(mr3, dy, ay);
+                        az = f2_fma(mr3, dz, az);
+                    }
                 }
                 float h0, h1;
-                f2_unpack(ax, h0, h1);
-                b.v[1] = (T)(h0 + h1);
-                f2_unpack(ay, h0, h1);
-                b.v[2] = (T)(h0 + h1);
-                f2_unpack(az, h0, h1);
-                b.v[3] = (T)(h0 + h1);
+                if constexpr ((FIELDS & F_POT) != 0) {
+                    f2_unpack(ph, h0, h1);
+                    b.v[0] = -(T)(h0 + h1);
+                }
+                if constexpr ((FIELDS & F_ACC) != 0) {
+                    f2_unpack(ax, h0, h1);
+                    b.v[1] = (T)(h0 + h1);
+                    f2_unpack(ay, h0, h1);
+                    b.v[2] = (T)(h0 + h1);
+                    f2_unpack(az, h0, h1);
+                    b.v[3] = (T)(h0 + h1);
+                }
             } else if (GS == 32) {
 #pragma unroll 16
                 for (int i = 0; i < 32; i++) {
@@ -737,8 +755,9 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
             }
             __syncwarp();
             const f2 TX = f2_pack(tx, tx), TY = f2_pack(ty, ty), TZ = f2_pack(tz, tz);
-            const f2 C25 = f2_pack(-2.5f, -2.5f);
-            f2 ax = 0, ay = 0, az = 0;  // two partial sums each (bit pattern 0 is +0.0f, +0.0f)
+            const f2 C25 = f2_pack(-2.5f, -2.5f), CH = f2_pack(-0.5f, -0.5f);
+            // two partial sums each (bit pattern 0 is +0.0f, +0.0f); ph sums m/r + A/(2 r^5) = -phi
+            f2 ax = 0, ay = 0, az = 0, ph = 0;
             const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(buf) + 5 * ((slice * GS) >> 1);
 #pragma unroll 4
             for (int i = 0; i < (GS >> 1); i++) {
@@ -754,28 +773,38 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
                 const f2 ny = f2_fma(w4.x, dz, f2_fma(w3.y, dy, f2_mul(w2.y, dx)));
                 const f2 nz = f2_fma(w4.y, dz, f2_fma(w4.x, dy, f2_mul(w3.x, dx)));
                 const f2 A = f2_fma(dz, nz, f2_fma(dy, ny, f2_mul(dx, nx)));
-                const f2 t = f2_fma(f2_mul(A, C25), u, f2_mul(w1.y, r2));
-                ax = f2_fma(r5, f2_fma(t, dx, nx), ax);
-                ay = f2_fma(r5, f2_fma(t, dy, ny), ay);
-                az = f2_fma(r5, f2_fma(t, dz, nz), az);
+                // potential: m/r - (-A)/(2 r^5) summed, negated at the end (-m/r - A/(2 r^5))
+                if constexpr ((FIELDS & F_POT) != 0) ph = f2_fma(f2_mul(A, CH), r5, f2_fma(w1.y, rinv, ph));
+                if constexpr ((FIELDS & F_ACC) != 0) {
+                    const f2 t = f2_fma(f2_mul(A, C25), u, f2_mul(w1.y, r2));
+                    ax = f2_fma(r5, f2_fma(t, dx, nx), ax);
+                    ay = f2_fma(r5, f2_fma(t, dy, ny), ay);
+                    az = f2_fma(r5, f2_fma(t, dz, nz), az);
+                }
             }
             __syncwarp();
             Acc<T> b;
 #pragma unroll
             for (int c = 0; c < 10; c++) b.v[c] = T(0);
             float h0, h1;
-            f2_unpack(ax, h0, h1);
-            b.v[1] = h0 + h1;
-            f2_unpack(ay, h0, h1);
-            b.v[2] = h0 + h1;
-            f2_unpack(az, h0, h1);
-            b.v[3] = h0 + h1;
+            if constexpr ((FIELDS & F_POT) != 0) {
+                f2_unpack(ph, h0, h1);
+                b.v[0] = -(h0 + h1);
+            }
+            if constexpr ((FIELDS & F_ACC) != 0) {
+                f2_unpack(ax, h0, h1);
+                b.v[1] = h0 + h1;
+                f2_unpack(ay, h0, h1);
+                b.v[2] = h0 + h1;
+                f2_unpack(az, h0, h1);
+                b.v[3] = h0 + h1;
+            }
             kahan_add<T, FIELDS>(S, C, b);
             n_int += (unsigned long long)cnt * (unsigned long long)gr.y;
             n_qint += (unsigned long long)cnt * (unsigned long long)gr.y;
         };
         auto eval_nodes = [&](const int *list, int cnt) {
-            if constexpr (sizeof(T) == 4 && FIELDS == F_ACC) {
+            if constexpr (sizeof(T) == 4 && (FIELDS & F_TID) == 0) {
                 if (GS >= 2) {
                     eval_nodes_paired(list, cnt);
                     return;
