@@ -652,9 +652,11 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
             }
             // potential and/or acceleration with groups of 2 or more targets: sources staged as pairs
             // [x x y y] [z z m m] for the paired sweep; otherwise one 16-byte word per source. (The
-            // monopole walk of both fields together measured 2% slower paired: it stays unpaired.)
+            // monopole walk of both fields together measured 2% slower paired: it stays unpaired.) The
+            // tidal tensor alone is paired as well.
             bool paired = false;
-            if constexpr (sizeof(T) == 4 && (FIELDS & F_TID) == 0 && (QUAD || FIELDS != (F_POT | F_ACC)))
+            if constexpr (sizeof(T) == 4 && (FIELDS == F_TID || ((FIELDS & F_TID) == 0 &&
+                                                                  (QUAD || FIELDS != (F_POT | F_ACC)))))
                 paired = GS >= 2;
             if (paired) {
                 float *o = reinterpret_cast<float *>(sm.spos) + 8 * (lane >> 1) + (lane & 1);
@@ -674,8 +676,10 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
             if (paired) {
                 const f2 TX = f2_pack((float)tx, (float)tx), TY = f2_pack((float)ty, (float)ty);
                 const f2 TZ = f2_pack((float)tz, (float)tz);
-                // even and odd sources summed apart (bit pattern 0 is +0.0f); ph sums m/r
-                f2 ax = 0, ay = 0, az = 0, ph = 0;
+                // even and odd sources summed apart (bit pattern 0 is +0.0f); ph sums m/r; t0..t5 the
+                // tidal tensor's xx xy xz yy yz zz
+                f2 ax = 0, ay = 0, az = 0, ph = 0, t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, t5 = 0;
+                const f2 C3 = f2_pack(3.f, 3.f);
                 const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(sm.spos) + 2 * ((slice * GS) >> 1);
 #pragma unroll 4
                 for (int i = 0; i < (GS >> 1); i++) {
@@ -690,11 +694,31 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
                         ay = f2_fma(mr3, dy, ay);
                         az = f2_fma(mr3, dz, az);
                     }
+                    if constexpr ((FIELDS & F_TID) != 0) {  // T_ab += 3 m r^-5 d_a d_b - delta_ab m r^-3
+                        const f2 u = f2_mul(rinv, rinv);
+                        const f2 mr3 = f2_mul(mr, u);
+                        const f2 q3 = f2_mul(f2_mul(mr3, C3), u);
+                        const f2 qx = f2_mul(q3, dx), qy = f2_mul(q3, dy);
+                        t0 = f2_sub(f2_fma(qx, dx, t0), mr3);
+                        t1 = f2_fma(qx, dy, t1);
+                        t2 = f2_fma(qx, dz, t2);
+                        t3 = f2_sub(f2_fma(qy, dy, t3), mr3);
+                        t4 = f2_fma(qy, dz, t4);
+                        t5 = f2_sub(f2_fma(f2_mul(q3, dz), dz, t5), mr3);
+                    }
                 }
                 float h0, h1;
                 if constexpr ((FIELDS & F_POT) != 0) {
                     f2_unpack(ph, h0, h1);
                     b.v[0] = -(T)(h0 + h1);
+                }
+                if constexpr ((FIELDS & F_TID) != 0) {
+                    const f2 tt[6] = {t0, t1, t2, t3, t4, t5};
+#pragma unroll
+                    for (int c = 0; c < 6; c++) {
+                        f2_unpack(tt[c], h0, h1);
+                        b.v[4 + c] = (T)(h0 + h1);
+                    }
                 }
                 if constexpr ((FIELDS & F_ACC) != 0) {
                     f2_unpack(ax, h0, h1);
@@ -756,8 +780,9 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
             __syncwarp();
             const f2 TX = f2_pack(tx, tx), TY = f2_pack(ty, ty), TZ = f2_pack(tz, tz);
             const f2 C25 = f2_pack(-2.5f, -2.5f), CH = f2_pack(-0.5f, -0.5f);
-            // two partial sums each (bit pattern 0 is +0.0f, +0.0f); ph sums m/r + A/(2 r^5) = -phi
-            f2 ax = 0, ay = 0, az = 0, ph = 0;
+            // two partial sums each (bit pattern 0 is +0.0f, +0.0f); ph sums m/r + A/(2 r^5) = -phi;
+            // t0..t5 the tidal tensor's xx xy xz yy yz zz
+            f2 ax = 0, ay = 0, az = 0, ph = 0, t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, t5 = 0;
             const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(buf) + 5 * ((slice * GS) >> 1);
 #pragma unroll 4
             for (int i = 0; i < (GS >> 1); i++) {
@@ -781,6 +806,24 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
                     ay = f2_fma(r5, f2_fma(t, dy, ny), ay);
                     az = f2_fma(r5, f2_fma(t, dz, nz), az);
                 }
+                if constexpr ((FIELDS & F_TID) != 0) {
+                    // monopole + quadrupole, with n = -Q dx, A = dx.n and the staged w = -Q:
+                    // T_ab += g d_a d_b - w_ab r^-5 + 5 r^-7 (d_a n_b + d_b n_a) + delta_ab hd,
+                    // g = r^-2 (3 m r^-3 - 17.5 A r^-7), hd = 2.5 A r^-7 - m r^-3
+                    const f2 r7 = f2_mul(r5, u);
+                    const f2 mr3 = f2_mul(w1.y, f2_mul(rinv, u));
+                    const f2 Ar7 = f2_mul(A, r7);
+                    const f2 g = f2_mul(f2_fma(Ar7, f2_pack(-17.5f, -17.5f), f2_mul(mr3, f2_pack(3.f, 3.f))), u);
+                    const f2 hd = f2_sub(f2_mul(Ar7, f2_pack(2.5f, 2.5f)), mr3);
+                    const f2 s5 = f2_mul(r7, f2_pack(5.f, 5.f)), s10 = f2_mul(r7, f2_pack(10.f, 10.f));
+                    const f2 nr5 = f2_mul(r5, f2_pack(-1.f, -1.f));
+                    t0 = f2_add(f2_fma(w2.x, nr5, f2_fma(s10, f2_mul(dx, nx), f2_fma(g, f2_mul(dx, dx), t0))), hd);
+                    t1 = f2_fma(w2.y, nr5, f2_fma(s5, f2_fma(dx, ny, f2_mul(dy, nx)), f2_fma(g, f2_mul(dx, dy), t1)));
+                    t2 = f2_fma(w3.x, nr5, f2_fma(s5, f2_fma(dx, nz, f2_mul(dz, nx)), f2_fma(g, f2_mul(dx, dz), t2)));
+                    t3 = f2_add(f2_fma(w3.y, nr5, f2_fma(s10, f2_mul(dy, ny), f2_fma(g, f2_mul(dy, dy), t3))), hd);
+                    t4 = f2_fma(w4.x, nr5, f2_fma(s5, f2_fma(dy, nz, f2_mul(dz, ny)), f2_fma(g, f2_mul(dy, dz), t4)));
+                    t5 = f2_add(f2_fma(w4.y, nr5, f2_fma(s10, f2_mul(dz, nz), f2_fma(g, f2_mul(dz, dz), t5))), hd);
+                }
             }
             __syncwarp();
             Acc<T> b;
@@ -790,6 +833,14 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
             if constexpr ((FIELDS & F_POT) != 0) {
                 f2_unpack(ph, h0, h1);
                 b.v[0] = -(h0 + h1);
+            }
+            if constexpr ((FIELDS & F_TID) != 0) {
+                const f2 tt[6] = {t0, t1, t2, t3, t4, t5};
+#pragma unroll
+                for (int c = 0; c < 6; c++) {
+                    f2_unpack(tt[c], h0, h1);
+                    b.v[4 + c] = h0 + h1;
+                }
             }
             if constexpr ((FIELDS & F_ACC) != 0) {
                 f2_unpack(ax, h0, h1);
@@ -804,7 +855,7 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
             n_qint += (unsigned long long)cnt * (unsigned long long)gr.y;
         };
         auto eval_nodes = [&](const int *list, int cnt) {
-            if constexpr (sizeof(T) == 4 && (FIELDS & F_TID) == 0) {
+            if constexpr (sizeof(T) == 4 && ((FIELDS & F_TID) == 0 || FIELDS == F_TID)) {
                 if (GS >= 2) {
                     eval_nodes_paired(list, cnt);
                     return;
@@ -1338,9 +1389,16 @@ static tg_status launch_walk(WalkArgs<T> &a, int warps, cudaStream_t st) {
 
 template <typename T, int STACK>
 static tg_status dispatch_walk(WalkArgs<T> &a, int fields, bool quad, int warps, cudaStream_t st) {
-    // Fields computed: potential and/or acceleration alone, or everything when the tidal tensor is
-    // wanted (its setup already contains the other two).
+    // Fields computed: potential and/or acceleration alone; the tidal tensor alone in FP32 (its own
+    // paired sweeps); else everything when the tidal tensor is wanted (its setup already contains
+    // the other two).
     int fc = (fields & F_TID) ? (F_POT | F_ACC | F_TID) : fields;
+    if constexpr (sizeof(T) == 4) {
+        if (fields == F_TID) {
+            if (quad) return launch_walk<T, F_TID, true, STACK>(a, warps, st);
+            return launch_walk<T, F_TID, false, STACK>(a, warps, st);
+        }
+    }
     if (quad) {
         switch (fc) {
             case F_POT: return launch_walk<T, F_POT, true, STACK>(a, warps, st);

@@ -188,3 +188,38 @@ def test_tree_grouping_vs_oracle(tg, quad, G):
             assert rel_max(res[k], ref) < mtol, (prec, k, rel_max(res[k], ref))
     st = t.last_walk_stats()
     assert st[3] == len(S), "GPU and restated grouping differ in group count"
+
+
+@pytest.mark.parametrize("quad", [False, True])
+@pytest.mark.parametrize("gs", [8, 32])
+@pytest.mark.parametrize("grouping", ["blocks", "tree"])
+def test_tidal_alone_fp32_vs_oracle(tg, quad, gs, grouping):
+    """The tidal tensor requested alone takes its own FP32 walk (paired sweeps over leaves and
+    quadrupole nodes): against the oracle's FP64 grouped walk, and against the tidal part of the
+    all-fields walk, at the FP32 tolerances."""
+    rng = np.random.default_rng(31)
+    n = 60_000
+    x = plummer(n, rng)
+    keep = np.linalg.norm(x, axis=1) < 50
+    x = x[keep]
+    n = len(x)
+    m = rng.random(n) / n
+    h = np.full(n, 0.005)
+    ot = O.OracleTree(x, m, h, quadrupole=True)
+    idx = ot.TreewalkIndices
+    if grouping == "tree":
+        S, C = O.tree_groups(ot, gs)
+    else:
+        S = np.arange(0, n, gs, dtype=np.int64)
+        C = np.minimum(gs, n - S)
+    ref_sorted = O.fields_groups(ot, ot.Coordinates[:n], ot.Softenings[:n], S, C, False, False, True, quad, 0.7,
+                                 nthreads=O.num_threads())["tidal"]
+    ref = np.empty_like(ref_sorted)
+    ref[idx] = ref_sorted
+    t = tg.ConstructTree(x, m, h, quadrupole=True)
+    alone = t.fields(tidal=True, quadrupole=quad, group_size=gs, theta=0.7, grouping=grouping)["tidal"]
+    every = t.fields(potential=True, accel=True, tidal=True, quadrupole=quad, group_size=gs, theta=0.7,
+                     grouping=grouping)["tidal"]
+    assert rel_rms(alone, ref) < FP32_RMS and rel_max(alone, ref) < FP32_MAX
+    assert rel_rms(alone, every) < FP32_RMS
+    assert np.allclose(alone, np.swapaxes(alone, 1, 2))  # symmetric
