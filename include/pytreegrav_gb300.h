@@ -177,7 +177,10 @@ tg_status tg_bruteforce(const double *pos_t, const double *h_t, int64_t nt, cons
  * group_size 0 gives the per-target walk (treewalk.py:976-1030), group_size 1..32 the grouped walk
  * of that many consecutive targets (treewalk.py:1197-1294), pytreegrav's choice from 1000 targets.
  * FP64 in the reference's order of operations. Trees of one system only. TG_ERR_ITER_LIMIT if a walk
- * does not end within one visit per element. */
+ * does not end within one visit per element. pos NULL: the targets are the tree's own particles in
+ * walk (Morton) order, n must be its particle count, per-target rays are given in that order, and
+ * row i of out belongs to the caller's particle i (the results scattered through TreewalkIndices on
+ * the device, frontend.py:1450-1452). */
 tg_status tg_tree_column_density(tg_tree tree, const double *pos, int64_t n, const double *rays, int64_t nrays,
                                  int64_t ray_stride, int binned, double theta, int group_size, int mem, double *out,
                                  void *stream);

@@ -22,6 +22,10 @@ struct ColumnTree {
     // FP32 copy for the screen: coordinates split hi + lo, with the radius (hi.w) and, for nodes,
     // size * sqrt(3)/2 + delta (lo.w)
     const float4 *fhi, *flo;
+    // output row of target i: rows[i] (the targets are the tree's own particles, results go back to
+    // the caller's order), or i when null
+    const int64_t *rows = nullptr;
+    __device__ int64_t row(int64_t i) const { return rows ? rows[i] : i; }
 };
 
 __device__ __forceinline__ void split_f(double v, float &hi, float &lo) { d2f_split(v, hi, lo); }
@@ -159,8 +163,8 @@ __global__ void k_column_rays(ColumnTree t, const double *pos, int64_t n, const 
     if (p >= n * nrays) return;
     const int64_t i = p % n, j = p / n;
     const double *ray = rays + i * ray_stride + 3 * j;
-    out[i * nrays + j] = column_singleray(t, pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], ray[0], ray[1], ray[2],
-                                          runaway);
+    out[t.row(i) * nrays + j] = column_singleray(t, pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], ray[0], ray[1],
+                                                 ray[2], runaway);
 }
 
 // angular_bin (treewalk.py:49-70)
@@ -224,7 +228,7 @@ __global__ void k_column_binned(ColumnTree t, const double *pos, int64_t n, doub
         }
     }
 #pragma unroll
-    for (int k = 0; k < 6; k++) out[6 * i + k] = col[k];
+    for (int k = 0; k < 6; k++) out[6 * t.row(i) + k] = col[k];
 }
 
 // ColumnDensityBinned_grouped (treewalk.py:1197-1294): one warp per group of gsz (<= 32)
@@ -309,7 +313,7 @@ __global__ void k_column_binned_grouped(ColumnTree t, const double *pos, int64_t
     }
     if (mine)
 #pragma unroll
-        for (int k = 0; k < 6; k++) out[6 * ti + k] = col[k];
+        for (int k = 0; k < 6; k++) out[6 * t.row(ti) + k] = col[k];
 }
 
 }  // namespace
@@ -322,7 +326,9 @@ extern "C" {
 tg_status tg_tree_column_density(tg_tree t, const double *pos, int64_t n, const double *rays, int64_t nrays,
                                  int64_t ray_stride, int binned, double theta, int group_size, int mem, double *out,
                                  void *stream) {
-    if (!t || !out || n < 0 || (n > 0 && !pos)) return TG_ERR_BAD_ARG;
+    if (!t || !out || n < 0) return TG_ERR_BAD_ARG;
+    const bool own = !pos;  // the tree's own particles, results in the caller's order
+    if (own && n != t->ntot) return TG_ERR_BAD_ARG;
     if (binned && (group_size < 0 || group_size > 32)) return TG_ERR_BAD_ARG;
     if (mem != TG_MEM_HOST && mem != TG_MEM_DEVICE) return TG_ERR_BAD_ARG;
     if (binned) {
@@ -344,21 +350,25 @@ tg_status tg_tree_column_density(tg_tree t, const double *pos, int64_t n, const 
     ct.first = t->first; ct.next = t->next;
     ct.npart = t->ntot;
     ct.nelem = t->ntot + t->mtot;
+    ct.rows = own ? t->walk_idx : nullptr;
     const int64_t nray_vals = binned ? 0 : (ray_stride ? n * ray_stride : 3 * nrays);
     const double *dpos = pos, *drays = rays;
     double *dout = out, *owned = nullptr;
     int *flag = nullptr;
     // one allocation: flag, positions, rays and output when they come from or go to the host
     size_t bytes = 16;
-    if (mem == TG_MEM_HOST) bytes += sizeof(double) * (3 * n + nray_vals + n * nrays);
+    if (mem == TG_MEM_HOST) bytes += sizeof(double) * ((own ? 0 : 3 * n) + nray_vals + n * nrays);
     TG_CUDA(dev_malloc((void **)&owned, bytes, st));
     flag = (int *)owned;
     TG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    if (own) dpos = t->coord;  // rows [0, N) of the arena: the particles in walk order
     if (mem == TG_MEM_HOST) {
         double *p = owned + 2;
-        TG_CUDA(cudaMemcpyAsync(p, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
-        dpos = p;
-        p += 3 * n;
+        if (!own) {
+            TG_CUDA(cudaMemcpyAsync(p, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+            dpos = p;
+            p += 3 * n;
+        }
         if (nray_vals) {
             TG_CUDA(cudaMemcpyAsync(p, rays, sizeof(double) * nray_vals, cudaMemcpyHostToDevice, st));
             drays = p;

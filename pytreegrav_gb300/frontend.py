@@ -319,13 +319,15 @@ def ColumnDensity(pos, m, radii, rays=None, randomize_rays=False, healpix=False,
         warnings.warn("Some particle radii are <= 0; these particles are point-like and contribute no column "
                       "density. Supply a nonzero radius if their mass should be included.")
     pos = np.atleast_2d(_f64(pos))
-    if tree is None:
+    own = tree is None  # targets are the new tree's own particles: ordered and restored on the device
+    if own:
         tree = ConstructTree(pos, _f64(m), _f64(radii))
-        idx = tree.TreewalkIndices
+        npos = len(pos)
     else:
         _check_tree(tree)
         idx = morton_order(pos)
-    pos_sorted = np.ascontiguousarray(pos[idx])
+        pos_sorted = np.ascontiguousarray(pos[idx])
+        npos = len(pos_sorted)
 
     if type(rays) == int:
         if rays == 6:
@@ -355,24 +357,29 @@ def ColumnDensity(pos, m, radii, rays=None, randomize_rays=False, healpix=False,
     if device == "cuda" and (rays is None or randomize_rays):
         raise ValueError("device='cuda' supports only the ray-traced path: pass rays, and not randomize_rays")
 
+    # the walks over the new tree's own particles return rows already in the caller's order
+    walk = tree.column_density_self if own else (lambda *a: tree.column_density(pos_sorted, *a))
     if rays is None:  # pytreegrav groups the binned walk from COLUMN_GROUP_MIN_TARGETS targets on
-        grouped = len(pos_sorted) >= COLUMN_GROUP_MIN_TARGETS
+        grouped = npos >= COLUMN_GROUP_MIN_TARGETS
         if grouped and not 1 <= group_size <= 32:
             raise ValueError("group_size must be between 1 and 32 for the grouped binned walk")
-        columns = tree.column_density(pos_sorted, None, theta, group_size if grouped else 0)
+        columns = walk(None, theta, group_size if grouped else 0)
     elif randomize_rays:
-        per = np.empty((len(pos_sorted),) + rays.shape)
-        for i in range(len(pos_sorted)):
+        per = np.empty((npos,) + rays.shape)
+        for i in range(npos):
             per[i] = rays @ random_rotation(i)
-        columns = tree.column_density(pos_sorted, per)
+        columns = walk(per)
     else:
-        columns = tree.column_density(pos_sorted, rays)
+        columns = walk(rays)
     if device == "cuda":  # pytreegrav's device path returns float32
         columns = columns.astype(np.float32)
     if np.any(np.isnan(columns)):
         print("WARNING some column densities are NaN!")
-    unsorted = np.empty_like(columns)
-    unsorted[idx] = columns
+    if own:
+        unsorted = columns
+    else:
+        unsorted = np.empty_like(columns)
+        unsorted[idx] = columns
     if return_tree:
         return unsorted, tree
     return unsorted

@@ -243,6 +243,29 @@ class Octree:
         _lib.check(rc, "column density")
         return out
 
+    def column_density_self(self, rays=None, theta=0.5, group_size=0):
+        """column_density with this tree's own particles as the targets, taken in walk (Morton)
+        order on the device; per-target rays (NumParticles, nrays, 3) are in that order too. The
+        rows come back in the caller's original particle order (TreewalkIndices undone on the
+        device), so no host gather or scatter is needed."""
+        n = self.NumParticles
+        L = _lib.load()
+        if rays is None:
+            out = np.empty((n, 6))
+            rc = L.tg_tree_column_density(self._h, None, n, None, 0, 0, 1, float(theta), int(group_size),
+                                          _lib.TG_MEM_HOST, _lib.ptr(out), None)
+        else:
+            rays = np.ascontiguousarray(rays, np.float64)
+            per_target = rays.ndim == 3
+            nrays = rays.shape[-2]
+            if rays.shape[-1] != 3 or (per_target and rays.shape[0] != n):
+                raise ValueError("rays must be (nrays, 3), or (n, nrays, 3) for per-target rays")
+            out = np.empty((n, nrays))
+            rc = L.tg_tree_column_density(self._h, None, n, _lib.ptr(rays), nrays, 3 * nrays if per_target else 0,
+                                          0, 0.0, 0, _lib.TG_MEM_HOST, _lib.ptr(out), None)
+        _lib.check(rc, "column density")
+        return out
+
     def last_walk_stats(self):
         """(interactions, node tests, deepest stack, groups) of the last walk on this tree."""
         v = [ctypes.c_int64() for _ in range(4)]

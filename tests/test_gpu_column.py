@@ -169,3 +169,20 @@ def test_cuda_context_is_reusable_and_float32(tg):
         tg.ColumnDensity(x, m, h, rays=None, device="cuda")
     dev = tg.ColumnDensity(x, m, h, rays=6, device="cuda")
     assert dev.dtype == np.float32
+
+
+def test_own_particles_form_equals_the_explicit_targets(tg):
+    """tg_tree_column_density with pos NULL walks the tree's own particles in walk order and writes
+    each row at its caller index: the same numbers as the explicit Morton-ordered targets, unsorted."""
+    x, m, h = cloud(3000, seed=17)
+    t = tg.ConstructTree(x, m, h)
+    idx = t.TreewalkIndices
+    xs = x[idx]
+    rng = np.random.default_rng(4)
+    per = rng.normal(size=(len(x), 4, 3))
+    per /= np.linalg.norm(per, axis=2)[:, :, None]
+    for args in ((SIX_RAYS,), (per,), (None, 0.5, 0), (None, 0.7, 16)):
+        explicit = t.column_density(xs, *args)
+        unsorted = np.empty_like(explicit)
+        unsorted[idx] = explicit
+        assert np.array_equal(t.column_density_self(*args), unsorted)
