@@ -164,3 +164,45 @@ def test_nonfinite_input_raises_like_construct_tree(tg, capsys, where, bad):
     # the library is usable right after a rejected call
     x2 = rng.random((300, 3))
     assert np.all(np.isfinite(tg.Accel(x2, np.ones(300), np.full(300, 0.01), method="tree")))
+
+
+def test_tree_used_on_other_streams_right_after_the_build(tg):
+    """A build returns with its moment pass still running on its stream: a walk, a copy-out and a
+    column-density call issued at once on other streams must see the finished tree (each entry
+    orders its stream after the build), and so give the results of a synchronised build."""
+    import ctypes
+
+    import torch
+
+    from pytreegrav_gb300 import _lib
+
+    L = _lib.load()
+    vp = ctypes.c_void_p
+    rng = np.random.default_rng(12)
+    n = 200_000
+    x = rng.normal(size=(n, 3))
+    m = np.full(n, 1.0 / n)
+    h = np.full(n, 0.01)
+    dx, dm, dh = (torch.from_numpy(a).cuda() for a in (x, m, h))
+    ref_tree = tg.ConstructTree(x, m, h, quadrupole=True)
+    ref = ref_tree.fields(accel=True, quadrupole=True, group_size=32, grouping="tree")["accel"]
+    sa, sb = torch.cuda.Stream(), torch.cuda.Stream()
+    for _ in range(3):
+        t = vp()
+        torch.cuda.synchronize()
+        _lib.check(L.tg_tree_build(vp(dx.data_ptr()), vp(dm.data_ptr()), vp(dh.data_ptr()), n, 1, 1,
+                                   _lib.TG_MEM_DEVICE, vp(sa.cuda_stream), ctypes.byref(t)), "build")
+        out = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+        _lib.check(L.tg_tree_fields(t, None, None, n, _lib.TG_FIELD_ACCEL, 1, 0.7, 1.0, 32, _lib.TG_GROUP_TREE,
+                                    _lib.TG_ORDER_TREE, _lib.TG_FP32, None, _lib.TG_MEM_DEVICE, vp(out.data_ptr()),
+                                    vp(sb.cuda_stream)), "walk")
+        info = _lib.TreeInfo()
+        _lib.check(L.tg_tree_info_get(t, ctypes.byref(info)))
+        mass = np.empty(int(info.num_nodes))
+        _lib.check(L.tg_tree_copy_out(t, None, _lib.ptr(mass), None, None, None, None, None, None, None,
+                                      vp(sb.cuda_stream)), "copy out")
+        sb.synchronize()
+        assert np.array_equal(out.cpu().numpy(), ref)
+        assert mass[n] == ref_tree.Masses[n]  # the root's mass comes from the moment pass
+        L.tg_tree_free(t)
+        torch.cuda.synchronize()
