@@ -1712,8 +1712,10 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
         TG_TRY(dalloc(&nk, M, st));
         { k_kids<<<LAUNCH(M)>>>(N, M, T->first, T->next, kids, nk); tg::note_launch(); }
         // a level with few nodes is latency-bound: 16 lanes per node there; one thread per node
-        // on the large levels, which are FP64-throughput-bound
-        const int few = 128 * num_sms();
+        // on the large levels, which are FP64-throughput-bound (16 lanes per node issue about 2.5x
+        // the FP64 warp instructions; from ~48 nodes per SM one thread per node was faster at 1e6,
+        // against thresholds of 8, 24 and 128)
+        const int few = 48 * num_sms();
         for (int d = DEPTH_CAP - 1; d >= 0; d--) {
             const int c = hs.depth_hist[d];
             if (c <= 0) continue;
