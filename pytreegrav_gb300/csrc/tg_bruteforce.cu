@@ -7,7 +7,9 @@
 //
 // FP32: the fast path (the numba-cuda CudaPotentialBruteforce/CudaAccelBruteforce of cuda.py:627-796
 // rebuilt): tiles of 256 sources in shared memory, two targets per thread so every broadcast source
-// load feeds two interactions, rsqrt, and tile sums added into Kahan-compensated accumulators.
+// load feeds two interactions, rsqrt, and tile sums added into Kahan-compensated accumulators. For
+// the potential and acceleration, four lanes share each pair of targets (k_bf32_split) and the two
+// targets are computed with paired f32x2 arithmetic.
 #include "tg_common.cuh"
 
 namespace tg {
@@ -292,11 +294,174 @@ __global__ void __launch_bounds__(BF32_THREADS) k_bf32(const double *pt, const d
     }
 }
 
+// Potential and/or acceleration, the main FP32 form: BF32S_LANES lanes share each pair of targets,
+// lane q of the group taking the sources k = q (mod BF32S_LANES) of every shared-memory tile, so a
+// target set of 1e5 still fills the GPU; the lanes' Kahan-compensated sums are combined at the end
+// by a fixed pattern of shuffles (deterministic). The two targets of a lane are computed together
+// with paired f32x2 arithmetic for every source outside both softening lengths (with a 1e-5 margin)
+// and not coincident; any other source takes bf32_pair for each target.
+constexpr int BF32S_THREADS = 256;
+constexpr int BF32S_LANES = 4;
+constexpr int BF32S_TARGETS = 2 * BF32S_THREADS / BF32S_LANES;  // per block
+
+typedef unsigned long long bf2;
+__device__ __forceinline__ bf2 bf2_pack(float a, float b) {
+    bf2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void bf2_unpack(bf2 v, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ bf2 bf2_fma(bf2 a, bf2 b, bf2 c) {
+    bf2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ bf2 bf2_mul(bf2 a, bf2 b) {
+    bf2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ bf2 bf2_sub(bf2 a, bf2 b) {
+    bf2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+template <int FIELDS, bool MUTUAL>
+__global__ void __launch_bounds__(BF32S_THREADS) k_bf32_split(const double *pt, const double *ht, int64_t nt,
+                                                              const double *ps, const double *ms,
+                                                              const double *hs, int64_t ns, double G,
+                                                              double *out, int W) {
+    __shared__ float4 spos[BF32S_THREADS];
+    __shared__ float sh[BF32S_THREADS], sh2[BF32S_THREADS];
+    const int q = threadIdx.x % BF32S_LANES;
+    const int64_t pair = (int64_t)blockIdx.x * (BF32S_THREADS / BF32S_LANES) + threadIdx.x / BF32S_LANES;
+    float tx[2], ty[2], tz[2], th[2], th2[2];
+    int64_t ti[2];
+    float S[2][4], C[2][4];
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+        ti[u] = 2 * pair + u;
+        const int64_t i = ti[u] < nt ? ti[u] : 0;
+        tx[u] = (float)pt[3 * i];
+        ty[u] = (float)pt[3 * i + 1];
+        tz[u] = (float)pt[3 * i + 2];
+        th[u] = (float)ht[i];
+        th2[u] = th[u] * th[u];
+#pragma unroll
+        for (int c = 0; c < 4; c++) S[u][c] = C[u][c] = 0.f;
+    }
+    const bf2 TX = bf2_pack(tx[0], tx[1]), TY = bf2_pack(ty[0], ty[1]), TZ = bf2_pack(tz[0], tz[1]);
+    for (int64_t base = 0; base < ns; base += BF32S_THREADS) {
+        const int64_t j = base + threadIdx.x;
+        if (j < ns) {
+            const float hj = (float)hs[j];
+            spos[threadIdx.x] = make_float4((float)ps[3 * j], (float)ps[3 * j + 1], (float)ps[3 * j + 2], (float)ms[j]);
+            sh[threadIdx.x] = hj;
+            sh2[threadIdx.x] = hj * hj;
+        }
+        __syncthreads();
+        const int lim = (int)((ns - base) < BF32S_THREADS ? (ns - base) : BF32S_THREADS);
+        bf2 ph = 0, ax = 0, ay = 0, az = 0;  // the two targets' tile sums (bit pattern 0 is +0.0f, +0.0f)
+        float P[2][10];
+#pragma unroll
+        for (int u = 0; u < 2; u++)
+#pragma unroll
+            for (int c = 0; c < 10; c++) P[u][c] = 0.f;
+        for (int k = q; k < lim; k += BF32S_LANES) {
+            const float4 s = spos[k];
+            const bf2 dx = bf2_sub(bf2_pack(s.x, s.x), TX), dy = bf2_sub(bf2_pack(s.y, s.y), TY);
+            const bf2 dz = bf2_sub(bf2_pack(s.z, s.z), TZ);
+            const bf2 r2 = bf2_fma(dz, dz, bf2_fma(dy, dy, bf2_mul(dx, dx)));
+            float r20, r21;
+            bf2_unpack(r2, r20, r21);
+            const float hs2 = sh2[k];
+            const float lim0 = fmaxf(hs2, th2[0]) * 1.00001f, lim1 = fmaxf(hs2, th2[1]) * 1.00001f;
+            bool slow = !(r20 > lim0) || !(r21 > lim1) || !(r20 > 0.f) || !(r21 > 0.f);
+            if (MUTUAL) slow = slow || base + k == ti[0] || base + k == ti[1];
+            if (slow) {
+                float d[3][2];
+                bf2_unpack(dx, d[0][0], d[0][1]);
+                bf2_unpack(dy, d[1][0], d[1][1]);
+                bf2_unpack(dz, d[2][0], d[2][1]);
+#pragma unroll
+                for (int u = 0; u < 2; u++) {
+                    const bool skip = MUTUAL && (base + k == ti[u]);
+                    bf32_pair<FIELDS>(s.w, sh[k], th[u], d[0][u], d[1][u], d[2][u], skip, P[u]);
+                }
+            } else {
+                const float r0 = rsqrtf(r20), r1 = rsqrtf(r21);
+                const bf2 rinv = bf2_pack(r0, r1);
+                const bf2 mr = bf2_mul(bf2_pack(s.w, s.w), rinv);
+                if (FIELDS & BF_POT) ph = bf2_sub(ph, mr);
+                if (FIELDS & BF_ACC) {
+                    const bf2 K = bf2_mul(mr, bf2_mul(rinv, rinv));
+                    ax = bf2_fma(K, dx, ax);
+                    ay = bf2_fma(K, dy, ay);
+                    az = bf2_fma(K, dz, az);
+                }
+            }
+        }
+        float a0, a1;
+        if (FIELDS & BF_POT) {
+            bf2_unpack(ph, a0, a1);
+            P[0][0] += a0;
+            P[1][0] += a1;
+        }
+        if (FIELDS & BF_ACC) {
+            bf2_unpack(ax, a0, a1);
+            P[0][1] += a0;
+            P[1][1] += a1;
+            bf2_unpack(ay, a0, a1);
+            P[0][2] += a0;
+            P[1][2] += a1;
+            bf2_unpack(az, a0, a1);
+            P[0][3] += a0;
+            P[1][3] += a1;
+        }
+#pragma unroll
+        for (int u = 0; u < 2; u++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const float yv = P[u][c] - C[u][c];
+                const float tv = S[u][c] + yv;
+                C[u][c] = (tv - S[u][c]) - yv;
+                S[u][c] = tv;
+            }
+        __syncthreads();
+    }
+    // the group's lanes combined in double, the same fixed pattern on every lane
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+        double v[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            v[c] = (double)S[u][c] - (double)C[u][c];
+#pragma unroll
+            for (int o = 1; o < BF32S_LANES; o <<= 1) v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
+        }
+        if (q != 0 || ti[u] >= nt) continue;
+        double *o = out + ti[u] * W;
+        int k = 0;
+        if (FIELDS & BF_POT) o[k++] = G * v[0];
+        if (FIELDS & BF_ACC) {
+            o[k] = G * v[1];
+            o[k + 1] = G * v[2];
+            o[k + 2] = G * v[3];
+        }
+    }
+}
+
 template <int FIELDS, bool MUTUAL>
 static void launch_bf(int precision, const double *pt, const double *ht, int64_t nt, const double *ps,
                       const double *ms, const double *hs, int64_t ns, double G, double *out, int W, cudaStream_t st) {
     if (precision == TG_FP64) {
         { k_bf64<FIELDS, MUTUAL><<<div_up(nt, BF64_THREADS), BF64_THREADS, 0, st>>>(pt, ht, nt, ps, ms, hs, ns, G, out, W); tg::note_launch(); }
+    } else if constexpr ((FIELDS & BF_TID) == 0) {
+        { k_bf32_split<FIELDS, MUTUAL><<<div_up(nt, BF32S_TARGETS), BF32S_THREADS, 0, st>>>(pt, ht, nt, ps, ms, hs, ns,
+                                                                                          G, out, W); tg::note_launch(); }
     } else {
         { k_bf32<FIELDS, MUTUAL><<<div_up(nt, BF32_THREADS * BF32_TPT), BF32_THREADS, 0, st>>>(pt, ht, nt, ps, ms, hs, ns,
                                                                                            G, out, W); tg::note_launch(); }
