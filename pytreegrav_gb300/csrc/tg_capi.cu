@@ -163,7 +163,7 @@ static tg_status build_common(const double *pos, const double *m, const double *
         auto stage = [&]() -> tg_status {
             TG_TRY(stage_in(pos, 3 * n, mem, st, dp));
             // the input check runs ahead of the build on the stream; the build reads its flag back
-            // with its first summary and reports non-finite input at its end
+            // with its first summary and reports non-finite input with its closing read-back
             TG_CUDA(tg::dev_malloc((void **)&flag, sizeof(int), st));
             TG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
             if (mem == TG_MEM_HOST && (m || h)) {
