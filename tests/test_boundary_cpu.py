@@ -116,3 +116,50 @@ def test_quadrupole_guard():
     with pytest.raises(ValueError, match="quadrupole"):
         tg.checkTreeQuadrupoles(Fake(), True)
     tg.checkTreeQuadrupoles(Fake(), False)
+
+
+class _FakeColumnTree:
+    """Records the column-density calls the frontend makes; results encode the call."""
+
+    def __init__(self, n):
+        self.n = n
+        self.calls = []
+
+    def column_density_self(self, rays=None, theta=0.5, group_size=0):
+        self.calls.append(("self", None if rays is None else np.shape(rays), theta, group_size))
+        w = 6 if rays is None else np.shape(rays)[-2]
+        return np.arange(self.n * w, dtype=float).reshape(self.n, w)
+
+    def column_density(self, pos, rays=None, theta=0.5, group_size=0):
+        self.calls.append(("explicit", np.array(pos), None if rays is None else np.shape(rays), theta, group_size))
+        w = 6 if rays is None else np.shape(rays)[-2]
+        return np.arange(len(pos) * w, dtype=float).reshape(len(pos), w)
+
+
+def test_column_density_dispatch_own_and_given_trees(monkeypatch):
+    """ColumnDensity on a tree it builds asks the library for the tree's own particles (rows come back
+    in the caller's order, so no host gather or scatter); on a given tree it Morton-orders the targets,
+    walks them and undoes the order (frontend.py:1440-1452). Dispatch only, no GPU work."""
+    from pytreegrav_gb300 import frontend
+
+    n = 1200
+    x = np.random.default_rng(3).normal(size=(n, 3))
+    fake = _FakeColumnTree(n)
+    monkeypatch.setattr(frontend, "ConstructTree", lambda *a, **k: fake)
+    monkeypatch.setattr(frontend, "_check_tree", lambda t: None)
+    perm = np.random.default_rng(4).permutation(n)
+    monkeypatch.setattr(frontend, "morton_order", lambda p: perm)
+    m, h = np.ones(n), np.full(n, 0.1)
+
+    out = frontend.ColumnDensity(x, m, h, rays=6)
+    assert fake.calls[-1] == ("self", (6, 3), 0.5, 0)
+    assert np.array_equal(out, np.arange(n * 6, dtype=float).reshape(n, 6))
+    frontend.ColumnDensity(x, m, h)  # binned, grouped from 1000 targets with pytreegrav's group size 16
+    assert fake.calls[-1] == ("self", None, 0.5, 16)
+
+    out = frontend.ColumnDensity(x, m, h, rays=6, tree=fake)
+    kind, pos, shape, theta, gs = fake.calls[-1]
+    assert kind == "explicit" and shape == (6, 3) and np.array_equal(pos, x[perm])
+    expect = np.empty((n, 6))
+    expect[perm] = np.arange(n * 6, dtype=float).reshape(n, 6)
+    assert np.array_equal(out, expect)
