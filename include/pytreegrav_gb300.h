@@ -138,6 +138,35 @@ tg_status tg_walk_graph_launch(tg_walk_graph graph, void *stream);
 tg_status tg_walk_graph_status(tg_walk_graph graph, void *stream);
 tg_status tg_walk_graph_free(tg_walk_graph graph);
 
+/* External target points prepared once for walks of one single-system source tree: the target forms
+ * PotentialTarget / AccelTarget / TidalTensorTarget (frontend.py:296-418, 563-685, 792-901), which
+ * pytreegrav walks in blocks of group_size consecutive targets after sorting them by their own
+ * Morton keys (_morton_order, grouped_treewalk.py:269-275; that grouping is tg_tree_fields with
+ * TG_ORDER_MORTON). Here the targets get an octree of their own (the radix build, no masses) and
+ * are grouped by it -- subtrees and runs of siblings of at most group_size targets, the rule of
+ * TG_GROUP_TREE -- so no group straddles a jump of the Morton curve. pos (n, 3) and h (n,; NULL:
+ * zeros) are read from host or device memory (mem); the source tree must outlive the set. */
+typedef struct tg_targets_s *tg_targets;
+tg_status tg_targets_create(tg_tree source, const double *pos, const double *h, int64_t n, int group_size, int mem,
+                            void *stream, tg_targets *out);
+tg_status tg_targets_free(tg_targets targets);
+
+/* Target count and group count of a target set. */
+tg_status tg_targets_info(tg_targets targets, int64_t *n, int64_t *ngroups);
+
+/* The groups of a target set: first target and count (walk order, int32, ngroups each), the deepest
+ * node of the source tree whose cell holds each group's bounding box (int32), and each walk-order
+ * target's index in the caller's arrays (int64, n). Any pointer may be NULL; host or device per mem. */
+tg_status tg_targets_groups_copy(tg_targets targets, int32_t *first, int32_t *count, int32_t *src_node,
+                                 int64_t *walk_idx, int mem, void *stream);
+
+/* FieldsTarget_grouped (grouped_treewalk.py:350-397) of the source tree at the target set's groups:
+ * fields as tg_tree_fields, rows in the caller's order. tol_per_group: optional device array of one
+ * tolerance per group for the mass-aware acceptance test of tg_tree_fields_grouped (FP32 only;
+ * NULL: pytreegrav's criterion at theta). */
+tg_status tg_targets_fields(tg_targets targets, int fields, int quadrupole, double theta, double G, int precision,
+                            const float *tol_per_group, int mem, double *out, void *stream);
+
 /* Interaction statistics of the last tg_tree_fields call on this tree: total interactions and
  * node tests, the deepest node stack seen, and the number of groups. */
 tg_status tg_tree_last_walk_stats(tg_tree tree, int64_t *interactions, int64_t *node_tests,
@@ -153,8 +182,9 @@ tg_status tg_morton_order(const double *pos, int64_t n, int mem, int64_t *perm, 
  * current device; every temporary lives in one fixed scratch array of TG_NOALLOC_SCRATCH_BYTES that
  * the library holds on each GPU that loads it, until exit. n above TG_NOALLOC_MAX_POINTS returns
  * TG_ERR_BAD_ARG. All calls on a device share that array: calls whose GPU work overlaps race, so
- * order them (e.g. one stream). The first call on a device looks the array up; make it before
- * any stream capture on that device. Returns when perm is written (the stream is synchronised).
+ * order them (e.g. one stream). The first call on a device looks the array up (again after the
+ * device's context is reset); make it before any stream capture on that device. Returns when perm
+ * is written (the stream is synchronised).
  * The result equals tg_morton_order's. */
 #define TG_NOALLOC_MAX_POINTS 262144
 #define TG_NOALLOC_SCRATCH_BYTES 6358528

@@ -123,6 +123,20 @@ tg_status tg_tree_fields_learned(tg_tree tree, int fields, int quadrupole, doubl
                                  tg_theta_model model, float log10_lambda, double theta_fallback, int mem,
                                  double *out, void *stream);
 
+/* The learned acceptance test for external targets (tg_targets_create's groups of the source tree's
+ * walk): tg_tree_fields_learned's walk, with each group's features taken from its targets and from
+ * the deepest source node holding its box, and the tolerance unit from the RMS of the coarse field
+ * at the targets. Groups over the model's error budget are walked again at theta_fallback. */
+tg_status tg_targets_fields_learned(tg_targets targets, int fields, int quadrupole, double G, tg_theta_model model,
+                                    float log10_lambda, double theta_fallback, int mem, double *out, void *stream);
+
+/* Features of a target set's groups (ngroups x TG_THETA_NFEAT float32, device), as tg_theta_features. */
+tg_status tg_targets_features(tg_targets targets, int quadrupole, float *features, void *stream);
+
+/* Per-group tolerances of a target set's groups from u (log10 relative tolerance per group), as
+ * tg_theta_tolerances. */
+tg_status tg_targets_tolerances(tg_targets targets, int quadrupole, const float *u, float *tol, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

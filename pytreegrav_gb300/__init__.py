@@ -10,10 +10,10 @@ built in-tree by ``python -m pytreegrav_gb300.build``.
 from .frontend import (Accel, AccelTarget, ColumnDensity, ConstructTree, Field, Potential, PotentialTarget,
                        TidalTensor, TidalTensorTarget, checkTreeQuadrupoles, valueTestMethod,
                        warn_if_coincident_positions)
-from .tree import Octree, bruteforce, morton_order
+from .tree import Octree, TargetSet, bruteforce, morton_order
 
 __all__ = [
     "Accel", "AccelTarget", "ColumnDensity", "ConstructTree", "Field", "Potential", "PotentialTarget", "TidalTensor",
     "TidalTensorTarget", "checkTreeQuadrupoles", "valueTestMethod", "warn_if_coincident_positions", "Octree",
-    "bruteforce", "morton_order",
+    "TargetSet", "bruteforce", "morton_order",
 ]

@@ -46,6 +46,11 @@ EXPORTS = [
     "tg_tree_copy_out",
     "tg_tree_free",
     "tg_tree_fields",
+    "tg_targets_create",
+    "tg_targets_free",
+    "tg_targets_info",
+    "tg_targets_groups_copy",
+    "tg_targets_fields",
     "tg_tree_last_walk_stats",
     "tg_tree_set_walk_config",
     "tg_walk_graph_create",
@@ -81,6 +86,9 @@ THETA_EXPORTS = [
     "tg_theta_infer",
     "tg_tree_fields_grouped",
     "tg_tree_fields_learned",
+    "tg_targets_fields_learned",
+    "tg_targets_features",
+    "tg_targets_tolerances",
 ]
 # every extern "C" symbol declared in include/pytreegrav_gb300_measure.h (measurement and self-checks)
 MEASURE_EXPORTS = [
@@ -140,6 +148,11 @@ def _declare(L):
     L.tg_tree_free.argtypes = [vp]
     L.tg_tree_fields.argtypes = [vp, vp, vp, i64, ci, ci, dbl, dbl, ci, ci, ci, ci, vp, ci, vp, vp]
     L.tg_tree_last_walk_stats.argtypes = [vp, vp, vp, vp, vp]
+    L.tg_targets_create.argtypes = [vp, vp, vp, i64, ci, ci, vp, ctypes.POINTER(vp)]
+    L.tg_targets_free.argtypes = [vp]
+    L.tg_targets_info.argtypes = [vp, vp, vp]
+    L.tg_targets_groups_copy.argtypes = [vp, vp, vp, vp, vp, ci, vp]
+    L.tg_targets_fields.argtypes = [vp, ci, ci, dbl, dbl, ci, vp, ci, vp, vp]
     L.tg_tree_set_walk_config.argtypes = [vp, ci, ci]
     L.tg_walk_graph_create.argtypes = [vp, ci, ci, dbl, dbl, ci, ci, vp, ctypes.POINTER(vp)]
     L.tg_walk_graph_launch.argtypes = [vp, vp]
@@ -173,6 +186,9 @@ def _declare(L):
     L.tg_theta_infer.argtypes = [vp, vp, i64, flt, vp, vp]
     L.tg_tree_fields_grouped.argtypes = [vp, ci, ci, dbl, ci, dbl, vp, vp, ci, vp, vp]
     L.tg_tree_fields_learned.argtypes = [vp, ci, ci, dbl, ci, vp, flt, dbl, ci, vp, vp]
+    L.tg_targets_fields_learned.argtypes = [vp, ci, ci, dbl, vp, flt, dbl, ci, vp, vp]
+    L.tg_targets_features.argtypes = [vp, ci, vp, vp]
+    L.tg_targets_tolerances.argtypes = [vp, ci, vp, vp, vp]
     for name in THETA_EXPORTS:
         getattr(L, name).restype = ci
 

@@ -57,8 +57,6 @@ __global__ void k_bbox_init(unsigned long long *mn, unsigned long long *mx, int 
     }
 }
 
-constexpr int BB_THREADS = 256, BB_ITEMS = 8;
-
 __global__ void __launch_bounds__(BB_THREADS) k_bbox(const double *pos, int64_t n, const int64_t *sys_off, int nsys,
                                                      unsigned long long *mn, unsigned long long *mx) {
     int64_t tile0 = (int64_t)blockIdx.x * BB_THREADS * BB_ITEMS;

@@ -14,6 +14,17 @@ constexpr int MAX_LEVEL = MORTON_BITS;            // a run sharing all 63 key bi
 constexpr int MORTON_MAX_ROUNDS = 3;
 constexpr uint32_t FULL = 0xffffffffu;
 
+// Launch geometry of the bounding-box kernel (k_bbox, tg_build.cu) and of the two-kernel radix
+// passes (radix_hist / radix_scatter, tg_sort.cu), shared with every file that launches them
+// (tg_noalloc.cu sizes its fixed scratch array from these).
+constexpr int BB_THREADS = 256, BB_ITEMS = 8;   // k_bbox: 256 threads x 8 points per block
+constexpr int RS_WARPS = 8;
+constexpr int RS_THREADS = RS_WARPS * 32;
+constexpr int RS_ROUNDS = 16;                   // keys per thread
+constexpr int RS_WARP_KEYS = RS_ROUNDS * 32;    // 512 consecutive keys per warp
+constexpr int RS_TILE = RS_WARPS * RS_WARP_KEYS;  // 4096 keys per CTA
+constexpr int RS_BINS = 256;                    // 8-bit digits
+
 void set_last_error(const char *where, cudaError_t e);
 void set_last_error_msg(const char *msg);
 const char *last_error();

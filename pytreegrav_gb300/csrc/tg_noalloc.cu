@@ -45,10 +45,12 @@ __global__ void radix_scatter(const uint64_t *keys, const uint32_t *vals, int64_
 
 namespace {
 
-// Launch geometry those kernels are written for: k_bbox covers 256 threads x 8 points per block;
-// the radix kernels run 256-thread CTAs over tiles of 4096 keys with 256 digit bins.
-constexpr int BBOX_THREADS = 256, BBOX_POINTS = 256 * 8;
-constexpr int SORT_THREADS = 256, SORT_TILE = 4096, SORT_BINS = 256;
+// Launch geometry those kernels are written for, taken from their own definitions (tg_common.cuh):
+// k_bbox covers BB_THREADS x BB_ITEMS points per block; the radix kernels run RS_THREADS-thread CTAs
+// over tiles of RS_TILE keys with RS_BINS digit bins.
+constexpr int BBOX_THREADS = BB_THREADS, BBOX_POINTS = BB_THREADS * BB_ITEMS;
+constexpr int SORT_THREADS = RS_THREADS, SORT_TILE = RS_TILE, SORT_BINS = RS_BINS;
+static_assert(SORT_BINS == 256, "the passes below take 8-bit digits (shift += 8)");
 constexpr int KEY_BITS = 63;
 
 constexpr int64_t MAX_POINTS = TG_NOALLOC_MAX_POINTS;
@@ -77,9 +79,34 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[SCRATCH_BYTES];
 
 constexpr int MAX_DEVICES = 64;
 std::mutex g_addr_mutex;
-unsigned char *g_addr[MAX_DEVICES] = {};
+// The address looked up on each device, with the CUDA context it belongs to: after a device reset
+// (cudaDeviceReset, or a reset of the primary context by the host application) the context is a
+// new one and the address is looked up again.
+struct ScratchAddr {
+    void *ctx = nullptr;
+    unsigned char *addr = nullptr;
+};
+ScratchAddr g_addr[MAX_DEVICES];
 
-// Device address of the scratch array on the current device, looked up once per device.
+// The calling thread's current CUDA context (the driver's cuCtxGetCurrent, reached through the
+// runtime's entry-point query so that the library needs no link to the driver library), or null.
+void *current_context() {
+    using CtxGetCurrent = int (*)(void **);
+    static CtxGetCurrent fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (CtxGetCurrent)p;
+    });
+    void *ctx = nullptr;
+    if (fn && fn(&ctx) != 0) ctx = nullptr;
+    return ctx;
+}
+
+// Device address of the scratch array on the current device, looked up once per device and context.
 tg_status scratch_on_current_device(unsigned char **out) {
     int dev = 0;
     TG_CUDA(cudaGetDevice(&dev));
@@ -88,12 +115,15 @@ tg_status scratch_on_current_device(unsigned char **out) {
         return TG_ERR_BAD_ARG;
     }
     std::lock_guard<std::mutex> lock(g_addr_mutex);
-    if (!g_addr[dev]) {
+    ScratchAddr &c = g_addr[dev];
+    void *ctx = current_context();
+    if (!c.addr || !ctx || c.ctx != ctx) {
         void *p = nullptr;
-        TG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        g_addr[dev] = (unsigned char *)p;
+        TG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));  // makes the device's context current if needed
+        c.addr = (unsigned char *)p;
+        c.ctx = current_context();
     }
-    *out = g_addr[dev];
+    *out = c.addr;
     return TG_OK;
 }
 

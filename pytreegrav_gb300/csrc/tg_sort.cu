@@ -168,12 +168,7 @@ tg_status exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n, cudaStr
 
 // ---------------------------------------------------------------------------------------------
 // Radix sort.
-constexpr int RS_WARPS = 8;
-constexpr int RS_THREADS = RS_WARPS * 32;
-constexpr int RS_ROUNDS = 16;                      // keys per thread
-constexpr int RS_WARP_KEYS = RS_ROUNDS * 32;       // 512 consecutive keys per warp
-constexpr int RS_TILE = RS_WARPS * RS_WARP_KEYS;   // 4096 keys per CTA
-constexpr int RS_BINS = 256;
+// RS_* (tile geometry of the two-kernel passes) are defined in tg_common.cuh.
 
 // Per-warp stable ranking of the warp's ROUNDS * 32 keys; leaves per-warp digit counts in wcount.
 template <int ROUNDS = RS_ROUNDS>

@@ -1,0 +1,198 @@
+// External target points prepared once for walks of one source tree: the target forms
+// (PotentialTarget / AccelTarget / TidalTensorTarget, frontend.py:296-418, 563-685, 792-901) with the
+// targets grouped by their own octree instead of in consecutive Morton blocks.
+//
+// pytreegrav sorts the targets by their Morton keys in their own bounding cube (_morton_order,
+// grouped_treewalk.py:269-275) and walks consecutive blocks of group_size of them. A block that
+// straddles a jump of the Morton curve gets a bounding box spanning both sides and opens far more of
+// the source tree than either half would. Here the targets get an octree of their own (the same
+// radix build as the sources, without masses or moments) and its tree grouping: subtrees and runs
+// of siblings of at most group_size targets, which never straddle such a jump. Walks of the source
+// tree then take those groups; results are scattered back to the caller's order through the
+// target tree's TreewalkIndices.
+#include <new>
+
+#include "tg_targets.cuh"
+
+namespace tg {
+
+tg_status tree_groups(tg_tree_s *t, int G, cudaStream_t st);
+template <typename T>
+tg_status build_arena(tg_tree_s *t, Arena<T> &ar, cudaStream_t st);
+tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t ntargets, const int2 *groups,
+                   const int *group_root, const int *group_order, int64_t ngroups, const int64_t *scatter, int fields,
+                   int quadrupole, double theta, double G, int group_size, int precision, const float *theta_group,
+                   const float *tol_group, double *out, cudaStream_t st);
+
+namespace {
+
+bool valid_gs(int gs) { return gs == 1 || gs == 2 || gs == 4 || gs == 8 || gs == 16 || gs == 32; }
+
+int width_of(int fields) { return ((fields & 1) ? 1 : 0) + ((fields & 2) ? 3 : 0) + ((fields & 4) ? 9 : 0); }
+
+// One thread per group: the group's FP64 bounding box, then a descent from the source root (node 0)
+// through the node child whose cell (cell centre +- size / 2) holds the whole box, as long as one
+// does. Children come from the walk arena's traversal records (first node child << 4 | count). The
+// descent goes one level deeper per step; it is bounded by the node count in any case.
+__global__ void k_target_src_nodes(int64_t ntot, int64_t mtot, const double *cell, const double *size, Arena<float> ar,
+                                   const double *tpos, const int2 *groups, int64_t ng, int *node) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    const int2 gr = groups[g];
+    double lo[3], hi[3];
+    for (int k = 0; k < 3; k++) lo[k] = hi[k] = tpos[3 * (int64_t)gr.x + k];
+    for (int i = 1; i < gr.y; i++)
+        for (int k = 0; k < 3; k++) {
+            const double v = tpos[3 * ((int64_t)gr.x + i) + k];
+            lo[k] = fmin(lo[k], v);
+            hi[k] = fmax(hi[k], v);
+        }
+    int j = 0;
+    if (!(ar.bad && *ar.bad)) {
+        for (int64_t steps = 0; steps < mtot; steps++) {
+            const int cb = __float_as_int(ar.n_trav[2 * j + 1].z);
+            const int fc = cb >> 4, nc = cb & 15;
+            int nxt = -1;
+            for (int c = fc; c < fc + nc; c++) {
+                if (c < 0 || c >= mtot) break;
+                const double hs = 0.5 * size[ntot + c];
+                bool inside = true;
+                for (int k = 0; k < 3; k++)
+                    inside = inside && lo[k] >= cell[3 * (int64_t)c + k] - hs && hi[k] <= cell[3 * (int64_t)c + k] + hs;
+                if (inside) {
+                    nxt = c;
+                    break;
+                }
+            }
+            if (nxt < 0) break;
+            j = nxt;
+        }
+    }
+    node[g] = j;
+}
+
+}  // namespace
+
+tg_status targets_src_nodes(tg_targets_s *ts, cudaStream_t st) {
+    if (ts->src_node) return TG_OK;
+    tg_tree_s *src = ts->src, *tt = ts->tt;
+    TG_TRY(build_arena(src, src->arena32, st));
+    const int64_t ng = tt->ngroups;
+    TG_CUDA(dev_malloc((void **)&ts->src_node, sizeof(int) * std::max<int64_t>(ng, 1), st));
+    if (ng > 0) {
+        k_target_src_nodes<<<div_up(ng, 128), 128, 0, st>>>(src->ntot, src->mtot, src->cell_center, src->size,
+                                                            src->arena32, tt->coord, tt->groups, ng, ts->src_node);
+        note_launch();
+        TG_CUDA(cudaGetLastError());
+    }
+    return TG_OK;
+}
+
+}  // namespace tg
+
+using namespace tg;
+
+extern "C" {
+
+tg_status tg_targets_create(tg_tree src, const double *pos, const double *h, int64_t n, int group_size, int mem,
+                            void *stream, tg_targets *out) {
+    if (!out) return TG_ERR_BAD_ARG;
+    *out = nullptr;
+    if (!src || !pos || n < 1 || !valid_gs(group_size) || (mem != TG_MEM_HOST && mem != TG_MEM_DEVICE))
+        return TG_ERR_BAD_ARG;
+    if (src->nsys != 1 || src->sys_node_off.empty() || src->sys_node_off[0] != 0) {
+        set_last_error_msg("target sets need a single-system source tree");
+        return TG_ERR_BAD_ARG;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    tg_targets_s *ts = new (std::nothrow) tg_targets_s();
+    if (!ts) return TG_ERR_OOM;
+    ts->src = src;
+    ts->group_size = group_size;
+    ts->n = n;
+    ts->stream = st;
+    // the targets' own octree: positions and softenings, no masses, no moments
+    tg_status rc = tg_tree_build(pos, nullptr, h, n, 0, 0, mem, stream, &ts->tt);
+    if (rc == TG_OK) {
+        tree_wait_built(ts->tt, st);
+        rc = tree_groups(ts->tt, group_size, st);
+    }
+    if (rc != TG_OK) {
+        tg_targets_free(ts);
+        return rc;
+    }
+    *out = ts;
+    return TG_OK;
+}
+
+tg_status tg_targets_free(tg_targets ts) {
+    if (!ts) return TG_OK;
+    if (ts->src_node) cudaFreeAsync(ts->src_node, ts->stream);
+    if (ts->tt) tg_tree_free(ts->tt);
+    delete ts;
+    return TG_OK;
+}
+
+tg_status tg_targets_info(tg_targets ts, int64_t *n, int64_t *ngroups) {
+    if (!ts) return TG_ERR_BAD_ARG;
+    if (n) *n = ts->n;
+    if (ngroups) *ngroups = ts->tt->ngroups;
+    return TG_OK;
+}
+
+tg_status tg_targets_groups_copy(tg_targets ts, int32_t *first, int32_t *count, int32_t *src_node, int64_t *walk_idx,
+                                 int mem, void *stream) {
+    if (!ts || (mem != TG_MEM_HOST && mem != TG_MEM_DEVICE)) return TG_ERR_BAD_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    tg_tree_s *tt = ts->tt;
+    const int64_t ng = tt->ngroups;
+    tree_wait_built(ts->src, st);
+    if (src_node) TG_TRY(targets_src_nodes(ts, st));
+    const cudaMemcpyKind kind = mem == TG_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (first || count) {
+        std::vector<int2> g(ng);
+        TG_CUDA(cudaMemcpyAsync(g.data(), tt->groups, sizeof(int2) * ng, cudaMemcpyDeviceToHost, st));
+        TG_CUDA(cudaStreamSynchronize(st));
+        std::vector<int32_t> a(ng), b(ng);
+        for (int64_t i = 0; i < ng; i++) {
+            a[i] = g[i].x;
+            b[i] = g[i].y;
+        }
+        if (first) TG_CUDA(cudaMemcpyAsync(first, a.data(), sizeof(int32_t) * ng, mem == TG_MEM_HOST ?
+                                           cudaMemcpyHostToHost : cudaMemcpyHostToDevice, st));
+        if (count) TG_CUDA(cudaMemcpyAsync(count, b.data(), sizeof(int32_t) * ng, mem == TG_MEM_HOST ?
+                                           cudaMemcpyHostToHost : cudaMemcpyHostToDevice, st));
+        TG_CUDA(cudaStreamSynchronize(st));
+    }
+    if (src_node) TG_CUDA(cudaMemcpyAsync(src_node, ts->src_node, sizeof(int32_t) * ng, kind, st));
+    if (walk_idx) TG_CUDA(cudaMemcpyAsync(walk_idx, tt->walk_idx, sizeof(int64_t) * ts->n, kind, st));
+    TG_CUDA(cudaStreamSynchronize(st));
+    return TG_OK;
+}
+
+tg_status tg_targets_fields(tg_targets ts, int fields, int quadrupole, double theta, double G, int precision,
+                            const float *tol_per_group, int mem, double *out, void *stream) {
+    if (!ts || !out || (fields & 7) == 0 || (fields & ~7) || !(theta > 0) ||
+        (precision != TG_FP32 && precision != TG_FP64) || (mem != TG_MEM_HOST && mem != TG_MEM_DEVICE))
+        return TG_ERR_BAD_ARG;
+    if (tol_per_group && precision != TG_FP32) return TG_ERR_BAD_ARG;
+    tg_tree_s *src = ts->src, *tt = ts->tt;
+    if (quadrupole && !src->quad) return TG_ERR_NO_QUADRUPOLES;
+    cudaStream_t st = (cudaStream_t)stream;
+    tree_wait_built(src, st);
+    tree_wait_built(tt, st);
+    const int64_t n = ts->n;
+    const int W = width_of(fields);
+    double *dout = out;
+    if (mem == TG_MEM_HOST) TG_CUDA(dev_malloc((void **)&dout, sizeof(double) * n * W, st));
+    tg_status rc = run_walk(src, tt->coord, tt->soft, n, tt->groups, tt->group_root, nullptr, tt->ngroups,
+                            tt->walk_idx, fields, quadrupole, theta, G, ts->group_size, precision, nullptr,
+                            tol_per_group, dout, st);
+    if (rc == TG_OK && mem == TG_MEM_HOST)
+        TG_CUDA(cudaMemcpyAsync(out, dout, sizeof(double) * n * W, cudaMemcpyDeviceToHost, st));
+    if (mem == TG_MEM_HOST) cudaFreeAsync(dout, st);
+    TG_CUDA(cudaStreamSynchronize(st));
+    return rc;
+}
+
+}  // extern "C"

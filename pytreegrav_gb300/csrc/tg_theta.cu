@@ -13,7 +13,7 @@
 
 #include <cuda_bf16.h>
 
-#include "tg_tree.cuh"
+#include "tg_targets.cuh"
 #include "../../include/pytreegrav_gb300_theta.h"
 
 namespace tg {
@@ -115,8 +115,11 @@ __global__ void k_top_records(int64_t ntot, const double *coord, const double *m
 
 // One warp per group (see tg_theta_features for the list), in FP32 on coordinates relative to the
 // root's centre of mass.
+// Targets at tcoord/tsoft (the tree's own particles, or an external target set in its walk order);
+// coord, mass and size are the source tree's, and group_node indexes its nodes.
 __global__ void k_features(int64_t ntot, const double *coord, const double *mass, const double *size,
-                           const double *soft, const int2 *groups, const int *group_node, int64_t ngroups,
+                           const double *tcoord, const double *tsoft, const int2 *groups, const int *group_node,
+                           int64_t ngroups,
                            const float4 *rec, const float *hs2, const int *ntop_p, const float4 *origin, int quad,
                            float log10n, float *feat, unsigned long long *field_sums) {
     const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -131,10 +134,10 @@ __global__ void k_features(int64_t ntot, const double *coord, const double *mass
         const float o[3] = {o4.x, o4.y, o4.z};
         for (int k = 0; k < 3; k++) {  // (hi - o) + lo: the offset from the origin to ~1 float ulp
             float ch, cl;
-            d2f_split(coord[3 * t + k], ch, cl);
+            d2f_split(tcoord[3 * t + k], ch, cl);
             lo[k] = hi[k] = (ch - o[k]) + cl;
         }
-        hm = d2f(soft[t]);
+        hm = d2f(tsoft[t]);
     }
 #pragma unroll
     for (int s = 16; s; s >>= 1) {
@@ -502,15 +505,16 @@ namespace {
 
 using namespace tg;
 
-// Features of every group into feat (ngroups x NF); field_sums (2 x uint64, device, may be NULL)
-// receives the sums behind the tolerance unit.
-tg_status features_device(tg_tree_s *t, int group_size, int quadrupole, float *feat, cudaStream_t st,
-                          unsigned long long *field_sums = nullptr) {
+// Features of ng groups of targets (tcoord/tsoft in walk order; group_node: the source tree's node
+// holding each group) into feat (ng x NF); field_sums (2 x uint64, device, may be NULL) receives the
+// sums behind the tolerance unit.
+tg_status features_of_groups(tg_tree_s *t, const double *tcoord, const double *tsoft, const int2 *groups,
+                             const int *group_node, int64_t ng, int quadrupole, float *feat, cudaStream_t st,
+                             unsigned long long *field_sums) {
     if (t->nsys != 1) {
         set_last_error_msg("learned opening angles need a single-system tree");
         return TG_ERR_BAD_ARG;
     }
-    TG_TRY(tree_groups(t, group_size, st));
     TG_TRY(build_arena(t, t->arena32, st));
     // one scratch block: top count + indices, then the FP32 records and the origin
     const size_t rec_off = 16 * ((sizeof(int) * (TOP_MAX + 1) + 15) / 16);
@@ -525,10 +529,9 @@ tg_status features_device(tg_tree_s *t, int group_size, int quadrupole, float *f
     { k_top_nodes<<<1, 256, 0, st>>>(t->arena32, top + 1, top); note_launch(); }
     { k_top_records<<<div_up(TOP_MAX, 128), 128, 0, st>>>(t->ntot, t->coord, t->mass, t->size, top + 1, top, rec, hs2,
                                                          origin); note_launch(); }
-    const int64_t ng = t->ngroups;
     if (ng > 0) {
-        k_features<<<div_up(ng * 32, 256), 256, 0, st>>>(t->ntot, t->coord, t->mass, t->size, t->soft, t->groups,
-                                                         t->group_node, ng, rec, hs2, top, origin, quadrupole,
+        k_features<<<div_up(ng * 32, 256), 256, 0, st>>>(t->ntot, t->coord, t->mass, t->size, tcoord, tsoft, groups,
+                                                         group_node, ng, rec, hs2, top, origin, quadrupole,
                                                          (float)log10((double)t->ntot), feat, sums);
         note_launch();
     }
@@ -537,10 +540,29 @@ tg_status features_device(tg_tree_s *t, int group_size, int quadrupole, float *f
     return TG_OK;
 }
 
-// field_sums: from features_device; scale: one float of scratch (device).
-tg_status tolerances_device(tg_tree_s *t, const unsigned long long *field_sums, const float *u, float umin, float *tol,
-                            float *scale, cudaStream_t st) {
-    const int64_t ng = t->ngroups;
+// Features of the tree grouping of the tree's own particles (see features_of_groups).
+tg_status features_device(tg_tree_s *t, int group_size, int quadrupole, float *feat, cudaStream_t st,
+                          unsigned long long *field_sums = nullptr) {
+    if (t->nsys != 1) {
+        set_last_error_msg("learned opening angles need a single-system tree");
+        return TG_ERR_BAD_ARG;
+    }
+    TG_TRY(tree_groups(t, group_size, st));
+    return features_of_groups(t, t->coord, t->soft, t->groups, t->group_node, t->ngroups, quadrupole, feat, st,
+                              field_sums);
+}
+
+// Features of an external target set's groups (see features_of_groups).
+tg_status features_targets(tg_targets_s *ts, int quadrupole, float *feat, cudaStream_t st,
+                           unsigned long long *field_sums = nullptr) {
+    TG_TRY(targets_src_nodes(ts, st));
+    return features_of_groups(ts->src, ts->tt->coord, ts->tt->soft, ts->tt->groups, ts->src_node, ts->tt->ngroups,
+                              quadrupole, feat, st, field_sums);
+}
+
+// field_sums: from features_of_groups over the ng groups; scale: one float of scratch (device).
+tg_status tolerances_device(tg_tree_s *t, const unsigned long long *field_sums, const float *u, int64_t ng, float umin,
+                            float *tol, float *scale, cudaStream_t st) {
     if (ng <= 0) return TG_OK;
     { k_tol_scale<<<1, 1, 0, st>>>(field_sums, t->mass, t->size, t->ntot, scale); note_launch(); }
     { k_u_to_tol<<<div_up(ng, 256), 256, 0, st>>>(u, ng, scale, umin, tol); note_launch(); }
@@ -556,6 +578,59 @@ tg_status infer_device(const tg_theta_model_s *m, const float *feat, int64_t n, 
     { k_theta_infer<<<grid, INF_WARPS * 32, 0, st>>>(m->dev, feat, n, loglam, m->tmin, m->tmax, theta); note_launch(); }
     TG_CUDA(cudaGetLastError());
     return TG_OK;
+}
+
+// The walk of ng groups of targets (tpos/tsoft in walk order, results scattered through `scatter`)
+// with each group's acceptance test from the model (see tg_tree_fields_learned); feats(feat, sums)
+// writes the groups' features and the tolerance unit's sums. The source tree t must be built and
+// its FP32 arena packed or packable on st.
+template <typename FeatFn>
+tg_status learned_walk(tg_tree_s *t, FeatFn feats, const double *tpos, const double *tsoft, int64_t nt,
+                       const int2 *groups, const int *groot, int64_t ng, const int64_t *scatter, int fields,
+                       int quadrupole, double G, int group_size, const tg_theta_model_s *m, float log10_lambda,
+                       double theta_fallback, int mem, double *out, cudaStream_t st) {
+    float *tg_theta = nullptr, *feat = nullptr, *tol = nullptr;
+    double theta = theta_fallback;
+    // every device buffer of this call, released on any exit
+    struct Bufs {
+        float **p[3];
+        cudaStream_t st;
+        ~Bufs() {
+            for (float **q : p)
+                if (*q) cudaFreeAsync(*q, st);
+        }
+    } bufs{{&tg_theta, &feat, &tol}, st};
+    if (m) {
+        const int64_t ng1 = std::max<int64_t>(ng, 1);
+        TG_CUDA(dev_malloc((void **)&feat, sizeof(float) * (NF * ng1 + 8), st));
+        TG_CUDA(dev_malloc((void **)&tg_theta, sizeof(float) * ng1, st));
+        unsigned long long *sums = (unsigned long long *)(feat + (NF * ng1 + 1) / 2 * 2);
+        TG_TRY(feats(feat, sums));
+        TG_TRY(infer_device(m, feat, ng, log10_lambda, tg_theta, st));
+        if (m->kind == TG_THETA_KIND_ANGLE) {
+            { k_theta_guard<<<div_up(ng, 256), 256, 0, st>>>(tg_theta, ng, (float)theta_fallback, m->tmin, m->tmax); note_launch(); }
+            TG_CUDA(cudaGetLastError());
+        } else {
+            TG_CUDA(dev_malloc((void **)&tol, sizeof(float) * ng1, st));
+            TG_TRY(tolerances_device(t, sums, tg_theta, ng, m->tmin, tol, (float *)(sums + 2), st));
+            cudaFreeAsync(tg_theta, st);
+            tg_theta = nullptr;
+            theta = m->theta_max;
+        }
+    }
+    const int W = field_width_of(fields);
+    double *dout = out;
+    if (mem == TG_MEM_HOST) TG_CUDA(dev_malloc((void **)&dout, sizeof(double) * nt * W, st));
+    t->err_budget = (m && tol) ? m->err_budget : 0.f;
+    t->rewalk_theta = theta_fallback;
+    tg_status rc = run_walk(t, tpos, tsoft, nt, groups, groot, nullptr, ng, scatter, fields, quadrupole, theta, G,
+                            group_size, TG_FP32, tg_theta, tol, dout, st);
+    t->err_budget = 0.f;
+    if (rc == TG_OK && mem == TG_MEM_HOST)
+        TG_CUDA(cudaMemcpyAsync(out, dout, sizeof(double) * nt * W, cudaMemcpyDeviceToHost, st));
+    if (mem == TG_MEM_HOST) cudaFreeAsync(dout, st);
+    TG_CUDA(cudaStreamSynchronize(st));
+    return rc;
 }
 
 tg_status stage_to_host(const float *src, int64_t n, int mem, std::vector<float> &dst) {
@@ -618,7 +693,7 @@ tg_status tg_theta_model_set_error_budget(tg_theta_model m, float budget) {
 tg_status tg_tree_last_group_error(tg_tree t, float *out, int mem, void *stream) {
     if (!t || !out || !t->gerr) return TG_ERR_BAD_ARG;
     cudaStream_t st = (cudaStream_t)stream;
-    TG_CUDA(cudaMemcpyAsync(out, t->gerr, sizeof(float) * t->ngroups,
+    TG_CUDA(cudaMemcpyAsync(out, t->gerr, sizeof(float) * t->last_stats.groups,
                             mem == TG_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
     TG_CUDA(cudaStreamSynchronize(st));
     return TG_OK;
@@ -627,7 +702,7 @@ tg_status tg_tree_last_group_error(tg_tree t, float *out, int mem, void *stream)
 tg_status tg_tree_last_group_stats(tg_tree t, uint32_t *out, int mem, void *stream) {
     if (!t || !out || !t->gstats) return TG_ERR_BAD_ARG;
     cudaStream_t st = (cudaStream_t)stream;
-    const int64_t ng = t->ngroups;
+    const int64_t ng = t->last_stats.groups;  // the groups of the last walk (tree grouping or a target set)
     TG_CUDA(cudaMemcpyAsync(out, t->gstats, sizeof(uint32_t) * 3 * ng,
                             mem == TG_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
     TG_CUDA(cudaStreamSynchronize(st));
@@ -781,7 +856,7 @@ tg_status tg_theta_tolerances(tg_tree t, int group_size, int quadrupole, const f
     TG_CUDA(dev_malloc((void **)&feat, sizeof(float) * (nfeat + 8), st));
     unsigned long long *sums = (unsigned long long *)(feat + (nfeat + 1) / 2 * 2);
     tg_status rc = features_device(t, group_size, quadrupole, feat, st, sums);
-    if (rc == TG_OK) rc = tolerances_device(t, sums, u, -30.f, tol, (float *)(sums + 2), st);
+    if (rc == TG_OK) rc = tolerances_device(t, sums, u, t->ngroups, -30.f, tol, (float *)(sums + 2), st);
     cudaFreeAsync(feat, st);
     return rc;
 }
@@ -817,42 +892,47 @@ tg_status tg_tree_fields_learned(tg_tree t, int fields, int quadrupole, double G
     cudaStream_t st = (cudaStream_t)stream;
     tree_wait_built(t, st);
     TG_TRY(tree_groups_with_arena(t, group_size, false, st));
-    const int64_t ng = t->ngroups, nt = t->ntot;
-    float *tg_theta = nullptr, *feat = nullptr, *tol = nullptr;
-    double theta = theta_fallback;
-    if (m) {
-        const int64_t ng1 = std::max<int64_t>(ng, 1);
-        TG_CUDA(dev_malloc((void **)&feat, sizeof(float) * (NF * ng1 + 8), st));
-        TG_CUDA(dev_malloc((void **)&tg_theta, sizeof(float) * ng1, st));
-        unsigned long long *sums = (unsigned long long *)(feat + (NF * ng1 + 1) / 2 * 2);
-        TG_TRY(features_device(t, group_size, quadrupole, feat, st, sums));
-        TG_TRY(infer_device(m, feat, ng, log10_lambda, tg_theta, st));
-        if (m->kind == TG_THETA_KIND_ANGLE) {
-            { k_theta_guard<<<div_up(ng, 256), 256, 0, st>>>(tg_theta, ng, (float)theta_fallback, m->tmin, m->tmax); note_launch(); }
-            TG_CUDA(cudaGetLastError());
-        } else {
-            TG_CUDA(dev_malloc((void **)&tol, sizeof(float) * ng1, st));
-            TG_TRY(tolerances_device(t, sums, tg_theta, m->tmin, tol, (float *)(sums + 2), st));
-            cudaFreeAsync(tg_theta, st);
-            tg_theta = nullptr;
-            theta = m->theta_max;
-        }
-    }
-    const int W = field_width_of(fields);
-    double *dout = out;
-    if (mem == TG_MEM_HOST) TG_CUDA(dev_malloc((void **)&dout, sizeof(double) * nt * W, st));
-    t->err_budget = (m && tol) ? m->err_budget : 0.f;
-    t->rewalk_theta = theta_fallback;
-    tg_status rc = run_walk(t, t->coord, t->soft, nt, t->groups, t->group_root, nullptr, ng, t->walk_idx, fields,
-                            quadrupole, theta, G, group_size, TG_FP32, tg_theta, tol, dout, st);
-    t->err_budget = 0.f;
-    if (feat) cudaFreeAsync(feat, st);
-    if (tg_theta) cudaFreeAsync(tg_theta, st);
-    if (tol) cudaFreeAsync(tol, st);
-    if (rc == TG_OK && mem == TG_MEM_HOST)
-        TG_CUDA(cudaMemcpyAsync(out, dout, sizeof(double) * nt * W, cudaMemcpyDeviceToHost, st));
-    if (mem == TG_MEM_HOST) cudaFreeAsync(dout, st);
-    TG_CUDA(cudaStreamSynchronize(st));
+    auto feats = [&](float *feat, unsigned long long *sums) {
+        return features_device(t, group_size, quadrupole, feat, st, sums);
+    };
+    return learned_walk(t, feats, t->coord, t->soft, t->ntot, t->groups, t->group_root, t->ngroups, t->walk_idx,
+                        fields, quadrupole, G, group_size, m, log10_lambda, theta_fallback, mem, out, st);
+}
+
+tg_status tg_targets_fields_learned(tg_targets ts, int fields, int quadrupole, double G, tg_theta_model m,
+                                    float log10_lambda, double theta_fallback, int mem, double *out, void *stream) {
+    if (!ts || !out || (fields & 7) == 0 || (fields & ~7) || !(theta_fallback > 0)) return TG_ERR_BAD_ARG;
+    tg_tree_s *t = ts->src, *tt = ts->tt;
+    if (quadrupole && !t->quad) return TG_ERR_NO_QUADRUPOLES;
+    cudaStream_t st = (cudaStream_t)stream;
+    tree_wait_built(t, st);
+    tree_wait_built(tt, st);
+    auto feats = [&](float *feat, unsigned long long *sums) { return features_targets(ts, quadrupole, feat, st, sums); };
+    return learned_walk(t, feats, tt->coord, tt->soft, ts->n, tt->groups, tt->group_root, tt->ngroups, tt->walk_idx,
+                        fields, quadrupole, G, ts->group_size, m, log10_lambda, theta_fallback, mem, out, st);
+}
+
+tg_status tg_targets_features(tg_targets ts, int quadrupole, float *features, void *stream) {
+    if (!ts || !features) return TG_ERR_BAD_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    tree_wait_built(ts->src, st);
+    tree_wait_built(ts->tt, st);
+    return features_targets(ts, quadrupole, features, st);
+}
+
+tg_status tg_targets_tolerances(tg_targets ts, int quadrupole, const float *u, float *tol, void *stream) {
+    if (!ts || !u || !tol) return TG_ERR_BAD_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    tree_wait_built(ts->src, st);
+    tree_wait_built(ts->tt, st);
+    const int64_t ng = ts->tt->ngroups;
+    float *feat = nullptr;
+    const int64_t nfeat = NF * std::max<int64_t>(ng, 1);
+    TG_CUDA(dev_malloc((void **)&feat, sizeof(float) * (nfeat + 8), st));
+    unsigned long long *sums = (unsigned long long *)(feat + (nfeat + 1) / 2 * 2);
+    tg_status rc = features_targets(ts, quadrupole, feat, st, sums);
+    if (rc == TG_OK) rc = tolerances_device(ts->src, sums, u, ng, -30.f, tol, (float *)(sums + 2), st);
+    cudaFreeAsync(feat, st);
     return rc;
 }
 

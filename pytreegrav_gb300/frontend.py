@@ -13,14 +13,15 @@ Differences a caller can see, all deliberate:
     FP32 for device="cuda", matching what each device meant in pytreegrav.
   * ``grouping`` (keyword, extension): "blocks" (default) groups ``group_size`` consecutive
     Morton-ordered targets per traversal, pytreegrav's grouping, so the accepted node set is
-    pytreegrav's exactly; "tree" takes groups of at most ``group_size`` particles from the tree
-    itself (self-gravity with a freshly built tree only), which never straddle a jump of the Morton
-    curve and is the engine's fast path.
-  * ``learned`` / ``error_ratio`` (keywords, extension; Potential, Accel, TidalTensor, Field):
+    pytreegrav's exactly; "tree" takes groups of at most ``group_size`` particles from a tree -- the
+    freshly built tree itself for self-gravity, or an octree of the external targets -- which never
+    straddle a jump of the Morton curve: the engine's fast path.
+  * ``learned`` / ``error_ratio`` (keywords, extension; every field function and Field):
     ``learned=True`` lets the packaged network set each group's acceptance test (a mass-aware
-    tolerance per group, trained on the GPU against brute force) instead of one global theta, for a
-    freshly built tree; ``error_ratio`` asks for that RMS force error relative to the plain walk at
-    theta = 0.7. See ``pytreegrav_gb300.theta``.
+    tolerance per group, trained on the GPU against brute force) instead of one global theta;
+    ``error_ratio`` asks for that RMS force error relative to the plain walk at theta = 0.7. See
+    ``pytreegrav_gb300.theta``. With external targets (the *Target forms, or a given tree), the
+    targets are grouped by an octree of their own (``TargetSet``), as with ``grouping="tree"``.
   * ``morton_order=False``/``radix=False`` in ConstructTree still build the radix tree (pytreegrav
     documents both builds as giving identical fields on generic data); ``vel`` (the velocity tree
     used only by the correlation functions) is not provided.
@@ -141,21 +142,22 @@ def _self_field(key, pos, m, softening, G, theta, tree, return_tree, method, qua
                               precision=precision, grouping=grouping, learned=learned,
                               error_ratio=error_ratio)[key]
         else:
-            if learned:
-                raise ValueError("learned=True evaluates a freshly built tree (tree=None)")
             _check_tree(tree)
             checkTreeQuadrupoles(tree, quadrupole)
-            # targets sorted by their own Morton order, not the tree's stored permutation
+            # targets sorted by their own Morton order, not the tree's stored permutation (with
+            # grouping="tree" or learned=True, grouped by their own octree)
             res = tree.fields(pos, softening, potential=key == "potential", accel=key == "accel",
                               tidal=key == "tidal", quadrupole=quadrupole, group_size=group_size, theta=theta, G=G,
-                              order="morton", precision=precision)[key]
+                              order="morton", precision=precision, grouping=grouping, learned=learned,
+                              error_ratio=error_ratio)[key]
     if return_tree:
         return res, tree
     return res
 
 
 def _target_field(key, pos_target, pos_source, m_source, softening_target, softening_source, G, theta, tree,
-                  return_tree, method, quadrupole, group_size, precision):
+                  return_tree, method, quadrupole, group_size, precision, grouping="blocks", learned=None,
+                  error_ratio=None):
     valueTestMethod(method)
     if tree is None and (pos_source is None or m_source is None):
         raise ValueError("Must pass either pos_source & m_source or source tree.")
@@ -186,7 +188,8 @@ def _target_field(key, pos_target, pos_source, m_source, softening_target, softe
         checkTreeQuadrupoles(tree, quadrupole)
         res = tree.fields(pos_target, softening_target, potential=key == "potential", accel=key == "accel",
                           tidal=key == "tidal", quadrupole=quadrupole, group_size=group_size, theta=theta, G=G,
-                          order="morton", precision=precision)[key]
+                          order="morton", precision=precision, grouping=grouping, learned=learned,
+                          error_ratio=error_ratio)[key]
     if return_tree:
         return res, tree
     return res
@@ -218,26 +221,29 @@ def TidalTensor(pos, m, softening=None, G=1.0, theta=0.7, tree=None, return_tree
 
 def PotentialTarget(pos_target, pos_source, m_source, softening_target=None, softening_source=None, G=1.0,
                     theta=0.7, tree=None, return_tree=False, parallel=False, method="adaptive", quadrupole=False,
-                    group_size=8, *, precision="fp32"):
+                    group_size=8, *, precision="fp32", grouping="blocks", learned=None,
+                    error_ratio=None):
     """Potential at arbitrary target points from a set of sources (frontend.py:296-418)."""
     return _target_field("potential", pos_target, pos_source, m_source, softening_target, softening_source, G, theta,
-                         tree, return_tree, method, quadrupole, group_size, precision)
+                         tree, return_tree, method, quadrupole, group_size, precision, grouping, learned, error_ratio)
 
 
 def AccelTarget(pos_target, pos_source, m_source, softening_target=None, softening_source=None, G=1.0, theta=0.7,
                 tree=None, return_tree=False, parallel=False, method="adaptive", quadrupole=False, group_size=8, *,
-                precision="fp32"):
+                precision="fp32", grouping="blocks", learned=None,
+                error_ratio=None):
     """Acceleration at arbitrary target points from a set of sources (frontend.py:563-685)."""
     return _target_field("accel", pos_target, pos_source, m_source, softening_target, softening_source, G, theta,
-                         tree, return_tree, method, quadrupole, group_size, precision)
+                         tree, return_tree, method, quadrupole, group_size, precision, grouping, learned, error_ratio)
 
 
 def TidalTensorTarget(pos_target, pos_source, m_source, softening_target=None, softening_source=None, G=1.0,
                       theta=0.7, tree=None, return_tree=False, parallel=False, method="adaptive", quadrupole=False,
-                      group_size=8, *, precision="fp32"):
+                      group_size=8, *, precision="fp32", grouping="blocks", learned=None,
+                      error_ratio=None):
     """Tidal tensor at arbitrary target points from a set of sources (frontend.py:792-901)."""
     return _target_field("tidal", pos_target, pos_source, m_source, softening_target, softening_source, G, theta,
-                         tree, return_tree, method, quadrupole, group_size, precision)
+                         tree, return_tree, method, quadrupole, group_size, precision, grouping, learned, error_ratio)
 
 
 class Field:
@@ -283,7 +289,8 @@ class Field:
         if softening_target is None:
             softening_target = zeros(len(pos_target))
         softening_target = np.atleast_1d(_f64(softening_target))
-        return self.tree.fields(pos_target, softening_target, order="morton", **kw)
+        return self.tree.fields(pos_target, softening_target, order="morton", grouping=self.grouping,
+                                learned=self.learned, error_ratio=self.error_ratio, **kw)
 
     def potential(self, pos_target=None, **kwargs):
         return self.evaluate(potential=True, pos_target=pos_target, **kwargs)["potential"]

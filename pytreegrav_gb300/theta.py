@@ -196,10 +196,14 @@ def features(tree, group_size, quadrupole):
 
 
 def collect(pos, m, h, quadrupole=True, group_size=GROUP_SIZE, sample=0.25, seed=0, G=1.0, label="", kind="tolerance",
-            theta_max=THETA_CAP):
+            theta_max=THETA_CAP, targets=None):
     """Training tables of one particle system (see the module docstring): for every value of the
     kind's grid, each sampled group's cost and squared force error, both relative to the plain
-    walk at theta = 0.7 (summed over the sampled groups, the plain walk's are 1)."""
+    walk at theta = 0.7 (summed over the sampled groups, the plain walk's are 1).
+
+    targets=None: the system's own particles are the targets, in the tree grouping. targets=(pos_t,
+    h_t): external targets, grouped by their own octree (a TargetSet), judged against the same
+    sources (tolerance models only)."""
     import torch
 
     L = _lib.load()
@@ -210,22 +214,45 @@ def collect(pos, m, h, quadrupole=True, group_size=GROUP_SIZE, sample=0.25, seed
     tree, keep = _tree_device(torch, pos, m, h, quadrupole)
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     grid = grid_of(kind)
+    tset = None
     try:
-        first, count, node = groups_of(tree, group_size)
+        if targets is None:
+            first, count, node = groups_of(tree, group_size)
+            walk_idx = np.empty(n, np.int64)
+            _check(L.tg_tree_copy_out(tree, None, None, None, None, None, None, None, None, _lib.ptr(walk_idx),
+                                      None), "copy out")
+            feat = features(tree, group_size, quadrupole)
+            tpos, th_ = pos, h
+            nt = n
+        else:
+            if kind != "tolerance":
+                raise ValueError("external-target tables are made for tolerance models")
+            tpos = np.ascontiguousarray(targets[0], np.float64)
+            th_ = np.ascontiguousarray(targets[1], np.float64)
+            nt = len(tpos)
+            tset = ctypes.c_void_p()
+            _check(L.tg_targets_create(tree, _lib.ptr(tpos), _lib.ptr(th_), nt, group_size, _lib.TG_MEM_HOST, None,
+                                       ctypes.byref(tset)), "target set")
+            ngv = ctypes.c_int64()
+            _check(L.tg_targets_info(tset, None, ctypes.byref(ngv)), "target set")
+            first, count, node = (np.empty(ngv.value, np.int32) for _ in range(3))
+            walk_idx = np.empty(nt, np.int64)
+            _check(L.tg_targets_groups_copy(tset, _lib.ptr(first), _lib.ptr(count), _lib.ptr(node), _lib.ptr(walk_idx),
+                                            _lib.TG_MEM_HOST, None), "target groups")
+            fd = torch.empty((max(ngv.value, 1), NF), dtype=torch.float32, device="cuda")
+            _check(L.tg_targets_features(tset, int(quadrupole), _vp(fd), st), "target features")
+            torch.cuda.synchronize()
+            feat = fd[:ngv.value].cpu().numpy()
         ng = len(first)
-        walk_idx = np.empty(n, np.int64)
-        _check(L.tg_tree_copy_out(tree, None, None, None, None, None, None, None, None, _lib.ptr(walk_idx), None),
-               "copy out")
-        feat = features(tree, group_size, quadrupole)
         rng = np.random.default_rng(seed)
         S = np.sort(rng.choice(ng, size=max(1, int(sample * ng)), replace=False))
         seg = np.concatenate([[0], np.cumsum(count[S])])
-        targets = np.concatenate([np.arange(first[g], first[g] + count[g]) for g in S])
-        idx = walk_idx[targets]
-        # judge: FP32 Kahan-compensated direct sum over all sources
+        sel = np.concatenate([np.arange(first[g], first[g] + count[g]) for g in S])
+        idx = walk_idx[sel]
+        # judge: FP32 Kahan-compensated direct sum over all sources (self pairs at r == 0 skipped)
         t0 = time.time()
-        dpt = torch.from_numpy(pos[idx]).cuda()
-        dht = torch.from_numpy(h[idx]).cuda()
+        dpt = torch.from_numpy(np.ascontiguousarray(tpos[idx])).cuda()
+        dht = torch.from_numpy(np.ascontiguousarray(th_[idx])).cuda()
         aref = torch.empty((len(idx), 3), dtype=torch.float64, device="cuda")
         _check(L.tg_bruteforce(_vp(dpt), _vp(dht), len(idx), _vp(keep[0]), _vp(keep[1]), _vp(keep[2]), n,
                                _lib.TG_FIELD_ACCEL, 0, G, _lib.TG_FP32, _lib.TG_MEM_DEVICE, _vp(aref), st),
@@ -234,7 +261,7 @@ def collect(pos, m, h, quadrupole=True, group_size=GROUP_SIZE, sample=0.25, seed
         t_bf = time.time() - t0
         aref_h = aref.cpu().numpy()
         rms2 = float(np.mean(np.sum(aref_h ** 2, axis=1)))
-        out = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+        out = torch.empty((nt, 3), dtype=torch.float64, device="cuda")
         didx = torch.from_numpy(idx).cuda()
         stats = np.empty((ng, 3), np.uint32)
         u = torch.empty(max(ng, 1), dtype=torch.float32, device="cuda")
@@ -242,14 +269,17 @@ def collect(pos, m, h, quadrupole=True, group_size=GROUP_SIZE, sample=0.25, seed
         _check(L.tg_tree_record_group_stats(tree, 1), "record")
 
         def measure(angle, tol_dev=None):
-            if tol_dev is None:
+            tp = None if tol_dev is None else _vp(tol_dev)
+            if tset is not None:
+                _check(L.tg_targets_fields(tset, _lib.TG_FIELD_ACCEL, int(quadrupole), float(angle), G, _lib.TG_FP32,
+                                           tp, _lib.TG_MEM_DEVICE, _vp(out), st), "target walk")
+            elif tol_dev is None:
                 _check(L.tg_tree_fields(tree, None, None, n, _lib.TG_FIELD_ACCEL, int(quadrupole), float(angle), G,
                                         group_size, _lib.TG_GROUP_TREE, _lib.TG_ORDER_TREE, _lib.TG_FP32, None,
                                         _lib.TG_MEM_DEVICE, _vp(out), st), "walk")
             else:
                 _check(L.tg_tree_fields_grouped(tree, _lib.TG_FIELD_ACCEL, int(quadrupole), G, group_size,
-                                                float(angle), None, _vp(tol_dev), _lib.TG_MEM_DEVICE, _vp(out), st),
-                       "walk")
+                                                float(angle), None, tp, _lib.TG_MEM_DEVICE, _vp(out), st), "walk")
             _check(L.tg_tree_last_group_stats(tree, _lib.ptr(stats), _lib.TG_MEM_HOST, st), "group stats")
             a = out.index_select(0, didx).cpu().numpy()
             d2 = np.sum((a - aref_h) ** 2, axis=1) / rms2
@@ -263,16 +293,23 @@ def collect(pos, m, h, quadrupole=True, group_size=GROUP_SIZE, sample=0.25, seed
                 cost[:, k], err[:, k] = measure(v)
             else:
                 u.fill_(float(v))
-                _check(L.tg_theta_tolerances(tree, group_size, int(quadrupole), _vp(u), _vp(tol), st), "tolerances")
+                if tset is not None:
+                    _check(L.tg_targets_tolerances(tset, int(quadrupole), _vp(u), _vp(tol), st), "tolerances")
+                else:
+                    _check(L.tg_theta_tolerances(tree, group_size, int(quadrupole), _vp(u), _vp(tol), st),
+                           "tolerances")
                 cost[:, k], err[:, k] = measure(theta_max, tol)
         _check(L.tg_tree_record_group_stats(tree, 0), "record")
     finally:
+        if tset is not None:
+            L.tg_targets_free(tset)
         L.tg_tree_free(tree)
     c0, e0 = c_plain.sum(), e_plain.sum()
     floor = 1e-6 / len(S)
     return dict(label=label, kind=kind, n=n, ngroups=ng, sampled=len(S), features=feat[S],
                 log_cost=np.log(cost / c0).astype(np.float32), log_err=np.log(err / e0 + floor).astype(np.float32),
-                plain_rms_rel=float(np.sqrt(e0 / len(idx))), bf_seconds=t_bf, quadrupole=bool(quadrupole))
+                plain_rms_rel=float(np.sqrt(e0 / len(idx))), bf_seconds=t_bf, quadrupole=bool(quadrupole),
+                targets=targets is not None)
 
 
 # ---------------------------------------------------------------------------------------------
@@ -383,13 +420,21 @@ def predicted_ratios(model, d, log10_lambda):
     return float(np.sqrt(table_at(d["log_err"], th, g).sum())), float(table_at(d["log_cost"], th, g).sum())
 
 
+MODES = ((True, False), (False, False), (True, True), (False, True))  # (quadrupole, external targets)
+
+
+def _lambda_key(quadrupole, targets):
+    return "log10_lambda" + ("_targets" if targets else "") + ("" if quadrupole else "_mono")
+
+
 def calibrate(model, datasets, target_ratio=0.85, grid=None):
     """Error-ratio curves of the training systems over a lambda grid, stored in the model; the
-    default lambda of each multipole order is the smallest (cheapest) one at which the median
-    error ratio of that order's systems is within target_ratio. Returns the per-system (error,
-    cost) ratios at the chosen lambdas."""
+    default lambda of each mode -- multipole order, and own particles or external targets as the
+    targets -- is the smallest (cheapest) one at which the median error ratio of that mode's systems
+    is within target_ratio. Returns the per-system (error, cost) ratios at the chosen lambdas."""
     grid = np.arange(LOG10_LAMBDA_RANGE[0], LOG10_LAMBDA_RANGE[1] + 1e-9, 0.05) if grid is None else grid
-    curves = {d["label"]: dict(quadrupole=d["quadrupole"], error=[], cost=[]) for d in datasets}
+    curves = {d["label"]: dict(quadrupole=d["quadrupole"], targets=bool(d.get("targets", False)), error=[], cost=[])
+              for d in datasets}
     for l10 in grid:
         for d in datasets:
             e, c = predicted_ratios(model, d, l10)
@@ -397,33 +442,45 @@ def calibrate(model, datasets, target_ratio=0.85, grid=None):
             curves[d["label"]]["cost"].append(c)
     model.meta["calibration"] = dict(grid=[float(g) for g in grid], target_ratio=target_ratio, systems=curves)
     chosen = {}
-    for quad in (True, False):
-        l10 = lambda_for_ratio(model, target_ratio, quad)
+    for quad, tgt in MODES:
+        l10 = lambda_for_ratio(model, target_ratio, quad, tgt)
         if l10 is not None:
-            chosen[quad] = l10
-    model.log10_lambda = chosen.get(True, chosen.get(False, 0.0))
-    model.meta["log10_lambda_mono"] = chosen.get(False, model.log10_lambda)
+            chosen[(quad, tgt)] = l10
+            model.meta[_lambda_key(quad, tgt)] = l10
+    model.log10_lambda = chosen.get((True, False), 0.0)
     out = []
     for d in datasets:
-        out.append(predicted_ratios(model, d, chosen.get(d["quadrupole"], model.log10_lambda)))
+        out.append(predicted_ratios(model, d, default_lambda(model, d["quadrupole"], d.get("targets", False))))
     return out
 
 
-def lambda_for_ratio(model, ratio, quadrupole):
-    """log10 lambda at which the median training system of this multipole order is predicted to
-    reach `ratio` times the plain walk's RMS force error (None without calibration curves)."""
+def lambda_for_ratio(model, ratio, quadrupole, targets=False):
+    """log10 lambda at which the median training system of this mode (multipole order; own particles
+    or external targets) is predicted to reach `ratio` times the plain walk's RMS force error (None
+    without calibration curves). Systems of the other target kind stand in when a mode has none."""
     cal = model.meta.get("calibration")
     if not cal:
         return None
-    sys_ = [v for v in cal["systems"].values() if v["quadrupole"] == bool(quadrupole)] or list(cal["systems"].values())
+    allv = list(cal["systems"].values())
+    sys_ = [v for v in allv if v["quadrupole"] == bool(quadrupole) and v.get("targets", False) == bool(targets)]
+    sys_ = sys_ or [v for v in allv if v.get("targets", False) == bool(targets)]
+    sys_ = sys_ or [v for v in allv if v["quadrupole"] == bool(quadrupole)] or allv
     med = np.median(np.array([v["error"] for v in sys_]), axis=0)
     grid = np.array(cal["grid"])
     ok = np.nonzero(med <= ratio)[0]
     return float(grid[ok[0]]) if len(ok) else float(grid[-1])
 
 
-def default_lambda(model, quadrupole):
-    return model.log10_lambda if quadrupole else float(model.meta.get("log10_lambda_mono", model.log10_lambda))
+def default_lambda(model, quadrupole, targets=False):
+    """The calibrated log10 lambda of a mode (see calibrate)."""
+    if quadrupole and not targets:
+        return model.log10_lambda
+    v = model.meta.get(_lambda_key(quadrupole, targets))
+    if v is None and targets:  # a model calibrated on own-particle systems only
+        v = model.meta.get(_lambda_key(quadrupole, False))
+    if v is None:
+        v = model.log10_lambda
+    return float(v)
 
 
 # ---------------------------------------------------------------------------------------------
@@ -431,16 +488,17 @@ def default_lambda(model, quadrupole):
 
 
 def training_systems(scale=1.0):
-    """(label, positions, softening, quadrupole) of the synthetic training systems. The seeds are
-    not the benchmark's, so the benchmark system is held out."""
+    """(label, positions, softening, quadrupole) of the synthetic training systems whose own particles
+    are the targets. The seeds are not the benchmark's, so the benchmark systems are held out."""
     from . import synthetic as S
 
-    n0, n1, n2, n3 = (int(v * scale) for v in (2_000_000, 1_000_000, 500_000, 250_000))
+    n4, n0, n1, n2, n3 = (int(v * scale) for v in (4_000_000, 2_000_000, 1_000_000, 500_000, 250_000))
     return [
         ("plummer_2e6_q", S.plummer(n0, 112), 0.005, True),
         ("plummer_1e6_q", S.plummer(n1, 101), 0.005, True),
         ("plummer_5e5_q", S.plummer(n2, 102), 0.005, True),
         ("plummer_2.5e5_q", S.plummer(n3, 109), 0.005, True),
+        ("clustered_4e6_q", S.clustered(n4, 113), 0.002, True),
         ("clustered_1e6_q", S.clustered(n1, 103), 0.002, True),
         ("clustered_5e5_q", S.clustered(n2, 104), 0.002, True),
         ("clustered_2.5e5_q", S.clustered(n3, 110), 0.002, True),
@@ -449,6 +507,36 @@ def training_systems(scale=1.0):
         ("plummer_2.5e5_m", S.plummer(n3, 111), 0.005, False),
         ("clustered_1e6_m", S.clustered(n1, 107), 0.002, False),
         ("uniform_5e5_m", S.uniform(n2, 108), 0.01, False),
+    ]
+
+
+def target_systems(scale=1.0):
+    """(label, source positions, source softenings, target positions, target softenings, quadrupole) of
+    the synthetic training systems with external targets: Plummer sources with lognormal softenings
+    and targets uniform in a ball of radius 5, or drawn from the sources' own distribution; clustered
+    sources with targets uniform in their box; uniform sources with uniform targets."""
+    from . import synthetic as S
+
+    def ball(k, seed, radius=5.0):
+        rng = np.random.default_rng(seed)
+        d = rng.normal(size=(k, 3))
+        d /= np.linalg.norm(d, axis=1)[:, None]
+        return d * (radius * rng.random(k) ** (1 / 3))[:, None]
+
+    def lognormal_h(k, seed):
+        return np.exp(np.random.default_rng(seed).normal(np.log(0.003), 0.7, k))
+
+    n4, n1, n2 = (int(v * scale) for v in (4_000_000, 1_000_000, 500_000))
+    t2, t1 = (int(v * scale) for v in (250_000, 100_000))
+    return [
+        ("plummer_4e6_ball_q", S.plummer(n4, 201), lognormal_h(n4, 202), ball(t2, 203), np.zeros(t2), True),
+        ("plummer_1e6_ball_q", S.plummer(n1, 204), lognormal_h(n1, 205), ball(t2, 206), np.zeros(t2), True),
+        ("plummer_5e5_self_dist_q", S.plummer(n2, 207), np.full(n2, 0.005), S.plummer(t1, 208), np.full(t1, 0.005),
+         True),
+        ("clustered_1e6_box_q", S.clustered(n1, 209), np.full(n1, 0.002),
+         np.random.default_rng(210).uniform(-10, 10, (t2, 3)), np.zeros(t2), True),
+        ("uniform_5e5_cube_q", S.uniform(n2, 211), np.full(n2, 0.01), S.uniform(t1, 212), np.zeros(t1), True),
+        ("plummer_1e6_ball_m", S.plummer(n1, 213), lognormal_h(n1, 214), ball(t2, 215), np.zeros(t2), False),
     ]
 
 
@@ -478,13 +566,50 @@ def group_errors(model, pos, h, quadrupole, log10_lambda=None, G=1.0):
     return eta
 
 
-def calibrate_error_budget(model, systems, factor=2.0):
-    """The error budget: `factor` times the largest per-group estimate seen on the training systems at
-    the model's calibrated lambda, so that only groups outside anything met in training (a network
-    asked about inputs unlike its data) are walked again at the global theta. Sets and returns it."""
+def target_group_errors(model, pos, h, pos_t, h_t, quadrupole, log10_lambda=None, G=1.0):
+    """group_errors for external targets (a TargetSet of the sources' tree, m = 1/N)."""
+    import torch
+
+    n = len(pos)
+    L = _lib.load()
+    tree, keep = _tree_device(torch, pos, np.full(n, 1.0 / n), h, quadrupole)
+    handle = model.handle()
+    tset = ctypes.c_void_p()
+    try:
+        pt = np.ascontiguousarray(pos_t, np.float64)
+        ht = np.ascontiguousarray(h_t, np.float64)
+        _check(L.tg_targets_create(tree, _lib.ptr(pt), _lib.ptr(ht), len(pt), GROUP_SIZE, _lib.TG_MEM_HOST, None,
+                                   ctypes.byref(tset)), "target set")
+        _check(L.tg_tree_record_group_stats(tree, 1), "group stats")
+        _check(L.tg_theta_model_set_error_budget(handle, 0.0), "error budget")
+        l10 = default_lambda(model, quadrupole, True) if log10_lambda is None else float(log10_lambda)
+        out = torch.empty((len(pt), 3), dtype=torch.float64, device="cuda")
+        st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        _check(L.tg_targets_fields_learned(tset, _lib.TG_FIELD_ACCEL, int(quadrupole), float(G), handle, float(l10),
+                                           0.7, _lib.TG_MEM_DEVICE, _vp(out), st), "learned target walk")
+        ng = ctypes.c_int64()
+        _check(L.tg_targets_info(tset, None, ctypes.byref(ng)), "target set")
+        eta = np.empty(ng.value, np.float32)
+        _check(L.tg_tree_last_group_error(tree, _lib.ptr(eta), _lib.TG_MEM_HOST, st), "group error")
+    finally:
+        _check(L.tg_theta_model_set_error_budget(handle, model.error_budget), "error budget")
+        if tset.value:
+            L.tg_targets_free(tset)
+        L.tg_tree_free(tree)
+    return eta
+
+
+def calibrate_error_budget(model, systems, factor=2.0, targets=()):
+    """The error budget: `factor` times the largest per-group estimate seen on the training systems
+    (own particles and external targets) at the model's calibrated lambdas, so that only groups
+    outside anything met in training (a network asked about inputs unlike its data) are walked again
+    at the global theta. Sets and returns it."""
     worst = 0.0
     for _, x, soft, quad in systems:
         eta = group_errors(model, x, soft, quad)
+        worst = max(worst, float(np.max(eta)) if len(eta) else 0.0)
+    for _, x, h, xt, ht, quad in targets:
+        eta = target_group_errors(model, x, h, xt, ht, quad)
         worst = max(worst, float(np.max(eta)) if len(eta) else 0.0)
     model.error_budget = factor * worst
     return model.error_budget
@@ -509,7 +634,7 @@ def main(argv=None):
     args = ap.parse_args(argv)
     if args.budget_only:
         model = ThetaModel.load(args.out)
-        budget = calibrate_error_budget(model, training_systems(args.scale))
+        budget = calibrate_error_budget(model, training_systems(args.scale), targets=target_systems(args.scale))
         model.save(args.out)
         print(json.dumps(dict(out=args.out, error_budget=budget)))
         return model
@@ -522,6 +647,14 @@ def main(argv=None):
         datasets.append(d)
         print(f"{label}: {d['ngroups']} groups, {d['sampled']} judged, plain RMS rel error {d['plain_rms_rel']:.3e}, "
               f"brute force {d['bf_seconds']:.2f} s", file=sys.stderr)
+    if args.kind == "tolerance":
+        for label, x, h, xt, ht, quad in target_systems(args.scale):
+            n = len(x)
+            d = collect(x, np.full(n, 1.0 / n), h, quadrupole=quad, sample=args.sample, seed=args.seed + len(datasets),
+                        label=label, kind=args.kind, theta_max=args.theta_max, targets=(xt, ht))
+            datasets.append(d)
+            print(f"{label}: {d['ngroups']} target groups, {d['sampled']} judged, plain RMS rel error "
+                  f"{d['plain_rms_rel']:.3e}, brute force {d['bf_seconds']:.2f} s", file=sys.stderr)
     t1 = time.time()
     if args.save_data:
         np.savez(args.save_data, **{f"{d['label']}/{k}": d[k] for d in datasets
@@ -530,12 +663,13 @@ def main(argv=None):
                   theta_max=args.theta_max)
     t2 = time.time()
     ratios = calibrate(model, datasets, target_ratio=args.target_ratio)
-    budget = calibrate_error_budget(model, training_systems(args.scale)) if model.kind == "tolerance" else 0.0
+    budget = (calibrate_error_budget(model, training_systems(args.scale), targets=target_systems(args.scale))
+              if model.kind == "tolerance" else 0.0)
     model.meta.update(collect_seconds=t1 - t0, train_seconds=t2 - t1, target_ratio=args.target_ratio)
     os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
     model.save(args.out)
     summary = dict(out=args.out, kind=model.kind, theta_max=model.theta_max, log10_lambda=model.log10_lambda,
-                   error_budget=budget,
+                   error_budget=budget, lambdas={_lambda_key(q, t): model.meta.get(_lambda_key(q, t)) for q, t in MODES},
                    ratios={d["label"]: dict(error=e, cost=c, speedup=1.0 / c) for d, (e, c) in zip(datasets, ratios)},
                    collect_s=round(t1 - t0, 1), train_s=round(t2 - t1, 1))
     print(json.dumps(summary))

@@ -145,14 +145,26 @@ class Octree:
         order="tree": the tree's own particles are the targets (pos/soft ignored); "morton": targets
         are Morton-sorted by their own bounding cube before grouping; "given": grouped as passed.
         grouping="blocks": group_size consecutive targets per group (pytreegrav's grouping);
-        "tree": groups taken from the tree (order="tree" only).
+        "tree": groups taken from the tree (order="tree"), or, for order="morton", from an octree
+        of the targets themselves (see TargetSet).
         learned (extension): True for the packaged opening-angle model, a path or a
         theta.ThetaModel -- the acceptance test of each group then comes from the network
-        (order="tree", tree grouping of 32, FP32); error_ratio asks for that RMS force error
+        (tree grouping of 32, FP32; order="tree", or order="morton" through a TargetSet);
+        error_ratio asks for that RMS force error
         relative to the plain walk at theta = 0.7 (default: the model's calibrated lambda), and
         `theta` is the fallback angle.
         Results come back in the caller's order (the tree's input order for order="tree").
         """
+        if order == "morton" and ((learned is not None and learned is not False) or grouping == "tree"):
+            # external targets grouped by their own octree (tg_targets_*)
+            ts = TargetSet(self, pos, soft, group_size=32 if learned not in (None, False) else group_size)
+            try:
+                if learned is not None and learned is not False:
+                    return ts.fields_learned(potential, accel, tidal, quadrupole, theta, G, precision, learned,
+                                             error_ratio)
+                return ts.fields(potential, accel, tidal, quadrupole, theta, G, precision)
+            finally:
+                ts.close()
         if learned is not None and learned is not False:
             return self._fields_learned(potential, accel, tidal, quadrupole, theta, G, order, precision, learned,
                                         error_ratio)
@@ -199,17 +211,7 @@ class Octree:
             raise ValueError("request at least one of potential=True, accel=True, tidal=True")
         if quadrupole and not self.HasQuads:
             _lib.check(_lib.TG_ERR_NO_QUADRUPOLES)
-        if isinstance(learned, th.ThetaModel):
-            model = learned
-        else:
-            model = _MODELS.get(learned)
-            if model is None:  # loaded and uploaded once per process, shared by every tree
-                model = th.ThetaModel.load(None if learned is True else learned)
-                _MODELS[learned] = model
-        l10 = (th.default_lambda(model, quadrupole) if error_ratio is None
-               else th.lambda_for_ratio(model, float(error_ratio), quadrupole))
-        if l10 is None:
-            l10 = th.default_lambda(model, quadrupole)
+        model, l10 = _model_and_lambda(learned, error_ratio, quadrupole)
         W = int(bool(potential)) + 3 * int(bool(accel)) + 9 * int(bool(tidal))
         out = np.empty((self.NumParticles, W))
         rc = _lib.load().tg_tree_fields_learned(self._h, fields, int(bool(quadrupole)), float(G), th.GROUP_SIZE,
@@ -271,6 +273,116 @@ class Octree:
         v = [ctypes.c_int64() for _ in range(4)]
         _lib.check(_lib.load().tg_tree_last_walk_stats(self._h, *[ctypes.byref(x) for x in v]))
         return tuple(int(x.value) for x in v)
+
+
+def _model_and_lambda(learned, error_ratio, quadrupole, targets=False):
+    """The ThetaModel named by `learned` (True: the packaged model; a path; or a model) and the log10
+    lambda that gives `error_ratio` (None: the model's calibrated default) for the tree's own
+    particles or, with targets=True, for external targets."""
+    from . import theta as th
+
+    if isinstance(learned, th.ThetaModel):
+        model = learned
+    else:
+        model = _MODELS.get(learned)
+        if model is None:  # loaded and uploaded once per process, shared by every tree
+            model = th.ThetaModel.load(None if learned is True else learned)
+            _MODELS[learned] = model
+    l10 = (th.default_lambda(model, quadrupole, targets) if error_ratio is None
+           else th.lambda_for_ratio(model, float(error_ratio), quadrupole, targets))
+    if l10 is None:
+        l10 = th.default_lambda(model, quadrupole, targets)
+    return model, l10
+
+
+class TargetSet:
+    """External target points prepared once for walks of one source tree (tg_targets_*; no
+    counterpart in pytreegrav, which groups the Morton-sorted targets in consecutive blocks of
+    group_size, grouped_treewalk.py:269-275). The targets get an octree of their own and are grouped
+    by it: subtrees and runs of siblings of at most group_size targets, so that no group straddles a
+    jump of the Morton curve. Results come back in the caller's order."""
+
+    def __init__(self, tree, pos, soft=None, group_size=32):
+        self.tree = tree  # the source tree must outlive the set
+        pos = _as_f64(pos, (-1, 3))
+        n = len(pos)
+        soft = np.zeros(n) if soft is None else _as_f64(soft, (n,))
+        self.n = n
+        self.group_size = int(group_size)
+        self._h = ctypes.c_void_p()
+        if n:
+            _lib.check(_lib.load().tg_targets_create(tree._h, _lib.ptr(pos), _lib.ptr(soft), n, self.group_size,
+                                                     _lib.TG_MEM_HOST, None, ctypes.byref(self._h)), "target set")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def ngroups(self):
+        ng = ctypes.c_int64()
+        if self._h.value:
+            _lib.check(_lib.load().tg_targets_info(self._h, None, ctypes.byref(ng)), "target set")
+        return int(ng.value)
+
+    def groups(self):
+        """(first, count, source node) per group (int32) and each walk-order target's caller index."""
+        ng = self.ngroups()
+        first, count, node = (np.empty(ng, np.int32) for _ in range(3))
+        widx = np.empty(self.n, np.int64)
+        if self.n:
+            _lib.check(_lib.load().tg_targets_groups_copy(self._h, _lib.ptr(first), _lib.ptr(count), _lib.ptr(node),
+                                                          _lib.ptr(widx), _lib.TG_MEM_HOST, None), "target groups")
+        return first, count, node, widx
+
+    def fields(self, potential=False, accel=False, tidal=False, quadrupole=False, theta=0.7, G=1.0, precision="fp32"):
+        fields = (_lib.TG_FIELD_POTENTIAL * bool(potential) + _lib.TG_FIELD_ACCEL * bool(accel)
+                  + _lib.TG_FIELD_TIDAL * bool(tidal))
+        if fields == 0:
+            raise ValueError("request at least one of potential=True, accel=True, tidal=True")
+        if quadrupole and not self.tree.HasQuads:
+            _lib.check(_lib.TG_ERR_NO_QUADRUPOLES)
+        W = int(bool(potential)) + 3 * int(bool(accel)) + 9 * int(bool(tidal))
+        out = np.empty((self.n, W))
+        if self.n:
+            prec = {"fp32": _lib.TG_FP32, "fp64": _lib.TG_FP64}[precision]
+            _lib.check(_lib.load().tg_targets_fields(self._h, fields, int(bool(quadrupole)), float(theta), float(G),
+                                                     prec, None, _lib.TG_MEM_HOST, _lib.ptr(out), None),
+                       "target walk")
+        return _split(out, potential, accel, tidal)
+
+    def fields_learned(self, potential=False, accel=False, tidal=False, quadrupole=False, theta=0.7, G=1.0,
+                       precision="fp32", learned=True, error_ratio=None):
+        """The walk with each group's acceptance test from the learned model (see Octree.fields);
+        theta is the fallback angle."""
+        if precision != "fp32":
+            raise ValueError("the learned opening test runs the FP32 walk")
+        fields = (_lib.TG_FIELD_POTENTIAL * bool(potential) + _lib.TG_FIELD_ACCEL * bool(accel)
+                  + _lib.TG_FIELD_TIDAL * bool(tidal))
+        if fields == 0:
+            raise ValueError("request at least one of potential=True, accel=True, tidal=True")
+        if quadrupole and not self.tree.HasQuads:
+            _lib.check(_lib.TG_ERR_NO_QUADRUPOLES)
+        model, l10 = _model_and_lambda(learned, error_ratio, quadrupole, targets=True)
+        W = int(bool(potential)) + 3 * int(bool(accel)) + 9 * int(bool(tidal))
+        out = np.empty((self.n, W))
+        if self.n:
+            _lib.check(_lib.load().tg_targets_fields_learned(self._h, fields, int(bool(quadrupole)), float(G),
+                                                             model.handle(), float(l10), float(theta),
+                                                             _lib.TG_MEM_HOST, _lib.ptr(out), None),
+                       "learned target walk")
+        return _split(out, potential, accel, tidal)
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.load().tg_targets_free(h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class WalkGraph:

@@ -209,8 +209,8 @@ def test_shipped_model_error_budget_rewalks_few_groups(env, plummer_tree):
 @pytest.mark.parametrize("quad", [1, 0])
 def test_shipped_model_beats_the_plain_walk_at_equal_error(env, quad):
     """On a Plummer system outside the training set, the learned walk at the model's default
-    lambda keeps the plain theta = 0.7 walk's RMS force error (FP32 brute force judge) with far
-    fewer interactions."""
+    lambda keeps the plain theta = 0.7 walk's RMS force error (FP64 brute force judge) with at most
+    0.6 of its interactions."""
     torch, _lib, L, theta = env
     if not os.path.exists(theta.DEFAULT_MODEL):
         pytest.skip("no trained model in the package")
@@ -226,7 +226,7 @@ def test_shipped_model_beats_the_plain_walk_at_equal_error(env, quad):
         ht = dev(torch, np.full(len(idx), 0.005), np.float64)
         ref = torch.empty((len(idx), 3), dtype=torch.float64, device="cuda")
         assert L.tg_bruteforce(vp(pt), vp(ht), len(idx), vp(keep[0]), vp(keep[1]), vp(keep[2]), n,
-                               _lib.TG_FIELD_ACCEL, 0, 1.0, _lib.TG_FP32, _lib.TG_MEM_DEVICE, vp(ref), None) == 0
+                               _lib.TG_FIELD_ACCEL, 0, 1.0, _lib.TG_FP64, _lib.TG_MEM_DEVICE, vp(ref), None) == 0
         ref = ref.cpu().numpy()
         rms = np.sqrt(np.mean(np.sum(ref ** 2, 1)))
         out = torch.empty((n, 3), dtype=torch.float64, device="cuda")
@@ -248,29 +248,46 @@ def test_shipped_model_beats_the_plain_walk_at_equal_error(env, quad):
     finally:
         L.tg_tree_free(tree)
         model.close()
-    assert e_learned <= 1.15 * e_plain, (e_learned, e_plain)
-    assert i_learned <= 0.7 * i_plain, (i_learned, i_plain)
+    assert e_learned <= e_plain, (e_learned, e_plain)
+    # monopole walks gain less (their error falls off one order slower with distance)
+    assert i_learned <= (0.6 if quad else 0.75) * i_plain, (i_learned, i_plain)
 
 
-def test_frontend_learned_keyword(env):
+def test_training_loop_end_to_end(env):
+    """theta.collect + theta.train + theta.calibrate on three small systems (a Plummer sphere, a
+    clustered mixture and a uniform cube, 2e5 particles each): the loss falls, and the trained model,
+    on a held-out Plummer system, stays within 1.25x the plain theta = 0.7 walk's RMS force error
+    (FP64 brute force judge) with at most 0.85 of its interactions."""
     torch, _lib, L, theta = env
-    if not os.path.exists(theta.DEFAULT_MODEL):
-        pytest.skip("no trained model in the package")
     import pytreegrav_gb300 as pg
     from pytreegrav_gb300 import synthetic
 
-    n = 50_000
-    x = synthetic.plummer(n, 12)
+    k = 200_000
+    systems = [("plummer", synthetic.plummer(k, 301), 0.005), ("clustered", synthetic.clustered(k, 302), 0.002),
+               ("uniform", synthetic.uniform(k, 304), 0.01)]
+    data = [theta.collect(x, np.full(len(x), 1.0 / len(x)), np.full(len(x), soft), quadrupole=True, sample=0.5,
+                          seed=i, label=label) for i, (label, x, soft) in enumerate(systems)]
+    model = theta.train(data, steps=1500, batch=8192, log_every=100, verbose=False)
+    hist = [v for _, v in model.meta["history"]]
+    ratios = theta.calibrate(model, data, target_ratio=1.0)
+    n = 200_000
+    x = synthetic.plummer(n, 303)
     m = np.full(n, 1.0 / n)
     h = np.full(n, 0.005)
-    a_plain = pg.Accel(x, m, h, quadrupole=True, method="tree")
-    a_learn = pg.Accel(x, m, h, quadrupole=True, method="tree", learned=True)
-    a_tight = pg.Accel(x, m, h, quadrupole=True, method="tree", learned=True, error_ratio=0.3)
-    ref = pg.AccelTarget(x[:2000], x, m, h[:2000], h, method="bruteforce")
+    samp = np.random.default_rng(4).choice(n, 3000, replace=False)
+    ref = pg.bruteforce(x[samp], h[samp], x, m, h, accel=True, precision="fp64")["accel"]
     rms = np.sqrt(np.mean(np.sum(ref ** 2, 1)))
-    e = [np.sqrt(np.mean(np.sum((a[:2000] - ref) ** 2, 1))) / rms for a in (a_plain, a_learn, a_tight)]
-    assert e[1] < 2e-3 and e[2] < e[1]
-    f = pg.Field(x, m, h, quadrupole=True, learned=True)
-    assert np.allclose(f.accel(), a_learn, rtol=0, atol=0)
-    with pytest.raises(ValueError):
-        pg.Accel(x, m, h, quadrupole=True, method="tree", learned=True, tree=pg.ConstructTree(x, m, h, quadrupole=True))
+    tree = pg.ConstructTree(x, m, h, quadrupole=True)
+    plain = tree.fields(accel=True, quadrupole=True, theta=0.7, group_size=32, grouping="tree")["accel"]
+    i_plain = tree.last_walk_stats()[0]
+    learned = tree.fields(accel=True, quadrupole=True, theta=0.7, learned=model)["accel"]
+    i_learned = tree.last_walk_stats()[0]
+    e_plain = np.sqrt(np.mean(np.sum((plain[samp] - ref) ** 2, 1))) / rms
+    e_learned = np.sqrt(np.mean(np.sum((learned[samp] - ref) ** 2, 1))) / rms
+    print(f"\ntraining loop: loss {hist[0]:.3g} -> {hist[-1]:.3g}; log10 lambda {model.log10_lambda:.2f}; predicted "
+          f"(error, cost) ratios {[(round(a, 3), round(b, 3)) for a, b in ratios]}; held out: plain {e_plain:.2e} "
+          f"({i_plain / n:.0f}/target), learned {e_learned:.2e} ({i_learned / n:.0f}/target)")
+    model.close()
+    assert hist[-1] < hist[0], hist
+    assert e_learned <= 1.25 * e_plain, (e_learned, e_plain)
+    assert i_learned <= 0.85 * i_plain, (i_learned, i_plain)
