@@ -33,6 +33,16 @@ int tg_measure_fp32_fma(double *tflops, double *ms, void *stream);
  * for bit (NaN results: NaN on both sides). *mismatches receives the count of differing values. */
 int tg_check_f32_conversion(const double *x, int64_t n, int64_t *mismatches, void *stream);
 
+/* Bounds of the library's bounded device loops, for tests that make each one run out (0 or less:
+ * the built-in bound): polls of one look-back word in a radix pass (built in: 2^22; running out
+ * gives TG_ERR_QUEUE_TIMEOUT), traversal steps of one group of a tree walk (the node count, which
+ * always suffices; TG_ERR_ITER_LIMIT), element visits of one column-density walk (the element count;
+ * TG_ERR_ITER_LIMIT), and list entries after which a group of a plain walk is split across warps
+ * (2^15; results stay within rounding). Every loop stays in bounds when its limit runs out, and the
+ * library stays usable. Process-wide, read when a call launches its kernels; not for concurrent
+ * use with other calls. Returns 0. */
+int tg_set_loop_limits(int64_t sort_spin, int64_t walk_steps, int64_t column_visits, int64_t heavy_entries);
+
 #ifdef __cplusplus
 }
 #endif

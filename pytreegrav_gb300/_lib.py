@@ -98,6 +98,7 @@ MEASURE_EXPORTS = [
     "tg_launch_count",
     "tg_measure_fp32_fma",
     "tg_check_f32_conversion",
+    "tg_set_loop_limits",
 ]
 TG_THETA_NFEAT = 16
 TG_MLP_H = 64

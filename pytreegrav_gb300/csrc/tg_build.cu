@@ -627,7 +627,6 @@ struct BuildSummary {
     int bad;                   // invalid references (bit flags)
     int nonfinite;             // the input check's flag, copied in before the read-back
     int depth_hist[DEPTH_CAP + 1];
-    int sort_error;  // the radix sorts' look-back flag, taken with the final read-back
 };
 
 // Slot validation (as above) plus the depth histogram, over the slots [0, M) with
@@ -1342,6 +1341,8 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     int64_t *sys_off = nullptr;
     TG_TRY(dalloc(&sys_off, nsys + 1, st));
     TG_CUDA(cudaMemcpyAsync(sys_off, sys_off_host.data(), sizeof(int64_t) * (nsys + 1), cudaMemcpyHostToDevice, st));
+    TG_TRY(dalloc(&T->sort_err, 1, st));  // every sort of this tree reports here
+    TG_CUDA(cudaMemsetAsync(T->sort_err, 0, sizeof(int), st));
 
     // 1. bounding cubes
     unsigned long long *mn = nullptr, *mx = nullptr;
@@ -1363,10 +1364,10 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     TG_TRY(dalloc(&perm, N, st));
     { k_keys<<<LAUNCH(N)>>>(pos, N, sys_off, nsys, center, size, keys, keys_orig, perm); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
-    TG_TRY(radix_sort_pairs(keys, perm, N, 63, st));
+    TG_TRY(radix_sort_pairs(keys, perm, N, 63, st, T->sort_err));
     if (nsys > 1) {
         { k_sys_of<<<LAUNCH(N)>>>(perm, N, sys_off, nsys, keys); tg::note_launch(); }
-        TG_TRY(radix_sort_pairs(keys, perm, N, sysbits, st));
+        TG_TRY(radix_sort_pairs(keys, perm, N, sysbits, st, T->sort_err));
     }
 
     // 3. arena element arrays; particles gathered into Morton order
@@ -1432,10 +1433,10 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
             TG_TRY(dalloc(&rv, E, st));
             { k_rekey_keys<<<LAUNCH(E)>>>(v, E, pc, rk, rv); tg::note_launch(); }
             TG_CUDA(cudaMemcpyAsync(rk_elem, rk, sizeof(uint64_t) * E, cudaMemcpyDeviceToDevice, st));
-            TG_TRY(radix_sort_pairs(rk, rv, E, 63, st));
+            TG_TRY(radix_sort_pairs(rk, rv, E, 63, st, T->sort_err));
             if (sg.n > 1) {
                 { k_rekey_segkeys<<<LAUNCH(E)>>>(v, rv, E, rk); tg::note_launch(); }
-                TG_TRY(radix_sort_pairs(rk, rv, E, bits_for(sg.n - 1), st));
+                TG_TRY(radix_sort_pairs(rk, rv, E, bits_for(sg.n - 1), st, T->sort_err));
             }
             double *tc = nullptr, *tm = nullptr, *ts = nullptr;
             int64_t *tw = nullptr;
@@ -1567,7 +1568,7 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     const uint64_t root_key = key_bits < 64 ? (1ull << key_bits) : ~0ull;
     { k_number_keys<<<LAUNCH(M)>>>(nd, M, sys_off, nb, root_key, nkeys, nvals, root_slot, nonroot); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
-    TG_TRY(radix_sort_pairs(nkeys, nvals, M, sort_bits, st));
+    TG_TRY(radix_sort_pairs(nkeys, nvals, M, sort_bits, st, T->sort_err));
     // per-system node offsets (roots first within each system's block), on the device; the host
     // copy is read with the final synchronisation
     if (nsys == 1) {
@@ -1644,8 +1645,7 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     TG_CUDA(cudaEventRecord(T->ev_topo, st));
     int links_bad = 0, sort_bad = 0;
     std::vector<unsigned long long> rq(nsys, 0);
-    TG_TRY(sort_error_take(&sum->sort_error, st));
-    TG_CUDA(cudaMemcpyAsync(&sort_bad, &sum->sort_error, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TG_CUDA(cudaMemcpyAsync(&sort_bad, T->sort_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     TG_CUDA(cudaMemcpyAsync(&links_bad, &sum->bad, sizeof(int), cudaMemcpyDeviceToHost, st));
     if (nsys > 1)
         TG_CUDA(cudaMemcpyAsync(T->sys_node_off.data(), sys_node_off, sizeof(int64_t) * (nsys + 1),
@@ -1743,28 +1743,37 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
 tg_status morton_order_device(const double *pos, int64_t n, uint32_t *perm, cudaStream_t st) {
     if (n <= 0) return TG_OK;
     if (n > 0x7fffffffLL) return TG_ERR_BAD_ARG;
-    std::vector<int64_t> off = {0, n};
-    int64_t *sys_off = nullptr;
-    unsigned long long *mn = nullptr, *mx = nullptr;
-    double *center = nullptr, *size = nullptr;
-    uint64_t *keys = nullptr;
-    TG_TRY(dalloc(&sys_off, 2, st));
-    TG_TRY(dalloc(&mn, 3, st));
-    TG_TRY(dalloc(&mx, 3, st));
-    TG_TRY(dalloc(&center, 3, st));
-    TG_TRY(dalloc(&size, 1, st));
-    TG_TRY(dalloc(&keys, n, st));
-    TG_CUDA(cudaMemcpyAsync(sys_off, off.data(), sizeof(int64_t) * 2, cudaMemcpyHostToDevice, st));
-    { k_bbox_init<<<1, 32, 0, st>>>(mn, mx, 1); tg::note_launch(); }
-    { k_bbox<<<div_up(n, BB_THREADS * BB_ITEMS), BB_THREADS, 0, st>>>(pos, n, sys_off, 1, mn, mx); tg::note_launch(); }
-    { k_bbox_finish<<<1, 32, 0, st>>>(mn, mx, 1, center, size); tg::note_launch(); }
-    { k_keys<<<LAUNCH(n)>>>(pos, n, sys_off, 1, center, size, keys, nullptr, perm); tg::note_launch(); }
+    const int64_t off[2] = {0, n};
+    DevArray<int64_t> sys_off(st);
+    DevArray<unsigned long long> mn(st), mx(st);
+    DevArray<double> center(st), size(st);
+    DevArray<uint64_t> keys(st);
+    DevArray<int> err(st);
+    TG_CUDA(sys_off.alloc(2));
+    TG_CUDA(mn.alloc(3));
+    TG_CUDA(mx.alloc(3));
+    TG_CUDA(center.alloc(3));
+    TG_CUDA(size.alloc(1));
+    TG_CUDA(keys.alloc(n));
+    TG_CUDA(err.alloc(1));
+    TG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
+    TG_CUDA(cudaMemcpyAsync(sys_off.p, off, sizeof(int64_t) * 2, cudaMemcpyHostToDevice, st));
+    { k_bbox_init<<<1, 32, 0, st>>>(mn.p, mx.p, 1); tg::note_launch(); }
+    { k_bbox<<<div_up(n, BB_THREADS * BB_ITEMS), BB_THREADS, 0, st>>>(pos, n, sys_off.p, 1, mn.p, mx.p); tg::note_launch(); }
+    { k_bbox_finish<<<1, 32, 0, st>>>(mn.p, mx.p, 1, center.p, size.p); tg::note_launch(); }
+    { k_keys<<<LAUNCH(n)>>>(pos, n, sys_off.p, 1, center.p, size.p, keys.p, nullptr, perm); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
-    TG_TRY(radix_sort_pairs(keys, perm, n, 63, st));
-    dfree(sys_off, st); dfree(mn, st); dfree(mx, st); dfree(center, st); dfree(size, st); dfree(keys, st);
-    // the host vector `off` must outlive the copy
+    tg_status rc = radix_sort_pairs(keys.p, perm, n, 63, st, err.p);
+    int bad = 0;
+    if (rc == TG_OK) TG_CUDA(cudaMemcpyAsync(&bad, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    // the host array `off` must outlive its copy, also on error
     TG_CUDA(cudaStreamSynchronize(st));
-    return sort_error_check();
+    TG_TRY(rc);
+    if (bad) {
+        set_last_error_msg("radix sort: a tile's look-back did not complete within its bound");
+        return TG_ERR_QUEUE_TIMEOUT;
+    }
+    return TG_OK;
 }
 
 }  // namespace tg

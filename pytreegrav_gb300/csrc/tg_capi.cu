@@ -24,7 +24,8 @@ tg_status make_groups(tg_tree_s *t, const std::vector<int64_t> &sys_off_host, in
                       int **group_root, int64_t *ngroups, cudaStream_t st);
 tg_status tree_groups(tg_tree_s *t, int G, cudaStream_t st);
 tg_status tree_groups_with_arena(tg_tree_s *t, int G, bool fp64, cudaStream_t st);
-tg_status make_cost_order(const double *tpos, const int2 *groups, int64_t ngroups, int **order, cudaStream_t st);
+tg_status make_cost_order(const double *tpos, const int2 *groups, int64_t ngroups, int **order, cudaStream_t st,
+                          int *sort_err);
 tg_status run_bruteforce(const double *pt, const double *ht, int64_t nt, const double *ps, const double *ms,
                          const double *hs, int64_t ns, int fields, int mutual, double G, int precision, double *out,
                          cudaStream_t st);
@@ -115,7 +116,7 @@ void destroy(tg_tree_s *t) {
     free_arena(t->arena32, st);
     free_arena(t->arena64, st);
     if (t->stats_dev) cudaFreeAsync(t->stats_dev, st);
-    f(t->groups); f(t->group_root); f(t->group_node); f(t->gstats); f(t->gerr);
+    f(t->groups); f(t->group_root); f(t->group_node); f(t->gstats); f(t->gerr); f(t->sort_err);
     if (t->side) cudaStreamDestroy(t->side);  // released once its work is done
     if (t->ev_fork) cudaEventDestroy(t->ev_fork);
     if (t->ev_join) cudaEventDestroy(t->ev_join);
@@ -321,7 +322,7 @@ tg_status tg_tree_fields(tg_tree t, const double *pos, const double *h, int64_t 
             ngroups = t->ngroups;
         } else {
             TG_TRY(make_groups(t, t->sys_off, group_size, &groups, &groot, &ngroups, st));
-            TG_TRY(make_cost_order(t->coord, groups, ngroups, &gorder, st));
+            TG_TRY(make_cost_order(t->coord, groups, ngroups, &gorder, st, t->sort_err));
             wg = groups;
             wr = groot;
         }
@@ -358,7 +359,7 @@ tg_status tg_tree_fields(tg_tree t, const double *pos, const double *h, int64_t 
         }
         std::vector<int64_t> toff = {0, n};
         TG_TRY(make_groups(t, toff, group_size, &groups, &groot, &ngroups, st));
-        TG_TRY(make_cost_order(sp ? sp : dp.ptr, groups, ngroups, &gorder, st));
+        TG_TRY(make_cost_order(sp ? sp : dp.ptr, groups, ngroups, &gorder, st, t->sort_err));
         if (mem == TG_MEM_HOST) TG_CUDA(tg::dev_malloc((void **)&dout, sizeof(double) * nt * W, st));
         else dout = out;
         rc = run_walk(t, sp ? sp : dp.ptr, sh, nt, groups, groot, gorder, ngroups, scatter, fields, quadrupole, theta, G,
@@ -410,19 +411,18 @@ tg_status tg_morton_order(const double *pos, int64_t n, int mem, int64_t *perm, 
     const double *arrs[1] = {dp.ptr};
     int64_t counts[1] = {3 * n};
     TG_TRY(check_finite(arrs, counts, 1, st));
-    uint32_t *p32 = nullptr;
-    int64_t *p64 = nullptr;
-    TG_CUDA(tg::dev_malloc((void **)&p32, sizeof(uint32_t) * n, st));
-    TG_TRY(morton_order_device(dp.ptr, n, p32, st));
-    if (mem == TG_MEM_HOST) TG_CUDA(tg::dev_malloc((void **)&p64, sizeof(int64_t) * n, st));
-    else p64 = perm;
-    { k_u32_to_i64<<<div_up(n, 256), 256, 0, st>>>(p32, n, p64); tg::note_launch(); }
-    TG_CUDA(cudaGetLastError());
+    DevArray<uint32_t> p32(st);
+    DevArray<int64_t> p64buf(st);
+    TG_CUDA(p32.alloc(n));
+    TG_TRY(morton_order_device(dp.ptr, n, p32.p, st));
+    int64_t *p64 = perm;
     if (mem == TG_MEM_HOST) {
-        TG_CUDA(cudaMemcpyAsync(perm, p64, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, st));
-        TG_CUDA(cudaFreeAsync(p64, st));
+        TG_CUDA(p64buf.alloc(n));
+        p64 = p64buf.p;
     }
-    TG_CUDA(cudaFreeAsync(p32, st));
+    { k_u32_to_i64<<<div_up(n, 256), 256, 0, st>>>(p32.p, n, p64); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
+    if (mem == TG_MEM_HOST) TG_CUDA(cudaMemcpyAsync(perm, p64, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, st));
     TG_CUDA(cudaStreamSynchronize(st));
     return TG_OK;
 }

@@ -19,6 +19,7 @@ struct ColumnTree {
     const double *coord, *mass, *soft, *size, *delta;
     const int64_t *first, *next;
     int64_t npart, nelem;
+    int64_t max_visits;  // visits one walk may make (one per element always suffices)
     // FP32 copy for the screen: coordinates split hi + lo, with the radius (hi.w) and, for nodes,
     // size * sqrt(3)/2 + delta (lo.w)
     const float4 *fhi, *flo;
@@ -64,7 +65,7 @@ __device__ double column_singleray(const ColumnTree &t, double px, double py, do
     int64_t no = N;
     const int64_t stop = t.next[N];
     for (int64_t guard = 0; no > -1 && no != stop; guard++) {
-        if (guard > t.nelem || no >= t.nelem) {
+        if (guard > t.max_visits || no >= t.nelem) {
             atomicOr(runaway, 1);
             return column;
         }
@@ -185,7 +186,7 @@ __global__ void k_column_binned(ColumnTree t, const double *pos, int64_t n, doub
     int64_t no = N;
     const int64_t stop = t.next[N];
     for (int64_t guard = 0; no > -1 && no != stop; guard++) {
-        if (guard > t.nelem || no >= t.nelem) {
+        if (guard > t.max_visits || no >= t.nelem) {
             atomicOr(runaway, 1);
             break;
         }
@@ -257,7 +258,7 @@ __global__ void k_column_binned_grouped(ColumnTree t, const double *pos, int64_t
     int64_t no = N;
     const int64_t stop = t.next[N];
     for (int64_t guard = 0; no > -1 && no != stop; guard++) {
-        if (guard > t.nelem || no >= t.nelem) {
+        if (guard > t.max_visits || no >= t.nelem) {
             if (lane == 0) atomicOr(runaway, 1);
             break;
         }
@@ -350,6 +351,7 @@ tg_status tg_tree_column_density(tg_tree t, const double *pos, int64_t n, const 
     ct.first = t->first; ct.next = t->next;
     ct.npart = t->ntot;
     ct.nelem = t->ntot + t->mtot;
+    ct.max_visits = loop_limits().column_visits > 0 ? std::min<int64_t>(loop_limits().column_visits, ct.nelem) : ct.nelem;
     ct.rows = own ? t->walk_idx : nullptr;
     const int64_t nray_vals = binned ? 0 : (ray_stride ? n * ray_stride : 3 * nrays);
     const double *dpos = pos, *drays = rays;

@@ -202,13 +202,21 @@ tg_status exclusive_scan_i64(const int64_t *in, int64_t *out, int64_t n, int64_t
 tg_status exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s);
 
 // Stable LSD radix sort of (key, value) pairs on the low `bits` bits of the keys. keys/vals are
-// sorted in place (scratch buffers are allocated stream-ordered and freed before return).
-tg_status radix_sort_pairs(uint64_t *keys, uint32_t *vals, int64_t n, int bits, cudaStream_t s);
-// After a synchronisation: TG_ERR_QUEUE_TIMEOUT (and the flag cleared) if a sort's look-back ran
-// out of its bound since the last check.
-tg_status sort_error_check();
-// The same flag taken into *dst (device) on `st` and cleared, without a synchronisation.
-tg_status sort_error_take(int *dst, cudaStream_t st);
+// sorted in place (scratch buffers are allocated stream-ordered and freed before return). A tile
+// look-back that does not complete within its bound sets *err (a device int the caller owns and
+// reads back with its results; nonzero: the sort failed) and leaves keys[i] = i and vals[i] = i, a
+// sorted, well-formed result, so every later kernel stays in bounds.
+tg_status radix_sort_pairs(uint64_t *keys, uint32_t *vals, int64_t n, int bits, cudaStream_t s, int *err);
+
+// Bounds of the library's bounded device loops, overridable (tg_set_loop_limits in the measurement
+// header) so that tests can make each one run out; 0 selects the built-in bound. Process-wide.
+struct LoopLimits {
+    long long sort_spin = 0;      // polls of one look-back word in a radix pass
+    long long walk_steps = 0;     // traversal steps of one group of a tree walk
+    long long column_visits = 0;  // element visits of one column-density walk
+    long long heavy_entries = 0;  // list entries after which a walk's group is split (see tg_walk.cu)
+};
+LoopLimits &loop_limits();
 
 int num_sms();
 
@@ -221,6 +229,20 @@ int num_sms();
 #define TG_POOL_KEEP_BYTES (4ull << 30)
 #endif
 cudaError_t dev_malloc(void **p, size_t bytes, cudaStream_t s);
+
+// A stream-ordered device array from dev_malloc, freed on `st` when it goes out of scope.
+template <typename T>
+struct DevArray {
+    T *p = nullptr;
+    cudaStream_t st = nullptr;
+    explicit DevArray(cudaStream_t s) : st(s) {}
+    ~DevArray() {
+        if (p) cudaFreeAsync(p, st);
+    }
+    DevArray(const DevArray &) = delete;
+    DevArray &operator=(const DevArray &) = delete;
+    cudaError_t alloc(int64_t n) { return dev_malloc((void **)&p, sizeof(T) * (size_t)(n > 1 ? n : 1), st); }
+};
 
 // Counts kernel launches (every launch site calls it; read through tg_launch_count()).
 void note_launch();

@@ -10,6 +10,8 @@ static std::atomic<int64_t> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void note_launches(int64_t delta) { g_launches.fetch_add(delta, std::memory_order_relaxed); }
 int64_t launches_so_far() { return g_launches.load(); }
+static LoopLimits g_limits;
+LoopLimits &loop_limits() { return g_limits; }
 }  // namespace tg
 
 namespace {
@@ -96,3 +98,13 @@ int tg_check_f32_conversion(const double *x, int64_t n, int64_t *mismatches, voi
 }
 
 }  // extern "C"
+
+extern "C" int tg_set_loop_limits(int64_t sort_spin, int64_t walk_steps, int64_t column_visits,
+                                  int64_t heavy_entries) {
+    tg::LoopLimits &l = tg::loop_limits();
+    l.sort_spin = sort_spin > 0 ? sort_spin : 0;
+    l.walk_steps = walk_steps > 0 ? walk_steps : 0;
+    l.column_visits = column_visits > 0 ? column_visits : 0;
+    l.heavy_entries = heavy_entries > 0 ? heavy_entries : 0;
+    return 0;
+}

@@ -254,8 +254,8 @@ __global__ void __launch_bounds__(RS_THREADS) radix_scatter(const uint64_t *keys
 // then each pass is one kernel: a CTA takes the next tile from an atomic counter (so every earlier
 // tile belongs to a CTA that is already running), ranks its keys stably as above, publishes its
 // per-digit count, looks back over earlier tiles' published words for its exclusive prefix, and
-// scatters. A look-back spin is bounded; running out sets g_sort_error (checked by sort_error_check)
-// instead of hanging.
+// scatters. A look-back spin is bounded; running out sets the sort's own error word instead of
+// hanging, and the sort then leaves the identity permutation (k_sort_fallback).
 
 constexpr int MAX_PASSES = 8;
 constexpr int OS_ROUNDS = 8;                        // keys per thread in a one-sweep pass
@@ -264,7 +264,6 @@ constexpr int OS_TILE = RS_WARPS * OS_WARP_KEYS;   // 2048 keys per CTA (8 per t
 constexpr unsigned long long ST_AGG = 1ull << 62, ST_INC = 2ull << 62, ST_VAL = (1ull << 62) - 1;
 constexpr long long SPIN_LIMIT = 1ll << 22;
 constexpr int LB = 4;  // predecessors read per look-back round trip
-__device__ int g_sort_error;
 
 __global__ void __launch_bounds__(256) k_sort_hist_all(const uint64_t *keys, int64_t n, int npass, int *hist) {
     __shared__ int h[MAX_PASSES * RS_BINS];
@@ -293,7 +292,8 @@ __global__ void k_sort_digit_offsets(int *hist, int npass) {
 __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const uint64_t *keys, const uint32_t *vals, int64_t n,
                                                          int shift, const int *digit_off,
                                                          unsigned long long *status, int *tile_counter,
-                                                         uint64_t *keys_out, uint32_t *vals_out) {
+                                                         uint64_t *keys_out, uint32_t *vals_out, int *err,
+                                                         long long spin_limit) {
     __shared__ int wcount[RS_WARPS][RS_BINS];
     __shared__ int prefix[RS_BINS];
     __shared__ int tile_s;
@@ -336,9 +336,9 @@ __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const uint64_t *keys, c
                     if (done || j - k < 0) break;
                     unsigned long long wd = w[k];
                     const volatile unsigned long long *src = status + (j - k) * RS_BINS + d;
-                    for (long long spins = 0; !(wd & ~ST_VAL) && spins < SPIN_LIMIT; spins++) wd = *src;
+                    for (long long spins = 0; !(wd & ~ST_VAL) && spins < spin_limit; spins++) wd = *src;
                     if (!(wd & ~ST_VAL)) {
-                        atomicExch(&g_sort_error, 1);
+                        atomicExch(err, 1);
                         done = true;
                         break;
                     }
@@ -363,34 +363,23 @@ __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const uint64_t *keys, c
     }
 }
 
-__global__ void k_take_sort_error(int *dst) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) dst[0] = atomicExch(&g_sort_error, 0);
-}
-
-// Stream-ordered: *dst (device) receives the flag and the flag is cleared, for a caller that reads
-// it back with its own results instead of synchronising for it.
-tg_status sort_error_take(int *dst, cudaStream_t st) {
-    k_take_sort_error<<<1, 32, 0, st>>>(dst);
-    note_launch();
-    TG_CUDA(cudaGetLastError());
-    return TG_OK;
-}
-
-tg_status sort_error_check() {
-    int e = 0;
-    TG_CUDA(cudaMemcpyFromSymbol(&e, g_sort_error, sizeof(int)));
-    if (e) {
-        int z = 0;
-        cudaMemcpyToSymbol(g_sort_error, &z, sizeof(int));
-        set_last_error_msg("radix sort: a tile's look-back did not complete within its bound");
-        return TG_ERR_QUEUE_TIMEOUT;
+// After the passes: if a look-back gave up (some keys went to wrong places, some places were never
+// written), every value becomes its own index and every key its own position -- sorted pairs and a
+// valid permutation, so every later kernel sees well-formed input -- and the caller's flag is set.
+__global__ void k_sort_fallback(uint64_t *keys, uint32_t *vals, int64_t n, const int *local_err, int *err) {
+    if (!*local_err) return;
+    const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i0 == 0) atomicExch(err, 1);
+    for (int64_t i = i0; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        keys[i] = (uint64_t)i;
+        vals[i] = (uint32_t)i;
     }
-    return TG_OK;
 }
 
-tg_status radix_sort_pairs(uint64_t *keys, uint32_t *vals, int64_t n, int bits, cudaStream_t s) {
+tg_status radix_sort_pairs(uint64_t *keys, uint32_t *vals, int64_t n, int bits, cudaStream_t s, int *err) {
     if (n <= 1 || bits <= 0) return TG_OK;
-    if (n > (int64_t)0x7fffffff) return TG_ERR_BAD_ARG;
+    if (n > (int64_t)0x7fffffff || !err) return TG_ERR_BAD_ARG;
+    const long long spin_limit = loop_limits().sort_spin > 0 ? loop_limits().sort_spin : SPIN_LIMIT;
     const int ntiles = div_up(n, OS_TILE);
     const int npass = std::min((bits + 7) / 8, MAX_PASSES);
     uint64_t *k2 = nullptr;
@@ -400,11 +389,12 @@ tg_status radix_sort_pairs(uint64_t *keys, uint32_t *vals, int64_t n, int bits, 
     const size_t hist_bytes = sizeof(int) * MAX_PASSES * RS_BINS;
     TG_CUDA(tg::dev_malloc((void **)&k2, sizeof(uint64_t) * n, s));
     TG_CUDA(tg::dev_malloc((void **)&v2, sizeof(uint32_t) * n, s));
-    TG_CUDA(tg::dev_malloc((void **)&scr, st_bytes + hist_bytes + sizeof(int) * MAX_PASSES, s));
+    TG_CUDA(tg::dev_malloc((void **)&scr, st_bytes + hist_bytes + sizeof(int) * (MAX_PASSES + 1), s));
     unsigned long long *status = (unsigned long long *)scr;
     int *hist = (int *)(scr + st_bytes);
     int *counters = hist + MAX_PASSES * RS_BINS;
-    TG_CUDA(cudaMemsetAsync(hist, 0, hist_bytes + sizeof(int) * MAX_PASSES, s));
+    int *local_err = counters + MAX_PASSES;
+    TG_CUDA(cudaMemsetAsync(hist, 0, hist_bytes + sizeof(int) * (MAX_PASSES + 1), s));
     const int hblocks = (int)std::min<int64_t>(div_up(n, 256 * 16), (int64_t)num_sms() * 4);
     { k_sort_hist_all<<<hblocks, 256, 0, s>>>(keys, n, npass, hist); tg::note_launch(); }
     { k_sort_digit_offsets<<<1, RS_BINS, 0, s>>>(hist, npass); tg::note_launch(); }
@@ -413,7 +403,7 @@ tg_status radix_sort_pairs(uint64_t *keys, uint32_t *vals, int64_t n, int bits, 
     for (int p = 0; p < npass; p++) {
         TG_CUDA(cudaMemsetAsync(status, 0, st_bytes, s));
         { k_onesweep<<<ntiles, RS_THREADS, 0, s>>>(kin, vin, n, 8 * p, hist + p * RS_BINS, status, counters + p, kout,
-                                                   vout); tg::note_launch(); }
+                                                   vout, local_err, spin_limit); tg::note_launch(); }
         TG_CUDA(cudaGetLastError());
         uint64_t *tk = kin; kin = kout; kout = tk;
         uint32_t *tv = vin; vin = vout; vout = tv;
@@ -422,6 +412,8 @@ tg_status radix_sort_pairs(uint64_t *keys, uint32_t *vals, int64_t n, int bits, 
         TG_CUDA(cudaMemcpyAsync(keys, kin, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, s));
         TG_CUDA(cudaMemcpyAsync(vals, vin, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s));
     }
+    { k_sort_fallback<<<std::min(div_up(n, 256), 4 * num_sms()), 256, 0, s>>>(keys, vals, n, local_err, err); tg::note_launch(); }
+    TG_CUDA(cudaGetLastError());
     TG_CUDA(cudaFreeAsync(k2, s));
     TG_CUDA(cudaFreeAsync(v2, s));
     TG_CUDA(cudaFreeAsync(scr, s));

@@ -72,6 +72,10 @@ struct tg_tree_s {
     int2 *node_range = nullptr;   // per node: particle range [lo, hi) of its subtree
     double *cell_center = nullptr;  // per node: geometric centre of its cell (3)
 
+    // The look-back error word of every radix sort made for this tree (build, grouping, queue
+    // order), read back by the build and by each walk (nonzero: a sort failed).
+    int *sort_err = nullptr;
+
     tg::Arena<float> arena32;
     tg::Arena<double> arena64;
     tg::WalkStats last_stats;

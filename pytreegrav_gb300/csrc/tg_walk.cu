@@ -340,6 +340,16 @@ struct WalkArgs {
     float *gerr = nullptr;
     int *rewalk = nullptr, *rewalk_count = nullptr;
     double rewalk_theta = 0.0;  // the global theta of the rewalk pass
+    // Heavy groups: with heavy set, a group whose evaluated list entries exceed heavy_budget stops
+    // (its partial work taken back) and is appended to heavy, for the split walk (walk_heavy).
+    int *heavy = nullptr, *heavy_count = nullptr;
+    unsigned heavy_budget = 0;
+    // Item mode (the split walk): unit k walks, for group item_group[k], the subtree of item_node[k]
+    // (a node; or a particle, ~leaf, taken as one interaction) and writes its unscaled partial sums,
+    // 10 components for each of gs target slots, to partial + 10 * gs * k.
+    const int *item_group = nullptr, *item_node = nullptr;
+    double *partial = nullptr;
+    int64_t step_limit = 0;  // traversal steps per group (0: the node count, which always suffices)
 };
 
 template <typename T, bool QUAD, int STACK>
@@ -508,6 +518,25 @@ __device__ __forceinline__ bool accept_exact(int64_t f, const double *tc, const 
     return r_min > crit;
 }
 
+// One target's row of the output: G times the requested fields of v (pot | accel(3) | tidal(6 unique
+// components, written as the full symmetric 3x3)).
+__device__ __forceinline__ void write_fields(double *o, int out_fields, const double *v, double G) {
+    int k = 0;
+    if (out_fields & F_POT) o[k++] = G * v[0];
+    if (out_fields & F_ACC) {
+        o[k] = G * v[1];
+        o[k + 1] = G * v[2];
+        o[k + 2] = G * v[3];
+        k += 3;
+    }
+    if (out_fields & F_TID) {
+        const double txx = G * v[4], txy = G * v[5], txz = G * v[6], tyy = G * v[7], tyz = G * v[8], tzz = G * v[9];
+        o[k] = txx; o[k + 1] = txy; o[k + 2] = txz;
+        o[k + 3] = txy; o[k + 4] = tyy; o[k + 5] = tyz;
+        o[k + 6] = txz; o[k + 7] = tyz; o[k + 8] = tzz;
+    }
+}
+
 // Register caps (registers are granted 8 per thread at a time): the FP32 quadrupole acceleration
 // walk with the small stack runs at 72, which with its shared memory lets 7 blocks of 4 warps share
 // an SM (6 at 80); the other small-stack walks at 80 (6 blocks of 4 warps, 3 of 8; 81 would round
@@ -537,7 +566,15 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
         if (lane == 0) g = atomicAdd(a.queue, 1);
         g = __shfl_sync(FULL, g, 0);
         if (g >= ngroups) break;
-        if (a.group_order) g = a.group_order[g];
+        const int unit = g;
+        int start;  // the node the traversal starts from (an item may be a particle: ~leaf)
+        if (a.item_group) {
+            start = a.item_node[unit];
+            g = a.item_group[unit];
+        } else {
+            if (a.group_order) g = a.group_order[g];
+            start = a.group_root[g];
+        }
         const int2 gr = a.groups[g];
         // lanes per target slot: the smallest power of two holding the group (at most a.gs); the
         // other lanes of the warp take interleaved shares of every source batch
@@ -899,11 +936,17 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
 
         unsigned g_mono = 0, g_quad = 0, g_tests = 0, g_steps = 0;  // this group's counters (warp-uniform)
         int sp = 1, ni = 0, nn = 0;
-        if (lane == 0) sm.stack[0] = a.group_root[g];
+        if (start >= 0) {
+            if (lane == 0) sm.stack[0] = start;
+        } else {  // an item that is one particle
+            if (lane == 0) sm.ilist[0] = start;
+            sp = 0;
+            ni = 1;
+        }
         __syncwarp();
-        bool overflow = false, runaway = false;
+        bool overflow = false, runaway = false, heavy = false;
         // a traversal tests every node at most once, and each step tests at least one
-        int64_t steps_left = a.ar.n_nodes + 2;
+        int64_t steps_left = a.step_limit > 0 && a.step_limit < a.ar.n_nodes + 2 ? a.step_limit : a.ar.n_nodes + 2;
         for (;;) {
             if (--steps_left < 0) {
                 runaway = true;
@@ -998,12 +1041,17 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
                 }
             }
             if (sp == 0) break;
+            if (a.heavy && g_mono + g_quad > a.heavy_budget) {  // warp-uniform
+                heavy = true;
+                break;
+            }
         }
-        if (overflow && a.retry) {
-            // handed to the large-stack pass; its counts so far are taken back so the statistics
-            // count the group once
+        if ((overflow && a.retry) || heavy) {
+            // handed to the large-stack pass or to the split walk; its counts so far are taken back
+            // so the statistics count the group once
             if (lane == 0) {
-                a.retry[atomicAdd(a.retry_count, 1)] = g;
+                if (heavy) a.heavy[atomicAdd(a.heavy_count, 1)] = g;
+                else a.retry[atomicAdd(a.retry_count, 1)] = g;
                 n_tests -= g_tests;
             }
             n_int -= (unsigned long long)(g_mono + g_quad) * (unsigned long long)gr.y;
@@ -1055,23 +1103,16 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
             }
         }
         if (slice == 0 && valid) {
-            const int64_t row = a.scatter ? a.scatter[t] : t;
-            double *o = a.out + row * a.out_w;
-            int k = 0;
-            const double G = a.G;
-            auto val = [&](int c) { return G * ((double)S.v[c] - (double)C.v[c]); };
-            if (a.out_fields & F_POT) o[k++] = val(0);
-            if (a.out_fields & F_ACC) {
-                o[k] = val(1);
-                o[k + 1] = val(2);
-                o[k + 2] = val(3);
-                k += 3;
-            }
-            if (a.out_fields & F_TID) {
-                double txx = val(4), txy = val(5), txz = val(6), tyy = val(7), tyz = val(8), tzz = val(9);
-                o[k] = txx; o[k + 1] = txy; o[k + 2] = txz;
-                o[k + 3] = txy; o[k + 4] = tyy; o[k + 5] = tyz;
-                o[k + 6] = txz; o[k + 7] = tyz; o[k + 8] = tzz;
+            double v[10];
+#pragma unroll
+            for (int c = 0; c < 10; c++) v[c] = comp<FIELDS>(c) ? (double)S.v[c] - (double)C.v[c] : 0.0;
+            if (a.partial) {  // an item of a split walk: unscaled partial sums of this target slot
+                double *o = a.partial + ((int64_t)unit * a.gs + tl) * 10;
+#pragma unroll
+                for (int c = 0; c < 10; c++) o[c] = v[c];
+            } else {
+                const int64_t row = a.scatter ? a.scatter[t] : t;
+                write_fields(a.out + row * a.out_w, a.out_fields, v, a.G);
             }
         }
         __syncwarp();
@@ -1363,6 +1404,172 @@ __global__ void k_prep_targets(const double *tpos, const double *th, int64_t n, 
 
 // Persistent grid: as many blocks of `warps` warps as fit on the GPU (fewer when every group has a
 // warp anyway; all of them for the retry pass, whose group count is known only on the device).
+// ---------------------------------------------------------------------------------------------
+// Split walk of heavy groups. A group of consecutive Morton targets that straddles a jump of the
+// Morton curve gets a bounding box spanning both sides and can open most of the tree: at 1e6
+// Plummer particles and pytreegrav's groups of 8, one group evaluates ~9e5 list entries, ~450x the
+// median, and one warp would work through it alone. Such a group stops once it passes an entry
+// budget; k_walk_top then walks it down to subtrees of at most split_npart particles without
+// evaluating anything and lists the pieces -- every node it accepts, every particle of a node it
+// opens, and every node child small enough -- as items; all warps walk the items (k_walk in item
+// mode) and k_reduce_items adds each group's item sums in item order. The items together cover the
+// group's accepted set exactly: each decision here is the exact FP64 criterion, which the walk's
+// own test reproduces, and an item node is tested again when its walk starts. Only the summation
+// order differs from an unsplit walk, and it is fixed, so results do not vary between runs.
+constexpr int TOP_WARPS = 4;
+constexpr int TOP_STACK = 2048;
+
+template <typename T>
+struct TopArgs {
+    Arena<T> ar;
+    int64_t ntot;
+    const double *tc, *ts, *tsize, *tdelta;
+    const double *tpos, *th;
+    const int2 *groups;
+    const int *group_root;
+    const int *heavy;  // unit -> group
+    int nheavy;
+    double theta;
+    const float *theta_group;
+    const int2 *node_range;
+    int split_npart;
+    int *items;       // item_cap per unit
+    int *item_count;  // per unit
+    int item_cap;
+    int *status;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(TOP_WARPS * 32) k_walk_top(TopArgs<T> a) {
+    __shared__ int stack_all[TOP_WARPS][TOP_STACK];
+    int *stack = stack_all[threadIdx.x >> 5];
+    const int lane = lane_id();
+    const unsigned lt = lanemask_lt();
+    const int u = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (u >= a.nheavy) return;
+    if (a.ar.bad && *a.ar.bad) {
+        if (lane == 0) atomicOr(a.status, 1 << TG_ERR_CUDA);
+        return;
+    }
+    const int g = a.heavy[u];
+    const int2 gr = a.groups[g];
+    const int64_t t = gr.x + (lane < gr.y ? lane : 0);
+    double bmin[3], bmax[3], hmax = a.th[t];
+    for (int k = 0; k < 3; k++) bmin[k] = bmax[k] = a.tpos[3 * t + k];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            bmin[k] = fmin(bmin[k], __shfl_xor_sync(FULL, bmin[k], o));
+            bmax[k] = fmax(bmax[k], __shfl_xor_sync(FULL, bmax[k], o));
+        }
+        hmax = fmax(hmax, __shfl_xor_sync(FULL, hmax, o));
+    }
+    const double theta = a.theta_group ? (double)a.theta_group[g] : a.theta;
+    int *items = a.items + (int64_t)u * a.item_cap;
+    int nitems = 0, sp = 1;
+    if (lane == 0) stack[0] = a.group_root[g];
+    __syncwarp();
+    bool failed = false;
+    for (int64_t steps_left = a.ar.n_nodes + 2; sp > 0; ) {
+        if (--steps_left < 0) {
+            if (lane == 0) atomicOr(a.status, 1 << TG_ERR_ITER_LIMIT);
+            failed = true;
+            break;
+        }
+        const int cnt = min(sp, 32);
+        const int node = lane < cnt ? stack[sp - 1 - lane] : -1;
+        sp -= cnt;
+        __syncwarp();
+        bool acc = false;
+        int fc = 0, nc = 0, ls = 0, nl = 0;
+        if (node >= 0) {
+            acc = accept_exact(a.ntot + node, a.tc, a.ts, a.tsize, a.tdelta, bmin, bmax, hmax, theta);
+            if (!acc) {
+                const int cb = bits_int(a.ar.n_trav[2 * node + 1].z), lb = bits_int(a.ar.n_trav[2 * node + 1].w);
+                fc = cb >> 4;
+                nc = cb & 15;
+                ls = lb >> 4;
+                nl = lb & 15;
+            }
+        }
+        // this lane's items (the node itself, or its particles and small node children) and pushes
+        int nit = 0, npush = 0;
+        unsigned small = 0;
+        if (node >= 0) {
+            if (acc) {
+                nit = 1;
+            } else {
+                for (int j = 0; j < nc; j++) {
+                    const int2 r = a.node_range[fc + j];
+                    if (r.y - r.x <= a.split_npart) small |= 1u << j;
+                }
+                nit = nl + __popc(small);
+                npush = nc - __popc(small);
+            }
+        }
+        const int both = warp_inclusive_scan(nit | (npush << 16));
+        const int tot = __shfl_sync(FULL, both, 31);
+        const int toti = tot & 0xffff, totp = tot >> 16;
+        if (nitems + toti > a.item_cap || sp + totp > TOP_STACK) {
+            if (lane == 0) atomicOr(a.status, 1 << TG_ERR_STACK_OVERFLOW);
+            failed = true;
+            break;
+        }
+        int oi = nitems + (both & 0xffff) - nit, op = sp + (both >> 16) - npush;
+        if (node >= 0) {
+            if (acc) {
+                items[oi] = node;
+            } else {
+                for (int j = 0; j < nl; j++) items[oi++] = ~(ls + j);
+                for (int j = 0; j < nc; j++) {
+                    if ((small >> j) & 1u) items[oi++] = fc + j;
+                    else stack[op++] = fc + j;
+                }
+            }
+        }
+        nitems += toti;
+        sp += totp;
+        __syncwarp();
+        (void)lt;
+    }
+    if (lane == 0) a.item_count[u] = failed ? 0 : nitems;
+}
+
+// Items of every unit, flattened in unit order: item k -> (group, start node).
+__global__ void k_flatten_items(const int *heavy, int nheavy, const int *items, int item_cap, const int64_t *off,
+                                int *item_group, int *item_node) {
+    const int u = blockIdx.x;
+    if (u >= nheavy) return;
+    const int64_t o = off[u], n = off[u + 1] - off[u];
+    const int g = heavy[u];
+    for (int64_t k = threadIdx.x; k < n; k += blockDim.x) {
+        item_group[o + k] = g;
+        item_node[o + k] = items[(int64_t)u * item_cap + k];
+    }
+}
+
+// One thread per (unit, target slot): the unit's item sums added in item order, G times them written
+// to the target's row.
+__global__ void k_reduce_items(const int *heavy, int nheavy, const int64_t *off, const int2 *groups, int gs,
+                               const double *partial, const int64_t *scatter, int out_fields, int out_w, double G,
+                               double *out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)nheavy * gs) return;
+    const int u = (int)(i / gs), slot = (int)(i % gs);
+    const int2 gr = groups[heavy[u]];
+    if (slot >= gr.y) return;
+    double v[10];
+    for (int c = 0; c < 10; c++) v[c] = 0.0;
+    for (int64_t k = off[u]; k < off[u + 1]; k++) {
+        const double *p = partial + (k * gs + slot) * 10;
+        for (int c = 0; c < 10; c++) v[c] += p[c];
+    }
+    const int64_t t = gr.x + slot;
+    const int64_t row = scatter ? scatter[t] : t;
+    write_fields(out + row * out_w, out_fields, v, G);
+}
+
 template <typename T, int FIELDS, bool QUAD, int STACK>
 static tg_status launch_walk(WalkArgs<T> &a, int warps, cudaStream_t st) {
     size_t smem = sizeof(WarpSmem<T, QUAD, STACK>) * warps;
@@ -1417,8 +1624,13 @@ static tg_status dispatch_walk(WalkArgs<T> &a, int fields, bool quad, int warps,
 
 // Scratch of one walk, in ints: queue, status, retry count, retry queue, then the retry list.
 constexpr int WS_QUEUE = 0, WS_STATUS = 1, WS_RETRY_COUNT = 2, WS_RETRY_QUEUE = 3, WS_REWALK_COUNT = 4,
-              WS_REWALK_QUEUE = 5, WS_RETRY_LIST = 6;  // then the retry list, then the rewalk list
-inline int64_t walk_scratch_ints(int64_t ngroups) { return WS_RETRY_LIST + 2 * std::max<int64_t>(ngroups, 1); }
+              WS_REWALK_QUEUE = 5, WS_HEAVY_COUNT = 6, WS_HEAVY_QUEUE = 7,
+              WS_RETRY_LIST = 8;  // then the retry list, the rewalk list and the heavy list
+inline int64_t walk_scratch_ints(int64_t ngroups) { return WS_RETRY_LIST + 3 * std::max<int64_t>(ngroups, 1); }
+// List entries after which a group counts as heavy (split_heavy walks): the median group of 8 at 1e6
+// Plummer particles evaluates ~1.9e3, the 99.9th percentile ~7e3.
+constexpr unsigned HEAVY_ENTRIES = 1u << 15;
+constexpr int ITEM_CAP = 1 << 16;  // items per heavy group
 
 // Enqueue a whole walk on st (no host synchronisation, so it can be captured): with the small
 // first stack, the small-stack pass, then a large-stack pass over the groups that overflowed it
@@ -1426,12 +1638,18 @@ inline int64_t walk_scratch_ints(int64_t ngroups) { return WS_RETRY_LIST + 2 * s
 // walk_scratch_ints(a.ngroups) ints, zeroed here.
 template <typename T>
 static tg_status enqueue_walk(WalkArgs<T> a, int fields, bool quad, int warps, int first_stack, int *scratch,
-                              cudaStream_t st) {
+                              cudaStream_t st, bool split_heavy = false) {
     TG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int) * WS_RETRY_LIST, st));
     const int64_t ng1 = std::max<int64_t>(a.ngroups, 1);
     a.queue = scratch + WS_QUEUE;
     a.status = scratch + WS_STATUS;
     a.ngroups_dev = nullptr;
+    // heavy groups stop and are listed for walk_heavy (which needs host synchronisation)
+    a.heavy = split_heavy ? scratch + WS_RETRY_LIST + 2 * ng1 : nullptr;
+    a.heavy_count = split_heavy ? scratch + WS_HEAVY_COUNT : nullptr;
+    a.heavy_budget = loop_limits().heavy_entries > 0 ? (unsigned)std::min<long long>(loop_limits().heavy_entries, 1ll << 30)
+                                                     : HEAVY_ENTRIES;
+    a.step_limit = loop_limits().walk_steps;
     const bool budget = a.tol_group && a.err_budget > 0.f;
     a.rewalk = budget ? scratch + WS_RETRY_LIST + ng1 : nullptr;
     a.rewalk_count = budget ? scratch + WS_REWALK_COUNT : nullptr;
@@ -1457,6 +1675,7 @@ static tg_status enqueue_walk(WalkArgs<T> a, int fields, bool quad, int warps, i
     r.ngroups_dev = scratch + WS_REWALK_COUNT;
     r.retry = r.retry_count = nullptr;
     r.rewalk = r.rewalk_count = nullptr;
+    r.heavy = r.heavy_count = nullptr;
     r.tol_group = nullptr;
     r.theta_group = nullptr;
     r.gerr = nullptr;
@@ -1464,15 +1683,109 @@ static tg_status enqueue_walk(WalkArgs<T> a, int fields, bool quad, int warps, i
     return dispatch_walk<T, STACK_LARGE>(r, fields, quad, warps, st);
 }
 
-// Run a walk and time it on the stream; *status_out receives the device status word.
+// The heavy groups listed by a walk (see k_walk_top): split into items, the items walked by all warps,
+// each group's item sums reduced in item order into its rows. nheavy groups are listed at the heavy
+// list of scratch. Synchronises st twice (item counts, then the flattened list's size).
 template <typename T>
-static tg_status walk_with_fallback(WalkArgs<T> &a, int fields, bool quad, int warps, int first_stack, int *scratch,
-                                    cudaStream_t st, int *status_out, float *kernel_ms) {
+static tg_status walk_heavy(tg_tree_s *t, const WalkArgs<T> &a, Arena<T> &ar, int fields, bool quad, int warps,
+                            int *scratch, int nheavy, cudaStream_t st) {
+    const int64_t ng1 = std::max<int64_t>(a.ngroups, 1);
+    const int *heavy = scratch + WS_RETRY_LIST + 2 * ng1;
+    WalkArgs<T> b = a;
+    b.retry = b.retry_count = nullptr;
+    b.heavy = b.heavy_count = nullptr;
+    b.rewalk = b.rewalk_count = nullptr;
+    b.ngroups_dev = nullptr;
+    b.queue = scratch + WS_HEAVY_QUEUE;
+    if ((int64_t)nheavy * ITEM_CAP > ((int64_t)1 << 28)) {  // too many to list: walk them whole
+        TG_CUDA(cudaMemsetAsync(b.queue, 0, sizeof(int), st));
+        b.group_order = heavy;
+        b.ngroups = nheavy;
+        return dispatch_walk<T, STACK_LARGE>(b, fields, quad, warps, st);
+    }
+    int *items = nullptr, *counts = nullptr;
+    TG_CUDA(dev_malloc((void **)&items, sizeof(int) * (int64_t)nheavy * ITEM_CAP, st));
+    TG_CUDA(dev_malloc((void **)&counts, sizeof(int) * nheavy, st));
+    TopArgs<T> ta;
+    ta.ar = ar;
+    ta.ntot = a.ntot;
+    ta.tc = a.tc; ta.ts = a.ts; ta.tsize = a.tsize; ta.tdelta = a.tdelta;
+    ta.tpos = a.tpos; ta.th = a.th;
+    ta.groups = a.groups;
+    ta.group_root = a.group_root;
+    ta.heavy = heavy;
+    ta.nheavy = nheavy;
+    ta.theta = a.theta;
+    ta.theta_group = a.theta_group;
+    ta.node_range = t->node_range;
+    ta.split_npart = (int)std::max<int64_t>(1024, t->ntot / 2048);
+    ta.items = items;
+    ta.item_count = counts;
+    ta.item_cap = ITEM_CAP;
+    ta.status = a.status;
+    { k_walk_top<T><<<div_up(nheavy, TOP_WARPS), TOP_WARPS * 32, 0, st>>>(ta); note_launch(); }
+    TG_CUDA(cudaGetLastError());
+    std::vector<int> hc(nheavy);
+    TG_CUDA(cudaMemcpyAsync(hc.data(), counts, sizeof(int) * nheavy, cudaMemcpyDeviceToHost, st));
+    TG_CUDA(cudaStreamSynchronize(st));
+    std::vector<int64_t> off(nheavy + 1, 0);
+    for (int u = 0; u < nheavy; u++) off[u + 1] = off[u] + hc[u];
+    const int64_t total = off[nheavy];
+    int *item_group = nullptr, *item_node = nullptr;
+    int64_t *doff = nullptr;
+    double *partial = nullptr;
+    if (total > 0) {
+        TG_CUDA(dev_malloc((void **)&item_group, sizeof(int) * total, st));
+        TG_CUDA(dev_malloc((void **)&item_node, sizeof(int) * total, st));
+        TG_CUDA(dev_malloc((void **)&doff, sizeof(int64_t) * (nheavy + 1), st));
+        TG_CUDA(dev_malloc((void **)&partial, sizeof(double) * 10 * a.gs * total, st));
+        TG_CUDA(cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (nheavy + 1), cudaMemcpyHostToDevice, st));
+        { k_flatten_items<<<nheavy, 256, 0, st>>>(heavy, nheavy, items, ITEM_CAP, doff, item_group, item_node); note_launch(); }
+        TG_CUDA(cudaMemsetAsync(b.queue, 0, sizeof(int), st));
+        b.group_order = nullptr;
+        b.item_group = item_group;
+        b.item_node = item_node;
+        b.partial = partial;
+        b.ngroups = total;
+        tg_status rc = dispatch_walk<T, STACK_LARGE>(b, fields, quad, warps, st);
+        if (rc == TG_OK) {
+            k_reduce_items<<<div_up((int64_t)nheavy * a.gs, 256), 256, 0, st>>>(heavy, nheavy, doff, a.groups, a.gs,
+                                                                                partial, a.scatter, a.out_fields,
+                                                                                a.out_w, a.G, a.out);
+            note_launch();
+        }
+        TG_CUDA(cudaGetLastError());
+        // the host offsets above must outlive the copy
+        TG_CUDA(cudaStreamSynchronize(st));
+        cudaFreeAsync(item_group, st);
+        cudaFreeAsync(item_node, st);
+        cudaFreeAsync(doff, st);
+        cudaFreeAsync(partial, st);
+        TG_TRY(rc);
+    }
+    cudaFreeAsync(items, st);
+    cudaFreeAsync(counts, st);
+    return TG_OK;
+}
+
+// Run a walk and time it on the stream; *status_out receives the device status word. With
+// split_heavy, groups past the entry budget are walked by walk_heavy.
+template <typename T>
+static tg_status walk_with_fallback(tg_tree_s *t, WalkArgs<T> &a, Arena<T> &ar, int fields, bool quad, int warps,
+                                    int first_stack, int *scratch, bool split_heavy, cudaStream_t st, int *status_out,
+                                    float *kernel_ms) {
     cudaEvent_t e0, e1;
     TG_CUDA(cudaEventCreate(&e0));
     TG_CUDA(cudaEventCreate(&e1));
     TG_CUDA(cudaEventRecord(e0, st));
-    tg_status rc = enqueue_walk<T>(a, fields, quad, warps, first_stack, scratch, st);
+    tg_status rc = enqueue_walk<T>(a, fields, quad, warps, first_stack, scratch, st, split_heavy);
+    int hdr[WS_RETRY_LIST] = {0};
+    if (rc == TG_OK && split_heavy) {
+        TG_CUDA(cudaMemcpyAsync(hdr, scratch, sizeof(hdr), cudaMemcpyDeviceToHost, st));
+        TG_CUDA(cudaStreamSynchronize(st));
+        if (hdr[WS_HEAVY_COUNT] > 0)
+            rc = walk_heavy<T>(t, a, ar, fields, quad, warps, scratch, hdr[WS_HEAVY_COUNT], st);
+    }
     TG_CUDA(cudaEventRecord(e1, st));
     int status = 0;
     TG_CUDA(cudaMemcpyAsync(&status, scratch + WS_STATUS, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1510,6 +1823,9 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         TG_CUDA(cudaMemsetAsync(t->gstats, 0, sizeof(unsigned) * 3 * std::max<int64_t>(ngroups, 1), st));
         gstats = t->gstats;
     }
+    // plain walks split their heavy groups (walks with per-group counters or tolerances keep every
+    // group whole: their per-group results are read back)
+    const bool split_heavy = !t->record_group_stats && !tol_group;
     float *gerr = nullptr;
     if (t->record_group_stats && tol_group) {
         if (t->gerr) cudaFreeAsync(t->gerr, st);
@@ -1539,7 +1855,8 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         { k_prep_targets<double><<<div_up(ntargets, 256), 256, 0, st>>>(tpos, th, ntargets, thi, tlo); tg::note_launch(); }
         a.thi = thi;
         a.tlo = tlo;
-        rc = walk_with_fallback<double>(a, fields, quadrupole != 0, t->walk_warps, t->walk_stack, scratch, st, &status,
+        rc = walk_with_fallback<double>(t, a, t->arena64, fields, quadrupole != 0, t->walk_warps, t->walk_stack,
+                                        scratch, split_heavy, st, &status,
                                         &kms);
         cudaFreeAsync(thi, st);
         cudaFreeAsync(tlo, st);
@@ -1564,14 +1881,17 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         { k_prep_targets<float><<<div_up(ntargets, 256), 256, 0, st>>>(tpos, th, ntargets, thi, tlo); tg::note_launch(); }
         a.thi = thi;
         a.tlo = tlo;
-        rc = walk_with_fallback<float>(a, fields, quadrupole != 0, t->walk_warps, t->walk_stack, scratch, st, &status,
+        rc = walk_with_fallback<float>(t, a, t->arena32, fields, quadrupole != 0, t->walk_warps, t->walk_stack,
+                                       scratch, split_heavy, st, &status,
                                        &kms);
         cudaFreeAsync(thi, st);
         cudaFreeAsync(tlo, st);
     }
     if (rc != TG_OK) return rc;
     unsigned long long stats[8];
+    int sort_bad = 0;
     TG_CUDA(cudaMemcpyAsync(stats, t->stats_dev, sizeof(stats), cudaMemcpyDeviceToHost, st));
+    if (t->sort_err) TG_CUDA(cudaMemcpyAsync(&sort_bad, t->sort_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     TG_CUDA(cudaFreeAsync(scratch, st));
     TG_CUDA(cudaStreamSynchronize(st));
     t->last_stats.interactions = (int64_t)stats[0];
@@ -1581,7 +1901,11 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
     t->last_stats.steps = (int64_t)stats[3];
     t->last_stats.quad_interactions = (int64_t)stats[4];
     t->last_stats.kernel_ms = kms;
-    TG_TRY(sort_error_check());  // the grouping's sorts
+    if (sort_bad) {  // the grouping's or the queue order's sort (reported once; the groups are valid)
+        cudaMemsetAsync(t->sort_err, 0, sizeof(int), st);
+        set_last_error_msg("radix sort: a tile's look-back did not complete within its bound");
+        return TG_ERR_QUEUE_TIMEOUT;
+    }
     if (status & (1 << TG_ERR_CUDA)) {
         set_last_error_msg("internal error: tree links do not form a valid octree for the walk arena");
         return TG_ERR_CUDA;
@@ -1636,7 +1960,7 @@ tg_status tree_groups(tg_tree_s *t, int G, cudaStream_t st) {
     TG_CUDA(tg::dev_malloc((void **)&t->group_root, sizeof(int) * ng1, st));
     TG_CUDA(tg::dev_malloc((void **)&t->group_node, sizeof(int) * ng1, st));
     { k_group_start_keys<<<div_up(ng, 256), 256, 0, st>>>(g0, ng, keys, vals); tg::note_launch(); }
-    TG_TRY(radix_sort_pairs(keys, vals, ng, 32, st));
+    TG_TRY(radix_sort_pairs(keys, vals, ng, 32, st, t->sort_err));
     { k_permute_groups<<<div_up(ng, 256), 256, 0, st>>>(vals, ng, g0, r0, n0, t->groups, t->group_root, t->group_node); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
     TG_CUDA(cudaFreeAsync(keys, st));
@@ -1696,13 +2020,14 @@ tg_status tree_groups_with_arena(tg_tree_s *t, int G, bool fp64, cudaStream_t st
 }
 
 // Largest-first queue order of consecutive-block groups (see k_group_cost_keys).
-tg_status make_cost_order(const double *tpos, const int2 *groups, int64_t ngroups, int **order, cudaStream_t st) {
+tg_status make_cost_order(const double *tpos, const int2 *groups, int64_t ngroups, int **order, cudaStream_t st,
+                          int *sort_err) {
     uint64_t *keys = nullptr;
     TG_CUDA(tg::dev_malloc((void **)&keys, sizeof(uint64_t) * std::max<int64_t>(ngroups, 1), st));
     TG_CUDA(tg::dev_malloc((void **)order, sizeof(int) * std::max<int64_t>(ngroups, 1), st));
     { k_group_cost_keys<<<div_up(ngroups, 256), 256, 0, st>>>(tpos, groups, ngroups, keys, (uint32_t *)*order); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
-    TG_TRY(radix_sort_pairs(keys, (uint32_t *)*order, ngroups, 32, st));
+    TG_TRY(radix_sort_pairs(keys, (uint32_t *)*order, ngroups, 32, st, sort_err));
     TG_CUDA(cudaFreeAsync(keys, st));
     return TG_OK;
 }
@@ -1803,7 +2128,7 @@ tg_status tg_walk_graph_create(tg_tree t, int fields, int quadrupole, double the
         ng = t->ngroups;
     } else {
         if ((rc = make_groups(t, t->sys_off, group_size, &g->groups, &g->groot, &ng, cs)) != TG_OK) return fail(rc);
-        if ((rc = make_cost_order(t->coord, g->groups, ng, &g->gorder, cs)) != TG_OK) return fail(rc);
+        if ((rc = make_cost_order(t->coord, g->groups, ng, &g->gorder, cs, t->sort_err)) != TG_OK) return fail(rc);
         wg = g->groups;
         wr = g->groot;
     }
@@ -1816,7 +2141,14 @@ tg_status tg_walk_graph_create(tg_tree t, int fields, int quadrupole, double the
         dev_malloc((void **)&g->scratch, sizeof(int) * walk_scratch_ints(ng), cs) != cudaSuccess)
         return fail(TG_ERR_OOM);
     { k_prep_targets<float><<<div_up(n, 256), 256, 0, cs>>>(t->coord, t->soft, n, g->thi, g->tlo); note_launch(); }
+    int sort_bad = 0;
+    if (t->sort_err && cudaMemcpyAsync(&sort_bad, t->sort_err, sizeof(int), cudaMemcpyDeviceToHost, cs) != cudaSuccess)
+        return fail(TG_ERR_CUDA);
     if (cudaStreamSynchronize(cs) != cudaSuccess) return fail(TG_ERR_CUDA);
+    if (sort_bad) {  // the grouping's or the queue order's sort
+        set_last_error_msg("radix sort: a tile's look-back did not complete within its bound");
+        return fail(TG_ERR_QUEUE_TIMEOUT);
+    }
 
     WalkArgs<float> a;
     a.ar = t->arena32;
