@@ -17,6 +17,7 @@
 // within any target's softening length (checked once per source against the group box) take the
 // point-mass path; the rest take the full softened path. Each lane sums a batch in registers and
 // adds the batch total into a Kahan-compensated accumulator.
+#include <algorithm>
 #include <new>
 #include <type_traits>
 #include <vector>
@@ -1511,9 +1512,8 @@ __global__ void __launch_bounds__(TOP_WARPS * 32) k_walk_top(TopArgs<T> a) {
         const int both = warp_inclusive_scan(nit | (npush << 16));
         const int tot = __shfl_sync(FULL, both, 31);
         const int toti = tot & 0xffff, totp = tot >> 16;
-        if (nitems + toti > a.item_cap || sp + totp > TOP_STACK) {
-            if (lane == 0) atomicOr(a.status, 1 << TG_ERR_STACK_OVERFLOW);
-            failed = true;
+        if (nitems + toti > a.item_cap || sp + totp > TOP_STACK) {  // this group is walked whole instead
+            nitems = -1;
             break;
         }
         int oi = nitems + (both & 0xffff) - nit, op = sp + (both >> 16) - npush;
@@ -1533,7 +1533,7 @@ __global__ void __launch_bounds__(TOP_WARPS * 32) k_walk_top(TopArgs<T> a) {
         __syncwarp();
         (void)lt;
     }
-    if (lane == 0) a.item_count[u] = failed ? 0 : nitems;
+    if (lane == 0) a.item_count[u] = failed ? 0 : nitems;  // -1: too many items, walk the group whole
 }
 
 // Items of every unit, flattened in unit order: item k -> (group, start node).
@@ -1551,12 +1551,13 @@ __global__ void k_flatten_items(const int *heavy, int nheavy, const int *items, 
 
 // One thread per (unit, target slot): the unit's item sums added in item order, G times them written
 // to the target's row.
-__global__ void k_reduce_items(const int *heavy, int nheavy, const int64_t *off, const int2 *groups, int gs,
-                               const double *partial, const int64_t *scatter, int out_fields, int out_w, double G,
-                               double *out) {
+__global__ void k_reduce_items(const int *heavy, int nheavy, const int64_t *off, const int *count, const int2 *groups,
+                               int gs, const double *partial, const int64_t *scatter, int out_fields, int out_w,
+                               double G, double *out) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (int64_t)nheavy * gs) return;
     const int u = (int)(i / gs), slot = (int)(i % gs);
+    if (count[u] < 0) return;  // walked whole
     const int2 gr = groups[heavy[u]];
     if (slot >= gr.y) return;
     double v[10];
@@ -1697,15 +1698,19 @@ static tg_status walk_heavy(tg_tree_s *t, const WalkArgs<T> &a, Arena<T> &ar, in
     b.rewalk = b.rewalk_count = nullptr;
     b.ngroups_dev = nullptr;
     b.queue = scratch + WS_HEAVY_QUEUE;
-    if ((int64_t)nheavy * ITEM_CAP > ((int64_t)1 << 28)) {  // too many to list: walk them whole
+    // subtrees of at most split_npart particles become items; a top walk opens only larger nodes, of
+    // which a tree holds about 2 N / split_npart, each giving at most 16 items (8 particles, 8 nodes)
+    const int split_npart = (int)std::max<int64_t>(1024, t->ntot / 2048);
+    const int cap = (int)std::min<int64_t>(1 << 16, std::max<int64_t>(1024, 16 * (2 * t->ntot / split_npart + 8)));
+    if ((int64_t)nheavy * cap > ((int64_t)1 << 28)) {  // too many to list: walk them whole
         TG_CUDA(cudaMemsetAsync(b.queue, 0, sizeof(int), st));
         b.group_order = heavy;
         b.ngroups = nheavy;
         return dispatch_walk<T, STACK_LARGE>(b, fields, quad, warps, st);
     }
-    int *items = nullptr, *counts = nullptr;
-    TG_CUDA(dev_malloc((void **)&items, sizeof(int) * (int64_t)nheavy * ITEM_CAP, st));
-    TG_CUDA(dev_malloc((void **)&counts, sizeof(int) * nheavy, st));
+    DevArray<int> items(st), counts(st);
+    TG_CUDA(items.alloc((int64_t)nheavy * cap));
+    TG_CUDA(counts.alloc(nheavy));
     TopArgs<T> ta;
     ta.ar = ar;
     ta.ntot = a.ntot;
@@ -1718,53 +1723,58 @@ static tg_status walk_heavy(tg_tree_s *t, const WalkArgs<T> &a, Arena<T> &ar, in
     ta.theta = a.theta;
     ta.theta_group = a.theta_group;
     ta.node_range = t->node_range;
-    ta.split_npart = (int)std::max<int64_t>(1024, t->ntot / 2048);
-    ta.items = items;
-    ta.item_count = counts;
-    ta.item_cap = ITEM_CAP;
+    ta.split_npart = split_npart;
+    ta.items = items.p;
+    ta.item_count = counts.p;
+    ta.item_cap = cap;
     ta.status = a.status;
     { k_walk_top<T><<<div_up(nheavy, TOP_WARPS), TOP_WARPS * 32, 0, st>>>(ta); note_launch(); }
     TG_CUDA(cudaGetLastError());
-    std::vector<int> hc(nheavy);
-    TG_CUDA(cudaMemcpyAsync(hc.data(), counts, sizeof(int) * nheavy, cudaMemcpyDeviceToHost, st));
+    std::vector<int> hc(nheavy), hg(nheavy);
+    TG_CUDA(cudaMemcpyAsync(hc.data(), counts.p, sizeof(int) * nheavy, cudaMemcpyDeviceToHost, st));
+    TG_CUDA(cudaMemcpyAsync(hg.data(), heavy, sizeof(int) * nheavy, cudaMemcpyDeviceToHost, st));
     TG_CUDA(cudaStreamSynchronize(st));
     std::vector<int64_t> off(nheavy + 1, 0);
-    for (int u = 0; u < nheavy; u++) off[u + 1] = off[u] + hc[u];
+    std::vector<int> whole;  // groups with more items than the list holds
+    for (int u = 0; u < nheavy; u++) {
+        off[u + 1] = off[u] + std::max(hc[u], 0);
+        if (hc[u] < 0) whole.push_back(hg[u]);
+    }
+    std::sort(whole.begin(), whole.end());
     const int64_t total = off[nheavy];
-    int *item_group = nullptr, *item_node = nullptr;
-    int64_t *doff = nullptr;
-    double *partial = nullptr;
+    DevArray<int> item_group(st), item_node(st), dwhole(st);
+    DevArray<int64_t> doff(st);
+    DevArray<double> partial(st);
+    if (!whole.empty()) {
+        TG_CUDA(dwhole.alloc((int64_t)whole.size()));
+        TG_CUDA(cudaMemcpyAsync(dwhole.p, whole.data(), sizeof(int) * whole.size(), cudaMemcpyHostToDevice, st));
+        TG_CUDA(cudaMemsetAsync(b.queue, 0, sizeof(int), st));
+        WalkArgs<T> w = b;
+        w.group_order = dwhole.p;
+        w.ngroups = (int64_t)whole.size();
+        TG_TRY((dispatch_walk<T, STACK_LARGE>(w, fields, quad, warps, st)));
+    }
     if (total > 0) {
-        TG_CUDA(dev_malloc((void **)&item_group, sizeof(int) * total, st));
-        TG_CUDA(dev_malloc((void **)&item_node, sizeof(int) * total, st));
-        TG_CUDA(dev_malloc((void **)&doff, sizeof(int64_t) * (nheavy + 1), st));
-        TG_CUDA(dev_malloc((void **)&partial, sizeof(double) * 10 * a.gs * total, st));
-        TG_CUDA(cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (nheavy + 1), cudaMemcpyHostToDevice, st));
-        { k_flatten_items<<<nheavy, 256, 0, st>>>(heavy, nheavy, items, ITEM_CAP, doff, item_group, item_node); note_launch(); }
+        TG_CUDA(item_group.alloc(total));
+        TG_CUDA(item_node.alloc(total));
+        TG_CUDA(doff.alloc(nheavy + 1));
+        TG_CUDA(partial.alloc(10 * (int64_t)a.gs * total));
+        TG_CUDA(cudaMemcpyAsync(doff.p, off.data(), sizeof(int64_t) * (nheavy + 1), cudaMemcpyHostToDevice, st));
+        { k_flatten_items<<<nheavy, 256, 0, st>>>(heavy, nheavy, items.p, cap, doff.p, item_group.p, item_node.p); note_launch(); }
         TG_CUDA(cudaMemsetAsync(b.queue, 0, sizeof(int), st));
         b.group_order = nullptr;
-        b.item_group = item_group;
-        b.item_node = item_node;
-        b.partial = partial;
+        b.item_group = item_group.p;
+        b.item_node = item_node.p;
+        b.partial = partial.p;
         b.ngroups = total;
-        tg_status rc = dispatch_walk<T, STACK_LARGE>(b, fields, quad, warps, st);
-        if (rc == TG_OK) {
-            k_reduce_items<<<div_up((int64_t)nheavy * a.gs, 256), 256, 0, st>>>(heavy, nheavy, doff, a.groups, a.gs,
-                                                                                partial, a.scatter, a.out_fields,
-                                                                                a.out_w, a.G, a.out);
-            note_launch();
-        }
+        TG_TRY((dispatch_walk<T, STACK_LARGE>(b, fields, quad, warps, st)));
+        { k_reduce_items<<<div_up((int64_t)nheavy * a.gs, 256), 256, 0, st>>>(heavy, nheavy, doff.p, counts.p, a.groups,
+                                                                              a.gs, partial.p, a.scatter, a.out_fields,
+                                                                              a.out_w, a.G, a.out); note_launch(); }
         TG_CUDA(cudaGetLastError());
-        // the host offsets above must outlive the copy
-        TG_CUDA(cudaStreamSynchronize(st));
-        cudaFreeAsync(item_group, st);
-        cudaFreeAsync(item_node, st);
-        cudaFreeAsync(doff, st);
-        cudaFreeAsync(partial, st);
-        TG_TRY(rc);
     }
-    cudaFreeAsync(items, st);
-    cudaFreeAsync(counts, st);
+    // the host vectors above must outlive their copies
+    TG_CUDA(cudaStreamSynchronize(st));
     return TG_OK;
 }
 
