@@ -207,9 +207,11 @@ __global__ void k_sys_of(const uint32_t *vals, int64_t n, const int64_t *sys_off
 }
 
 // _permute_particles (octree.py:577-603)
+// sort_err set (the sort gave up and left the identity permutation): the keys stay the sort's
+// fallback keys i, so that every later kernel sees sorted keys (the build then reports the error).
 __global__ void k_gather(const uint32_t *perm, int64_t n, const double *pos, const double *m, const double *h,
                          const uint64_t *keys_in, double *coord, double *mass, double *soft, uint64_t *keys_sorted,
-                         int64_t *walk_idx) {
+                         int64_t *walk_idx, const int *sort_err) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int64_t o = perm[i];
@@ -218,7 +220,7 @@ __global__ void k_gather(const uint32_t *perm, int64_t n, const double *pos, con
     coord[3 * i + 2] = pos[3 * o + 2];
     mass[i] = m ? m[o] : 0.0;
     soft[i] = h ? h[o] : 0.0;
-    keys_sorted[i] = keys_in[o];
+    keys_sorted[i] = *sort_err ? (uint64_t)i : keys_in[o];
     walk_idx[i] = o;
 }
 
@@ -518,9 +520,10 @@ __global__ void k_rekey_segkeys(RoundView v, const uint32_t *vals, int64_t E, ui
     if (a < E) out[a] = (uint64_t)find_seg(v.eoff, v.nseg, (int64_t)vals[a]);
 }
 // gather the permuted slice into temporaries (by element), then write back
+// sort_err set: the segments' keys become their element indices (sorted within every segment).
 __global__ void k_rekey_gather(RoundView v, int64_t E, const uint32_t *vals, const double *coord, const double *mass,
                                const double *soft, const int64_t *widx, const uint64_t *newkeys_by_elem, double *tc,
-                               double *tm, double *ts, int64_t *tw, uint64_t *tk) {
+                               double *tm, double *ts, int64_t *tw, uint64_t *tk, const int *sort_err) {
     int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= E) return;
     int64_t esrc = vals[a];
@@ -533,7 +536,7 @@ __global__ void k_rekey_gather(RoundView v, int64_t E, const uint32_t *vals, con
     tm[a] = mass[isrc];
     ts[a] = soft[isrc];
     tw[a] = widx[isrc];
-    tk[a] = newkeys_by_elem[esrc];
+    tk[a] = *sort_err ? (uint64_t)a : newkeys_by_elem[esrc];
 }
 __global__ void k_rekey_scatter(RoundView v, int64_t E, const double *tc, const double *tm, const double *ts,
                                 const int64_t *tw, const uint64_t *tk, double *coord, double *mass, double *soft,
@@ -695,10 +698,16 @@ __global__ void k_number_keys(Nodes nd, int64_t count, const int64_t *sys_off, N
     atomicAdd(nonroot_count, 1);
 }
 
+// sort_err set (the numbering sort left the identity, roots not last): every slot keeps its own
+// index, a bijection onto the node range, so the arrays written from it stay in bounds.
 __global__ void k_final_index(const uint32_t *vals, int64_t count, const int32_t *nd_sys, int64_t ntot,
                               const int64_t *sys_node_off, int64_t *final_of_slot, const int64_t *root_slot_of_sys,
-                              int nsys) {
+                              int nsys, const int *sort_err) {
     int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (*sort_err) {
+        if (q < count) final_of_slot[q] = ntot + q;
+        return;
+    }
     if (q < count) {
         int64_t c = vals[q];
         int s = nd_sys[c];
@@ -1379,7 +1388,7 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     TG_TRY(dalloc(&ps, N, st));
     uint64_t *keys_sorted = keys;  // reuse
     if (m_h_ready) TG_CUDA(cudaStreamWaitEvent(st, m_h_ready, 0));
-    { k_gather<<<LAUNCH(N)>>>(perm, N, pos, m, h, keys_orig, pc, pm, ps, keys_sorted, T->walk_idx); tg::note_launch(); }
+    { k_gather<<<LAUNCH(N)>>>(perm, N, pos, m, h, keys_orig, pc, pm, ps, keys_sorted, T->walk_idx, T->sort_err); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
     dfree(keys_orig, st);
 
@@ -1446,7 +1455,7 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
             TG_TRY(dalloc(&ts, E, st));
             TG_TRY(dalloc(&tw, E, st));
             TG_TRY(dalloc(&tk, E, st));
-            { k_rekey_gather<<<LAUNCH(E)>>>(v, E, rv, pc, pm, ps, T->walk_idx, rk_elem, tc, tm, ts, tw, tk); tg::note_launch(); }
+            { k_rekey_gather<<<LAUNCH(E)>>>(v, E, rv, pc, pm, ps, T->walk_idx, rk_elem, tc, tm, ts, tw, tk, T->sort_err); tg::note_launch(); }
             { k_rekey_scatter<<<LAUNCH(E)>>>(v, E, tc, tm, ts, tw, tk, pc, pm, ps, T->walk_idx, keys_sorted); tg::note_launch(); }
             TG_CUDA(cudaGetLastError());
             dfree(rk, st); dfree(rk_elem, st); dfree(rv, st);
@@ -1585,7 +1594,7 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
         T->sys_node_off.assign(nsys + 1, 0);
     }
     { k_final_index<<<LAUNCH(std::max<int64_t>(M, nsys))>>>(nvals, M, nd.sys, N, sys_node_off, final_of_slot, root_slot,
-                                                         nsys); tg::note_launch(); }
+                                                         nsys, T->sort_err); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
     // capacity (NumNodes) per system: bucket reservations, read with the final synchronisation
     unsigned long long *req = nullptr;
