@@ -30,6 +30,9 @@ struct Arena {
     vec4<T> *n_pos = nullptr;   // interaction record: hi.xyz, M
     vec4<T> *n_lo = nullptr;    // lo.xyz, hmax
     vec4<T> *n_quad = nullptr;  // two per node: (xx, xy, xz, yy), (yz, zz, 0, 0)
+    // FP32 arenas: per node (M s^3)^(1/5) and (M s^2)^(1/4), the mass-aware acceptance test's
+    // node factor for quadrupole and monopole walks (a group's tolerance scales it)
+    float2 *n_tol = nullptr;
     int4 *n_link = nullptr;     // first node child, node children, leaf start, leaves (build scratch)
     // per leaf
     vec4<T> *l_pos = nullptr;  // hi.xyz, m

@@ -212,6 +212,16 @@ __global__ void k_arena_nodes(int64_t ntot, int64_t mtot, const double *coord, c
     ar.n_trav[2 * j] = vec4<T>{hx, hy, hz, narrow(size[f], T(0))};
     ar.n_trav[2 * j + 1] = vec4<T>{narrow(delta[f], T(0)), hm, int_bits((fc << 4) | lk.y, T(0)),
                                    int_bits((lk.z << 4) | lk.w, T(0))};
+    if (ar.n_tol) {  // log form: no underflow for tiny nodes; zero for massless or empty ones
+        const float mf = d2f(mass[f]), sf = d2f(size[f]);
+        float a3 = 0.f, a2 = 0.f;
+        if (mf > 0.f && sf > 0.f) {
+            const float lm = log2f(mf), ls = log2f(sf);
+            a3 = exp2f(0.2f * (lm + 3.f * ls));
+            a2 = exp2f(0.25f * (lm + 2.f * ls));
+        }
+        ar.n_tol[j] = make_float2(a3, a2);
+    }
     if (ar.n_quad) {
         const double *Q = quad + 9 * j;
         ar.n_quad[2 * j] = vec4<T>{narrow(Q[0], T(0)), narrow(Q[1], T(0)), narrow(Q[2], T(0)), narrow(Q[4], T(0))};
@@ -241,6 +251,7 @@ tg_status build_arena_topology(tg_tree_s *t, Arena<T> &ar, cudaStream_t st) {
     TG_CUDA(tg::dev_malloc((void **)&ar.n_trav, sizeof(vec4<T>) * 2 * M, st));
     TG_CUDA(tg::dev_malloc((void **)&ar.n_link, sizeof(int4) * M, st));
     if (ar.has_quad) TG_CUDA(tg::dev_malloc((void **)&ar.n_quad, sizeof(vec4<T>) * 2 * M, st));
+    if (sizeof(T) == 4) TG_CUDA(tg::dev_malloc((void **)&ar.n_tol, sizeof(float2) * M, st));
     TG_CUDA(tg::dev_malloc((void **)&ar.l_pos, sizeof(vec4<T>) * N, st));
     TG_CUDA(tg::dev_malloc((void **)&ar.l_lo, sizeof(vec4<T>) * N, st));
     int64_t *nleaf = nullptr, *lstart = nullptr, *ltot = nullptr;
@@ -288,6 +299,7 @@ void free_arena(Arena<T> &ar, cudaStream_t st) {
     if (ar.n_trav) cudaFreeAsync(ar.n_trav, st);
     if (ar.n_link) cudaFreeAsync(ar.n_link, st);
     if (ar.n_quad) cudaFreeAsync(ar.n_quad, st);
+    if (ar.n_tol) cudaFreeAsync(ar.n_tol, st);
     if (ar.l_pos) cudaFreeAsync(ar.l_pos, st);
     if (ar.l_lo) cudaFreeAsync(ar.l_lo, st);
     if (ar.bad) cudaFreeAsync(ar.bad, st);
@@ -351,7 +363,12 @@ struct WalkArgs {
     const int *item_group = nullptr, *item_node = nullptr;
     double *partial = nullptr;
     int64_t step_limit = 0;  // traversal steps per group (0: the node count, which always suffices)
+    // the arena does not fit in L2: records of pushed nodes, listed leaves and accepted nodes are
+    // prefetched into L2 when they are queued, ahead of the step or batch that reads them
+    int prefetch = 0;
 };
+
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 template <typename T, bool QUAD, int STACK>
 struct WarpSmem {
@@ -644,6 +661,8 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
         const bool track_err = mass_aware && (FIELDS & F_ACC) && (a.gerr || a.rewalk);
         float err_est = 0.f;  // this lane's share of the group's truncation estimate
         const T inv_tol = mass_aware ? (T)(1.0 / (double)tolg) : T(0);
+        // FP32: a node's mass-aware radius is its stored factor times tol^(-1/(p+2))
+        const float tol_k = (sizeof(T) == 4 && mass_aware) ? exp2f(-log2f(tolg) * (QUAD ? 0.2f : 0.25f)) : 0.f;
         const T rel_eps = sizeof(T) == 4 ? T(1e-5) : T(0);
         const T abs_eps = sizeof(T) == 4 ? T(1e-6) : T(0);
         // softening-path threshold: a source whose squared distance to the box exceeds this cannot
@@ -966,6 +985,10 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
                     n_tests++;
                     const vec4<T> p = a.ar.n_trav[2 * node];
                     r1 = a.ar.n_trav[2 * node + 1];
+                    float2 tq = make_float2(0.f, 0.f);
+                    if constexpr (sizeof(T) == 4) {
+                        if (mass_aware) tq = a.ar.n_tol[node];  // issued with the traversal record
+                    }
                     T dx = fmax(fmax(abmin[0] - p.x, p.x - abmax[0]), T(0));
                     T dy = fmax(fmax(abmin[1] - p.y, p.y - abmax[1]), T(0));
                     T dz = fmax(fmax(abmin[2] - p.z, p.z - abmax[2]), T(0));
@@ -974,10 +997,17 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
                     T c1 = p.w * inv_theta + r1.x, c2 = h + T(0.6) * p.w + r1.x;
                     T msp = T(0);  // M s^p of the node (tolerance test only)
                     if (mass_aware) {
-                        msp = a.ar.n_pos[node].w * (QUAD ? p.w * p.w * p.w : p.w * p.w);
-                        const T q = msp * inv_tol;
-                        const T rc = QUAD ? pow_fifth(q) : sqrt(sqrt(q));
-                        c1 = fmax(p.w * inv_theta, rc) + r1.x;
+                        if constexpr (sizeof(T) == 4) {
+                            const float av = QUAD ? tq.x : tq.y;
+                            const float av2 = av * av;
+                            msp = QUAD ? av2 * av2 * av : av2 * av2;
+                            c1 = fmax(p.w * inv_theta, av * tol_k) + r1.x;
+                        } else {
+                            msp = a.ar.n_pos[node].w * (QUAD ? p.w * p.w * p.w : p.w * p.w);
+                            const T q = msp * inv_tol;
+                            const T rc = QUAD ? pow_fifth(q) : sqrt(sqrt(q));
+                            c1 = fmax(p.w * inv_theta, rc) + r1.x;
+                        }
                     }
                     T crit = c1 > c2 ? c1 : c2;
                     // FP32 error bound: node positions near the boundary are within gscale + 2 crit of
@@ -1024,6 +1054,24 @@ __global__ void __launch_bounds__(MAX_WALK_WARPS * 32) __maxnreg__((walk_reg_cap
                 const int fc = cbits >> 4, ls = lbits >> 4;
                 for (int j = 0, o = sp + sc - nc; j < nc; j++) sm.stack[o + j] = fc + j;
                 for (int j = 0, o = ni + sl - nl; j < nl; j++) sm.ilist[o + j] = ~(ls + j);
+                if (a.prefetch) {  // warp-uniform; records are 16 or 32 bytes, lines 128
+                    if (nc > 0) {
+                        prefetch_l2(a.ar.n_trav + 2 * fc);
+                        if (nc > 2) prefetch_l2(a.ar.n_trav + 2 * (fc + nc - 1));
+                        if constexpr (sizeof(T) == 4) {
+                            if (mass_aware) prefetch_l2(a.ar.n_tol + fc);
+                        }
+                    }
+                    if (nl > 0) {
+                        prefetch_l2(a.ar.l_pos + ls);
+                        prefetch_l2(a.ar.l_lo + ls);
+                    }
+                    if (acc) {
+                        prefetch_l2(a.ar.n_pos + node);
+                        prefetch_l2(a.ar.n_lo + node);
+                        if (QUAD) prefetch_l2(a.ar.n_quad + 2 * node);
+                    }
+                }
                 sp += totc;
                 ni += totl;
                 max_sp = max(max_sp, sp);
@@ -1807,6 +1855,21 @@ static tg_status walk_with_fallback(tg_tree_s *t, WalkArgs<T> &a, Arena<T> &ar, 
     return rc;
 }
 
+// Whether a walk arena is larger than the GPU's L2 (the walk then prefetches the records it queues).
+template <typename T>
+static int arena_exceeds_l2(const Arena<T> &ar) {
+    static int l2 = -1;
+    if (l2 < 0) {
+        int dev = 0;
+        l2 = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+        if (l2 <= 0) l2 = 128 << 20;
+    }
+    const int64_t bytes = ar.n_nodes * (int64_t)sizeof(vec4<T>) * (ar.n_quad ? 6 : 4) +
+                          ar.n_leaves * (int64_t)sizeof(vec4<T>) * 2 + (ar.n_tol ? ar.n_nodes * 8 : 0);
+    return bytes > (int64_t)l2;
+}
+
 // Walk targets already in walk order (tpos/th on the device). groups/group_root describe the
 // grouping; scatter maps walk order to output rows.
 tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t ntargets, const int2 *groups,
@@ -1859,6 +1922,7 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         a.out_fields = fields; a.out_w = w; a.out = out; a.gs = group_size;
         a.stats = (unsigned long long *)t->stats_dev;
         a.gstats = gstats;
+        a.prefetch = arena_exceeds_l2(t->arena64);
         vec4<double> *thi = nullptr, *tlo = nullptr;
         TG_CUDA(tg::dev_malloc((void **)&thi, sizeof(vec4<double>) * std::max<int64_t>(ntargets, 1), st));
         TG_CUDA(tg::dev_malloc((void **)&tlo, sizeof(vec4<double>) * std::max<int64_t>(ntargets, 1), st));
@@ -1885,6 +1949,7 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         a.out_fields = fields; a.out_w = w; a.out = out; a.gs = group_size;
         a.stats = (unsigned long long *)t->stats_dev;
         a.gstats = gstats;
+        a.prefetch = arena_exceeds_l2(t->arena32);
         vec4<float> *thi = nullptr, *tlo = nullptr;
         TG_CUDA(tg::dev_malloc((void **)&thi, sizeof(vec4<float>) * std::max<int64_t>(ntargets, 1), st));
         TG_CUDA(tg::dev_malloc((void **)&tlo, sizeof(vec4<float>) * std::max<int64_t>(ntargets, 1), st));
