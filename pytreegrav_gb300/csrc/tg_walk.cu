@@ -1597,26 +1597,46 @@ __global__ void k_flatten_items(const int *heavy, int nheavy, const int *items, 
     }
 }
 
-// One thread per (unit, target slot): the unit's item sums added in item order, G times them written
-// to the target's row.
-__global__ void k_reduce_items(const int *heavy, int nheavy, const int64_t *off, const int *count, const int2 *groups,
-                               int gs, const double *partial, const int64_t *scatter, int out_fields, int out_w,
-                               double G, double *out) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (int64_t)nheavy * gs) return;
-    const int u = (int)(i / gs), slot = (int)(i % gs);
-    if (count[u] < 0) return;  // walked whole
+// One block per (unit, target slot): thread t sums the unit's items t, t + RED_THREADS, ... in order,
+// then a fixed-shape tree in shared memory adds the threads' sums (the same order on every run); G
+// times the total is written to the target's row.
+constexpr int RED_THREADS = 256;
+__global__ void __launch_bounds__(RED_THREADS) k_reduce_items(const int *heavy, int nheavy, const int64_t *off,
+                                                              const int *count, const int2 *groups, int gs,
+                                                              const double *partial, const int64_t *scatter,
+                                                              int out_fields, int out_w, double G, double *out) {
+    __shared__ double sh[10][RED_THREADS];
+    const int u = blockIdx.x / gs, slot = blockIdx.x % gs;
+    if (u >= nheavy || count[u] < 0) return;  // block-uniform: walked whole
     const int2 gr = groups[heavy[u]];
-    if (slot >= gr.y) return;
+    if (slot >= gr.y) return;  // block-uniform
+    const int t = threadIdx.x;
     double v[10];
+#pragma unroll
     for (int c = 0; c < 10; c++) v[c] = 0.0;
-    for (int64_t k = off[u]; k < off[u + 1]; k++) {
+    for (int64_t k = off[u] + t; k < off[u + 1]; k += RED_THREADS) {
         const double *p = partial + (k * gs + slot) * 10;
+#pragma unroll
         for (int c = 0; c < 10; c++) v[c] += p[c];
     }
-    const int64_t t = gr.x + slot;
-    const int64_t row = scatter ? scatter[t] : t;
-    write_fields(out + row * out_w, out_fields, v, G);
+#pragma unroll
+    for (int c = 0; c < 10; c++) sh[c][t] = v[c];
+    __syncthreads();
+    for (int w = RED_THREADS / 2; w > 0; w >>= 1) {
+        if (t < w) {
+#pragma unroll
+            for (int c = 0; c < 10; c++) sh[c][t] += sh[c][t + w];
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        double tot[10];
+#pragma unroll
+        for (int c = 0; c < 10; c++) tot[c] = sh[c][0];
+        const int64_t tg_ = gr.x + slot;
+        const int64_t row = scatter ? scatter[tg_] : tg_;
+        write_fields(out + row * out_w, out_fields, tot, G);
+    }
 }
 
 template <typename T, int FIELDS, bool QUAD, int STACK>
@@ -1816,9 +1836,9 @@ static tg_status walk_heavy(tg_tree_s *t, const WalkArgs<T> &a, Arena<T> &ar, in
         b.partial = partial.p;
         b.ngroups = total;
         TG_TRY((dispatch_walk<T, STACK_LARGE>(b, fields, quad, warps, st)));
-        { k_reduce_items<<<div_up((int64_t)nheavy * a.gs, 256), 256, 0, st>>>(heavy, nheavy, doff.p, counts.p, a.groups,
-                                                                              a.gs, partial.p, a.scatter, a.out_fields,
-                                                                              a.out_w, a.G, a.out); note_launch(); }
+        { k_reduce_items<<<(unsigned)((int64_t)nheavy * a.gs), RED_THREADS, 0, st>>>(heavy, nheavy, doff.p, counts.p,
+                                                                                     a.groups, a.gs, partial.p, a.scatter,
+                                                                                     a.out_fields, a.out_w, a.G, a.out); note_launch(); }
         TG_CUDA(cudaGetLastError());
     }
     // the host vectors above must outlive their copies
