@@ -144,8 +144,11 @@ tg_status tg_walk_graph_free(tg_walk_graph graph);
  * Morton keys (_morton_order, grouped_treewalk.py:269-275; that grouping is tg_tree_fields with
  * TG_ORDER_MORTON). Here the targets get an octree of their own (the radix build, no masses) and
  * are grouped by it -- subtrees and runs of siblings of at most group_size targets, the rule of
- * TG_GROUP_TREE -- so no group straddles a jump of the Morton curve. pos (n, 3) and h (n,; NULL:
- * zeros) are read from host or device memory (mem); the source tree must outlive the set. */
+ * TG_GROUP_TREE -- so no group straddles a jump of the Morton curve; a group whose box holds many
+ * more sources than targets (the deepest source cell around it, taken as evenly filled) is cut
+ * into runs of consecutive targets, so that, as in the source tree's own grouping, a group's box
+ * holds about as many sources as targets. pos (n, 3) and h (n,; NULL: zeros) are read from host or
+ * device memory (mem); the source tree must outlive the set. Synchronises `stream`. */
 typedef struct tg_targets_s *tg_targets;
 tg_status tg_targets_create(tg_tree source, const double *pos, const double *h, int64_t n, int group_size, int mem,
                             void *stream, tg_targets *out);

@@ -7,9 +7,12 @@
 // straddles a jump of the Morton curve gets a bounding box spanning both sides and opens far more of
 // the source tree than either half would. Here the targets get an octree of their own (the same
 // radix build as the sources, without masses or moments) and its tree grouping: subtrees and runs
-// of siblings of at most group_size targets, which never straddle such a jump. Walks of the source
-// tree then take those groups; results are scattered back to the caller's order through the
-// target tree's TreewalkIndices.
+// of siblings of at most group_size targets, which never straddle such a jump. Where the sources are
+// much denser than the targets (external targets in the core of a source distribution) such a group
+// still spans a region holding far more sources than targets and opens a large part of the tree, so
+// it is cut into shorter runs (targets_refine_groups): the groups then hold about as many sources as
+// targets, as the source tree's own groups do. Walks of the source tree take those groups; results
+// are scattered back to the caller's order through the target tree's TreewalkIndices.
 #include <new>
 
 #include "tg_targets.cuh"
@@ -34,8 +37,17 @@ int width_of(int fields) { return ((fields & 1) ? 1 : 0) + ((fields & 2) ? 3 : 0
 // through the node child whose cell (cell centre +- size / 2) holds the whole box, as long as one
 // does. Children come from the walk arena's traversal records (first node child << 4 | count). The
 // descent goes one level deeper per step; it is bounded by the node count in any case.
+// With nsub non-null, also the number of pieces the group is cut into (see k_split_groups). The
+// local source density comes from the smallest source cell that holds the box's centre and is at
+// least as large as the box (found by continuing the descent through the children holding the
+// centre): taking its n sources as spread evenly over its cell of size s, the box holds about
+// n_in = n (e / s)^3 sources (e the box's largest extent). A group whose box holds more than 2G
+// sources would open far more of the tree per target than a group of the sources' own tree does,
+// so it is cut into runs of k consecutive targets, k the largest power of two with
+// k n_in / count <= 2G.
 __global__ void k_target_src_nodes(int64_t ntot, int64_t mtot, const double *cell, const double *size, Arena<float> ar,
-                                   const double *tpos, const int2 *groups, int64_t ng, int *node) {
+                                   const int2 *node_range, const double *tpos, const int2 *groups, int64_t ng, int G,
+                                   int *node, int *nsub, int *sublen) {
     const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= ng) return;
     const int2 gr = groups[g];
@@ -69,6 +81,59 @@ __global__ void k_target_src_nodes(int64_t ntot, int64_t mtot, const double *cel
         }
     }
     node[g] = j;
+    if (nsub) {
+        int k = gr.y;
+        const double e = fmax(fmax(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+        const double ctr[3] = {0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1]), 0.5 * (lo[2] + hi[2])};
+        int d = j;  // the density cell: from j down through the children holding the centre
+        if (!(ar.bad && *ar.bad)) {
+            for (int64_t steps = 0; steps < mtot; steps++) {
+                const int cb = __float_as_int(ar.n_trav[2 * d + 1].z);
+                const int fc = cb >> 4, nc = cb & 15;
+                int nxt = -1;
+                for (int c = fc; c < fc + nc; c++) {
+                    if (c < 0 || c >= mtot) break;
+                    const double sc = size[ntot + c], hs = 0.5 * sc;
+                    if (sc < e) continue;
+                    bool inside = true;
+                    for (int q = 0; q < 3; q++)
+                        inside = inside && ctr[q] >= cell[3 * (int64_t)c + q] - hs && ctr[q] <= cell[3 * (int64_t)c + q] + hs;
+                    if (inside) {
+                        nxt = c;
+                        break;
+                    }
+                }
+                if (nxt < 0) break;
+                d = nxt;
+            }
+        }
+        const double sd = size[ntot + d];
+        if (!(ar.bad && *ar.bad) && sd > 0.0 && gr.y > 1) {
+            const double q = e / sd;
+            const double n_in = (double)(node_range[d].y - node_range[d].x) * q * q * q;
+            k = 1;  // the largest power of two (at most the count) with k n_in <= 2 G count
+            while (2 * k <= gr.y && (double)(2 * k) * n_in <= 2.0 * G * gr.y) k *= 2;
+            if (n_in <= 2.0 * G) k = gr.y;
+        }
+        nsub[g] = (gr.y + k - 1) / k;
+        sublen[g] = k;
+    }
+}
+
+// The refined groups: group g's targets cut into nsub[g] runs of sublen[g] (the last shorter), at
+// offset off[g], in start order.
+__global__ void k_split_groups(const int2 *groups, const int *gnode, int64_t ng, const int *nsub, const int *sublen,
+                               const int *off, int2 *out, int *out_root, int *out_node) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    const int2 gr = groups[g];
+    const int k = sublen[g], o = off[g];
+    for (int i = 0; i < nsub[g]; i++) {
+        const int first = gr.x + i * k;
+        out[o + i] = make_int2(first, min(k, gr.x + gr.y - first));
+        out_root[o + i] = 0;
+        out_node[o + i] = gnode[g];
+    }
 }
 
 }  // namespace
@@ -81,10 +146,52 @@ tg_status targets_src_nodes(tg_targets_s *ts, cudaStream_t st) {
     TG_CUDA(dev_malloc((void **)&ts->src_node, sizeof(int) * std::max<int64_t>(ng, 1), st));
     if (ng > 0) {
         k_target_src_nodes<<<div_up(ng, 128), 128, 0, st>>>(src->ntot, src->mtot, src->cell_center, src->size,
-                                                            src->arena32, tt->coord, tt->groups, ng, ts->src_node);
+                                                            src->arena32, src->node_range, tt->coord, tt->groups, ng,
+                                                            ts->group_size, ts->src_node, nullptr, nullptr);
         note_launch();
         TG_CUDA(cudaGetLastError());
     }
+    return TG_OK;
+}
+
+// Cuts the target tree's groups where the sources are denser than the targets (see
+// k_target_src_nodes); the groups stay in start order, so the result does not depend on timing.
+tg_status targets_refine_groups(tg_targets_s *ts, cudaStream_t st) {
+    tg_tree_s *src = ts->src, *tt = ts->tt;
+    const int64_t ng = tt->ngroups;
+    if (ng <= 0) return TG_OK;
+    tree_wait_built(src, st);
+    TG_TRY(build_arena(src, src->arena32, st));
+    DevArray<int> node(st), nsub(st), sublen(st), off(st);
+    TG_CUDA(node.alloc(ng));
+    TG_CUDA(nsub.alloc(ng + 1));
+    TG_CUDA(sublen.alloc(ng));
+    TG_CUDA(off.alloc(ng + 1));
+    TG_CUDA(cudaMemsetAsync(nsub.p + ng, 0, sizeof(int), st));
+    { k_target_src_nodes<<<div_up(ng, 128), 128, 0, st>>>(src->ntot, src->mtot, src->cell_center, src->size,
+                                                         src->arena32, src->node_range, tt->coord, tt->groups, ng,
+                                                         ts->group_size, node.p, nsub.p, sublen.p); note_launch(); }
+    TG_CUDA(cudaGetLastError());
+    TG_TRY(exclusive_scan_i32(nsub.p, off.p, ng + 1, st));
+    int total = 0;
+    TG_CUDA(cudaMemcpyAsync(&total, off.p + ng, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TG_CUDA(cudaStreamSynchronize(st));
+    if (total == ng) return TG_OK;  // nothing to cut
+    int2 *groups = nullptr;
+    int *root = nullptr, *gnode = nullptr;
+    TG_CUDA(dev_malloc((void **)&groups, sizeof(int2) * total, st));
+    TG_CUDA(dev_malloc((void **)&root, sizeof(int) * total, st));
+    TG_CUDA(dev_malloc((void **)&gnode, sizeof(int) * total, st));
+    { k_split_groups<<<div_up(ng, 128), 128, 0, st>>>(tt->groups, tt->group_node, ng, nsub.p, sublen.p, off.p, groups,
+                                                     root, gnode); note_launch(); }
+    TG_CUDA(cudaGetLastError());
+    cudaFreeAsync(tt->groups, st);
+    cudaFreeAsync(tt->group_root, st);
+    cudaFreeAsync(tt->group_node, st);
+    tt->groups = groups;
+    tt->group_root = root;
+    tt->group_node = gnode;
+    tt->ngroups = total;
     return TG_OK;
 }
 
@@ -117,6 +224,7 @@ tg_status tg_targets_create(tg_tree src, const double *pos, const double *h, int
         tree_wait_built(ts->tt, st);
         rc = tree_groups(ts->tt, group_size, st);
     }
+    if (rc == TG_OK) rc = targets_refine_groups(ts, st);
     if (rc != TG_OK) {
         tg_targets_free(ts);
         return rc;
