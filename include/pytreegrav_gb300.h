@@ -218,6 +218,42 @@ tg_status tg_tree_column_density(tg_tree tree, const double *pos, int64_t n, con
                                  int64_t ray_stride, int binned, double theta, int group_size, int mem, double *out,
                                  void *stream);
 
+/* Velocities of a tree's particles, and of its nodes as pytreegrav's DynamicOctree carries them
+ * (ConstructTree(..., vel=v), frontend.py:73-142 -> dynamic_tree.py:89-246, ComputeMomentsDynamic
+ * dynamic_tree.py:246-310): each node's mass-weighted mean velocity and its mass-weighted velocity
+ * dispersion (children's dispersions plus their spread about the mean), children in octant order.
+ * On inputs without coincident points the DynamicOctree has this tree's topology and traversal order,
+ * so the velocities are attached to the tree. vel (n, 3) in the caller's order, host or device per
+ * mem; synchronises `stream`. TG_ERR_ITER_LIMIT if the tree's parent links do not end. */
+tg_status tg_tree_set_velocities(tg_tree tree, const double *vel, int mem, void *stream);
+
+/* Host copies of the velocities (rows as tg_tree_copy_out: NumNodes x 3, padding zeros) and
+ * dispersions (NumNodes; particles 0) -- DynamicOctree.Velocities and .VelocityDisp. Either may be NULL. */
+tg_status tg_tree_copy_velocities(tg_tree tree, double *vel, double *vdisp, void *stream);
+
+/* The two-point functions (frontend.py:1047-1320, treewalk.py:344-818): per target, pytreegrav's walk
+ * bins the tree's elements by log10 distance into nbins bins with edges rbins (nbins + 1, logarithmic),
+ * whole nodes when they pass the opening test at theta and are smaller than max_bin_size_ratio times
+ * their bin's width -- spread over the bins they overlap (weighted_binning) or at a distance jittered
+ * by their size, drawn from a counter-based generator keyed by (seed, target index, draw); periodic
+ * when boxsize > 0. kind TG_CORR_DENSITY: binsums = sum over targets of the mass per bin (weight
+ * ignored; DensityCorrFunc divides by n; wtsums, if not NULL, gets the same sums); TG_CORR_VELOCITY /
+ * TG_CORR_STRUCTURE (trees with velocities): binsums = sum of weight * mass * v.V (resp. |v - V|^2, plus a
+ * node's dispersion) per bin and wtsums = sum of weight * mass (VelocityCorrFunc / VelocityStructFunc
+ * divide one by the other). Each contribution is multiplied by its target's weight (pytreegrav weights
+ * a target's per-bin sums: the same up to rounding). pos == NULL: the targets are the tree's own
+ * particles in tree (walk) order, with their velocities and masses as vel and weight (n, vel and weight
+ * ignored) -- what pytreegrav's frontends pass for a tree they build. Otherwise targets pos,
+ * vel (n, 3) and weight (n) in any order (the jitter stream follows it), host or device per mem, as are
+ * rbins, binsums and wtsums (nbins each). A bin index outside [0, nbins) from jitter or spreading is
+ * clamped into it (pytreegrav writes past its array there). FP64. Synchronises `stream`. */
+enum { TG_CORR_DENSITY = 0, TG_CORR_VELOCITY = 1, TG_CORR_STRUCTURE = 2 };
+#define TG_CORR_MAX_BINS 4096
+tg_status tg_tree_correlation(tg_tree tree, int kind, const double *pos, const double *vel, const double *weight,
+                              int64_t n, const double *rbins, int nbins, double max_bin_size_ratio, double theta,
+                              double boxsize, int weighted_binning, uint64_t seed, int mem, double *binsums,
+                              double *wtsums, void *stream);
+
 /* Number of visible CUDA devices (0, not an error, when there is no driver or device); the check
  * behind pytreegrav.cuda.is_available (cuda.py:70-80). */
 tg_status tg_device_count(int *count);

@@ -12,16 +12,16 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libtg_oracle.so")
-SRC = os.path.join(HERE, "tg_oracle.c")
+SRCS = [os.path.join(HERE, f) for f in ("tg_oracle.c", "tg_oracle_corr.c", "tg_oracle.h")]
 
 
 def build(force=False, verbose=False):
     os.makedirs(OUT_DIR, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(f) for f in SRCS):
         return LIB
     cmd = [
         "gcc", "-O2", "-fno-fast-math", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
-        "-Wall", "-o", LIB + ".tmp", SRC, "-lm",
+        "-Wall", "-o", LIB + ".tmp", *[f for f in SRCS if f.endswith(".c")], "-lm",
     ]
     if verbose:
         print(" ".join(cmd), file=sys.stderr)

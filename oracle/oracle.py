@@ -66,6 +66,12 @@ def lib():
         L.tgo_column_binned.argtypes = [ctypes.POINTER(_Tree), _dp, _i64, ctypes.c_double, _dp, ctypes.c_int]
         L.tgo_column_binned_grouped.argtypes = [ctypes.POINTER(_Tree), _dp, _i64, ctypes.c_double, _i64, _dp,
                                                 ctypes.c_int]
+        L.tgo_tree_velocities.argtypes = [ctypes.POINTER(_Tree), _dp, _dp, _dp]
+        L.tgo_corr_uniform.argtypes = [ctypes.c_uint64, _i64, _i64]
+        L.tgo_corr_uniform.restype = ctypes.c_double
+        L.tgo_correlation.argtypes = [ctypes.POINTER(_Tree), _dp, _dp, ctypes.c_int, _dp, _dp, _dp, _i64, _dp,
+                                      ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                      ctypes.c_uint64, ctypes.c_int, _dp, _dp, ctypes.c_int]
         for k in ("tgo_force_kernel", "tgo_potential_kernel", "tgo_tidal_kernel"):
             getattr(L, k).argtypes = [ctypes.c_double, ctypes.c_double]
             getattr(L, k).restype = ctypes.c_double
@@ -373,6 +379,48 @@ def column_binned_grouped(tree, pos, theta=0.5, group_size=16, nthreads=0):
     lib().tgo_column_binned_grouped(ctypes.byref(tree._t), _d(pos), len(pos), float(theta), int(group_size),
                                     _d(out), int(nthreads))
     return out
+
+
+def tree_velocities(tree, vel):
+    """Node velocities and dispersions of pytreegrav's DynamicOctree (dynamic_tree.py:246-310) on the
+    oracle tree: (NumNodes, 3) and (NumNodes,), particles in tree order."""
+    vel = _f64c(vel, (-1, 3))
+    v = np.zeros((tree.NumNodes, 3))
+    d = np.zeros(tree.NumNodes)
+    lib().tgo_tree_velocities(ctypes.byref(tree._t), _d(vel), _d(v), _d(d))
+    return v, d
+
+
+CORR_KINDS = {"density": 0, "velocity": 1, "structure": 2}
+
+
+def correlation(tree, kind, pos, rbins, vel=None, weight=None, tree_vel=None, max_bin_size_ratio=100, theta=1.0,
+                boxsize=0.0, weighted_binning=False, seed=0, absval=False, nthreads=0):
+    """The density (treewalk.py:378-510), velocity-correlation (515-663) or structure-function
+    (668-818) walk of every target in pos, summed over targets: (binsums, wtsums). tree_vel is
+    tree_velocities(tree, v) for the velocity kinds. absval sums |contribution| instead."""
+    k = CORR_KINDS[kind]
+    pos = _f64c(pos, (-1, 3))
+    n = len(pos)
+    rbins = _f64c(rbins)
+    nb = len(rbins) - 1
+    bs, ws = np.zeros(nb), np.zeros(nb)
+    args = [None, None, None, None]
+    if k:
+        tv, td = tree_vel
+        args = [_f64c(tv), _f64c(td), _f64c(vel, (n, 3)), _f64c(weight, (n,))]
+    keep = args
+    rc = lib().tgo_correlation(ctypes.byref(tree._t), *(None if a is None else _d(a) for a in keep[:2]), k, _d(pos),
+                               *(None if a is None else _d(a) for a in keep[2:]), n, _d(rbins), nb,
+                               float(max_bin_size_ratio), float(theta), float(boxsize), int(bool(weighted_binning)),
+                               int(seed) & (2**64 - 1), int(bool(absval)), _d(bs), _d(ws), int(nthreads))
+    if rc:
+        raise RuntimeError(f"oracle correlation failed ({rc})")
+    return bs, ws
+
+
+def corr_uniform(seed, target, draw):
+    return lib().tgo_corr_uniform(int(seed) & (2**64 - 1), int(target), int(draw))
 
 
 def force_kernel(r, h):

@@ -85,6 +85,16 @@ int tgo_bruteforce(const double *pos_t, const double *h_t, int64_t nt, const dou
                    const double *m_s, const double *h_s, int64_t ns, int want_pot, int want_acc,
                    int want_tidal, int mode, double G, double *out, int nthreads);
 
+/* Two-point functions (tg_oracle_corr.c): node velocities and dispersions of the DynamicOctree moment
+ * pass (vel_in (n, 3) in the caller's order; vel (num_nodes, 3), disp (num_nodes)), and the density /
+ * velocity-correlation / structure-function walks (kind 0 / 1 / 2) summed over targets. */
+void tgo_tree_velocities(const tgo_tree *t, const double *vel_in, double *vel, double *disp);
+double tgo_corr_uniform(uint64_t seed, int64_t target, int64_t draw);
+int tgo_correlation(const tgo_tree *t, const double *vel, const double *disp, int kind, const double *pos,
+                    const double *tvel, const double *weight, int64_t n, const double *rbins, int nbins,
+                    double max_bin_size_ratio, double theta, double boxsize, int weighted_binning, uint64_t seed,
+                    int absval, double *binsums, double *wtsums, int nthreads);
+
 double tgo_force_kernel(double r, double h);
 double tgo_potential_kernel(double r, double h);
 double tgo_tidal_kernel(double r, double h);

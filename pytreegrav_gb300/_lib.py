@@ -36,6 +36,8 @@ TG_ORDER_GIVEN = 2
 TG_GROUP_BLOCKS = 0
 TG_GROUP_TREE = 1
 TG_NOALLOC_MAX_POINTS = 262144
+TG_CORR_KINDS = {"density": 0, "velocity": 1, "structure": 2}
+TG_CORR_MAX_BINS = 4096
 
 # every extern "C" symbol declared in include/pytreegrav_gb300.h
 EXPORTS = [
@@ -61,6 +63,9 @@ EXPORTS = [
     "tg_morton_order_noalloc",
     "tg_bruteforce",
     "tg_tree_column_density",
+    "tg_tree_set_velocities",
+    "tg_tree_copy_velocities",
+    "tg_tree_correlation",
     "tg_device_count",
     "tg_sources_create",
     "tg_sources_bruteforce",
@@ -163,6 +168,10 @@ def _declare(L):
     L.tg_morton_order_noalloc.argtypes = [vp, i64, vp, vp]
     L.tg_bruteforce.argtypes = [vp, vp, i64, vp, vp, vp, i64, ci, ci, dbl, ci, ci, vp, vp]
     L.tg_tree_column_density.argtypes = [vp, vp, i64, vp, i64, i64, ci, dbl, ci, ci, vp, vp]
+    L.tg_tree_set_velocities.argtypes = [vp, vp, ci, vp]
+    L.tg_tree_copy_velocities.argtypes = [vp, vp, vp, vp]
+    L.tg_tree_correlation.argtypes = [vp, ci, vp, vp, vp, i64, vp, ci, dbl, dbl, dbl, ci, ctypes.c_uint64, ci, vp,
+                                      vp, vp]
     L.tg_device_count.argtypes = [ctypes.POINTER(ci)]
     L.tg_sources_create.argtypes = [vp, vp, vp, i64, ci, vp, ctypes.POINTER(vp)]
     L.tg_sources_bruteforce.argtypes = [vp, vp, vp, i64, ci, dbl, ci, ci, vp, vp]

@@ -116,7 +116,7 @@ void destroy(tg_tree_s *t) {
     free_arena(t->arena32, st);
     free_arena(t->arena64, st);
     if (t->stats_dev) cudaFreeAsync(t->stats_dev, st);
-    f(t->groups); f(t->group_root); f(t->group_node); f(t->gstats); f(t->gerr); f(t->sort_err);
+    f(t->groups); f(t->group_root); f(t->group_node); f(t->gstats); f(t->gerr); f(t->sort_err); f(t->vel); f(t->vdisp);
     if (t->side) cudaStreamDestroy(t->side);  // released once its work is done
     if (t->ev_fork) cudaEventDestroy(t->ev_fork);
     if (t->ev_join) cudaEventDestroy(t->ev_join);

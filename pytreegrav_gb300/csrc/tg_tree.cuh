@@ -79,6 +79,10 @@ struct tg_tree_s {
     // order), read back by the build and by each walk (nonzero: a sort failed).
     int *sort_err = nullptr;
 
+    // Velocities (tg_tree_set_velocities): per element, particles' own and nodes' mass-weighted mean
+    // (3 each), and per element the velocity dispersion (particles 0); null until set.
+    double *vel = nullptr, *vdisp = nullptr;
+
     tg::Arena<float> arena32;
     tg::Arena<double> arena64;
     tg::WalkStats last_stats;

@@ -23,8 +23,11 @@ Differences a caller can see, all deliberate:
     ``pytreegrav_gb300.theta``. With external targets (the *Target forms, or a given tree), the
     targets are grouped by an octree of their own (``TargetSet``), as with ``grouping="tree"``.
   * ``morton_order=False``/``radix=False`` in ConstructTree still build the radix tree (pytreegrav
-    documents both builds as giving identical fields on generic data); ``vel`` (the velocity tree
-    used only by the correlation functions) is not provided.
+    documents both builds as giving identical fields on generic data); with ``vel`` the radix tree
+    carries the DynamicOctree's node velocities and dispersions.
+  * The correlation functions' default binning jitters a node's distance with a counter-based
+    generator keyed by ``seed`` (keyword, extension; None draws it from numpy's global generator)
+    instead of numba's np.random stream, and clamps a jittered bin index into range.
 """
 
 import warnings
@@ -93,10 +96,12 @@ def ConstructTree(pos, m=None, softening=None, quadrupole=False, vel=None, compu
     """Build a tree of the particle data on the GPU for subsequent field evaluation.
 
     Same arguments as pytreegrav.ConstructTree (frontend.py:73-142). Returns an Octree whose arrays
-    are bit-identical to pytreegrav's radix build.
+    are bit-identical to pytreegrav's radix build. With vel, the tree also carries the velocities
+    and velocity dispersions of pytreegrav's DynamicOctree (Velocities, VelocityDisp): that
+    insertion-built tree has the radix tree's topology and traversal order on inputs without
+    coincident points, and its moments agree to rounding, so the velocities are attached to this
+    tree rather than to a second one.
     """
-    if vel is not None:
-        raise NotImplementedError("the velocity-carrying DynamicOctree (vel=...) is not provided by pytreegrav_gb300")
     pos = np.atleast_2d(_f64(pos))
     if m is None:
         compute_moments = False
@@ -112,6 +117,8 @@ def ConstructTree(pos, m=None, softening=None, quadrupole=False, vel=None, compu
     except _lib.NonFiniteInput:
         print(_lib.NONFINITE_MSG)
         raise RuntimeError(_lib.NONFINITE_MSG) from None
+    if vel is not None:
+        tree.set_velocities(np.atleast_2d(_f64(vel)))
     warn_if_coincident_positions(tree, softening)
     return tree
 
@@ -390,3 +397,77 @@ def ColumnDensity(pos, m, radii, rays=None, randomize_rays=False, healpix=False,
     if return_tree:
         return unsorted, tree
     return unsorted
+
+
+def _default_rbins(pos):
+    """frontend.py:1091-1093: log-spaced edges from the 11th-nearest to the farthest distance from the
+    median position, N^(1/3) of them."""
+    r = np.sort(np.sqrt(np.sum((pos - np.median(pos, axis=0)) ** 2, axis=1)))
+    return 10 ** np.linspace(np.log10(r[10]), np.log10(r[-1]), int(len(r) ** (1.0 / 3)))
+
+
+def _corr(kind, pos, m, v, rbins, max_bin_size_ratio, theta, tree, boxsize, weighted_binning, seed):
+    """The frontends' common path (frontend.py:1090-1130, 1176-1224, 1270-1318): targets are the
+    tree's own particles in walk order when the tree is built here (no host gather: the library
+    reads them, their velocities and masses from the tree), else pos in its own Morton order."""
+    pos = np.atleast_2d(_f64(pos))
+    if rbins is None:
+        rbins = _default_rbins(pos)
+    rbins = np.ascontiguousarray(_f64(rbins))
+    if tree is None:
+        tree = ConstructTree(pos, _f64(m), zeros(len(pos)), vel=v)
+        bs, ws = tree.correlation(kind, None, rbins, max_bin_size_ratio=max_bin_size_ratio, theta=theta,
+                                  boxsize=boxsize, weighted_binning=weighted_binning, seed=seed)
+    else:
+        _check_tree(tree)
+        idx = morton_order(pos)
+        vs = ms = None
+        if v is not None:
+            vs = np.take(np.atleast_2d(_f64(v)), idx, axis=0)
+            ms = np.take(np.atleast_1d(_f64(m)), idx, axis=0)
+        bs, ws = tree.correlation(kind, np.take(pos, idx, axis=0), rbins, vel=vs, weight=ms,
+                                  max_bin_size_ratio=max_bin_size_ratio, theta=theta, boxsize=boxsize,
+                                  weighted_binning=weighted_binning, seed=seed)
+    return rbins, bs, ws, tree
+
+
+def DensityCorrFunc(pos, m, rbins=None, max_bin_size_ratio=100, theta=1.0, tree=None, return_tree=False,
+                    parallel=False, boxsize=0, weighted_binning=False, *, seed=None):
+    """Mean mass in logarithmic radial bins around each point, averaged over the points
+    (frontend.py:1047-1130; treewalk.py:378-510): returns (rbins, mbins[, tree]).
+
+    rbins None: N^(1/3) log-spaced edges from the points' spread about their median. A node is
+    binned whole once it passes the opening test at theta and is smaller than max_bin_size_ratio
+    bin widths: spread over the bins it overlaps (weighted_binning) or at a distance jittered by its
+    size (keyed by seed). Periodic when boxsize > 0. tree: any tree (not necessarily of pos).
+    The walks run on the GPU in FP64 (one thread per target).
+    """
+    rbins, bs, _, tree = _corr("density", pos, m, None, rbins, max_bin_size_ratio, theta, tree, boxsize,
+                               weighted_binning, seed)
+    mbins = bs / len(np.atleast_2d(pos))
+    return (rbins, mbins, tree) if return_tree else (rbins, mbins)
+
+
+def VelocityCorrFunc(pos, m, v, rbins=None, max_bin_size_ratio=100, theta=1.0, tree=None, return_tree=False,
+                     parallel=False, boxsize=0, weighted_binning=False, *, seed=None):
+    """Mass-weighted mean of v . v' in logarithmic radial bins, averaged over the points
+    (frontend.py:1133-1224; treewalk.py:515-663): returns (rbins, corr[, tree]). A given tree must
+    carry velocities (ConstructTree(..., vel=...)); v may be any vector field. Arguments as
+    DensityCorrFunc."""
+    rbins, bs, ws, tree = _corr("velocity", pos, m, v, rbins, max_bin_size_ratio, theta, tree, boxsize,
+                                weighted_binning, seed)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        corr = bs / ws
+    return (rbins, corr, tree) if return_tree else (rbins, corr)
+
+
+def VelocityStructFunc(pos, m, v, rbins=None, max_bin_size_ratio=100, theta=1.0, tree=None, return_tree=False,
+                       parallel=False, boxsize=0, weighted_binning=False, *, seed=None):
+    """Mass-weighted mean of |v - v'|^2 in logarithmic radial bins, averaged over the points, a
+    node's own velocity dispersion included (frontend.py:1227-1318; treewalk.py:668-818): returns
+    (rbins, Sv[, tree]). Arguments as VelocityCorrFunc."""
+    rbins, bs, ws, tree = _corr("structure", pos, m, v, rbins, max_bin_size_ratio, theta, tree, boxsize,
+                                weighted_binning, seed)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        Sv = bs / ws
+    return (rbins, Sv, tree) if return_tree else (rbins, Sv)

@@ -30,8 +30,11 @@ class Octree:
 
     Attributes mirror pytreegrav's Octree jitclass: NumParticles, NumNodes, HasQuads,
     HasCoincidentPoints, Coordinates, Masses, Sizes, Deltas, Softenings, Quadrupoles,
-    FirstSubnode, NextBranch, TreewalkIndices.
+    FirstSubnode, NextBranch, TreewalkIndices; and, for a tree built with velocities (the
+    DynamicOctree's role), Velocities and VelocityDisp.
     """
+
+    HasVelocities = False
 
     def __init__(self, pos, m=None, softening=None, quadrupole=False, compute_moments=True):
         L = _lib.load()
@@ -267,6 +270,75 @@ class Octree:
                                           0, 0.0, 0, _lib.TG_MEM_HOST, _lib.ptr(out), None)
         _lib.check(rc, "column density")
         return out
+
+    # -- velocities and two-point functions -----------------------------------------------------
+    def set_velocities(self, vel):
+        """Attach particle velocities (n, 3), caller's order, and roll up every node's mass-weighted
+        mean velocity and velocity dispersion as pytreegrav's DynamicOctree does
+        (dynamic_tree.py:246-310; tg_tree_set_velocities)."""
+        vel = _as_f64(vel, (-1, 3))
+        if len(vel) != self.NumParticles:
+            raise ValueError(f"vel has {len(vel)} rows for a tree of {self.NumParticles} particles")
+        _lib.check(_lib.load().tg_tree_set_velocities(self._h, _lib.ptr(vel), _lib.TG_MEM_HOST, None),
+                   "tree velocities")
+        self._vel = None
+        self.HasVelocities = True
+
+    def _velocities(self):
+        if not getattr(self, "HasVelocities", False):
+            raise AttributeError("this tree has no velocities (ConstructTree(..., vel=v))")
+        if getattr(self, "_vel", None) is None:
+            v, d = np.empty((self.NumNodes, 3)), np.empty(self.NumNodes)
+            _lib.check(_lib.load().tg_tree_copy_velocities(self._h, _lib.ptr(v), _lib.ptr(d), None),
+                       "copy velocities")
+            self._vel = (v, d)
+        return self._vel
+
+    @property
+    def Velocities(self):
+        """(NumNodes, 3): particle velocities (tree order) and nodes' mass-weighted mean velocities."""
+        return self._velocities()[0]
+
+    @property
+    def VelocityDisp(self):
+        """(NumNodes,): nodes' mass-weighted velocity dispersions (particles 0)."""
+        return self._velocities()[1]
+
+    def correlation(self, kind, pos, rbins, vel=None, weight=None, max_bin_size_ratio=100, theta=1.0, boxsize=0,
+                    weighted_binning=False, seed=None):
+        """Sums of the density / velocity-correlation / structure-function walks of the targets pos
+        (taken in the order given) over this tree (tg_tree_correlation): (binsums, wtsums), nbins each.
+        pos=None: the tree's own particles in tree order, weighted by their masses, with their own
+        velocities (vel and weight ignored). seed: the jitter stream's key (None: drawn from numpy's
+        global generator)."""
+        k = _lib.TG_CORR_KINDS[kind]
+        if k and not self.HasVelocities:
+            raise ValueError(f"the {kind} function needs a tree with velocities: ConstructTree(..., vel=v)")
+        rbins = _as_f64(rbins)
+        nb = len(rbins) - 1
+        if nb < 1 or nb > _lib.TG_CORR_MAX_BINS:
+            raise ValueError(f"rbins must hold 2 to {_lib.TG_CORR_MAX_BINS + 1} edges")
+        if not (rbins[0] > 0 and np.all(np.diff(rbins) > 0)):
+            raise ValueError("rbins must be positive and increasing (logarithmically spaced)")
+        vp = wp = pp = None
+        n = self.NumParticles
+        if pos is not None:
+            pos = _as_f64(pos, (-1, 3))
+            n = len(pos)
+            pp = _lib.ptr(pos)
+            if k:
+                vel = _as_f64(vel, (n, 3))
+                weight = _as_f64(weight, (n,))
+                vp, wp = _lib.ptr(vel), _lib.ptr(weight)
+        if seed is None:
+            seed = int(np.random.randint(0, 2**63 - 1, dtype=np.int64))
+        bs, ws = np.zeros(nb), np.zeros(nb)
+        rc = _lib.load().tg_tree_correlation(self._h, k, pp, vp, wp, n, _lib.ptr(rbins), nb,
+                                             float(max_bin_size_ratio), float(theta), float(boxsize),
+                                             int(bool(weighted_binning)), int(seed) & (2**64 - 1),
+                                             _lib.TG_MEM_HOST, _lib.ptr(bs), _lib.ptr(ws), None)
+        _lib.check(rc, "correlation walk")
+        return bs, ws
 
     def last_walk_stats(self):
         """(interactions, node tests, deepest stack, groups) of the last walk on this tree."""

@@ -8,6 +8,7 @@ Run from the repository root, with the pytreegrav checkout's src/ directory as t
 
     python tests/golden/make_golden.py /path/to/pytreegrav/src            (all fixtures)
     python tests/golden/make_golden.py /path/to/pytreegrav/src column     (golden_column.npz only)
+    python tests/golden/make_golden.py /path/to/pytreegrav/src corr       (golden_corr.npz only)
 
 Writes tests/golden/golden_*.npz. Small cases store full arrays; large cases store SHA-256 digests of
 each array, so the fixtures stay a few hundred KB. Seeds are fixed; rerunning reproduces the files.
@@ -250,11 +251,76 @@ def column(src):
     print("wrote golden_column.npz")
 
 
+def corr(src):
+    """golden_corr.npz: pytreegrav's DynamicOctree velocity moments (dynamic_tree.py:246-310) and its
+    DensityCorrFunc / VelocityCorrFunc / VelocityStructFunc (frontend.py:1047-1320) with
+    weighted_binning=True, or with max_bin_size_ratio so small that every particle is binned on its
+    own -- the deterministic forms (the default binning jitters with np.random)."""
+    sys.path.insert(0, os.path.join(HERE, "_numba_shim"))
+    sys.path.insert(0, src)
+    warnings.simplefilter("ignore")
+    from pytreegrav import ConstructTree, DensityCorrFunc, VelocityCorrFunc, VelocityStructFunc
+
+    rng = np.random.default_rng(23)
+    n = 800
+    x = plummer(n, rng)
+    m = rng.random(n) / n
+    v = 0.3 * x + rng.normal(size=(n, 3))  # a bulk flow correlated with position, plus noise
+    out = {"pos": x, "m": m, "v": v}
+    dt = ConstructTree(x, m, np.zeros(n), vel=v)
+    order, nodes = [], []  # DynamicOctree node numbering is its own: store nodes in traversal preorder
+    First, Next = np.asarray(dt.FirstSubnode), np.asarray(dt.NextBranch)
+    st = [n]
+    while st:
+        no = st.pop()
+        if no < n:
+            order.append(no)
+            continue
+        nodes.append(np.concatenate([[dt.Masses[no]], dt.Coordinates[no], [dt.Sizes[no], dt.Deltas[no]],
+                                     dt.Velocities[no], [dt.VelocityDisp[no]]]))
+        kids, c, stop = [], First[no], Next[no]
+        while c != -1 and c != stop:
+            kids.append(c)
+            c = Next[c]
+        st.extend(reversed(kids))
+    out["dyn/order"] = np.array(order, np.int64)
+    out["dyn/TreewalkIndices"] = np.asarray(dt.TreewalkIndices)
+    out["dyn/nodes_preorder"] = np.array(nodes)  # mass, com(3), size, delta, vel(3), vdisp
+    rb, out["density_weighted"] = DensityCorrFunc(x, m, weighted_binning=True)
+    out["rbins_default"] = rb
+    rb2 = 10 ** np.linspace(-1.5, 1.0, 13)
+    out["rbins"] = rb2
+    _, out["density_pairs"] = DensityCorrFunc(x, m, rb2, max_bin_size_ratio=1e-300)
+    _, out["density_weighted_t0.5"] = DensityCorrFunc(x, m, rb2, theta=0.5, weighted_binning=True)
+    _, out["velocity_weighted"] = VelocityCorrFunc(x, m, v, rb2, weighted_binning=True)
+    _, out["velocity_pairs"] = VelocityCorrFunc(x, m, v, rb2, max_bin_size_ratio=1e-300)
+    _, out["structure_weighted"] = VelocityStructFunc(x, m, v, rb2, weighted_binning=True)
+    _, out["structure_weighted_t0.6_mbr3"] = VelocityStructFunc(x, m, v, rb2, theta=0.6, max_bin_size_ratio=3.0,
+                                                                weighted_binning=True)
+    # periodic box, and targets other than the tree's particles (a supplied tree)
+    xu = rng.random((600, 3))
+    mu = np.full(600, 1.0 / 600)
+    vu = rng.normal(size=(600, 3))
+    rb3 = 10 ** np.linspace(-1.7, -0.4, 9)
+    out["box/pos"], out["box/m"], out["box/v"], out["box/rbins"] = xu, mu, vu, rb3
+    _, out["box/density_weighted"] = DensityCorrFunc(xu, mu, rb3, boxsize=1.0, weighted_binning=True)
+    _, out["box/structure_weighted"] = VelocityStructFunc(xu, mu, vu, rb3, boxsize=1.0, weighted_binning=True)
+    xt = rng.random((150, 3)) * 2 - 1
+    tree = ConstructTree(x, m, np.zeros(n))
+    out["targets/pos"] = xt
+    _, out["targets/density_weighted"] = DensityCorrFunc(xt, np.ones(150), rb2, tree=tree, weighted_binning=True)
+    np.savez_compressed(os.path.join(OUT, "golden_corr.npz"), **out)
+    print("wrote golden_corr.npz")
+
+
 if __name__ == "__main__":
     if len(sys.argv) == 3 and sys.argv[2] == "column":
         column(sys.argv[1])
+    elif len(sys.argv) == 3 and sys.argv[2] == "corr":
+        corr(sys.argv[1])
     elif len(sys.argv) != 2:
         sys.exit(__doc__)
     else:
         main(sys.argv[1])
         column(sys.argv[1])
+        corr(sys.argv[1])

@@ -32,6 +32,13 @@ def test_theta_constants_agree_with_header():
     assert int(consts["TG_THETA_FEAT_LAMBDA"]) == _lib.TG_THETA_FEAT_LAMBDA
 
 
+def test_corr_constants_agree_with_header():
+    src = open(os.path.join(ROOT, "include", "pytreegrav_gb300.h")).read()
+    assert int(re.search(r"^#define TG_CORR_MAX_BINS (\d+)", src, re.M).group(1)) == _lib.TG_CORR_MAX_BINS
+    kinds = re.search(r"enum \{ TG_CORR_DENSITY = (\d), TG_CORR_VELOCITY = (\d), TG_CORR_STRUCTURE = (\d) \}", src)
+    assert [int(k) for k in kinds.groups()] == [_lib.TG_CORR_KINDS[k] for k in ("density", "velocity", "structure")]
+
+
 def test_library_builds_loads_and_exports_every_symbol():
     from pytreegrav_gb300 import build
 
