@@ -243,6 +243,7 @@ struct Nodes {  // node slots in discovery order
     int64_t cap = 0, count = 0;
     int64_t *lo = nullptr, *hi = nullptr, *parent = nullptr, *first = nullptr, *next = nullptr;
     int64_t *aparent = nullptr, *rank = nullptr;  // allocating parent slot, sibling order key
+    int8_t *digit = nullptr;  // octant digit at the slot's level: the sibling order among split nodes
     int32_t *depth = nullptr, *sys = nullptr;
     int32_t *seg = nullptr;  // segment of the round that made the slot (for k_node_centers)
     int8_t *level = nullptr;
@@ -328,12 +329,25 @@ __device__ __forceinline__ int64_t lower_prefix(const uint64_t *keys, int64_t a,
     return a;
 }
 
+// lower_prefix over [a, b] where keys[b] has prefix p, by galloping down from b: cheap when the
+// run of prefix p starts near b (a node's particles end at or after i, and most runs are short).
+__device__ __forceinline__ int64_t gallop_lower_prefix(const uint64_t *keys, int64_t a, int64_t b, uint64_t p,
+                                                       int level) {
+    int64_t step = 1;
+    while (b - step >= a && prefix(keys[b - step], level) >= p) {
+        b -= step;
+        step <<= 1;
+    }
+    const int64_t lo = b - step + 1 > a ? b - step + 1 : a;  // keys[b - step] (if >= a) is below p
+    return lower_prefix(keys, lo, b, p, level);
+}
+
 // slot of the node at `level` containing particle i (level >= lvl0 of the segment root)
 __device__ __forceinline__ int64_t node_at(const RoundView &v, const int8_t *L, const int64_t *nstart,
                                            int64_t slot_base, const uint64_t *keys, int s, int64_t i, int level) {
     if (level == 0 && v.seg_root[s] >= 0) return v.seg_root[s];
     int64_t lo = v.seg_lo[s];
-    int64_t p_lo = lower_prefix(keys, lo, i + 1, prefix(keys[i], level), level);
+    int64_t p_lo = gallop_lower_prefix(keys, lo, i, prefix(keys[i], level), level);
     int64_t pe = v.eoff[s] + (p_lo - lo);
     return slot_base + nstart[pe] + (level - lvl0(v, L, s, pe, p_lo));
 }
@@ -380,6 +394,7 @@ __global__ void k_nodes(RoundView v, int64_t E, const int8_t *L, const int64_t *
         nd.parent[slot] = par;
         nd.aparent[slot] = par;
         nd.rank[slot] = i;
+        nd.digit[slot] = k > 0 ? (int8_t)((key >> (63 - 3 * k)) & 7) : (int8_t)0;
         nd.seg[slot] = s;
         if (k == MAX_LEVEL) {
             nd.first[slot] = -1;  // set by the re-key round or the bucket
@@ -588,6 +603,7 @@ __global__ void k_bucket(const int64_t *exh, int n, const int64_t *chain_off, in
         nd.parent[sl] = (j == 1) ? x : sl - 1;
         nd.aparent[sl] = x;
         nd.rank[sl] = lo + 7 * j;
+        nd.digit[sl] = 0;
         nd.center[3 * sl] = c0;
         nd.center[3 * sl + 1] = c1;
         nd.center[3 * sl + 2] = c2;
@@ -677,8 +693,14 @@ struct NumberingBits {
 };
 
 // root_key sorts after every other key (1 << the key width, or all ones when the width is 64).
+// Nodes are numbered by allocating parent (its particle range's end, descending, then its depth) and
+// among one parent's children by first particle. Without bucket chains a parent's children are split
+// cells, whose first particles are in octant-digit order: compact keys then carry the 3-bit digit
+// instead of the first particle, which saves sort passes. (A bucket chain hangs all its nodes on one
+// allocating parent, so it needs the full first-particle rank.)
 __global__ void k_number_keys(Nodes nd, int64_t count, const int64_t *sys_off, NumberingBits b, uint64_t root_key,
-                              uint64_t *keys, uint32_t *vals, int64_t *root_slot_of_sys, int *nonroot_count) {
+                              int compact, uint64_t *keys, uint32_t *vals, int64_t *root_slot_of_sys,
+                              int *nonroot_count) {
     int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= count) return;
     int s = nd.sys[c];
@@ -691,8 +713,10 @@ __global__ void k_number_keys(Nodes nd, int64_t count, const int64_t *sys_off, N
     }
     int64_t off = sys_off[s];
     int64_t nsys_part = sys_off[s + 1] - off;
-    uint64_t k = ((uint64_t)s << (2 * b.lb + b.db)) | ((uint64_t)(nsys_part - (nd.hi[ap] - off)) << (b.lb + b.db)) |
-                 ((uint64_t)nd.depth[ap] << b.lb) | (uint64_t)(nd.rank[c] - off);
+    const int low = compact ? 3 : b.lb;  // bits of the sibling order key
+    const uint64_t sib = compact ? (uint64_t)(nd.digit[c] & 7) : (uint64_t)(nd.rank[c] - off);
+    uint64_t k = ((uint64_t)s << (b.lb + b.db + low)) | ((uint64_t)(nsys_part - (nd.hi[ap] - off)) << (b.db + low)) |
+                 ((uint64_t)nd.depth[ap] << low) | sib;
     keys[c] = k;
     vals[c] = (uint32_t)c;
     atomicAdd(nonroot_count, 1);
@@ -957,6 +981,14 @@ __device__ void node_moments(const MomentArgs &a, int64_t f) {
 // the softening maximum alone, which is the reference's skipping it. A warp's lanes thus part only
 // on the node children's quadrupole term, and a warp of nodes with equal child counts (see
 // k_moments_sorted) runs with every lane busy.
+// CG: read the children through L2 (ld.cg), for kernels in which another SM may have finished them.
+template <bool CG>
+__device__ __forceinline__ double ldm(const double *p) {
+    if (CG) return __ldcg(p);
+    return *p;
+}
+
+template <bool CG>
 __device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j, const int32_t *kids, int n) {
     const int4 k0 = *reinterpret_cast<const int4 *>(kids + 8 * j);
     const int4 k1 = *reinterpret_cast<const int4 *>(kids + 8 * j + 4);
@@ -969,15 +1001,15 @@ __device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j
             const int32_t c = ch[q];
             const bool part = c >= 0;
             const int64_t g = part ? (int64_t)c : N + (int64_t)(~c);
-            const double mc = a.mass[g];
+            const double mc = ldm<CG>(a.mass + g);
             const double *src = part ? a.coord + 3 * g : a.acc + 3 * (int64_t)(~c);
             const double w = part ? mc : 1.0;
             const bool use = part || mc != 0.0;
-            const double hc = a.soft[g];
+            const double hc = ldm<CG>(a.soft + g);
             m = dadd(m, use ? mc : -0.0);
-            ax = dadd(ax, use ? dmul(w, src[0]) : -0.0);
-            ay = dadd(ay, use ? dmul(w, src[1]) : -0.0);
-            az = dadd(az, use ? dmul(w, src[2]) : -0.0);
+            ax = dadd(ax, use ? dmul(w, ldm<CG>(src)) : -0.0);
+            ay = dadd(ay, use ? dmul(w, ldm<CG>(src + 1)) : -0.0);
+            az = dadd(az, use ? dmul(w, ldm<CG>(src + 2)) : -0.0);
             h = use ? pymax(h, hc) : h;
         }
     }
@@ -987,7 +1019,7 @@ __device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j
     a.acc[3 * j] = ax;
     a.acc[3 * j + 1] = ay;
     a.acc[3 * j + 2] = az;
-    double com[3] = {a.coord[3 * f], a.coord[3 * f + 1], a.coord[3 * f + 2]};
+    double com[3] = {ldm<CG>(a.coord + 3 * f), ldm<CG>(a.coord + 3 * f + 1), ldm<CG>(a.coord + 3 * f + 2)};
     if (m != 0.0) {
         double inv = ddiv(1.0, m);
         double accs[3] = {ax, ay, az};
@@ -1010,14 +1042,14 @@ __device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j
                 const int32_t c = ch[q];
                 const bool part = c >= 0;
                 const int64_t g = part ? (int64_t)c : N + (int64_t)(~c);
-                const double mc = a.mass[g];
+                const double mc = ldm<CG>(a.mass + g);
                 if (part || mc != 0.0) {
                     if (!part) {
 #pragma unroll
-                        for (int k = 0; k < 9; k++) Q[k] = dadd(Q[k], a.quad[9 * (int64_t)(~c) + k]);
+                        for (int k = 0; k < 9; k++) Q[k] = dadd(Q[k], ldm<CG>(a.quad + 9 * (int64_t)(~c) + k));
                     }
-                    shift_quad(Q, mc, dsub(a.coord[3 * g], com[0]), dsub(a.coord[3 * g + 1], com[1]),
-                               dsub(a.coord[3 * g + 2], com[2]));
+                    shift_quad(Q, mc, dsub(ldm<CG>(a.coord + 3 * g), com[0]), dsub(ldm<CG>(a.coord + 3 * g + 1), com[1]),
+                               dsub(ldm<CG>(a.coord + 3 * g + 2), com[2]));
                 }
             }
         }
@@ -1029,7 +1061,8 @@ __device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j
 // Large levels (FP64-throughput-bound): one thread per node, the block's nodes first ordered by
 // child count (a counting sort in shared memory, most children first) so that a warp's lanes run
 // the same number of child steps. Which thread takes which node does not change any result.
-constexpr int MOM_BLOCK = 256;
+// MOM_BLOCK: 64, 128 or 256 threads.
+template <int MOM_BLOCK>
 __global__ void __launch_bounds__(MOM_BLOCK) k_moments_sorted(MomentArgs a, const int32_t *list, int count,
                                                               const int32_t *kids, const int8_t *nk) {
     __shared__ int bin[9];
@@ -1056,106 +1089,125 @@ __global__ void __launch_bounds__(MOM_BLOCK) k_moments_sorted(MomentArgs a, cons
     __syncthreads();
     const int j = order[t];
     if (j < 0) return;
-    node_moments_kids(a, j, kids, nk[j]);
+    node_moments_kids<false>(a, j, kids, nk[j]);
 }
 
-// One quadrupole entry e = 3a + b of shift_quad's update for a child of mass m at offset r.
-__device__ __forceinline__ double quad_term(int e, double m, double r0, double r1, double r2) {
-    const int ia = e / 3, ib = e - 3 * ia;
-    const double ra = ia == 0 ? r0 : (ia == 1 ? r1 : r2);
-    if (ia == ib) {
-        double rsq = dadd(dadd(dmul(r0, r0), dmul(r1, r1)), dmul(r2, r2));
-        return dmul(m, dsub(dmul(dmul(3.0, ra), ra), rsq));
-    }
-    const double rb = ib == 0 ? r0 : (ib == 1 ? r1 : r2);
-    return dmul(dmul(dmul(m, 3.0), ra), rb);
-}
+// Small levels. GB300 runs FP64 on one unit per SM sub-partition at about 76 cycles per warp
+// instruction, with any number of lanes active, so a level whose nodes fill fewer warps than there
+// are sub-partitions is bound by the length of one warp's FP64 instruction stream (~400 for a node
+// with eight children and quadrupoles), not by lanes. Here 32 nodes share a block of nine warps
+// (lane = node) and the stream is cut into stages that run side by side: the children's terms
+// (one warp per child slot), the five mass-pass sums (one warp each), the centre of mass and Delta,
+// the children's offsets (one warp per child slot), and the nine quadrupole entries (one warp each).
+// Every sum takes its terms in node_moments_kids's order with the same operations, so the results
+// are identical.
+constexpr int WIDE_NODES = 32, WIDE_WARPS = 9, WIDE_THREADS = WIDE_NODES * WIDE_WARPS;
+constexpr int WIDE_MAX_LEVEL = 4096;  // levels up to this many nodes use k_moments_wide
 
-// Small levels (latency-bound: too few nodes to hide a thread's long FP64 chain): 16 lanes per
-// node over k_kids's child list. Lanes 0-4 each carry one of the mass pass's sums (mass, three
-// mass-weighted coordinates, softening max) and lanes 0-8 one quadrupole entry each; every sum
-// takes its terms in the same order as node_moments, so the results are identical.
-__global__ void k_moments_level_coop(MomentArgs a, const int32_t *list, int count, const int32_t *kids,
-                                     const int8_t *nk) {
-    const int lane = threadIdx.x & 31, sub = lane & 15, half = lane >> 4;
-    const int node = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 4);
-    if (node >= count) return;  // whole half-warps leave together
-    const unsigned hmask = 0xFFFFu << (16 * half);
+__global__ void __launch_bounds__(WIDE_THREADS) k_moments_wide(MomentArgs a, const int32_t *list, int count,
+                                                              const int32_t *kids, const int8_t *nk) {
+    __shared__ double s_m[8][WIDE_NODES], s_t[3][8][WIDE_NODES], s_h[8][WIDE_NODES];  // child terms
+    __shared__ double s_r[4][8][WIDE_NODES];                                           // offsets, |r|^2
+    __shared__ double s_sum[5][WIDE_NODES], s_com[3][WIDE_NODES];
+    __shared__ int32_t s_c[8][WIDE_NODES];
+    __shared__ int8_t s_use[8][WIDE_NODES];  // child enters the sums (a particle, or a node of nonzero mass)
+    __shared__ int s_n[WIDE_NODES];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int idx = blockIdx.x * WIDE_NODES + lane;
     const int64_t N = a.ntot;
-    const int64_t j = list[node];
-    const int64_t f = N + j;
-    const int n = nk[j];
-    const int4 k0 = *reinterpret_cast<const int4 *>(kids + 8 * j);
-    const int4 k1 = *reinterpret_cast<const int4 *>(kids + 8 * j + 4);
-    const int32_t ch[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
-    double v = 0.0;
-    if (sub < 5) {
-#pragma unroll
-        for (int q = 0; q < 8; q++) {
-            if (q < n) {
-                const int32_t c = ch[q];
-                const bool part = c >= 0;
-                const int64_t g = part ? (int64_t)c : N + (int64_t)(~c);
-                const double mc = a.mass[g];
-                const bool use = part || mc != 0.0;
-                if (sub == 0) {
-                    v = dadd(v, use ? mc : -0.0);
-                } else if (sub < 4) {
-                    const double x = part ? a.coord[3 * g + sub - 1] : a.acc[3 * (int64_t)(~c) + sub - 1];
-                    v = dadd(v, use ? dmul(part ? mc : 1.0, x) : -0.0);
-                } else if (use) {
-                    v = pymax(v, a.soft[g]);
-                }
-            }
-        }
+    const int64_t j = idx < count ? (int64_t)list[idx] : -1;
+    // stage 0: child lists
+    if (w < 8) {
+        const int n = j >= 0 ? (int)nk[j] : 0;
+        s_c[w][lane] = w < n ? kids[8 * j + w] : 0;
+        if (w == 0) s_n[lane] = n;
     }
-    const double m = __shfl_sync(hmask, v, 0, 16);
-    const double ax = __shfl_sync(hmask, v, 1, 16), ay = __shfl_sync(hmask, v, 2, 16);
-    const double az = __shfl_sync(hmask, v, 3, 16), h = __shfl_sync(hmask, v, 4, 16);
-    double com0 = 0.0, com1 = 0.0, com2 = 0.0;
-    if (sub == 0) {
+    __syncthreads();
+    const int n = s_n[lane];
+    // stage 1: warp q, child q of every node: the mass-pass terms (use ? term : -0.0)
+    if (w < 8 && w < n) {
+        const int32_t c = s_c[w][lane];
+        const bool part = c >= 0;
+        const int64_t g = part ? (int64_t)c : N + (int64_t)(~c);
+        const double mc = a.mass[g];
+        const bool use = part || mc != 0.0;
+        const double *src = part ? a.coord + 3 * g : a.acc + 3 * (int64_t)(~c);
+        const double wgt = part ? mc : 1.0;
+        s_m[w][lane] = use ? mc : -0.0;
+#pragma unroll
+        for (int k = 0; k < 3; k++) s_t[k][w][lane] = use ? dmul(wgt, src[k]) : -0.0;
+        s_h[w][lane] = use ? a.soft[g] : 0.0;
+        s_use[w][lane] = use ? 1 : 0;
+    }
+    __syncthreads();
+    // stage 2: the five sums, child order
+    if (w < 5 && j >= 0) {
+        double v = 0.0;
+        for (int q = 0; q < n; q++) {
+            if (w == 0) v = dadd(v, s_m[q][lane]);
+            else if (w < 4) v = dadd(v, s_t[w - 1][q][lane]);
+            else if (s_use[q][lane]) v = pymax(v, s_h[q][lane]);
+        }
+        s_sum[w][lane] = v;
+    }
+    __syncthreads();
+    // stage 3: mass, softening, centre of mass and Delta
+    if (w == 0 && j >= 0) {
+        const int64_t f = N + j;
+        const double m = s_sum[0][lane];
+        const double acc[3] = {s_sum[1][lane], s_sum[2][lane], s_sum[3][lane]};
         a.mass[f] = m;
-        a.soft[f] = h;
-        a.acc[3 * j] = ax;
-        a.acc[3 * j + 1] = ay;
-        a.acc[3 * j + 2] = az;
+        a.soft[f] = s_sum[4][lane];
+        a.acc[3 * j] = acc[0];
+        a.acc[3 * j + 1] = acc[1];
+        a.acc[3 * j + 2] = acc[2];
         double com[3] = {a.coord[3 * f], a.coord[3 * f + 1], a.coord[3 * f + 2]};
         if (m != 0.0) {
-            double inv = ddiv(1.0, m);
-            double accs[3] = {ax, ay, az};
+            const double inv = ddiv(1.0, m);
             double d2 = 0.0;
 #pragma unroll
             for (int k = 0; k < 3; k++) {
-                double cm = dmul(accs[k], inv);
-                double dx = dsub(cm, com[k]);
+                const double cm = dmul(acc[k], inv);
+                const double dx = dsub(cm, com[k]);
                 d2 = dadd(d2, dmul(dx, dx));
                 com[k] = cm;
                 a.coord[3 * f + k] = cm;
             }
             a.delta[f] = __dsqrt_rn(d2);
         }
-        com0 = com[0]; com1 = com[1]; com2 = com[2];
-    }
-    com0 = __shfl_sync(hmask, com0, 0, 16);
-    com1 = __shfl_sync(hmask, com1, 0, 16);
-    com2 = __shfl_sync(hmask, com2, 0, 16);
-    if (a.quads && sub < 9) {
-        double Q = 0.0;
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
-            if (q < n) {
-                const int32_t c = ch[q];
-                const bool part = c >= 0;
-                const int64_t g = part ? (int64_t)c : N + (int64_t)(~c);
-                const double mc = a.mass[g];
-                if (part || mc != 0.0) {
-                    if (!part) Q = dadd(Q, a.quad[9 * (int64_t)(~c) + sub]);
-                    Q = dadd(Q, quad_term(sub, mc, dsub(a.coord[3 * g], com0), dsub(a.coord[3 * g + 1], com1),
-                                          dsub(a.coord[3 * g + 2], com2)));
-                }
-            }
+        for (int k = 0; k < 3; k++) s_com[k][lane] = com[k];
+    }
+    __syncthreads();
+    if (!a.quads) return;  // (uniform over the block)
+    // stage 4: warp q, child q: offset from the centre of mass and its squared length
+    if (w < 8 && w < n && s_use[w][lane]) {
+        const int32_t c = s_c[w][lane];
+        const int64_t g = c >= 0 ? (int64_t)c : N + (int64_t)(~c);
+        const double r0 = dsub(a.coord[3 * g], s_com[0][lane]), r1 = dsub(a.coord[3 * g + 1], s_com[1][lane]);
+        const double r2 = dsub(a.coord[3 * g + 2], s_com[2][lane]);
+        s_r[0][w][lane] = r0;
+        s_r[1][w][lane] = r1;
+        s_r[2][w][lane] = r2;
+        s_r[3][w][lane] = dadd(dadd(dmul(r0, r0), dmul(r1, r1)), dmul(r2, r2));
+    }
+    __syncthreads();
+    // stage 5: warp e, quadrupole entry e = 3 ia + ib (shift_quad's terms, child order)
+    if (j >= 0) {
+        const int e = w, ia = e / 3, ib = e - 3 * ia;
+        double Q = 0.0;
+        for (int q = 0; q < n; q++) {
+            if (!s_use[q][lane]) continue;
+            const int32_t c = s_c[q][lane];
+            const double m = s_m[q][lane];  // the child's mass (it enters the sums)
+            if (c < 0) Q = dadd(Q, a.quad[9 * (int64_t)(~c) + e]);
+            const double ra = s_r[ia][q][lane];
+            double t;
+            if (ia == ib) t = dmul(m, dsub(dmul(dmul(3.0, ra), ra), s_r[3][q][lane]));
+            else t = dmul(dmul(dmul(m, 3.0), ra), s_r[ib][q][lane]);
+            Q = dadd(Q, t);
         }
-        a.quad[9 * j + sub] = Q;
+        a.quad[9 * j + e] = Q;
     }
 }
 
@@ -1265,6 +1317,7 @@ static tg_status nodes_reserve(Nodes &nd, int64_t need, cudaStream_t s) {
     TG_TRY(grow_copy(&nd.next, nd.count, nc, 1, s));
     TG_TRY(grow_copy(&nd.aparent, nd.count, nc, 1, s));
     TG_TRY(grow_copy(&nd.rank, nd.count, nc, 1, s));
+    TG_TRY(grow_copy(&nd.digit, nd.count, nc, 1, s));
     TG_TRY(grow_copy(&nd.depth, nd.count, nc, 1, s));
     TG_TRY(grow_copy(&nd.sys, nd.count, nc, 1, s));
     TG_TRY(grow_copy(&nd.seg, nd.count, nc, 1, s));
@@ -1276,7 +1329,7 @@ static tg_status nodes_reserve(Nodes &nd, int64_t need, cudaStream_t s) {
 }
 static void nodes_free(Nodes &nd, cudaStream_t s) {
     dfree(nd.lo, s); dfree(nd.hi, s); dfree(nd.parent, s); dfree(nd.first, s); dfree(nd.next, s);
-    dfree(nd.aparent, s); dfree(nd.rank, s); dfree(nd.depth, s); dfree(nd.sys, s); dfree(nd.seg, s);
+    dfree(nd.aparent, s); dfree(nd.rank, s); dfree(nd.digit, s); dfree(nd.depth, s); dfree(nd.sys, s); dfree(nd.seg, s);
     dfree(nd.level, s);
     dfree(nd.center, s); dfree(nd.size, s);
 }
@@ -1572,10 +1625,11 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     TG_TRY(dalloc(&sys_node_off, nsys + 1, st));
     TG_TRY(dalloc(&nonroot, 1, st));
     TG_CUDA(cudaMemsetAsync(nonroot, 0, sizeof(int), st));
-    const int key_bits = sysbits + 2 * nb.lb + nb.db;
+    const int compact = n_bucket == 0;
+    const int key_bits = sysbits + nb.lb + nb.db + (compact ? 3 : nb.lb);
     const int sort_bits = key_bits < 64 ? key_bits + 1 : 64;
     const uint64_t root_key = key_bits < 64 ? (1ull << key_bits) : ~0ull;
-    { k_number_keys<<<LAUNCH(M)>>>(nd, M, sys_off, nb, root_key, nkeys, nvals, root_slot, nonroot); tg::note_launch(); }
+    { k_number_keys<<<LAUNCH(M)>>>(nd, M, sys_off, nb, root_key, compact, nkeys, nvals, root_slot, nonroot); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
     TG_TRY(radix_sort_pairs(nkeys, nvals, M, sort_bits, st, T->sort_err));
     // per-system node offsets (roots first within each system's block), on the device; the host
@@ -1693,7 +1747,8 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     a.arrived = nullptr;
     if (quadrupole) {
         TG_TRY(dalloc(&T->quad, 9 * M, st));
-        TG_CUDA(cudaMemsetAsync(T->quad, 0, sizeof(double) * 9 * M, st));
+        // with moments every node's quadrupole is written by the pass below
+        if (!compute_moments) TG_CUDA(cudaMemsetAsync(T->quad, 0, sizeof(double) * 9 * M, st));
         a.quad = T->quad;
     }
     if (compute_moments) {
@@ -1718,21 +1773,23 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
         TG_TRY(dalloc(&kids, 8 * M, st));
         TG_TRY(dalloc(&nk, M, st));
         { k_kids<<<LAUNCH(M)>>>(N, M, T->first, T->next, kids, nk); tg::note_launch(); }
-        // a level with few nodes is latency-bound: 16 lanes per node there; one thread per node
-        // on the large levels, which are FP64-throughput-bound (16 lanes per node issue about 2.5x
-        // the FP64 warp instructions; from ~48 nodes per SM one thread per node was faster at 1e6,
-        // against thresholds of 8, 24 and 128)
-        const int few = 48 * num_sms();
+        // one launch per depth, deepest first: k_moments_wide on the small levels (latency-bound),
+        // k_moments_sorted on the large ones (FP64-throughput-bound), with the largest block that still
+        // gives every SM about four blocks (the mid-size levels need the smaller ones to cover the SMs)
+        const int64_t want = 4 * (int64_t)num_sms();
         for (int d = DEPTH_CAP - 1; d >= 0; d--) {
             const int c = hs.depth_hist[d];
             if (c <= 0) continue;
-            if (c < few) {
-                k_moments_level_coop<<<div_up((int64_t)c * 16, 128), 128, 0, st>>>(a, lvl_list + off[d], c, kids, nk);
-                tg::note_launch();
-            } else {
-                k_moments_sorted<<<div_up(c, MOM_BLOCK), MOM_BLOCK, 0, st>>>(a, lvl_list + off[d], c, kids, nk);
-                tg::note_launch();
-            }
+            const int32_t *lst = lvl_list + off[d];
+            if (c <= WIDE_MAX_LEVEL)
+                k_moments_wide<<<div_up(c, WIDE_NODES), WIDE_THREADS, 0, st>>>(a, lst, c, kids, nk);
+            else if (div_up(c, 256) >= want)
+                k_moments_sorted<256><<<div_up(c, 256), 256, 0, st>>>(a, lst, c, kids, nk);
+            else if (div_up(c, 128) >= want)
+                k_moments_sorted<128><<<div_up(c, 128), 128, 0, st>>>(a, lst, c, kids, nk);
+            else
+                k_moments_sorted<64><<<div_up(c, 64), 64, 0, st>>>(a, lst, c, kids, nk);
+            tg::note_launch();
         }
         TG_CUDA(cudaGetLastError());
         dfree(kids, st); dfree(nk, st);

@@ -171,17 +171,29 @@ tg_status exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n, cudaStr
 // RS_* (tile geometry of the two-kernel passes) are defined in tg_common.cuh.
 
 // Per-warp stable ranking of the warp's ROUNDS * 32 keys; leaves per-warp digit counts in wcount.
+// kv: the slice's keys, one per round, loaded here up front (one memory round trip per slice) and
+// left to the caller.
+template <int ROUNDS>
+__device__ __forceinline__ void rank_loaded_slice(const uint64_t *kv, int64_t n, int64_t wbase, int shift,
+                                                  int *wcount, int *digit, int *rank);
+
 template <int ROUNDS = RS_ROUNDS>
 __device__ __forceinline__ void rank_warp_slice(const uint64_t *keys, int64_t n, int64_t wbase, int shift,
-                                                int *wcount, int *digit, int *rank) {
+                                                int *wcount, int *digit, int *rank, uint64_t *kv) {
     const int lane = lane_id();
-    const unsigned lt = lanemask_lt();
-    uint64_t kv[ROUNDS];  // every round's key loaded up front: one memory round trip per slice
 #pragma unroll
     for (int r = 0; r < ROUNDS; r++) {
         const int64_t i = wbase + r * 32 + lane;
         kv[r] = i < n ? __ldg(keys + i) : 0ull;
     }
+    rank_loaded_slice<ROUNDS>(kv, n, wbase, shift, wcount, digit, rank);
+}
+
+template <int ROUNDS>
+__device__ __forceinline__ void rank_loaded_slice(const uint64_t *kv, int64_t n, int64_t wbase, int shift,
+                                                  int *wcount, int *digit, int *rank) {
+    const int lane = lane_id();
+    const unsigned lt = lanemask_lt();
 #pragma unroll
     for (int r = 0; r < ROUNDS; r++) {
         int64_t i = wbase + r * 32 + lane;
@@ -205,7 +217,8 @@ __global__ void __launch_bounds__(RS_THREADS) radix_hist(const uint64_t *keys, i
     int w = threadIdx.x >> 5;
     int64_t wbase = (int64_t)blockIdx.x * RS_TILE + (int64_t)w * RS_WARP_KEYS;
     int digit[RS_ROUNDS], rank[RS_ROUNDS];
-    rank_warp_slice(keys, n, wbase, shift, wcount[w], digit, rank);
+    uint64_t kv[RS_ROUNDS];
+    rank_warp_slice(keys, n, wbase, shift, wcount[w], digit, rank, kv);
     __syncthreads();
     for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS) {
         int s = 0;
@@ -224,7 +237,8 @@ __global__ void __launch_bounds__(RS_THREADS) radix_scatter(const uint64_t *keys
     int w = threadIdx.x >> 5;
     int64_t wbase = (int64_t)blockIdx.x * RS_TILE + (int64_t)w * RS_WARP_KEYS;
     int digit[RS_ROUNDS], rank[RS_ROUNDS];
-    rank_warp_slice(keys, n, wbase, shift, wcount[w], digit, rank);
+    uint64_t kv[RS_ROUNDS];
+    rank_warp_slice(keys, n, wbase, shift, wcount[w], digit, rank, kv);
     __syncthreads();
     // warp offsets within the tile, then the tile's global offset per digit
     for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS) {
@@ -243,7 +257,7 @@ __global__ void __launch_bounds__(RS_THREADS) radix_scatter(const uint64_t *keys
         int64_t i = wbase + r * 32 + lane;
         if (i < n) {
             int pos = wcount[w][digit[r]] + rank[r];
-            keys_out[pos] = keys[i];
+            keys_out[pos] = kv[r];
             vals_out[pos] = vals[i];
         }
     }
@@ -258,12 +272,22 @@ __global__ void __launch_bounds__(RS_THREADS) radix_scatter(const uint64_t *keys
 // hanging, and the sort then leaves the identity permutation (k_sort_fallback).
 
 constexpr int MAX_PASSES = 8;
-constexpr int OS_ROUNDS = 8;                        // keys per thread in a one-sweep pass
+#ifndef TG_OS_ROUNDS
+#define TG_OS_ROUNDS 8
+#endif
+#ifndef TG_OS_LB
+#define TG_OS_LB 4
+#endif
+constexpr int OS_ROUNDS = TG_OS_ROUNDS;             // keys per thread in a one-sweep pass
 constexpr int OS_WARP_KEYS = OS_ROUNDS * 32;
 constexpr int OS_TILE = RS_WARPS * OS_WARP_KEYS;   // 2048 keys per CTA (8 per thread; measured against 2, 4 and 16)
-constexpr unsigned long long ST_AGG = 1ull << 62, ST_INC = 2ull << 62, ST_VAL = (1ull << 62) - 1;
+// A status word: flag (bits 62-63: aggregate or inclusive), the pass it belongs to (bits 56-61, pass + 1),
+// value (bits 0-55). Words of an earlier pass read as not yet published, so the status array is
+// cleared once per sort rather than once per pass.
+constexpr unsigned long long ST_AGG = 1ull << 62, ST_INC = 2ull << 62, ST_FLAGS = 3ull << 62;
+constexpr unsigned long long ST_TAGS = 63ull << 56, ST_VAL = (1ull << 56) - 1;
 constexpr long long SPIN_LIMIT = 1ll << 22;
-constexpr int LB = 4;  // predecessors read per look-back round trip
+constexpr int LB = TG_OS_LB;  // predecessors read per look-back round trip
 
 __global__ void __launch_bounds__(256) k_sort_hist_all(const uint64_t *keys, int64_t n, int npass, int *hist) {
     __shared__ int h[MAX_PASSES * RS_BINS];
@@ -289,11 +313,12 @@ __global__ void k_sort_digit_offsets(int *hist, int npass) {
     }
 }
 
-__global__ void __launch_bounds__(RS_THREADS) k_onesweep(const uint64_t *keys, const uint32_t *vals, int64_t n,
-                                                         int shift, const int *digit_off,
+__global__ void __launch_bounds__(RS_THREADS, 4) k_onesweep(const uint64_t *keys, const uint32_t *vals, int64_t n,
+                                                         int shift, int pass, const int *digit_off,
                                                          unsigned long long *status, int *tile_counter,
                                                          uint64_t *keys_out, uint32_t *vals_out, int *err,
                                                          long long spin_limit) {
+    const unsigned long long tag = (unsigned long long)(pass + 1) << 56;
     __shared__ int wcount[RS_WARPS][RS_BINS];
     __shared__ int prefix[RS_BINS];
     __shared__ int tile_s;
@@ -304,7 +329,18 @@ __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const uint64_t *keys, c
     const int w = threadIdx.x >> 5;
     const int64_t wbase = (int64_t)t * OS_TILE + (int64_t)w * OS_WARP_KEYS;
     int digit[OS_ROUNDS], rank[OS_ROUNDS];
-    rank_warp_slice<OS_ROUNDS>(keys, n, wbase, shift, wcount[w], digit, rank);
+    uint64_t kv[OS_ROUNDS];
+    uint32_t vv[OS_ROUNDS];  // values loaded with the keys, so the scatter reads nothing from memory
+    {
+        const int lane = lane_id();
+#pragma unroll
+        for (int r = 0; r < OS_ROUNDS; r++) {
+            const int64_t i = wbase + r * 32 + lane;
+            kv[r] = i < n ? __ldg(keys + i) : 0ull;
+            vv[r] = i < n ? __ldg(vals + i) : 0u;
+        }
+    }
+    rank_loaded_slice<OS_ROUNDS>(kv, n, wbase, shift, wcount[w], digit, rank);
     __syncthreads();
     {  // one thread per digit: offsets of the warps within the tile, then the tile's prefix
         const int d = threadIdx.x;
@@ -318,9 +354,9 @@ __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const uint64_t *keys, c
         volatile unsigned long long *st = status + (int64_t)t * RS_BINS + d;
         long long acc = 0;
         if (t == 0) {
-            *st = ST_INC | (unsigned long long)run;
+            *st = ST_INC | tag | (unsigned long long)run;
         } else {
-            *st = ST_AGG | (unsigned long long)run;
+            *st = ST_AGG | tag | (unsigned long long)run;
             // earlier tiles publish their aggregate without waiting on anyone, so each wait ends
             // once that tile's CTA (already running: it took its tile before this one) has ranked.
             // The words of LB predecessors are read together (independent loads, one round trip),
@@ -336,17 +372,18 @@ __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const uint64_t *keys, c
                     if (done || j - k < 0) break;
                     unsigned long long wd = w[k];
                     const volatile unsigned long long *src = status + (j - k) * RS_BINS + d;
-                    for (long long spins = 0; !(wd & ~ST_VAL) && spins < spin_limit; spins++) wd = *src;
-                    if (!(wd & ~ST_VAL)) {
+                    auto ready = [tag](unsigned long long x) { return (x & ST_FLAGS) && (x & ST_TAGS) == tag; };
+                    for (long long spins = 0; !ready(wd) && spins < spin_limit; spins++) wd = *src;
+                    if (!ready(wd)) {
                         atomicExch(err, 1);
                         done = true;
                         break;
                     }
                     acc += (long long)(wd & ST_VAL);
-                    if ((wd & ~ST_VAL) == ST_INC) done = true;
+                    if ((wd & ST_FLAGS) == ST_INC) done = true;
                 }
             }
-            *st = ST_INC | (unsigned long long)(acc + run);
+            *st = ST_INC | tag | (unsigned long long)(acc + run);
         }
         prefix[d] = digit_off[d] + (int)acc;
     }
@@ -357,8 +394,8 @@ __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const uint64_t *keys, c
         int64_t i = wbase + r * 32 + lane;
         if (i < n) {
             int pos = prefix[digit[r]] + wcount[w][digit[r]] + rank[r];
-            keys_out[pos] = keys[i];
-            vals_out[pos] = vals[i];
+            keys_out[pos] = kv[r];
+            vals_out[pos] = vv[r];
         }
     }
 }
@@ -394,15 +431,14 @@ tg_status radix_sort_pairs(uint64_t *keys, uint32_t *vals, int64_t n, int bits, 
     int *hist = (int *)(scr + st_bytes);
     int *counters = hist + MAX_PASSES * RS_BINS;
     int *local_err = counters + MAX_PASSES;
-    TG_CUDA(cudaMemsetAsync(hist, 0, hist_bytes + sizeof(int) * (MAX_PASSES + 1), s));
+    TG_CUDA(cudaMemsetAsync(scr, 0, st_bytes + hist_bytes + sizeof(int) * (MAX_PASSES + 1), s));
     const int hblocks = (int)std::min<int64_t>(div_up(n, 256 * 16), (int64_t)num_sms() * 4);
     { k_sort_hist_all<<<hblocks, 256, 0, s>>>(keys, n, npass, hist); tg::note_launch(); }
     { k_sort_digit_offsets<<<1, RS_BINS, 0, s>>>(hist, npass); tg::note_launch(); }
     uint64_t *kin = keys, *kout = k2;
     uint32_t *vin = vals, *vout = v2;
     for (int p = 0; p < npass; p++) {
-        TG_CUDA(cudaMemsetAsync(status, 0, st_bytes, s));
-        { k_onesweep<<<ntiles, RS_THREADS, 0, s>>>(kin, vin, n, 8 * p, hist + p * RS_BINS, status, counters + p, kout,
+        { k_onesweep<<<ntiles, RS_THREADS, 0, s>>>(kin, vin, n, 8 * p, p, hist + p * RS_BINS, status, counters + p, kout,
                                                    vout, local_err, spin_limit); tg::note_launch(); }
         TG_CUDA(cudaGetLastError());
         uint64_t *tk = kin; kin = kout; kout = tk;
