@@ -635,9 +635,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--config", choices=["plummer", "batched", "column", "uniform", "precision", "clustered",
-                                         "largest"], default="plummer",
+                                         "largest", "corr"], default="plummer",
                     help="batched: the 4096-system configuration; column: ray-traced column density; uniform, "
-                         "precision, clustered, largest: see bench_configs.py (each its own JSON line)")
+                         "precision, clustered, largest, corr: see bench_configs.py (each its own JSON line)")
     ap.add_argument("--sources", type=int, default=32_000_000, help="source count of --config largest")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -645,7 +645,7 @@ def main():
         res = run_batched(args)
     elif args.config == "column" and args.impl == "ours":
         res = run_column(args)
-    elif args.config in ("uniform", "precision", "clustered", "largest") and args.impl == "ours":
+    elif args.config in ("uniform", "precision", "clustered", "largest", "corr") and args.impl == "ours":
         import bench_configs
 
         res = getattr(bench_configs, "run_" + args.config)(args)

@@ -15,6 +15,8 @@
   learned walk for external targets (plain-theta fallback for groups over the error budget) next to
   the plain theta = 0.7 walk on the same target groups; errors against FP32 Kahan-compensated direct
   sums, over all sources on 1e4 sampled targets and over a 2e5-source subset.
+* ``corr``: VelocityStructFunc with pytreegrav's defaults on N = 1e6 Plummer particles with velocities
+  (0.3 x + unit normal noise): tree build, velocity moments and the FP64 walk of every particle.
 
 Every input is seeded synthetic data with the configuration's shapes and distributions. Steps are
 timed with CUDA events on the launching stream, inputs resident in HBM, L2 flushed (256 MiB
@@ -448,3 +450,89 @@ def run_largest(args):
                                        f"block of 8 Morton-ordered targets, walk time scaled to all {nt}: "
                                        f"{cpu_s:.1f} s per step"},
             "gpu_launches_per_step": int(launches / (steps + args.warmup))}
+
+
+def run_corr(args):
+    """VelocityStructFunc on 1e6 Plummer particles with velocities (0.3 x + unit normal noise, seeded),
+    pytreegrav's defaults: rbins from the N^(1/3) heuristic, theta = 1, max_bin_size_ratio = 100,
+    jittered binning. A step is the tree build, the node velocity moments and the FP64 walk of all N
+    targets (the tree's own particles), inputs resident in HBM; e2e is the public call from host arrays."""
+    import pytreegrav_gb300 as tg
+    from oracle import oracle as O
+    from pytreegrav_gb300.frontend import _default_rbins
+
+    torch, _lib, L, st = _env()
+    n = args.n
+    rng = np.random.default_rng(SEED + 5)
+    import bench
+
+    x = bench.plummer(n, SEED)
+    m = np.full(n, 1.0 / n)
+    v = 0.3 * x + rng.normal(size=(n, 3))
+    rb = _default_rbins(x)
+    nb = len(rb) - 1
+    dx, dm, dv, drb = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (x, m, v, rb))
+    dz = torch.zeros(n, dtype=torch.float64, device="cuda")
+    bins = torch.zeros(2 * nb, dtype=torch.float64, device="cuda")
+    vp = ctypes.c_void_p
+    walk_ev = []
+
+    def step():
+        t = vp()
+        _lib.check(L.tg_tree_build(_vp(dx), _vp(dm), _vp(dz), n, 0, 1, _lib.TG_MEM_DEVICE, st, ctypes.byref(t)), "build")
+        _lib.check(L.tg_tree_set_velocities(t, _vp(dv), _lib.TG_MEM_DEVICE, st), "velocities")
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        _lib.check(L.tg_tree_correlation(t, _lib.TG_CORR_KINDS["structure"], None, None, None, 0, _vp(drb), nb, 100.0,
+                                         1.0, 0.0, 0, 12345, _lib.TG_MEM_DEVICE, _vp(bins),
+                                         vp(bins.data_ptr() + 8 * nb), st), "correlation")
+        b.record()
+        walk_ev.append((a, b))
+        L.tg_tree_free(t)
+
+    l0 = L.tg_launch_count()
+    steps = max(3, min(args.steps, 10))
+    ms, _ = timed(torch, step, steps, args.warmup)
+    launches = (L.tg_launch_count() - l0) // (steps + args.warmup)
+    walk_ms = statistics.mean(a.elapsed_time(b) for a, b in walk_ev[-steps:])
+    sv = (bins[:nb] / bins[nb:]).cpu().numpy()
+    # end to end through the public call
+    tg.VelocityStructFunc(x, m, v, seed=12345)
+    e2e_t = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, sv_e2e = tg.VelocityStructFunc(x, m, v, seed=12345)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = statistics.median(e2e_t)
+    # CPU baseline: the oracle (pytreegrav's walk in C, FP64, OpenMP on all host cores): build and
+    # moments of all N, the walk of every 64th target, extrapolated
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ot = O.OracleTree(x, m, np.zeros(n))
+    otv = O.tree_velocities(ot, v)
+    t1 = time.perf_counter()
+    idx = ot.TreewalkIndices[::64]
+    O.correlation(ot, "structure", x[idx], rb, vel=v[idx], weight=m[idx], tree_vel=otv, theta=1.0, seed=12345,
+                  nthreads=cores)
+    t2 = time.perf_counter()
+    cpu_s = (t1 - t0) + (t2 - t1) * 64
+    return {"metric": "VelocityStructFunc targets/s, 1e6 Plummer with velocities (pytreegrav defaults)",
+            "value": round(n / (ms * 1e-3), 1), "unit": "targets/s", "n_gpus": 1, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic (seeded Plummer sphere a=1 r<50; velocities 0.3 x + N(0,1))",
+            "config": {"workload": f"VelocityStructFunc, N={n}, m=1/N, {nb} log bins from the N^(1/3) heuristic, "
+                                   "theta=1, max_bin_size_ratio=100, jittered binning",
+                       "step": "tree build + node velocity moments + FP64 walk of all N targets, inputs resident in HBM",
+                       "l2": "flushed between timed steps"},
+            "walk_ms": round(walk_ms, 3), "walk_targets_per_s": round(n / (walk_ms * 1e-3), 1),
+            "same_as_e2e_call": bool(np.allclose(sv, sv_e2e, rtol=1e-12, equal_nan=True)),
+            "e2e": {"value": round(n / e2e_s, 1), "unit": "targets/s",
+                    "h2d_bytes_per_step": int(x.nbytes + m.nbytes + v.nbytes + rb.nbytes),
+                    "d2h_bytes_per_step": int(16 * nb), "api": "pytreegrav_gb300.VelocityStructFunc(pos, m, v, seed=...)",
+                    "ms_per_step": round(1e3 * e2e_s, 3)},
+            "cpu_baseline": {"value": round(n / cpu_s, 1), "unit": "targets/s", "cores": cores, "kind": "port",
+                             "sample": "oracle build and velocity moments of all N + the structure-function walk "
+                                       f"(C, FP64, OpenMP) of every 64th target, extrapolated; {cpu_s:.2f} s per step"},
+            "gpu_launches": int(launches)}

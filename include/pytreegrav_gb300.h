@@ -60,7 +60,7 @@ typedef struct {
     const double *size;     /* (node_hi,) Sizes */
     const double *delta;    /* (node_hi,) Deltas */
     const double *soft;     /* (node_hi,) Softenings */
-    const double *quad;     /* (node_hi, 3, 3) Quadrupoles or NULL */
+    const double *quad;     /* (node_hi, 3, 3) Quadrupoles once computed (tg_tree_quadrupoles), else NULL */
     const int64_t *first;   /* (node_hi,) FirstSubnode */
     const int64_t *next;    /* (node_hi,) NextBranch */
     const int64_t *walk_idx;/* (npart,) TreewalkIndices */
@@ -90,6 +90,13 @@ tg_status tg_tree_build_batched(const double *pos, const double *m, const double
 /* Sizes and flags of a tree, and its device arrays (complete once the build's stream has passed the
  * build; see tg_tree_build). */
 tg_status tg_tree_info_get(tg_tree tree, tg_tree_info *info);
+
+/* The FP64 quadrupoles of a quadrupole tree (the Octree's Quadrupoles, octree.py:234-292, bit for bit):
+ * the build sums FP32 quadrupoles for FP32 walks and computes these on `stream` the first time they
+ * are needed (this call, tg_tree_copy_out, an FP64 walk). *quad receives the device array (mtot x 9,
+ * node rows only; tg_tree_info.quad points there from then on), complete on `stream`; NULL for a
+ * monopole tree. */
+tg_status tg_tree_quadrupoles(tg_tree tree, const double **quad, void *stream);
 
 /* Copy the Octree arrays to host buffers sized for info.num_nodes rows (rows past node_hi are
  * written as the reference leaves them: zeros, and -1 links). Any pointer may be NULL. */

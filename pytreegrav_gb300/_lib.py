@@ -45,6 +45,7 @@ EXPORTS = [
     "tg_tree_build",
     "tg_tree_build_batched",
     "tg_tree_info_get",
+    "tg_tree_quadrupoles",
     "tg_tree_copy_out",
     "tg_tree_free",
     "tg_tree_fields",
@@ -150,6 +151,7 @@ def _declare(L):
     L.tg_tree_build.argtypes = [vp, vp, vp, i64, ci, ci, ci, vp, ctypes.POINTER(vp)]
     L.tg_tree_build_batched.argtypes = [vp, vp, vp, vp, i32, ci, ci, vp, ctypes.POINTER(vp)]
     L.tg_tree_info_get.argtypes = [vp, ctypes.POINTER(TreeInfo)]
+    L.tg_tree_quadrupoles.argtypes = [vp, ctypes.POINTER(vp), vp]
     L.tg_tree_copy_out.argtypes = [vp] * 10 + [vp]
     L.tg_tree_free.argtypes = [vp]
     L.tg_tree_fields.argtypes = [vp, vp, vp, i64, ci, ci, dbl, dbl, ci, ci, ci, ci, vp, ci, vp, vp]

@@ -749,11 +749,15 @@ __device__ __forceinline__ int64_t resolve(int64_t ref, const int64_t *final_of_
 // Besides the node arrays, files every node into the list of its depth (lvl_list, sections at
 // lvl_off[d]; depths >= DEPTH_CAP share the last section) for the level-by-level moment pass.
 __global__ void k_write_nodes(Nodes nd, int64_t count, const int64_t *final_of_slot, double *coord, double *size,
-                              int64_t *first, int64_t *next, int64_t *parent, int2 *range, double *cell, int64_t ntot,
-                              const int *lvl_off, int *lvl_cursor, int32_t *lvl_list, int8_t *fdepth) {
+                              double *mass, double *soft, double *delta, int64_t *first, int64_t *next,
+                              int64_t *parent, int2 *range, double *cell, int64_t ntot, const int *lvl_off,
+                              int *lvl_cursor, int32_t *lvl_list, int8_t *fdepth) {
     int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= count) return;
     int64_t f = final_of_slot[c];
+    mass[f] = 0.0;  // the moment pass fills these
+    soft[f] = 0.0;
+    delta[f] = 0.0;
     {
         int d = nd.depth[c];
         d = d < 0 ? 0 : (d > DEPTH_CAP ? DEPTH_CAP : d);
@@ -778,11 +782,18 @@ __global__ void k_write_nodes(Nodes nd, int64_t count, const int64_t *final_of_s
     parent[f] = nd.parent[c] < 0 ? -1 : final_of_slot[nd.parent[c]];
 }
 
+// Particle rows of the final arrays, the Morton-ordered coordinates, masses and softenings included.
 __global__ void k_write_particles(int64_t ntot, const int64_t *p_parent, const int64_t *p_next,
-                                  const int64_t *final_of_slot, int64_t *first, int64_t *next, int64_t *parent,
-                                  double *size, double *delta) {
+                                  const int64_t *final_of_slot, const double *pc, const double *pm, const double *ps,
+                                  double *coord, double *mass, double *soft, int64_t *first, int64_t *next,
+                                  int64_t *parent, double *size, double *delta) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ntot) return;
+    coord[3 * i] = pc[3 * i];
+    coord[3 * i + 1] = pc[3 * i + 1];
+    coord[3 * i + 2] = pc[3 * i + 2];
+    mass[i] = pm[i];
+    soft[i] = ps[i];
     first[i] = -1;
     next[i] = resolve(p_next[i], final_of_slot);
     parent[i] = final_of_slot[p_parent[i]];
@@ -859,11 +870,12 @@ __global__ void k_count_node_children(int64_t ntot, int64_t mtot, const int64_t 
 
 struct MomentArgs {
     int64_t ntot, mtot;
-    double *coord, *mass, *soft, *delta, *quad;  // quad: per node (9)
-    double *acc;                                  // per node (3)
+    double *coord, *mass, *soft, *delta;
+    double *acc;                     // per node (3): mass-weighted coordinate sums
+    float4 *quad32;                  // per node (2): FP32 quadrupole (xx xy xz yy)(yz zz 0 0), or null
+    double *quad;                    // per node (9): FP64 quadrupole (the quadrupole pass only)
     const int64_t *first, *next, *parent;
     int *nchild, *arrived;
-    int quads;
 };
 
 __device__ __forceinline__ void shift_quad(double *Q, double m, double r0, double r1, double r2) {
@@ -880,114 +892,51 @@ __device__ __forceinline__ void shift_quad(double *Q, double m, double r0, doubl
     t = dmul(m, dsub(dmul(dmul(3.0, r2), r2), rsq)); Q[8] = dadd(Q[8], t);
 }
 
-// One node's moments from its (finished) children: RollupMoments + RollupQuadrupoles restricted
-// to this node (octree.py:199-292). The children (at most 8: octants, or a bucket node's 7
-// particles and 1 node) are gathered first, then visited in fixed, unrolled slots: threads of a
-// warp whose nodes differ in their mix of children then part only for one slot's short body
-// and meet again after it, instead of running their loops apart. Summation order as in the
-// reference: particle children in chain (Morton) order, then node children in reverse chain
-// order (descending index), zero-mass nodes skipped.
-__device__ void node_moments(const MomentArgs &a, int64_t f) {
-    const int64_t stop = a.next[f];
-    const int64_t ne = a.ntot + a.mtot;
-    int64_t ch[8];
-    int n = 0;
-    for (int64_t c = a.first[f]; c != stop && c >= 0 && c < ne && n < 8; c = a.next[c]) ch[n++] = c;
-    double m = 0.0, ax = 0.0, ay = 0.0, az = 0.0, h = 0.0;
-#pragma unroll
-    for (int q = 0; q < 8; q++) {
-        if (q < n && ch[q] < a.ntot) {
-            const int64_t c = ch[q];
-            double mi = __ldcg(a.mass + c);
-            m = dadd(m, mi);
-            ax = dadd(ax, dmul(mi, __ldcg(a.coord + 3 * c)));
-            ay = dadd(ay, dmul(mi, __ldcg(a.coord + 3 * c + 1)));
-            az = dadd(az, dmul(mi, __ldcg(a.coord + 3 * c + 2)));
-            h = pymax(h, __ldcg(a.soft + c));
-        }
-    }
-#pragma unroll
-    for (int q = 7; q >= 0; q--) {
-        if (q < n && ch[q] >= a.ntot) {
-            const int64_t c = ch[q];
-            double mc = __ldcg(a.mass + c);
-            if (mc != 0.0) {
-                int64_t cj = c - a.ntot;
-                m = dadd(m, mc);
-                ax = dadd(ax, __ldcg(a.acc + 3 * cj));
-                ay = dadd(ay, __ldcg(a.acc + 3 * cj + 1));
-                az = dadd(az, __ldcg(a.acc + 3 * cj + 2));
-                h = pymax(h, __ldcg(a.soft + c));
-            }
-        }
-    }
-    int64_t j = f - a.ntot;
-    a.mass[f] = m;
-    a.soft[f] = h;
-    a.acc[3 * j] = ax;
-    a.acc[3 * j + 1] = ay;
-    a.acc[3 * j + 2] = az;
-    double com[3] = {a.coord[3 * f], a.coord[3 * f + 1], a.coord[3 * f + 2]};
-    if (m != 0.0) {
-        double inv = ddiv(1.0, m);
-        double accs[3] = {ax, ay, az};
-        double d2 = 0.0;
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            double cm = dmul(accs[k], inv);
-            double dx = dsub(cm, com[k]);
-            d2 = dadd(d2, dmul(dx, dx));
-            com[k] = cm;
-            a.coord[3 * f + k] = cm;
-        }
-        a.delta[f] = __dsqrt_rn(d2);
-    }
-    if (a.quads) {
-        double Q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-#pragma unroll
-        for (int q = 0; q < 8; q++) {
-            if (q < n && ch[q] < a.ntot) {
-                const int64_t c = ch[q];
-                shift_quad(Q, __ldcg(a.mass + c), dsub(__ldcg(a.coord + 3 * c), com[0]),
-                           dsub(__ldcg(a.coord + 3 * c + 1), com[1]), dsub(__ldcg(a.coord + 3 * c + 2), com[2]));
-            }
-        }
-#pragma unroll
-        for (int q = 7; q >= 0; q--) {
-            if (q < n && ch[q] >= a.ntot) {
-                const int64_t c = ch[q];
-                double mc = __ldcg(a.mass + c);
-                if (mc != 0.0) {
-                    int64_t cj = c - a.ntot;
-#pragma unroll
-                    for (int k = 0; k < 9; k++) Q[k] = dadd(Q[k], __ldcg(a.quad + 9 * cj + k));
-                    shift_quad(Q, mc, dsub(__ldcg(a.coord + 3 * c), com[0]), dsub(__ldcg(a.coord + 3 * c + 1), com[1]),
-                               dsub(__ldcg(a.coord + 3 * c + 2), com[2]));
-                }
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < 9; k++) a.quad[9 * j + k] = Q[k];
-    }
+// The FP32 quadrupole the FP32 walk uses, Q = (xx, xy, xz, yy, yz, zz): the same shift (a child of
+// mass m at offset r from the node's centre of mass adds m (3 r_a r_b - delta_ab r^2), a node child
+// its own quadrupole too) summed in FP32, the offsets taken in FP64 and rounded once. GB300 issues
+// FP64 at 1/73 of the FP32 rate and these sums were most of the moment pass's FP64 instructions;
+// the FP64 quadrupoles (pytreegrav's, bit for bit) come from the quadrupole pass when first needed.
+// Each child's term T = (its quadrupole, for a node) + shift is formed apart and then added to the
+// node's sum in child order, every operation rounded once, so every kernel gives the same FP32 value.
+__device__ __forceinline__ void quad32_term(float *T, float m, float rx, float ry, float rz) {
+    const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(rx, rx), __fmul_rn(ry, ry)), __fmul_rn(rz, rz));
+    const float m3 = __fmul_rn(3.f, m);
+    T[0] = __fadd_rn(T[0], __fmul_rn(m, __fsub_rn(__fmul_rn(__fmul_rn(3.f, rx), rx), r2)));
+    T[1] = __fadd_rn(T[1], __fmul_rn(__fmul_rn(m3, rx), ry));
+    T[2] = __fadd_rn(T[2], __fmul_rn(__fmul_rn(m3, rx), rz));
+    T[3] = __fadd_rn(T[3], __fmul_rn(m, __fsub_rn(__fmul_rn(__fmul_rn(3.f, ry), ry), r2)));
+    T[4] = __fadd_rn(T[4], __fmul_rn(__fmul_rn(m3, ry), rz));
+    T[5] = __fadd_rn(T[5], __fmul_rn(m, __fsub_rn(__fmul_rn(__fmul_rn(3.f, rz), rz), r2)));
+}
+__device__ __forceinline__ void load_quad32(float *T, float4 a, float4 b) {
+    T[0] = a.x; T[1] = a.y; T[2] = a.z; T[3] = a.w; T[4] = b.x; T[5] = b.y;
+}
+__device__ __forceinline__ void store_quad32(float4 *q32, int64_t j, const float *Q) {
+    q32[2 * j] = make_float4(Q[0], Q[1], Q[2], Q[3]);
+    q32[2 * j + 1] = make_float4(Q[4], Q[5], 0.f, 0.f);
 }
 
-// Level by level, deepest first: one launch per depth over that depth's node list, so every lane
-// of a warp works on a node (FP64 throughput is scarce on this GPU, and a warp instruction costs
-// the same with one lane active as with 32). Children are finished by the previous launch, so the
-// level kernels read them through L1.
-// node_moments over the child list k_kids made. Every child takes the same instructions: a
-// particle adds (m, m x, softening) and a node (m, its mass-weighted coordinate sum times 1.0,
-// which is exact, softening); a zero-mass node adds -0.0, the exact identity of a sum, and leaves
-// the softening maximum alone, which is the reference's skipping it. A warp's lanes thus part only
-// on the node children's quadrupole term, and a warp of nodes with equal child counts (see
-// k_moments_sorted) runs with every lane busy.
 // CG: read the children through L2 (ld.cg), for kernels in which another SM may have finished them.
 template <bool CG>
 __device__ __forceinline__ double ldm(const double *p) {
     if (CG) return __ldcg(p);
     return *p;
 }
+template <bool CG>
+__device__ __forceinline__ float4 ldm4(const float4 *p) {
+    if (CG) return __ldcg(p);
+    return *p;
+}
 
+// One node's moments from its (finished) children, RollupMoments (octree.py:199-231) restricted to
+// this node in FP64, plus the FP32 quadrupole. kids: the child list of k_kids (summation order as in
+// the reference: particle children in chain (Morton) order, then node children in reverse chain order,
+// zero-mass nodes skipped). Every child takes the same instructions: a particle adds (m, m x,
+// softening) and a node (m, its mass-weighted coordinate sum times 1.0, which is exact, softening); a
+// zero-mass node adds -0.0, the exact identity of a sum, and leaves the softening maximum alone, which
+// is the reference's skipping it. A warp's lanes thus part only on the quadrupole's node-child term,
+// and a warp of nodes with equal child counts (see k_moments_sorted) runs with every lane busy.
 template <bool CG>
 __device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j, const int32_t *kids, int n) {
     const int4 k0 = *reinterpret_cast<const int4 *>(kids + 8 * j);
@@ -1034,8 +983,8 @@ __device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j
         }
         a.delta[f] = __dsqrt_rn(d2);
     }
-    if (a.quads) {
-        double Q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (a.quad32) {
+        float Q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
         for (int q = 0; q < 8; q++) {
             if (q < n) {
@@ -1044,17 +993,16 @@ __device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j
                 const int64_t g = part ? (int64_t)c : N + (int64_t)(~c);
                 const double mc = ldm<CG>(a.mass + g);
                 if (part || mc != 0.0) {
-                    if (!part) {
+                    float T[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                    if (!part) load_quad32(T, ldm4<CG>(a.quad32 + 2 * (int64_t)(~c)), ldm4<CG>(a.quad32 + 2 * (int64_t)(~c) + 1));
+                    quad32_term(T, d2f(mc), d2f(dsub(ldm<CG>(a.coord + 3 * g), com[0])),
+                                d2f(dsub(ldm<CG>(a.coord + 3 * g + 1), com[1])), d2f(dsub(ldm<CG>(a.coord + 3 * g + 2), com[2])));
 #pragma unroll
-                        for (int k = 0; k < 9; k++) Q[k] = dadd(Q[k], ldm<CG>(a.quad + 9 * (int64_t)(~c) + k));
-                    }
-                    shift_quad(Q, mc, dsub(ldm<CG>(a.coord + 3 * g), com[0]), dsub(ldm<CG>(a.coord + 3 * g + 1), com[1]),
-                               dsub(ldm<CG>(a.coord + 3 * g + 2), com[2]));
+                    for (int e = 0; e < 6; e++) Q[e] = __fadd_rn(Q[e], T[e]);
                 }
             }
         }
-#pragma unroll
-        for (int k = 0; k < 9; k++) a.quad[9 * j + k] = Q[k];
+        store_quad32(a.quad32, j, Q);
     }
 }
 
@@ -1094,21 +1042,20 @@ __global__ void __launch_bounds__(MOM_BLOCK) k_moments_sorted(MomentArgs a, cons
 
 // Small levels. GB300 runs FP64 on one unit per SM sub-partition at about 76 cycles per warp
 // instruction, with any number of lanes active, so a level whose nodes fill fewer warps than there
-// are sub-partitions is bound by the length of one warp's FP64 instruction stream (~400 for a node
-// with eight children and quadrupoles), not by lanes. Here 32 nodes share a block of nine warps
-// (lane = node) and the stream is cut into stages that run side by side: the children's terms
-// (one warp per child slot), the five mass-pass sums (one warp each), the centre of mass and Delta,
-// the children's offsets (one warp per child slot), and the nine quadrupole entries (one warp each).
-// Every sum takes its terms in node_moments_kids's order with the same operations, so the results
-// are identical.
-constexpr int WIDE_NODES = 32, WIDE_WARPS = 9, WIDE_THREADS = WIDE_NODES * WIDE_WARPS;
-constexpr int WIDE_MAX_LEVEL = 4096;  // levels up to this many nodes use k_moments_wide
+// are sub-partitions is bound by the length of one warp's FP64 instruction stream, not by lanes.
+// Here 32 nodes share a block of eight warps (lane = node) and the stream is cut into stages that
+// run side by side: the children's terms (one warp per child slot), the five mass-pass sums (one
+// warp each), the centre of mass and Delta, and the children's FP32 quadrupole terms (one warp per
+// child slot). Every FP64 sum takes its terms in node_moments_kids's order with the same
+// operations, so the results are identical.
+constexpr int WIDE_NODES = 32, WIDE_WARPS = 8, WIDE_THREADS = WIDE_NODES * WIDE_WARPS;
+constexpr int WIDE_MAX_LEVEL = 12288;  // levels up to this many nodes use k_moments_wide
 
 __global__ void __launch_bounds__(WIDE_THREADS) k_moments_wide(MomentArgs a, const int32_t *list, int count,
                                                               const int32_t *kids, const int8_t *nk) {
     __shared__ double s_m[8][WIDE_NODES], s_t[3][8][WIDE_NODES], s_h[8][WIDE_NODES];  // child terms
-    __shared__ double s_r[4][8][WIDE_NODES];                                           // offsets, |r|^2
     __shared__ double s_sum[5][WIDE_NODES], s_com[3][WIDE_NODES];
+    __shared__ float s_q[6][8][WIDE_NODES];  // the children's FP32 quadrupole terms
     __shared__ int32_t s_c[8][WIDE_NODES];
     __shared__ int8_t s_use[8][WIDE_NODES];  // child enters the sums (a particle, or a node of nonzero mass)
     __shared__ int s_n[WIDE_NODES];
@@ -1117,7 +1064,7 @@ __global__ void __launch_bounds__(WIDE_THREADS) k_moments_wide(MomentArgs a, con
     const int64_t N = a.ntot;
     const int64_t j = idx < count ? (int64_t)list[idx] : -1;
     // stage 0: child lists
-    if (w < 8) {
+    {
         const int n = j >= 0 ? (int)nk[j] : 0;
         s_c[w][lane] = w < n ? kids[8 * j + w] : 0;
         if (w == 0) s_n[lane] = n;
@@ -1125,7 +1072,7 @@ __global__ void __launch_bounds__(WIDE_THREADS) k_moments_wide(MomentArgs a, con
     __syncthreads();
     const int n = s_n[lane];
     // stage 1: warp q, child q of every node: the mass-pass terms (use ? term : -0.0)
-    if (w < 8 && w < n) {
+    if (w < n) {
         const int32_t c = s_c[w][lane];
         const bool part = c >= 0;
         const int64_t g = part ? (int64_t)c : N + (int64_t)(~c);
@@ -1143,10 +1090,13 @@ __global__ void __launch_bounds__(WIDE_THREADS) k_moments_wide(MomentArgs a, con
     // stage 2: the five sums, child order
     if (w < 5 && j >= 0) {
         double v = 0.0;
-        for (int q = 0; q < n; q++) {
-            if (w == 0) v = dadd(v, s_m[q][lane]);
-            else if (w < 4) v = dadd(v, s_t[w - 1][q][lane]);
-            else if (s_use[q][lane]) v = pymax(v, s_h[q][lane]);
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            if (q < n) {
+                if (w == 0) v = dadd(v, s_m[q][lane]);
+                else if (w < 4) v = dadd(v, s_t[w - 1][q][lane]);
+                else if (s_use[q][lane]) v = pymax(v, s_h[q][lane]);
+            }
         }
         s_sum[w][lane] = v;
     }
@@ -1179,59 +1129,114 @@ __global__ void __launch_bounds__(WIDE_THREADS) k_moments_wide(MomentArgs a, con
         for (int k = 0; k < 3; k++) s_com[k][lane] = com[k];
     }
     __syncthreads();
-    if (!a.quads) return;  // (uniform over the block)
-    // stage 4: warp q, child q: offset from the centre of mass and its squared length
-    if (w < 8 && w < n && s_use[w][lane]) {
+    if (!a.quad32) return;  // (uniform over the block)
+    // stage 4: warp q, child q: its FP32 quadrupole term
+    if (w < n && s_use[w][lane]) {
+        float T[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         const int32_t c = s_c[w][lane];
         const int64_t g = c >= 0 ? (int64_t)c : N + (int64_t)(~c);
-        const double r0 = dsub(a.coord[3 * g], s_com[0][lane]), r1 = dsub(a.coord[3 * g + 1], s_com[1][lane]);
-        const double r2 = dsub(a.coord[3 * g + 2], s_com[2][lane]);
-        s_r[0][w][lane] = r0;
-        s_r[1][w][lane] = r1;
-        s_r[2][w][lane] = r2;
-        s_r[3][w][lane] = dadd(dadd(dmul(r0, r0), dmul(r1, r1)), dmul(r2, r2));
+        if (c < 0) load_quad32(T, a.quad32[2 * (int64_t)(~c)], a.quad32[2 * (int64_t)(~c) + 1]);
+        quad32_term(T, d2f(s_m[w][lane]), d2f(dsub(a.coord[3 * g], s_com[0][lane])),
+                    d2f(dsub(a.coord[3 * g + 1], s_com[1][lane])), d2f(dsub(a.coord[3 * g + 2], s_com[2][lane])));
+#pragma unroll
+        for (int e = 0; e < 6; e++) s_q[e][w][lane] = T[e];
     }
     __syncthreads();
-    // stage 5: warp e, quadrupole entry e = 3 ia + ib (shift_quad's terms, child order)
-    if (j >= 0) {
-        const int e = w, ia = e / 3, ib = e - 3 * ia;
-        double Q = 0.0;
-        for (int q = 0; q < n; q++) {
-            if (!s_use[q][lane]) continue;
-            const int32_t c = s_c[q][lane];
-            const double m = s_m[q][lane];  // the child's mass (it enters the sums)
-            if (c < 0) Q = dadd(Q, a.quad[9 * (int64_t)(~c) + e]);
-            const double ra = s_r[ia][q][lane];
-            double t;
-            if (ia == ib) t = dmul(m, dsub(dmul(dmul(3.0, ra), ra), s_r[3][q][lane]));
-            else t = dmul(dmul(dmul(m, 3.0), ra), s_r[ib][q][lane]);
-            Q = dadd(Q, t);
-        }
-        a.quad[9 * j + e] = Q;
+    // stage 5: warp 0 adds the children's terms in child order
+    if (w == 0 && j >= 0) {
+        float Q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+            if (q < n && s_use[q][lane])
+#pragma unroll
+                for (int e = 0; e < 6; e++) Q[e] = __fadd_rn(Q[e], s_q[e][q][lane]);
+        store_quad32(a.quad32, j, Q);
     }
 }
 
 // Nodes at depth >= DEPTH_CAP (chains of re-keyed cells and coincident-point buckets, whose depth
 // is unbounded): every such node without node children starts a thread; the last child to finish
 // a parent carries on with the parent, up to the first ancestor above DEPTH_CAP, which the level
-// pass then handles.
-__global__ void k_moments_deep(MomentArgs a, const int32_t *list, int count, const int8_t *fdepth) {
+// pass then handles. Children are read through L2.
+__global__ void k_moments_deep(MomentArgs a, const int32_t *list, int count, const int8_t *fdepth,
+                               const int32_t *kids, const int8_t *nk) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
     int64_t j = list[i];
     if (a.nchild[j] != 0) return;
-    int64_t f = a.ntot + j;
     for (int64_t guard = 0; guard < a.mtot + 1; guard++) {
-        node_moments(a, f);
+        node_moments_kids<true>(a, j, kids, nk[j]);
         __threadfence();
-        int64_t p = a.parent[f];
+        int64_t p = a.parent[a.ntot + j];
         if (p < a.ntot || p >= a.ntot + a.mtot) return;
         int64_t pj = p - a.ntot;
         if (fdepth[pj] < DEPTH_CAP) return;
         int prev = atomicAdd(&a.arrived[pj], 1);
         if (prev != a.nchild[pj] - 1) return;
         __threadfence();
-        f = p;
+        j = pj;
+    }
+}
+
+// The quadrupole pass: node j's FP64 quadrupole (RollupQuadrupoles, octree.py:234-292) from its
+// children's final masses, centres of mass and FP64 quadrupoles, with the order and operations the
+// moment pass used to take (shift_quad per child in k_kids's order, a node child's quadrupole added
+// first), so the values are pytreegrav's bit for bit. The node's centre of mass is its final
+// coordinate (its cell centre when massless, as in the moment pass).
+template <bool CG>
+__device__ __forceinline__ void node_quad64(const MomentArgs &a, int64_t j, const int32_t *kids, int n) {
+    const int4 k0 = *reinterpret_cast<const int4 *>(kids + 8 * j);
+    const int4 k1 = *reinterpret_cast<const int4 *>(kids + 8 * j + 4);
+    const int32_t ch[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+    const int64_t N = a.ntot, f = N + j;
+    const double com[3] = {ldm<CG>(a.coord + 3 * f), ldm<CG>(a.coord + 3 * f + 1), ldm<CG>(a.coord + 3 * f + 2)};
+    double Q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        if (q < n) {
+            const int32_t c = ch[q];
+            const bool part = c >= 0;
+            const int64_t g = part ? (int64_t)c : N + (int64_t)(~c);
+            const double mc = ldm<CG>(a.mass + g);
+            if (part || mc != 0.0) {
+                if (!part) {
+#pragma unroll
+                    for (int k = 0; k < 9; k++) Q[k] = dadd(Q[k], ldm<CG>(a.quad + 9 * (int64_t)(~c) + k));
+                }
+                shift_quad(Q, mc, dsub(ldm<CG>(a.coord + 3 * g), com[0]), dsub(ldm<CG>(a.coord + 3 * g + 1), com[1]),
+                           dsub(ldm<CG>(a.coord + 3 * g + 2), com[2]));
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) a.quad[9 * j + k] = Q[k];
+}
+
+__global__ void k_quad64_level(MomentArgs a, const int32_t *list, int count, const int32_t *kids, const int8_t *nk) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const int64_t j = list[i];
+    node_quad64<false>(a, j, kids, nk[j]);
+}
+
+// The quadrupole pass below DEPTH_CAP, climbing as k_moments_deep does.
+__global__ void k_quad64_deep(MomentArgs a, const int32_t *list, int count, const int8_t *fdepth, const int32_t *kids,
+                              const int8_t *nk) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    int64_t j = list[i];
+    if (a.nchild[j] != 0) return;
+    for (int64_t guard = 0; guard < a.mtot + 1; guard++) {
+        node_quad64<true>(a, j, kids, nk[j]);
+        __threadfence();
+        int64_t p = a.parent[a.ntot + j];
+        if (p < a.ntot || p >= a.ntot + a.mtot) return;
+        int64_t pj = p - a.ntot;
+        if (fdepth[pj] < DEPTH_CAP) return;
+        int prev = atomicAdd(&a.arrived[pj], 1);
+        if (prev != a.nchild[pj] - 1) return;
+        __threadfence();
+        j = pj;
     }
 }
 
@@ -1265,6 +1270,28 @@ __global__ void k_fold_only(MomentArgs a) {
 }
 
 // ---------------------------------------------------------------------------------------------
+// A non-blocking stream per host thread (and device) for build work that can run beside the
+// build's own stream, with its fork and join events; created once.
+struct BuildSide {
+    int dev = -1;
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+static tg_status build_side(BuildSide *&out) {
+    static thread_local BuildSide side;
+    int dev = 0;
+    TG_CUDA(cudaGetDevice(&dev));
+    if (side.s && side.dev != dev) side = BuildSide();  // another device: this thread's old one is kept alive
+    if (!side.s) {
+        TG_CUDA(cudaStreamCreateWithFlags(&side.s, cudaStreamNonBlocking));
+        TG_CUDA(cudaEventCreateWithFlags(&side.fork, cudaEventDisableTiming));
+        TG_CUDA(cudaEventCreateWithFlags(&side.join, cudaEventDisableTiming));
+        side.dev = dev;
+    }
+    out = &side;
+    return TG_OK;
+}
+
 template <typename T>
 static tg_status dalloc(T **p, int64_t n, cudaStream_t s) {
     *p = nullptr;
@@ -1466,6 +1493,8 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     BuildSummary hs;
     memset(&hs, 0, sizeof(hs));
     bool summary_final = false;
+    BuildSide *side = nullptr;  // k_node_centers of the last round runs there when set
+    bool centers_forked = false;
     // Non-finite input is reported once the build has run to its end and freed its memory: every
     // kernel stays in bounds on such input (keys of NaN quantize to 0, every link is checked).
     bool nonfinite_seen = false;
@@ -1559,7 +1588,22 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
             TG_TRY(run_round());
         }
         nd.count = slot_base + Mr;
-        if (Mr > 0) { k_node_centers<<<div_up(Mr, CENTER_BLOCK), CENTER_BLOCK, 0, st>>>(v, nd, slot_base, Mr, keys_sorted); tg::note_launch(); }
+        if (Mr > 0) {
+            // the last round's centres (nothing re-keys or grows the slots after it) run beside the
+            // node numbering, which does not read them; k_write_nodes joins them
+            cudaStream_t cs = st;
+            if (hs.n_exh == 0) {
+                TG_TRY(build_side(side));
+                TG_CUDA(cudaEventRecord(side->fork, st));
+                TG_CUDA(cudaStreamWaitEvent(side->s, side->fork, 0));
+                cs = side->s;
+            }
+            { k_node_centers<<<div_up(Mr, CENTER_BLOCK), CENTER_BLOCK, 0, cs>>>(v, nd, slot_base, Mr, keys_sorted); tg::note_launch(); }
+            if (cs != st) {
+                TG_CUDA(cudaEventRecord(side->join, cs));
+                centers_forked = true;
+            }
+        }
         n_exh = (int)hs.n_exh;
         dfree(L, st); dfree(cnt, st); dfree(nstart, st);
         if (n_exh == 0) {
@@ -1573,7 +1617,7 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
             TG_CUDA(cudaGetLastError());
         }
     }
-    segs_free(sg, st);
+    if (!centers_forked) segs_free(sg, st);  // else k_node_centers still reads them: freed after the join
     dfree(root_first, st);
 
     // 5. buckets for runs still exhausted after three re-keys
@@ -1670,13 +1714,6 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     TG_TRY(dalloc(&T->first, NE, st));
     TG_TRY(dalloc(&T->next, NE, st));
     TG_TRY(dalloc(&T->parent, NE, st));
-    TG_CUDA(cudaMemcpyAsync(T->coord, pc, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, st));
-    TG_CUDA(cudaMemcpyAsync(T->mass, pm, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
-    TG_CUDA(cudaMemcpyAsync(T->soft, ps, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
-    TG_CUDA(cudaMemsetAsync(T->mass + N, 0, sizeof(double) * M, st));
-    TG_CUDA(cudaMemsetAsync(T->soft + N, 0, sizeof(double) * M, st));
-    TG_CUDA(cudaMemsetAsync(T->delta + N, 0, sizeof(double) * M, st));
-    dfree(pc, st); dfree(pm, st); dfree(ps, st);
     TG_TRY(dalloc(&T->node_range, M, st));
     TG_TRY(dalloc(&T->cell_center, 3 * M, st));
     int *lvl = nullptr;  // section offsets, then cursors, of the depth lists
@@ -1686,10 +1723,16 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     TG_TRY(dalloc(&lvl_list, M, st));
     TG_TRY(dalloc(&fdepth, M, st));
     { k_level_offsets<<<1, 32, 0, st>>>(sum, lvl, lvl + DEPTH_CAP + 1); tg::note_launch(); }
-    { k_write_nodes<<<LAUNCH(M)>>>(nd, M, final_of_slot, T->coord, T->size, T->first, T->next, T->parent,
-                                 T->node_range, T->cell_center, N, lvl, lvl + DEPTH_CAP + 1, lvl_list, fdepth); tg::note_launch(); }
-    { k_write_particles<<<LAUNCH(N)>>>(N, p_parent, p_next, final_of_slot, T->first, T->next, T->parent, T->size,
-                                     T->delta); tg::note_launch(); }
+    if (centers_forked) {
+        TG_CUDA(cudaStreamWaitEvent(st, side->join, 0));
+        segs_free(sg, st);
+    }
+    { k_write_nodes<<<LAUNCH(M)>>>(nd, M, final_of_slot, T->coord, T->size, T->mass, T->soft, T->delta, T->first,
+                                 T->next, T->parent, T->node_range, T->cell_center, N, lvl, lvl + DEPTH_CAP + 1,
+                                 lvl_list, fdepth); tg::note_launch(); }
+    { k_write_particles<<<LAUNCH(N)>>>(N, p_parent, p_next, final_of_slot, pc, pm, ps, T->coord, T->mass, T->soft,
+                                     T->first, T->next, T->parent, T->size, T->delta); tg::note_launch(); }
+    dfree(pc, st); dfree(pm, st); dfree(ps, st);
     TG_CUDA(cudaMemsetAsync(&sum->bad, 0, sizeof(int), st));
     { k_validate_links<<<LAUNCH(NE)>>>(NE, T->first, T->next, T->parent, &sum->bad); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
@@ -1734,29 +1777,34 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
         T->sys_capacity[s] = reference_capacity(np, std::max<int64_t>(node_hi, (int64_t)rq[s]));
     }
     // 9. moments: nodes deeper than DEPTH_CAP by climbing, then one launch per depth, deepest first
-    // (the moment kernels bound every link they follow)
+    // (the moment kernels bound every link they follow). With quadrupoles the pass sums them in FP32
+    // for the FP32 walk; the FP64 quadrupoles come from ensure_quad64 when first needed, which the
+    // depth lists are kept for.
     MomentArgs a;
     a.ntot = N;
     a.mtot = M;
     a.coord = T->coord; a.mass = T->mass; a.soft = T->soft; a.delta = T->delta;
     a.first = T->first; a.next = T->next; a.parent = T->parent;
-    a.quads = (quadrupole && compute_moments) ? 1 : 0;
     a.quad = nullptr;
+    a.quad32 = nullptr;
     a.acc = nullptr;
     a.nchild = nullptr;
     a.arrived = nullptr;
     if (quadrupole) {
-        TG_TRY(dalloc(&T->quad, 9 * M, st));
-        // with moments every node's quadrupole is written by the pass below
-        if (!compute_moments) TG_CUDA(cudaMemsetAsync(T->quad, 0, sizeof(double) * 9 * M, st));
-        a.quad = T->quad;
+        TG_TRY(dalloc(&T->quad32, 2 * M, st));
+        if (compute_moments) a.quad32 = T->quad32;  // every node's is written by the pass below
+        else TG_CUDA(cudaMemsetAsync(T->quad32, 0, sizeof(float4) * 2 * M, st));
     }
+    T->lvl_off.assign(DEPTH_CAP + 2, 0);
+    for (int d = 0; d <= DEPTH_CAP; d++) T->lvl_off[d + 1] = T->lvl_off[d] + hs.depth_hist[d];
     if (compute_moments) {
-        int off[DEPTH_CAP + 1];
-        for (int d = 0, run = 0; d <= DEPTH_CAP; d++) {
-            off[d] = run;
-            run += hs.depth_hist[d];
-        }
+        const int *off = T->lvl_off.data();
+        // every node's children once, in summation order
+        int32_t *kids = nullptr;
+        int8_t *nk = nullptr;
+        TG_TRY(dalloc(&kids, 8 * M, st));
+        TG_TRY(dalloc(&nk, M, st));
+        { k_kids<<<LAUNCH(M)>>>(N, M, T->first, T->next, kids, nk); tg::note_launch(); }
         TG_TRY(dalloc(&a.acc, 3 * M, st));
         const int ndeep = hs.depth_hist[DEPTH_CAP];
         if (ndeep > 0) {
@@ -1765,14 +1813,8 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
             TG_CUDA(cudaMemsetAsync(a.nchild, 0, sizeof(int) * M, st));
             TG_CUDA(cudaMemsetAsync(a.arrived, 0, sizeof(int) * M, st));
             { k_count_node_children<<<LAUNCH(M)>>>(N, M, T->parent, a.nchild); tg::note_launch(); }
-            { k_moments_deep<<<div_up(ndeep, 128), 128, 0, st>>>(a, lvl_list + off[DEPTH_CAP], ndeep, fdepth); tg::note_launch(); }
+            { k_moments_deep<<<div_up(ndeep, 128), 128, 0, st>>>(a, lvl_list + off[DEPTH_CAP], ndeep, fdepth, kids, nk); tg::note_launch(); }
         }
-        // every node's children once, in summation order, for the level passes
-        int32_t *kids = nullptr;
-        int8_t *nk = nullptr;
-        TG_TRY(dalloc(&kids, 8 * M, st));
-        TG_TRY(dalloc(&nk, M, st));
-        { k_kids<<<LAUNCH(M)>>>(N, M, T->first, T->next, kids, nk); tg::note_launch(); }
         // one launch per depth, deepest first: k_moments_wide on the small levels (latency-bound),
         // k_moments_sorted on the large ones (FP64-throughput-bound), with the largest block that still
         // gives every SM about four blocks (the mid-size levels need the smaller ones to cover the SMs)
@@ -1799,8 +1841,65 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
         TG_CUDA(cudaGetLastError());
     }
 
-    dfree(lvl, st); dfree(lvl_list, st); dfree(fdepth, st);
+    dfree(lvl, st);
+    if (quadrupole && compute_moments) {  // kept for the FP64 quadrupole pass
+        T->lvl_list = lvl_list;
+        T->fdepth = fdepth;
+    } else {
+        dfree(lvl_list, st); dfree(fdepth, st);
+    }
     TG_CUDA(cudaEventRecord(T->ev_built, st));
+    return TG_OK;
+}
+
+// The FP64 quadrupoles of a quadrupole tree (pytreegrav's Octree.Quadrupoles, bit for bit), computed
+// on `st` the first time something needs them: copy-out, the tree's info, an FP64 walk. One launch
+// per depth over the depth lists the build kept, deepest first; nodes deeper than DEPTH_CAP climb.
+tg_status ensure_quad64(tg_tree_s *T, cudaStream_t st) {
+    if (!T->has_quads || T->quad) return TG_OK;
+    tree_wait_built(T, st);
+    const int64_t N = T->ntot, M = T->mtot;
+    double *q = nullptr;
+    TG_TRY(dalloc(&q, 9 * M, st));
+    if (!T->compute_moments || !T->lvl_list) {
+        TG_CUDA(cudaMemsetAsync(q, 0, sizeof(double) * 9 * M, st));
+        T->quad = q;
+        return TG_OK;
+    }
+    MomentArgs a;
+    a.ntot = N;
+    a.mtot = M;
+    a.coord = T->coord; a.mass = T->mass; a.soft = T->soft; a.delta = T->delta;
+    a.first = T->first; a.next = T->next; a.parent = T->parent;
+    a.quad = q;
+    a.quad32 = nullptr;
+    a.acc = nullptr;
+    a.nchild = nullptr;
+    a.arrived = nullptr;
+    const int *off = T->lvl_off.data();
+    int32_t *kids = nullptr;
+    int8_t *nk = nullptr;
+    TG_TRY(dalloc(&kids, 8 * M, st));
+    TG_TRY(dalloc(&nk, M, st));
+    { k_kids<<<LAUNCH(M)>>>(N, M, T->first, T->next, kids, nk); tg::note_launch(); }
+    const int ndeep = off[DEPTH_CAP + 1] - off[DEPTH_CAP];
+    if (ndeep > 0) {
+        TG_TRY(dalloc(&a.nchild, M, st));
+        TG_TRY(dalloc(&a.arrived, M, st));
+        TG_CUDA(cudaMemsetAsync(a.nchild, 0, sizeof(int) * M, st));
+        TG_CUDA(cudaMemsetAsync(a.arrived, 0, sizeof(int) * M, st));
+        { k_count_node_children<<<LAUNCH(M)>>>(N, M, T->parent, a.nchild); tg::note_launch(); }
+        { k_quad64_deep<<<div_up(ndeep, 128), 128, 0, st>>>(a, T->lvl_list + off[DEPTH_CAP], ndeep, T->fdepth, kids, nk); tg::note_launch(); }
+    }
+    for (int d = DEPTH_CAP - 1; d >= 0; d--) {
+        const int c = off[d + 1] - off[d];
+        if (c <= 0) continue;
+        { k_quad64_level<<<div_up(c, 64), 64, 0, st>>>(a, T->lvl_list + off[d], c, kids, nk); tg::note_launch(); }
+    }
+    TG_CUDA(cudaGetLastError());
+    dfree(kids, st); dfree(nk, st); dfree(a.nchild, st); dfree(a.arrived, st);
+    dfree(T->lvl_list, st); dfree(T->fdepth, st);
+    T->quad = q;
     return TG_OK;
 }
 

@@ -116,7 +116,7 @@ void destroy(tg_tree_s *t) {
     free_arena(t->arena32, st);
     free_arena(t->arena64, st);
     if (t->stats_dev) cudaFreeAsync(t->stats_dev, st);
-    f(t->groups); f(t->group_root); f(t->group_node); f(t->gstats); f(t->gerr); f(t->sort_err); f(t->vel); f(t->vdisp);
+    f(t->groups); f(t->group_root); f(t->group_node); f(t->gstats); f(t->gerr); f(t->sort_err); f(t->vel); f(t->vdisp); f(t->quad32); f(t->lvl_list); f(t->fdepth);
     if (t->side) cudaStreamDestroy(t->side);  // released once its work is done
     if (t->ev_fork) cudaEventDestroy(t->ev_fork);
     if (t->ev_join) cudaEventDestroy(t->ev_join);
@@ -240,6 +240,15 @@ tg_status tg_tree_info_get(tg_tree t, tg_tree_info *info) {
     return TG_OK;
 }
 
+tg_status tg_tree_quadrupoles(tg_tree t, const double **quad, void *stream) {
+    if (!t || !quad) return TG_ERR_BAD_ARG;
+    *quad = nullptr;
+    if (!t->has_quads) return TG_OK;
+    TG_TRY(ensure_quad64(t, (cudaStream_t)stream));
+    *quad = t->quad;
+    return TG_OK;
+}
+
 tg_status tg_tree_copy_out(tg_tree t, double *coord, double *mass, double *size, double *delta, double *soft,
                            double *quad, int64_t *first, int64_t *next, int64_t *walk_idx, void *stream) {
     if (!t) return TG_ERR_BAD_ARG;
@@ -257,7 +266,10 @@ tg_status tg_tree_copy_out(tg_tree t, double *coord, double *mass, double *size,
     if (size) TG_TRY(cp(size, t->size, sizeof(double) * NE));
     if (delta) TG_TRY(cp(delta, t->delta, sizeof(double) * NE));
     if (soft) TG_TRY(cp(soft, t->soft, sizeof(double) * NE));
-    if (quad && t->quad) TG_TRY(cp(quad + 9 * t->ntot, t->quad, sizeof(double) * 9 * t->mtot));
+    if (quad && t->has_quads) {
+        TG_TRY(ensure_quad64(t, st));
+        TG_TRY(cp(quad + 9 * t->ntot, t->quad, sizeof(double) * 9 * t->mtot));
+    }
     if (first) TG_TRY(cp(first, t->first, sizeof(int64_t) * NE));
     if (next) TG_TRY(cp(next, t->next, sizeof(int64_t) * NE));
     if (walk_idx) TG_TRY(cp(walk_idx, t->walk_idx, sizeof(int64_t) * t->ntot));
@@ -301,7 +313,7 @@ tg_status tg_tree_fields(tg_tree t, const double *pos, const double *h, int64_t 
     if ((fields & 7) == 0 || (fields & ~7)) return TG_ERR_BAD_ARG;
     if (!(theta > 0) || !valid_group_size(group_size)) return TG_ERR_BAD_ARG;
     if (precision != TG_FP32 && precision != TG_FP64) return TG_ERR_BAD_ARG;
-    if (quadrupole && !t->quad) return TG_ERR_NO_QUADRUPOLES;
+    if (quadrupole && !t->has_quads) return TG_ERR_NO_QUADRUPOLES;
     cudaStream_t st = (cudaStream_t)stream;
     tree_wait_built(t, st);
     const int W = field_width(fields);

@@ -285,7 +285,7 @@ tg_status tg_targets_fields(tg_targets ts, int fields, int quadrupole, double th
         return TG_ERR_BAD_ARG;
     if (tol_per_group && precision != TG_FP32) return TG_ERR_BAD_ARG;
     tg_tree_s *src = ts->src, *tt = ts->tt;
-    if (quadrupole && !src->quad) return TG_ERR_NO_QUADRUPOLES;
+    if (quadrupole && !src->has_quads) return TG_ERR_NO_QUADRUPOLES;
     cudaStream_t st = (cudaStream_t)stream;
     tree_wait_built(src, st);
     tree_wait_built(tt, st);

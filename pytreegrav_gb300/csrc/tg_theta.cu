@@ -866,7 +866,7 @@ tg_status tg_tree_fields_grouped(tg_tree t, int fields, int quadrupole, double G
                                  void *stream) {
     if (!t || !out || (fields & 7) == 0 || (fields & ~7) || !valid_gs(group_size) || !(theta > 0))
         return TG_ERR_BAD_ARG;
-    if (quadrupole && !t->quad) return TG_ERR_NO_QUADRUPOLES;
+    if (quadrupole && !t->has_quads) return TG_ERR_NO_QUADRUPOLES;
     cudaStream_t st = (cudaStream_t)stream;
     tree_wait_built(t, st);
     TG_TRY(tree_groups(t, group_size, st));
@@ -888,7 +888,7 @@ tg_status tg_tree_fields_learned(tg_tree t, int fields, int quadrupole, double G
                                  float log10_lambda, double theta_fallback, int mem, double *out, void *stream) {
     if (!t || !out || (fields & 7) == 0 || (fields & ~7) || !valid_gs(group_size) || !(theta_fallback > 0))
         return TG_ERR_BAD_ARG;
-    if (quadrupole && !t->quad) return TG_ERR_NO_QUADRUPOLES;
+    if (quadrupole && !t->has_quads) return TG_ERR_NO_QUADRUPOLES;
     cudaStream_t st = (cudaStream_t)stream;
     tree_wait_built(t, st);
     TG_TRY(tree_groups_with_arena(t, group_size, false, st));
@@ -903,7 +903,7 @@ tg_status tg_targets_fields_learned(tg_targets ts, int fields, int quadrupole, d
                                     float log10_lambda, double theta_fallback, int mem, double *out, void *stream) {
     if (!ts || !out || (fields & 7) == 0 || (fields & ~7) || !(theta_fallback > 0)) return TG_ERR_BAD_ARG;
     tg_tree_s *t = ts->src, *tt = ts->tt;
-    if (quadrupole && !t->quad) return TG_ERR_NO_QUADRUPOLES;
+    if (quadrupole && !t->has_quads) return TG_ERR_NO_QUADRUPOLES;
     cudaStream_t st = (cudaStream_t)stream;
     tree_wait_built(t, st);
     tree_wait_built(tt, st);

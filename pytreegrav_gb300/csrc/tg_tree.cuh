@@ -67,7 +67,12 @@ struct tg_tree_s {
     double *size = nullptr;
     double *delta = nullptr;
     double *soft = nullptr;
-    double *quad = nullptr;    // 9 per NODE (mtot rows), or null
+    double *quad = nullptr;    // 9 per NODE (mtot rows): FP64 quadrupoles, null until ensure_quad64
+    float4 *quad32 = nullptr;  // 2 per NODE: FP32 quadrupoles (xx xy xz yy)(yz zz 0 0) for FP32 walks
+    // The depth lists of the moment pass, kept for ensure_quad64 (quadrupole trees until it has run).
+    int32_t *lvl_list = nullptr;
+    int8_t *fdepth = nullptr;
+    std::vector<int> lvl_off;  // host: section offsets per depth (DEPTH_CAP + 2)
     int64_t *first = nullptr;
     int64_t *next = nullptr;
     int64_t *walk_idx = nullptr;  // per particle: index into the caller's input arrays
@@ -128,4 +133,6 @@ namespace tg {
 inline void tree_wait_built(const tg_tree_s *t, cudaStream_t s) {
     if (t && t->ev_built) cudaStreamWaitEvent(s, t->ev_built, 0);
 }
+// The FP64 quadrupoles (t->quad) of a quadrupole tree, computed on s the first time they are needed.
+tg_status ensure_quad64(tg_tree_s *t, cudaStream_t s);
 }  // namespace tg

@@ -196,7 +196,7 @@ __global__ void k_arena_leaves(int64_t ntot, int64_t mtot, const int64_t *first,
 template <typename T>
 __global__ void k_arena_nodes(int64_t ntot, int64_t mtot, const double *coord, const double *mass,
                               const double *soft, const double *size, const double *delta, const double *quad,
-                              Arena<T> ar) {
+                              const float4 *quad32, Arena<T> ar) {
     int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= mtot) return;
     const int64_t f = ntot + j;
@@ -223,9 +223,14 @@ __global__ void k_arena_nodes(int64_t ntot, int64_t mtot, const double *coord, c
         ar.n_tol[j] = make_float2(a3, a2);
     }
     if (ar.n_quad) {
-        const double *Q = quad + 9 * j;
-        ar.n_quad[2 * j] = vec4<T>{narrow(Q[0], T(0)), narrow(Q[1], T(0)), narrow(Q[2], T(0)), narrow(Q[4], T(0))};
-        ar.n_quad[2 * j + 1] = vec4<T>{narrow(Q[5], T(0)), narrow(Q[8], T(0)), T(0), T(0)};
+        if constexpr (sizeof(T) == 4) {  // FP32 walks: the moment pass's FP32 quadrupoles
+            ar.n_quad[2 * j] = quad32[2 * j];
+            ar.n_quad[2 * j + 1] = quad32[2 * j + 1];
+        } else {
+            const double *Q = quad + 9 * j;
+            ar.n_quad[2 * j] = vec4<T>{narrow(Q[0], T(0)), narrow(Q[1], T(0)), narrow(Q[2], T(0)), narrow(Q[4], T(0))};
+            ar.n_quad[2 * j + 1] = vec4<T>{narrow(Q[5], T(0)), narrow(Q[8], T(0)), T(0), T(0)};
+        }
     }
 }
 
@@ -241,7 +246,7 @@ tg_status build_arena_topology(tg_tree_s *t, Arena<T> &ar, cudaStream_t st) {
     const int64_t M = t->mtot, N = t->ntot;
     ar.n_nodes = M;
     ar.n_leaves = N;
-    ar.has_quad = t->has_quads && t->quad;
+    ar.has_quad = t->has_quads;
     if (M >= (1 << 27) || N >= (1 << 27)) {  // node and leaf indices are packed with 4 count bits
         set_last_error_msg("tree too large for the walk arena (2^27 nodes or particles)");
         return TG_ERR_BAD_ARG;
@@ -278,8 +283,9 @@ tg_status build_arena_topology(tg_tree_s *t, Arena<T> &ar, cudaStream_t st) {
 template <typename T>
 tg_status build_arena_nodes(tg_tree_s *t, Arena<T> &ar, cudaStream_t st) {
     const int64_t M = t->mtot, N = t->ntot;
+    if (sizeof(T) == 8 && ar.n_quad) TG_TRY(ensure_quad64(t, st));
     { k_arena_nodes<T><<<div_up(M, 256), 256, 0, st>>>(N, M, t->coord, t->mass, t->soft, t->size, t->delta, t->quad,
-                                                      ar); tg::note_launch(); }
+                                                      t->quad32, ar); tg::note_launch(); }
     TG_CUDA(cudaGetLastError());
     ar.built = true;
     return TG_OK;
@@ -2200,7 +2206,7 @@ tg_status tg_walk_graph_create(tg_tree t, int fields, int quadrupole, double the
         group_size != 32)
         return TG_ERR_BAD_ARG;
     if (grouping != TG_GROUP_BLOCKS && grouping != TG_GROUP_TREE) return TG_ERR_BAD_ARG;
-    if (quadrupole && !t->quad) return TG_ERR_NO_QUADRUPOLES;
+    if (quadrupole && !t->has_quads) return TG_ERR_NO_QUADRUPOLES;
     *out_graph = nullptr;
     tg_walk_graph_s *g = new (std::nothrow) tg_walk_graph_s();
     if (!g) return TG_ERR_OOM;

@@ -148,6 +148,50 @@ def test_root_quadrupole_matches_analytic(tg):
         assert np.max(np.abs(t.Quadrupoles[root] - Qref)) / np.max(np.abs(Qref)) < 1e-10
 
 
+def test_fp64_quadrupoles_on_demand_and_fp32_ones_for_the_walk(tg):
+    """The build sums FP32 quadrupoles for the FP32 walk; the FP64 ones (bit-exact, the oracle's)
+    come when first asked for: through tg_tree_quadrupoles (device pointer, then also in the tree's
+    info) as through copy-out. The FP32 quadrupole walk, which reads the FP32 sums, stays within the
+    FP32 walk bar (1e-5 relative RMS) of the FP64 oracle walk over the same groups."""
+    import ctypes
+
+    import torch
+
+    from pytreegrav_gb300 import _lib
+
+    rng = np.random.default_rng(4)
+    n = 200_000
+    x, m, h = rng.normal(size=(n, 3)) ** 3, rng.random(n) / n, np.full(n, 0.01)
+    t = tg.ConstructTree(x, m, h, quadrupole=True)
+    L = _lib.load()
+    info = _lib.TreeInfo()
+    _lib.check(L.tg_tree_info_get(t._h, ctypes.byref(info)))
+    assert not info.quad  # nothing has needed the FP64 quadrupoles yet
+    q = ctypes.c_void_p()
+    _lib.check(L.tg_tree_quadrupoles(t._h, ctypes.byref(q), None))
+    torch.cuda.synchronize()
+    _lib.check(L.tg_tree_info_get(t._h, ctypes.byref(info)))
+    assert q.value and info.quad == q.value
+    qh = np.empty((t.NumNodes, 3, 3))
+    _lib.check(L.tg_tree_copy_out(t._h, None, None, None, None, None, _lib.ptr(qh), None, None, None, None))
+    ot = O.OracleTree(x, m, h, quadrupole=True)
+    assert np.array_equal(qh, ot.Quadrupoles)
+    assert np.array_equal(t.Quadrupoles, ot.Quadrupoles)
+    # the FP32 walk with quadrupoles stays at its bar against the FP64 oracle walk
+    got = t.fields(accel=True, quadrupole=True, theta=0.7, group_size=8)["accel"]
+    idx = ot.TreewalkIndices
+    sub = np.arange(0, n, 97)
+    inv = np.empty(n, np.int64)
+    inv[idx] = np.arange(n)
+    pos_s = np.sort(inv[sub])
+    starts = np.unique(pos_s // 8 * 8)
+    ref = O.fields_groups(ot, x[idx], h[idx], starts, np.minimum(8, n - starts), False, True, False, True, 0.7,
+                          nthreads=O.num_threads())["accel"]
+    a = got[idx[pos_s]]
+    r = ref[pos_s]
+    assert np.sqrt(np.mean(np.sum((a - r) ** 2, 1)) / np.mean(np.sum(r**2, 1))) < 1e-5
+
+
 @pytest.mark.parametrize("where", ["pos", "m", "softening"])
 @pytest.mark.parametrize("bad", [np.nan, np.inf, -np.inf])
 def test_nonfinite_input_raises_like_construct_tree(tg, capsys, where, bad):
