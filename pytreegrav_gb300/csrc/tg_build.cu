@@ -894,7 +894,7 @@ __device__ __forceinline__ void shift_quad(double *Q, double m, double r0, doubl
 
 // The FP32 quadrupole the FP32 walk uses, Q = (xx, xy, xz, yy, yz, zz): the same shift (a child of
 // mass m at offset r from the node's centre of mass adds m (3 r_a r_b - delta_ab r^2), a node child
-// its own quadrupole too) summed in FP32, the offsets taken in FP64 and rounded once. GB300 issues
+// its own quadrupole too) summed in FP32, the offsets formed from hi/lo FP32 splits (off32). GB300 issues
 // FP64 at 1/73 of the FP32 rate and these sums were most of the moment pass's FP64 instructions;
 // the FP64 quadrupoles (pytreegrav's, bit for bit) come from the quadrupole pass when first needed.
 // Each child's term T = (its quadrupole, for a node) + shift is formed apart and then added to the
@@ -911,6 +911,13 @@ __device__ __forceinline__ void quad32_term(float *T, float m, float rx, float r
 }
 __device__ __forceinline__ void load_quad32(float *T, float4 a, float4 b) {
     T[0] = a.x; T[1] = a.y; T[2] = a.z; T[3] = a.w; T[4] = b.x; T[5] = b.y;
+}
+// x - c in FP32 from the hi/lo FP32 splits of both (integer-unit conversions, no FP64 instruction):
+// the hi parts of nearby values cancel exactly, so the offset keeps ~2^-24 of its own size.
+__device__ __forceinline__ float off32(double x, float chi, float clo) {
+    float xhi, xlo;
+    d2f_split(x, xhi, xlo);
+    return __fadd_rn(__fsub_rn(xhi, chi), __fsub_rn(xlo, clo));
 }
 __device__ __forceinline__ void store_quad32(float4 *q32, int64_t j, const float *Q) {
     q32[2 * j] = make_float4(Q[0], Q[1], Q[2], Q[3]);
@@ -970,7 +977,7 @@ __device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j
     a.acc[3 * j + 2] = az;
     double com[3] = {ldm<CG>(a.coord + 3 * f), ldm<CG>(a.coord + 3 * f + 1), ldm<CG>(a.coord + 3 * f + 2)};
     if (m != 0.0) {
-        double inv = ddiv(1.0, m);
+        double inv = __drcp_rn(m);  // 1 / m correctly rounded: the same value as 1.0 / m
         double accs[3] = {ax, ay, az};
         double d2 = 0.0;
 #pragma unroll
@@ -985,6 +992,9 @@ __device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j
     }
     if (a.quad32) {
         float Q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float ch_[3], cl_[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) d2f_split(com[k], ch_[k], cl_[k]);
 #pragma unroll
         for (int q = 0; q < 8; q++) {
             if (q < n) {
@@ -995,8 +1005,9 @@ __device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j
                 if (part || mc != 0.0) {
                     float T[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
                     if (!part) load_quad32(T, ldm4<CG>(a.quad32 + 2 * (int64_t)(~c)), ldm4<CG>(a.quad32 + 2 * (int64_t)(~c) + 1));
-                    quad32_term(T, d2f(mc), d2f(dsub(ldm<CG>(a.coord + 3 * g), com[0])),
-                                d2f(dsub(ldm<CG>(a.coord + 3 * g + 1), com[1])), d2f(dsub(ldm<CG>(a.coord + 3 * g + 2), com[2])));
+                    quad32_term(T, d2f(mc), off32(ldm<CG>(a.coord + 3 * g), ch_[0], cl_[0]),
+                                off32(ldm<CG>(a.coord + 3 * g + 1), ch_[1], cl_[1]),
+                                off32(ldm<CG>(a.coord + 3 * g + 2), ch_[2], cl_[2]));
 #pragma unroll
                     for (int e = 0; e < 6; e++) Q[e] = __fadd_rn(Q[e], T[e]);
                 }
@@ -1113,7 +1124,7 @@ __global__ void __launch_bounds__(WIDE_THREADS) k_moments_wide(MomentArgs a, con
         a.acc[3 * j + 2] = acc[2];
         double com[3] = {a.coord[3 * f], a.coord[3 * f + 1], a.coord[3 * f + 2]};
         if (m != 0.0) {
-            const double inv = ddiv(1.0, m);
+            const double inv = __drcp_rn(m);  // 1 / m correctly rounded: the same value as 1.0 / m
             double d2 = 0.0;
 #pragma unroll
             for (int k = 0; k < 3; k++) {
@@ -1136,8 +1147,11 @@ __global__ void __launch_bounds__(WIDE_THREADS) k_moments_wide(MomentArgs a, con
         const int32_t c = s_c[w][lane];
         const int64_t g = c >= 0 ? (int64_t)c : N + (int64_t)(~c);
         if (c < 0) load_quad32(T, a.quad32[2 * (int64_t)(~c)], a.quad32[2 * (int64_t)(~c) + 1]);
-        quad32_term(T, d2f(s_m[w][lane]), d2f(dsub(a.coord[3 * g], s_com[0][lane])),
-                    d2f(dsub(a.coord[3 * g + 1], s_com[1][lane])), d2f(dsub(a.coord[3 * g + 2], s_com[2][lane])));
+        float ch_[3], cl_[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) d2f_split(s_com[k][lane], ch_[k], cl_[k]);
+        quad32_term(T, d2f(s_m[w][lane]), off32(a.coord[3 * g], ch_[0], cl_[0]), off32(a.coord[3 * g + 1], ch_[1], cl_[1]),
+                    off32(a.coord[3 * g + 2], ch_[2], cl_[2]));
 #pragma unroll
         for (int e = 0; e < 6; e++) s_q[e][w][lane] = T[e];
     }

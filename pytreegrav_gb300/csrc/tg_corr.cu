@@ -20,6 +20,7 @@
 // One thread per target, each of a fixed set of threads accumulating its targets (a fixed stride) into
 // a private row of bins in device memory; rows are added per bin by a fixed-shape reduction, so the
 // result does not depend on timing.
+#include <cmath>
 #include <cstring>
 #include <new>
 
@@ -121,6 +122,10 @@ struct CorrArgs {
     uint64_t seed;
     int nrows;
     double *rows;  // nrows x 2 nbins: bin sums, then weight sums
+    // the FP32 screen: per element hi parts of the position and, for nodes, the opening radius
+    // max(s / theta + delta, 0.6 s + delta) rounded to FP32 (-1 for particles); lo parts and the size
+    const float4 *ehi, *elo;
+    float rmin32, rmax32, lmin32, dl32, box32;
 };
 
 // Bin of distance r: int(nbins (log10 r - log10 rbins[0]) / dlogr) as pytreegrav writes it, clamped to
@@ -168,91 +173,237 @@ __device__ void spread_bins(const CorrArgs &a, double *row, double r, int r_idx,
     }
 }
 
-// DensityCorrWalk / VelocityCorrWalk / VelocityStructWalk (treewalk.py:380-818) of target i, added
-// into row (bin sums at row[0..nbins), weight sums at row[nbins..2 nbins), kinds 1 and 2 only: for the
-// density they equal the bin sums). Each contribution is
-// formed in pytreegrav's order of operations and multiplied by the target's weight w (kinds 1 and 2;
-// pytreegrav multiplies the target's per-bin sums instead, which differs in rounding only). Every
-// operation is rounded separately (no contraction), as in the oracle.
+// Per-target state of a walk: the target, its velocity and weight, the rows it adds into, the FP64
+// bin constants, and the count of jitter draws so far.
+struct CorrTarget {
+    int64_t i;
+    double px, py, pz, w;
+    double tv[3];
+    double logr_min, dlogr;
+    double *bins, *wts;
+    int64_t draws;
+};
+
+// A particle's contribution (in bin r_idx): its mass, v . V M, or |v - V|^2 M summed over the
+// components, times the target's weight (w = 1 for the density).
+__device__ __forceinline__ void add_particle(const CorrArgs &a, CorrTarget &t, int64_t no, int r_idx) {
+    const double M = a.mass[no];
+    double amount = M;
+    if (a.kind == TG_CORR_VELOCITY) {
+        amount = 0.0;
+        for (int k = 0; k < 3; k++) amount = dadd(amount, dmul(dmul(t.tv[k], a.vel[3 * no + k]), M));
+    } else if (a.kind == TG_CORR_STRUCTURE) {
+        amount = 0.0;
+        for (int k = 0; k < 3; k++) {
+            const double u = dsub(t.tv[k], a.vel[3 * no + k]);
+            amount = dadd(amount, dmul(dmul(u, u), M));
+        }
+    }
+    bin_add(t.bins, r_idx, dmul(t.w, amount));
+    if (a.kind) bin_add(t.wts, r_idx, dmul(t.w, M));
+}
+
+// A node's quantity per unit mass: 1, v . V, or |v - V|^2 plus its dispersion.
+__device__ __forceinline__ double node_q(const CorrArgs &a, const CorrTarget &t, int64_t no) {
+    double q = 1.0;
+    if (a.kind == TG_CORR_VELOCITY) {
+        q = 0.0;
+        for (int k = 0; k < 3; k++) q = dadd(q, dmul(t.tv[k], a.vel[3 * no + k]));
+    } else if (a.kind == TG_CORR_STRUCTURE) {
+        q = 0.0;
+        for (int k = 0; k < 3; k++) {
+            const double u = dsub(t.tv[k], a.vel[3 * no + k]);
+            q = dadd(q, dmul(u, u));
+        }
+        q = dadd(q, a.disp[no]);
+    }
+    return q;
+}
+
+// A binned node's contribution at jittered bin j.
+__device__ __forceinline__ void add_node_at(const CorrArgs &a, CorrTarget &t, int64_t no, int j) {
+    const double M = a.mass[no];
+    bin_add(t.bins, j, dmul(t.w, a.kind ? dmul(node_q(a, t, no), M) : M));
+    if (a.kind) bin_add(t.wts, j, dmul(t.w, M));
+}
+
+// The FP64 distance from the target to element no (nearest periodic image when box > 0).
+__device__ __forceinline__ double dist64(const CorrArgs &a, const CorrTarget &t, int64_t no) {
+    double dx = dsub(a.coord[3 * no], t.px), dy = dsub(a.coord[3 * no + 1], t.py), dz = dsub(a.coord[3 * no + 2], t.pz);
+    if (a.box > 0.0) {
+        dx = nearest_image(dx, a.box);
+        dy = nearest_image(dy, a.box);
+        dz = nearest_image(dz, a.box);
+    }
+    return sqrt(dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)));
+}
+
+// One element of DensityCorrWalk / VelocityCorrWalk / VelocityStructWalk (treewalk.py:380-818) in FP64,
+// pytreegrav's expressions with every operation rounded once: the contributions it makes, and the
+// element the walk goes to next.
+__device__ int64_t elem_exact(const CorrArgs &a, CorrTarget &t, int64_t no) {
+    const int nb = a.nbins;
+    const double r = dist64(a, t, no);
+    const bool part = no < a.ntot;
+    const double s = part ? 0.0 : a.size[no], del = part ? 0.0 : a.delta[no];
+    const bool far = !part && r > fmax(dadd(ddiv(s, a.theta), del), dadd(dmul(s, 0.6), del));
+    if (r > a.rbins[0] && r < a.rbins[nb]) {
+        const int r_idx = bin_of(r, t.logr_min, t.dlogr, nb);
+        if (part) {
+            add_particle(a, t, no, r_idx);
+            return a.next[no];
+        }
+        if (far && s < dmul(a.mbr, dsub(a.rbins[r_idx + 1], a.rbins[r_idx]))) {
+            const double M = a.mass[no];
+            if (a.weighted) {
+                const double q = node_q(a, t, no);
+                spread_bins(a, t.bins, r, r_idx, dmul(0.5, s), M, q, t.w);
+                if (a.kind) spread_bins(a, t.wts, r, r_idx, dmul(0.5, s), M, 1.0, t.w);
+            } else {
+                const double rnew = dadd(r, dmul(dsub(corr_uniform(a.seed, t.i, t.draws++), 0.5), s));
+                add_node_at(a, t, no, rnew > 0.0 ? bin_of(rnew, t.logr_min, t.dlogr, nb) : 0);
+            }
+            return a.next[no];
+        }
+        return a.first[no];
+    }
+    return (part || far) ? a.next[no] : a.first[no];
+}
+
+// x against threshold c known to within e: +1 above, -1 below, 0 undecided.
+__device__ __forceinline__ int side(float x, float c, float e) { return x > c + e ? 1 : (x < c - e ? -1 : 0); }
+
+// The bin of distance r (FP32, relative error below er / r) when the FP32 value of pytreegrav's bin
+// formula is farther than its error bound from a bin edge (the clamps included); -1 otherwise.
+__device__ __forceinline__ int bin_screen(const CorrArgs &a, float r, float er) {
+    const float lr = log10f(r);
+    const float tscale = (float)a.nbins / a.dl32;
+    const float t = __fdiv_rn(__fmul_rn((float)a.nbins, __fsub_rn(lr, a.lmin32)), a.dl32);
+    // log10f (a few ulp), the FP32 constants and r's own error, with a factor of 4 to spare
+    const float dt = tscale * (4e-6f * (1.f + fabsf(lr) + fabsf(a.lmin32)) + 2.f * er / r);
+    if (!(r > 0.f) || !(dt < 0.25f)) return -1;
+    if (t < -dt) return 0;
+    if (t - dt >= (float)a.nbins) return a.nbins - 1;
+    const float fl = floorf(t);
+    if (t - fl > dt && fl + 1.f - t > dt && fl >= 0.f && fl < (float)a.nbins) return (int)fl;
+    return -1;
+}
+
+// The walk of target i (treewalk.py:380-818). Every decision -- inside the radial range, the opening
+// test, the bin, a jittered node's bin -- is first taken in FP32 from hi/lo positions when the FP32
+// value lies farther from its threshold than a bound on its error; otherwise (and for weighted
+// binning) the element is evaluated by elem_exact. So the decisions are pytreegrav's FP64 ones, and
+// GB300 (FP64 at 1/73 of the FP32 rate) spends FP64 only on the sums. Contributions add into row
+// (bin sums at row[0..nbins), weight sums at row[nbins..2 nbins), kinds 1 and 2 only), each formed in
+// pytreegrav's order of operations and multiplied by the target's weight (pytreegrav multiplies the
+// target's per-bin sums instead, which differs in rounding only).
 __device__ void corr_walk(const CorrArgs &a, int64_t i, double *row) {
     const int64_t N = a.ntot;
     const int nb = a.nbins;
-    const double rmin = a.rbins[0], rmax = a.rbins[nb];
-    const double logr_min = log10(rmin), dlogr = dsub(log10(rmax), logr_min);
-    const double px = a.pos[3 * i], py = a.pos[3 * i + 1], pz = a.pos[3 * i + 2];
-    double tv[3] = {0.0, 0.0, 0.0};
+    CorrTarget t;
+    t.i = i;
+    t.px = a.pos[3 * i];
+    t.py = a.pos[3 * i + 1];
+    t.pz = a.pos[3 * i + 2];
+    t.tv[0] = t.tv[1] = t.tv[2] = 0.0;
     if (a.kind) {
-        tv[0] = a.tvel[3 * i];
-        tv[1] = a.tvel[3 * i + 1];
-        tv[2] = a.tvel[3 * i + 2];
+        t.tv[0] = a.tvel[3 * i];
+        t.tv[1] = a.tvel[3 * i + 1];
+        t.tv[2] = a.tvel[3 * i + 2];
     }
-    const double w = a.kind ? a.weight[i] : 1.0;
-    double *bins = row, *wts = row + nb;
-    int64_t draws = 0;
+    t.w = a.kind ? a.weight[i] : 1.0;
+    t.logr_min = log10(a.rbins[0]);
+    t.dlogr = dsub(log10(a.rbins[nb]), t.logr_min);
+    t.bins = row;
+    t.wts = row + nb;
+    t.draws = 0;
+    float phx, plx, phy, ply, phz, plz;
+    d2f_split(t.px, phx, plx);
+    d2f_split(t.py, phy, ply);
+    d2f_split(t.pz, phz, plz);
+    const float box = a.box32, half = 0.5f * a.box32;
+    // the hi/lo splits keep positions to ~2^-48 of their size: an absolute error term for very close pairs
+    const float eabs = 1e-12f * (fabsf(phx) + fabsf(phy) + fabsf(phz)) + 1e-30f;
     int64_t no = N;
     for (int64_t guard = 0; no > -1; guard++) {
         if (guard > a.nelem || no >= a.nelem) {  // one visit per element always suffices
             atomicOr(a.runaway, 1);
             return;
         }
-        double dx = dsub(a.coord[3 * no], px), dy = dsub(a.coord[3 * no + 1], py), dz = dsub(a.coord[3 * no + 2], pz);
+        const float4 h = a.ehi[no], l = a.elo[no];
+        float d[3] = {__fadd_rn(__fsub_rn(h.x, phx), __fsub_rn(l.x, plx)),
+                      __fadd_rn(__fsub_rn(h.y, phy), __fsub_rn(l.y, ply)),
+                      __fadd_rn(__fsub_rn(h.z, phz), __fsub_rn(l.z, plz))};
+        bool sure = true;
         if (a.box > 0.0) {
-            dx = nearest_image(dx, a.box);
-            dy = nearest_image(dy, a.box);
-            dz = nearest_image(dz, a.box);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const float ad = fabsf(d[k]);
+                const int sd = side(ad, half, 1e-6f * box);
+                if (sd == 0) sure = false;
+                else if (sd > 0) d[k] = -copysignf(__fsub_rn(box, ad), d[k]);
+            }
         }
-        const double r = sqrt(dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)));
+        const float r = sqrtf(__fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2])));
+        // hi/lo offsets (~1e-7 relative), the nearest image, the squares and the root
+        const float er = 2e-6f * (r + box) + 1e-12f * (fabsf(h.x) + fabsf(h.y) + fabsf(h.z)) + eabs;
         const bool part = no < N;
-        const double s = part ? 0.0 : a.size[no], del = part ? 0.0 : a.delta[no];
-        const bool far = !part && r > fmax(dadd(ddiv(s, a.theta), del), dadd(dmul(s, 0.6), del));
-        if (r > rmin && r < rmax) {
-            const int r_idx = bin_of(r, logr_min, dlogr, nb);
-            const double M = a.mass[no];
+        const int inlo = side(r, a.rmin32, er + 2e-7f * a.rmin32), inhi = side(r, a.rmax32, er + 2e-7f * a.rmax32);
+        const int fs = part ? -1 : side(r, h.w, er + 2e-7f * h.w);  // far: r > opening radius
+        if (!sure || inlo == 0 || inhi == 0 || fs == 0 || a.weighted) {
+            no = elem_exact(a, t, no);
+            continue;
+        }
+        if (inlo > 0 && inhi < 0) {  // inside (rbins[0], rbins[-1])
+            const int r_idx = bin_screen(a, r, er);
+            if (r_idx < 0) {
+                no = elem_exact(a, t, no);
+                continue;
+            }
             if (part) {
-                double amount = M;  // mass, v . V M, or |v - V|^2 M summed over components
-                if (a.kind == TG_CORR_VELOCITY) {
-                    amount = 0.0;
-                    for (int k = 0; k < 3; k++) amount = dadd(amount, dmul(dmul(tv[k], a.vel[3 * no + k]), M));
-                } else if (a.kind == TG_CORR_STRUCTURE) {
-                    amount = 0.0;
-                    for (int k = 0; k < 3; k++) {
-                        const double u = dsub(tv[k], a.vel[3 * no + k]);
-                        amount = dadd(amount, dmul(dmul(u, u), M));
-                    }
-                }
-                bin_add(bins, r_idx, dmul(w, amount));
-                if (a.kind) bin_add(wts, r_idx, dmul(w, M));
+                add_particle(a, t, no, r_idx);
                 no = a.next[no];
-            } else if (far && s < dmul(a.mbr, dsub(a.rbins[r_idx + 1], a.rbins[r_idx]))) {
-                double q = 1.0;  // per unit mass
-                if (a.kind == TG_CORR_VELOCITY) {
-                    q = 0.0;
-                    for (int k = 0; k < 3; k++) q = dadd(q, dmul(tv[k], a.vel[3 * no + k]));
-                } else if (a.kind == TG_CORR_STRUCTURE) {
-                    q = 0.0;
-                    for (int k = 0; k < 3; k++) {
-                        const double u = dsub(tv[k], a.vel[3 * no + k]);
-                        q = dadd(q, dmul(u, u));
-                    }
-                    q = dadd(q, a.disp[no]);
-                }
-                if (a.weighted) {
-                    spread_bins(a, bins, r, r_idx, dmul(0.5, s), M, q, w);
-                    if (a.kind) spread_bins(a, wts, r, r_idx, dmul(0.5, s), M, 1.0, w);
-                } else {
-                    const double rnew = dadd(r, dmul(dsub(corr_uniform(a.seed, i, draws++), 0.5), s));
-                    const int j = rnew > 0.0 ? bin_of(rnew, logr_min, dlogr, nb) : 0;
-                    bin_add(bins, j, dmul(w, a.kind ? dmul(q, M) : M));
-                    if (a.kind) bin_add(wts, j, dmul(w, M));
+            } else if (fs > 0 && a.size[no] < dmul(a.mbr, dsub(a.rbins[r_idx + 1], a.rbins[r_idx]))) {
+                // jittered distance r + (u - 0.5) s: its bin in FP32 when clear of the edges
+                const double u = corr_uniform(a.seed, i, t.draws);
+                const float rn = __fadd_rn(r, __fmul_rn((float)(u - 0.5), l.w));
+                const int j = rn > 4.f * er ? bin_screen(a, rn, er + 1e-6f * l.w) : -1;
+                if (j >= 0) {
+                    t.draws++;
+                    add_node_at(a, t, no, j);
+                } else {  // the FP64 distance, then pytreegrav's expression
+                    const double r64 = dist64(a, t, no);
+                    const double rnew = dadd(r64, dmul(dsub(corr_uniform(a.seed, i, t.draws++), 0.5), a.size[no]));
+                    add_node_at(a, t, no, rnew > 0.0 ? bin_of(rnew, t.logr_min, t.dlogr, nb) : 0);
                 }
                 no = a.next[no];
             } else {
                 no = a.first[no];
             }
         } else {
-            no = (part || far) ? a.next[no] : a.first[no];
+            no = (part || fs > 0) ? a.next[no] : a.first[no];
         }
     }
+}
+
+// FP32 element records of the screen: hi/lo position, the node's opening radius (pytreegrav's
+// max(s / theta + delta, 0.6 s + delta), formed in FP64 and rounded) or -1, the size.
+__global__ void k_corr_prep(int64_t ntot, int64_t nelem, const double *coord, const double *size, const double *delta,
+                            double theta, float4 *ehi, float4 *elo) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nelem) return;
+    float hx, lx, hy, ly, hz, lz;
+    d2f_split(coord[3 * e], hx, lx);
+    d2f_split(coord[3 * e + 1], hy, ly);
+    d2f_split(coord[3 * e + 2], hz, lz);
+    float crit = -1.f, s32 = 0.f;
+    if (e >= ntot) {
+        const double s = size[e], del = delta[e];
+        crit = d2f(fmax(dadd(ddiv(s, theta), del), dadd(dmul(s, 0.6), del)));
+        s32 = d2f(s);
+    }
+    ehi[e] = make_float4(hx, hy, hz, crit);
+    elo[e] = make_float4(lx, ly, lz, s32);
 }
 
 __global__ void __launch_bounds__(CORR_THREADS) k_corr(CorrArgs a) {
@@ -419,6 +570,29 @@ tg_status tg_tree_correlation(tg_tree t, int kind, const double *pos, const doub
     TG_CUDA(rows.alloc(nrows * 2 * nbins));
     a.rows = rows.p;
     TG_CUDA(dout.alloc(2 * nbins));
+    DevArray<float4> ehi(st), elo(st);
+    TG_CUDA(ehi.alloc(a.nelem));
+    TG_CUDA(elo.alloc(a.nelem));
+    { k_corr_prep<<<div_up(a.nelem, 256), 256, 0, st>>>(t->ntot, a.nelem, t->coord, t->size, t->delta, theta, ehi.p,
+                                                          elo.p); note_launch(); }
+    a.ehi = ehi.p;
+    a.elo = elo.p;
+    {  // FP32 copies of the radial range for the screen (its error bounds cover their rounding)
+        double rb0 = 0.0, rbn = 0.0;
+        if (host) {
+            rb0 = rbins[0];
+            rbn = rbins[nbins];
+        } else {
+            TG_CUDA(cudaMemcpyAsync(&rb0, rbins, sizeof(double), cudaMemcpyDeviceToHost, st));
+            TG_CUDA(cudaMemcpyAsync(&rbn, rbins + nbins, sizeof(double), cudaMemcpyDeviceToHost, st));
+            TG_CUDA(cudaStreamSynchronize(st));
+        }
+        a.rmin32 = (float)rb0;
+        a.rmax32 = (float)rbn;
+        a.lmin32 = (float)std::log10(rb0);
+        a.dl32 = (float)(std::log10(rbn) - std::log10(rb0));
+        a.box32 = (float)boxsize;
+    }
     { k_corr<<<div_up(nrows, CORR_THREADS), CORR_THREADS, 0, st>>>(a); note_launch(); }
     { k_corr_reduce<<<2 * nbins, CORR_RED, 0, st>>>(rows.p, a.nrows, nbins, dout.p); note_launch(); }
     TG_CUDA(cudaGetLastError());

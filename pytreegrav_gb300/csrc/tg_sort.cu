@@ -194,18 +194,34 @@ __device__ __forceinline__ void rank_loaded_slice(const uint64_t *kv, int64_t n,
                                                   int *wcount, int *digit, int *rank) {
     const int lane = lane_id();
     const unsigned lt = lanemask_lt();
+    // every round's lanes with the same digit first, from nine ballots (the eight digit bits and
+    // "in range"); independent of the counters, so the rounds overlap
+    unsigned peers[ROUNDS];
 #pragma unroll
     for (int r = 0; r < ROUNDS; r++) {
-        int64_t i = wbase + r * 32 + lane;
-        int d = RS_BINS;  // sentinel for keys past the end
-        if (i < n) d = (int)((kv[r] >> shift) & (RS_BINS - 1));
-        unsigned peers = __match_any_sync(FULL, d);
-        int base = (d < RS_BINS) ? wcount[d] : 0;
-        __syncwarp();
-        if (d < RS_BINS && (31 - __clz(peers)) == lane) wcount[d] = base + __popc(peers);
-        __syncwarp();
+        const int64_t i = wbase + r * 32 + lane;
+        const bool in = i < n;
+        const int d = in ? (int)((kv[r] >> shift) & (RS_BINS - 1)) : RS_BINS;  // RS_BINS: past the end
+        unsigned m = __ballot_sync(FULL, in);
+        m = in ? m : ~m;
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+            const bool bit = (d >> b) & 1;
+            const unsigned v = __ballot_sync(FULL, bit);
+            m &= bit ? v : ~v;
+        }
+        peers[r] = m;
         digit[r] = d;
-        rank[r] = base + __popc(peers & lt);
+    }
+    // then the per-warp digit counters, round by round
+#pragma unroll
+    for (int r = 0; r < ROUNDS; r++) {
+        const int d = digit[r];
+        const int base = (d < RS_BINS) ? wcount[d] : 0;
+        __syncwarp();
+        if (d < RS_BINS && (31 - __clz(peers[r])) == lane) wcount[d] = base + __popc(peers[r]);
+        __syncwarp();
+        rank[r] = base + __popc(peers[r] & lt);
     }
 }
 
@@ -321,6 +337,9 @@ __global__ void __launch_bounds__(RS_THREADS, 4) k_onesweep(const uint64_t *keys
     const unsigned long long tag = (unsigned long long)(pass + 1) << 56;
     __shared__ int wcount[RS_WARPS][RS_BINS];
     __shared__ int prefix[RS_BINS];
+    __shared__ int lstart[RS_BINS];  // the digit's first position within the tile
+    __shared__ uint64_t skey[OS_TILE];
+    __shared__ uint32_t sval[OS_TILE];
     __shared__ int tile_s;
     if (threadIdx.x == 0) tile_s = atomicAdd(tile_counter, 1);
     for (int i = threadIdx.x; i < RS_WARPS * RS_BINS; i += RS_THREADS) (&wcount[0][0])[i] = 0;
@@ -386,17 +405,31 @@ __global__ void __launch_bounds__(RS_THREADS, 4) k_onesweep(const uint64_t *keys
             *st = ST_INC | tag | (unsigned long long)(acc + run);
         }
         prefix[d] = digit_off[d] + (int)acc;
+        __shared__ int tot_s;
+        lstart[d] = block_exclusive_scan(run, &tot_s);
     }
     __syncthreads();
+    // the tile in digit order in shared memory, then written out: keys of one digit go to consecutive
+    // places, so consecutive threads write consecutive words instead of one scattered sector each
     const int lane = lane_id();
 #pragma unroll
     for (int r = 0; r < OS_ROUNDS; r++) {
-        int64_t i = wbase + r * 32 + lane;
+        const int64_t i = wbase + r * 32 + lane;
         if (i < n) {
-            int pos = prefix[digit[r]] + wcount[w][digit[r]] + rank[r];
-            keys_out[pos] = kv[r];
-            vals_out[pos] = vv[r];
+            const int loc = lstart[digit[r]] + wcount[w][digit[r]] + rank[r];
+            skey[loc] = kv[r];
+            sval[loc] = vv[r];
         }
+    }
+    __syncthreads();
+    const int64_t rest = n - (int64_t)t * OS_TILE;
+    const int cnt = rest < OS_TILE ? (int)rest : OS_TILE;
+    for (int i = threadIdx.x; i < cnt; i += RS_THREADS) {
+        const uint64_t k = skey[i];
+        const int d = (int)((k >> shift) & (RS_BINS - 1));
+        const int pos = prefix[d] + (i - lstart[d]);
+        keys_out[pos] = k;
+        vals_out[pos] = sval[i];
     }
 }
 

@@ -10,6 +10,9 @@
   same relative bar (1e-12 of the bin's absolute scale from the oracle).
 * A larger case (2e5 Plummer particles, theta 1 and 0.5) through the same comparison, and edge
   cases: no targets, a single bin, a tree without velocities asked for a velocity function.
+* The walk decides in FP32 when a decision is clear of its threshold and falls back to pytreegrav's
+  FP64 expression otherwise: a periodic lattice whose offsets are exactly half the box exercises the
+  fallback, against the oracle at the same bar.
 """
 
 import os
@@ -178,3 +181,28 @@ def test_edge_cases(tg):
         tg.VelocityCorrFunc(x[:10], m[:10], v[:10], rb, tree=plain)
     with pytest.raises(ValueError):
         t.correlation("density", None, np.array([1.0]))
+
+
+@pytest.mark.parametrize("kind", ["density", "velocity", "structure"])
+def test_screen_fallbacks_periodic_lattice(tg, kind):
+    """A lattice of spacing box/8 in a periodic box: many offsets are exactly half the box (the FP32
+    screen cannot decide the nearest image there and the FP64 expression does) and many distances are
+    equal. GPU sums against the oracle's at the same bar, jittered and weighted."""
+    g = np.arange(8) * 0.25
+    x = np.ascontiguousarray(np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3))
+    n = len(x)
+    rng = np.random.default_rng(9)
+    m = rng.random(n) / n
+    v = rng.normal(size=(n, 3))
+    t = tg.ConstructTree(x, m, None, vel=v)
+    ot = O.OracleTree(x, m, np.zeros(n))
+    otv = O.tree_velocities(ot, v)
+    idx = ot.TreewalkIndices
+    rb = 10 ** np.linspace(-0.93, 0.07, 7)  # edges away from the lattice's distances
+    for wb in (False, True):
+        kw = dict(theta=0.9, boxsize=2.0, weighted_binning=wb, seed=77)
+        gpu = t.correlation(kind, None, rb, **kw)
+        extra = {} if kind == "density" else dict(vel=v[idx], weight=m[idx], tree_vel=otv)
+        ora = O.correlation(ot, kind, x[idx], rb, **extra, **kw)
+        a, _ = O.correlation(ot, kind, x[idx], rb, absval=True, **extra, **kw)
+        compare(gpu, ora, a, kind)
