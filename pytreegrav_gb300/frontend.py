@@ -401,9 +401,17 @@ def ColumnDensity(pos, m, radii, rays=None, randomize_rays=False, healpix=False,
 
 def _default_rbins(pos):
     """frontend.py:1091-1093: log-spaced edges from the 11th-nearest to the farthest distance from the
-    median position, N^(1/3) of them."""
-    r = np.sort(np.sqrt(np.sum((pos - np.median(pos, axis=0)) ** 2, axis=1)))
-    return 10 ** np.linspace(np.log10(r[10]), np.log10(r[-1]), int(len(r) ** (1.0 / 3)))
+    median position, N^(1/3) of them. The two order statistics come from a partition and a maximum
+    (the same values as pytreegrav's full sort, in linear time)."""
+    # per contiguous column: numpy's median and the same sum of squares as np.sum(d ** 2, axis=1)
+    cols = [np.ascontiguousarray(pos[:, k]) for k in range(pos.shape[1])]
+    d = [c - np.median(c) for c in cols]
+    r = np.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) if len(d) == 3 else \
+        np.sqrt(np.sum((pos - np.median(pos, axis=0)) ** 2, axis=1))
+    if len(r) <= 10:
+        r = np.sort(r)  # too few points: pytreegrav's own failure (an IndexError) below
+        return 10 ** np.linspace(np.log10(r[10]), np.log10(r[-1]), int(len(r) ** (1.0 / 3)))
+    return 10 ** np.linspace(np.log10(np.partition(r, 10)[10]), np.log10(r.max()), int(len(r) ** (1.0 / 3)))
 
 
 def _corr(kind, pos, m, v, rbins, max_bin_size_ratio, theta, tree, boxsize, weighted_binning, seed):
