@@ -221,9 +221,10 @@ LoopLimits &loop_limits();
 int num_sms();
 
 // Stream-ordered device allocation from the library's own memory pool on the current device.
-// The pool keeps up to TG_POOL_KEEP_BYTES of freed memory mapped for later calls (a build and a
-// walk allocate and free their temporaries on every call; with the driver's default threshold of
-// zero, that memory would be unmapped at each synchronisation and mapped again by the next call).
+// The pool keeps freed memory mapped for later calls, up to a quarter of the device's memory and at
+// least TG_POOL_KEEP_BYTES: a build and a walk allocate and free their temporaries on every call, and
+// memory above the threshold is unmapped at each synchronisation and mapped again by the next call
+// (at 3.2e7 particles a build's temporaries exceed 4 GiB, and that cost ~10 ms per build).
 // Free with cudaFreeAsync.
 #ifndef TG_POOL_KEEP_BYTES
 #define TG_POOL_KEEP_BYTES (4ull << 30)

@@ -52,7 +52,9 @@ cudaError_t dev_malloc(void **p, size_t bytes, cudaStream_t s) {
                 pools[dev] = nullptr;
                 return e;
             }
+            size_t free_b = 0, total_b = 0;
             unsigned long long keep = TG_POOL_KEEP_BYTES;
+            if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && total_b / 4 > keep) keep = total_b / 4;
             e = cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
             if (e != cudaSuccess) return e;
         }
