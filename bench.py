@@ -404,6 +404,39 @@ def run_ours(args):
     ref_cfg["config"] = ("build + Accel walk with pytreegrav's grouping (group_size=8 consecutive Morton-ordered "
                          "targets), plain theta=0.7, quadrupole; the reference arm's configuration")
 
+    # the build alone (device arrays, L2 flushed before each), against the HBM copy rate on its
+    # algorithmic bytes: 638 B per particle and 969 B per node, summed over the build's kernels
+    # (profiles/build_plummer1e6.md)
+    vp = ctypes.c_void_p
+    bev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(10)]
+    nodes = 0
+    for k in range(13):
+        flush.zero_()
+        th_ = vp()
+        if k >= 3:
+            bev[k - 3][0].record()
+        _lib.check(L.tg_tree_build(vp(dpos.data_ptr()), vp(dm.data_ptr()), vp(dh.data_ptr()), n, 1, 1,
+                                   _lib.TG_MEM_DEVICE, vp(stream), ctypes.byref(th_)), "build")
+        if k >= 3:
+            bev[k - 3][1].record()
+        info = _lib.TreeInfo()
+        L.tg_tree_info_get(th_, ctypes.byref(info))
+        nodes = int(info.node_hi) - n
+        L.tg_tree_free(th_)
+    torch.cuda.synchronize()
+    build_ms = statistics.mean(a_.elapsed_time(b_) for a_, b_ in bev)
+    alg_bytes = 638 * n + 969 * nodes
+    hbm = None
+    try:
+        hbm = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs")
+    except Exception:
+        pass
+    build = {"ms": round(build_ms, 4), "nodes": nodes, "algorithmic_bytes": alg_bytes,
+             "achieved_gbs": round(alg_bytes / (build_ms * 1e-3) / 1e9, 1),
+             "hbm_peak_gbs": hbm, "frac_of_hbm": round(alg_bytes / (build_ms * 1e-3) / 1e9 / hbm, 4) if hbm else None,
+             "bound": "latency at this size (dependent launches) and FP64 issue in the moment pass; per-kernel "
+                      "traffic in profiles/build_plummer1e6.md"}
+
     base = cpu_baseline(x, m, h, os.cpu_count() or 1)
     return {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -422,7 +455,7 @@ def run_ours(args):
         "accuracy": acc_learned, "learned": learned, "plain": plain,
         "walk": {"interactions_per_target": st["interactions"] / n, "node_tests": st["node_tests"],
                  "groups": st["groups"], "quad_interactions": st["quad_interactions"]},
-        "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+        "roofline": roofline, "build": build, "cpu_baseline": base, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
         "reference_config_on_gpu": ref_cfg,
     }
 
