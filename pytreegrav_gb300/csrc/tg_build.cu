@@ -924,6 +924,17 @@ __device__ __forceinline__ void store_quad32(float4 *q32, int64_t j, const float
     q32[2 * j + 1] = make_float4(Q[4], Q[5], 0.f, 0.f);
 }
 
+// Tests of FP64 values on the integer units (GB300 issues one FP64 warp instruction every ~76 cycles
+// per SM sub-partition, comparisons included). nonzero64(x) is x != 0.0 for any x. fkey maps a
+// non-NaN double to a signed integer of the same order, -0.0 and +0.0 to the same key, so
+// fkey(b) > fkey(a) decides b > a exactly as the FP64 comparison does (pytreegrav's max keeps a on a
+// tie); the inputs are checked finite before a build.
+__device__ __forceinline__ bool nonzero64(double x) { return (__double_as_longlong(x) << 1) != 0; }
+__device__ __forceinline__ long long fkey(double x) {
+    const long long b = __double_as_longlong(x);
+    return b < 0 ? -(b & 0x7fffffffffffffffll) : b;
+}
+
 // CG: read the children through L2 (ld.cg), for kernels in which another SM may have finished them.
 template <bool CG>
 __device__ __forceinline__ double ldm(const double *p) {
@@ -940,10 +951,11 @@ __device__ __forceinline__ float4 ldm4(const float4 *p) {
 // this node in FP64, plus the FP32 quadrupole. kids: the child list of k_kids (summation order as in
 // the reference: particle children in chain (Morton) order, then node children in reverse chain order,
 // zero-mass nodes skipped). Every child takes the same instructions: a particle adds (m, m x,
-// softening) and a node (m, its mass-weighted coordinate sum times 1.0, which is exact, softening); a
-// zero-mass node adds -0.0, the exact identity of a sum, and leaves the softening maximum alone, which
-// is the reference's skipping it. A warp's lanes thus part only on the quadrupole's node-child term,
-// and a warp of nodes with equal child counts (see k_moments_sorted) runs with every lane busy.
+// softening) and a node (m, its mass-weighted coordinate sum, which 1.0 times the sum gives exactly,
+// softening); a zero-mass node adds -0.0, the exact identity of a sum, and leaves the softening
+// maximum alone, which is the reference's skipping it. A warp's lanes thus part only on the
+// quadrupole's node-child term, and a warp of nodes with equal child counts (see k_moments_sorted)
+// runs with every lane busy. The zero tests and the softening maximum run on the integer units.
 template <bool CG>
 __device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j, const int32_t *kids, int n) {
     const int4 k0 = *reinterpret_cast<const int4 *>(kids + 8 * j);
@@ -951,6 +963,7 @@ __device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j
     const int32_t ch[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
     const int64_t N = a.ntot;
     double m = 0.0, ax = 0.0, ay = 0.0, az = 0.0, h = 0.0;
+    long long hk = 0;  // fkey(h)
 #pragma unroll
     for (int q = 0; q < 8; q++) {
         if (q < n) {
@@ -959,14 +972,19 @@ __device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j
             const int64_t g = part ? (int64_t)c : N + (int64_t)(~c);
             const double mc = ldm<CG>(a.mass + g);
             const double *src = part ? a.coord + 3 * g : a.acc + 3 * (int64_t)(~c);
-            const double w = part ? mc : 1.0;
-            const bool use = part || mc != 0.0;
+            const bool use = part || nonzero64(mc);
             const double hc = ldm<CG>(a.soft + g);
+            const double s0 = ldm<CG>(src), s1 = ldm<CG>(src + 1), s2 = ldm<CG>(src + 2);
             m = dadd(m, use ? mc : -0.0);
-            ax = dadd(ax, use ? dmul(w, ldm<CG>(src)) : -0.0);
-            ay = dadd(ay, use ? dmul(w, ldm<CG>(src + 1)) : -0.0);
-            az = dadd(az, use ? dmul(w, ldm<CG>(src + 2)) : -0.0);
-            h = use ? pymax(h, hc) : h;
+            // a particle adds m x; a node child its coordinate sums (1.0 times them, exactly)
+            ax = dadd(ax, use ? (part ? dmul(mc, s0) : s0) : -0.0);
+            ay = dadd(ay, use ? (part ? dmul(mc, s1) : s1) : -0.0);
+            az = dadd(az, use ? (part ? dmul(mc, s2) : s2) : -0.0);
+            const long long ck = fkey(hc);
+            if (use && ck > hk) {  // pymax(h, hc)
+                h = hc;
+                hk = ck;
+            }
         }
     }
     const int64_t f = N + j;
@@ -976,7 +994,7 @@ __device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j
     a.acc[3 * j + 1] = ay;
     a.acc[3 * j + 2] = az;
     double com[3] = {ldm<CG>(a.coord + 3 * f), ldm<CG>(a.coord + 3 * f + 1), ldm<CG>(a.coord + 3 * f + 2)};
-    if (m != 0.0) {
+    if (nonzero64(m)) {
         double inv = __drcp_rn(m);  // 1 / m correctly rounded: the same value as 1.0 / m
         double accs[3] = {ax, ay, az};
         double d2 = 0.0;
@@ -1002,7 +1020,7 @@ __device__ __forceinline__ void node_moments_kids(const MomentArgs &a, int64_t j
                 const bool part = c >= 0;
                 const int64_t g = part ? (int64_t)c : N + (int64_t)(~c);
                 const double mc = ldm<CG>(a.mass + g);
-                if (part || mc != 0.0) {
+                if (part || nonzero64(mc)) {
                     float T[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
                     if (!part) load_quad32(T, ldm4<CG>(a.quad32 + 2 * (int64_t)(~c)), ldm4<CG>(a.quad32 + 2 * (int64_t)(~c) + 1));
                     quad32_term(T, d2f(mc), off32(ldm<CG>(a.coord + 3 * g), ch_[0], cl_[0]),
@@ -1067,46 +1085,73 @@ __global__ void __launch_bounds__(WIDE_THREADS) k_moments_wide(MomentArgs a, con
     __shared__ double s_m[8][WIDE_NODES], s_t[3][8][WIDE_NODES], s_h[8][WIDE_NODES];  // child terms
     __shared__ double s_sum[5][WIDE_NODES], s_com[3][WIDE_NODES];
     __shared__ float s_q[6][8][WIDE_NODES];  // the children's FP32 quadrupole terms
-    __shared__ int32_t s_c[8][WIDE_NODES];
     __shared__ int8_t s_use[8][WIDE_NODES];  // child enters the sums (a particle, or a node of nonzero mass)
-    __shared__ int s_n[WIDE_NODES];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int idx = blockIdx.x * WIDE_NODES + lane;
     const int64_t N = a.ntot;
+    // Global reads in three dependent rounds: the node; its child count, child w and (warp 0) its
+    // cell centre; then everything of child w the later stages need (its mass, softening,
+    // coordinates, and for a node child its coordinate sums and FP32 quadrupole), kept in registers,
+    // since warp w handles child w in every stage.
     const int64_t j = idx < count ? (int64_t)list[idx] : -1;
-    // stage 0: child lists
-    {
-        const int n = j >= 0 ? (int)nk[j] : 0;
-        s_c[w][lane] = w < n ? kids[8 * j + w] : 0;
-        if (w == 0) s_n[lane] = n;
+    int n = 0;
+    int32_t c = 0;
+    double com[3] = {0.0, 0.0, 0.0};
+    if (j >= 0) {
+        n = (int)nk[j];
+        c = kids[8 * j + w];  // slots past n are not used
+        if (w == 0) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) com[k] = a.coord[3 * (N + j) + k];
+        }
     }
-    __syncthreads();
-    const int n = s_n[lane];
-    // stage 1: warp q, child q of every node: the mass-pass terms (use ? term : -0.0)
-    if (w < n) {
-        const int32_t c = s_c[w][lane];
-        const bool part = c >= 0;
-        const int64_t g = part ? (int64_t)c : N + (int64_t)(~c);
-        const double mc = a.mass[g];
-        const bool use = part || mc != 0.0;
-        const double *src = part ? a.coord + 3 * g : a.acc + 3 * (int64_t)(~c);
-        const double wgt = part ? mc : 1.0;
+    const bool mine = w < n;  // this thread has a child
+    const bool part = c >= 0;
+    const int64_t g = part ? (int64_t)c : N + (int64_t)(~c);
+    double mc = 0.0, hc = 0.0, cx[3] = {0.0, 0.0, 0.0}, sx[3];
+    float4 qa = make_float4(0.f, 0.f, 0.f, 0.f), qb = qa;
+    if (mine) {
+        mc = a.mass[g];
+        hc = a.soft[g];
+#pragma unroll
+        for (int k = 0; k < 3; k++) cx[k] = a.coord[3 * g + k];
+        if (!part) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) sx[k] = a.acc[3 * (int64_t)(~c) + k];
+            if (a.quad32) {
+                qa = a.quad32[2 * (int64_t)(~c)];
+                qb = a.quad32[2 * (int64_t)(~c) + 1];
+            }
+        }
+    }
+    // stage 1: warp q, child q of every node: the mass-pass terms (use ? term : -0.0); a particle
+    // adds m x, a node child its coordinate sums (times 1.0 in node_moments_kids, which is exact)
+    const bool use = mine && (part || nonzero64(mc));
+    if (mine) {
         s_m[w][lane] = use ? mc : -0.0;
 #pragma unroll
-        for (int k = 0; k < 3; k++) s_t[k][w][lane] = use ? dmul(wgt, src[k]) : -0.0;
-        s_h[w][lane] = use ? a.soft[g] : 0.0;
+        for (int k = 0; k < 3; k++) s_t[k][w][lane] = use ? (part ? dmul(mc, cx[k]) : sx[k]) : -0.0;
+        s_h[w][lane] = hc;
         s_use[w][lane] = use ? 1 : 0;
     }
     __syncthreads();
-    // stage 2: the five sums, child order
+    // stage 2: the five sums, child order (the softening maximum on the integer units)
     if (w < 5 && j >= 0) {
         double v = 0.0;
+        long long vk = 0;
 #pragma unroll
         for (int q = 0; q < 8; q++) {
             if (q < n) {
                 if (w == 0) v = dadd(v, s_m[q][lane]);
                 else if (w < 4) v = dadd(v, s_t[w - 1][q][lane]);
-                else if (s_use[q][lane]) v = pymax(v, s_h[q][lane]);
+                else if (s_use[q][lane]) {
+                    const double hq = s_h[q][lane];
+                    const long long kq = fkey(hq);
+                    if (kq > vk) {  // pymax(v, hq)
+                        v = hq;
+                        vk = kq;
+                    }
+                }
             }
         }
         s_sum[w][lane] = v;
@@ -1122,8 +1167,7 @@ __global__ void __launch_bounds__(WIDE_THREADS) k_moments_wide(MomentArgs a, con
         a.acc[3 * j] = acc[0];
         a.acc[3 * j + 1] = acc[1];
         a.acc[3 * j + 2] = acc[2];
-        double com[3] = {a.coord[3 * f], a.coord[3 * f + 1], a.coord[3 * f + 2]};
-        if (m != 0.0) {
+        if (nonzero64(m)) {
             const double inv = __drcp_rn(m);  // 1 / m correctly rounded: the same value as 1.0 / m
             double d2 = 0.0;
 #pragma unroll
@@ -1142,16 +1186,13 @@ __global__ void __launch_bounds__(WIDE_THREADS) k_moments_wide(MomentArgs a, con
     __syncthreads();
     if (!a.quad32) return;  // (uniform over the block)
     // stage 4: warp q, child q: its FP32 quadrupole term
-    if (w < n && s_use[w][lane]) {
+    if (use) {
         float T[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        const int32_t c = s_c[w][lane];
-        const int64_t g = c >= 0 ? (int64_t)c : N + (int64_t)(~c);
-        if (c < 0) load_quad32(T, a.quad32[2 * (int64_t)(~c)], a.quad32[2 * (int64_t)(~c) + 1]);
+        if (!part) load_quad32(T, qa, qb);
         float ch_[3], cl_[3];
 #pragma unroll
         for (int k = 0; k < 3; k++) d2f_split(s_com[k][lane], ch_[k], cl_[k]);
-        quad32_term(T, d2f(s_m[w][lane]), off32(a.coord[3 * g], ch_[0], cl_[0]), off32(a.coord[3 * g + 1], ch_[1], cl_[1]),
-                    off32(a.coord[3 * g + 2], ch_[2], cl_[2]));
+        quad32_term(T, d2f(mc), off32(cx[0], ch_[0], cl_[0]), off32(cx[1], ch_[1], cl_[1]), off32(cx[2], ch_[2], cl_[2]));
 #pragma unroll
         for (int e = 0; e < 6; e++) s_q[e][w][lane] = T[e];
     }
