@@ -1800,8 +1800,8 @@ tg_status build_tree(tg_tree_s *T, const double *pos, const double *m, const dou
     // and the build returns while it runs; ev_topo marks the topology and geometry final, ev_built
     // the end of the moment pass.
     if (!T->ev_topo) {
-        TG_CUDA(cudaEventCreateWithFlags(&T->ev_topo, cudaEventDisableTiming));
-        TG_CUDA(cudaEventCreateWithFlags(&T->ev_built, cudaEventDisableTiming));
+        TG_CUDA(pool_event(&T->ev_topo, false));
+        TG_CUDA(pool_event(&T->ev_built, false));
     }
     TG_CUDA(cudaEventRecord(T->ev_topo, st));
     int links_bad = 0, sort_bad = 0;

@@ -117,11 +117,11 @@ void destroy(tg_tree_s *t) {
     free_arena(t->arena64, st);
     if (t->stats_dev) cudaFreeAsync(t->stats_dev, st);
     f(t->groups); f(t->group_root); f(t->group_node); f(t->gstats); f(t->gerr); f(t->sort_err); f(t->vel); f(t->vdisp); f(t->quad32); f(t->lvl_list); f(t->fdepth);
-    if (t->side) cudaStreamDestroy(t->side);  // released once its work is done
-    if (t->ev_fork) cudaEventDestroy(t->ev_fork);
-    if (t->ev_join) cudaEventDestroy(t->ev_join);
-    if (t->ev_topo) cudaEventDestroy(t->ev_topo);
-    if (t->ev_built) cudaEventDestroy(t->ev_built);
+    release_stream(t->side);  // back to the library's pool, its queued work still to run
+    release_event(t->ev_fork, false, t->dev);
+    release_event(t->ev_join, false, t->dev);
+    release_event(t->ev_topo, false, t->dev);
+    release_event(t->ev_built, false, t->dev);
     delete t;
 }
 
@@ -155,6 +155,7 @@ static tg_status build_common(const double *pos, const double *m, const double *
     if (n < 1) return TG_ERR_BAD_ARG;
     if (!m) compute_moments = 0;
     tg_tree_s *t = new (std::nothrow) tg_tree_s();
+    if (t) t->dev = current_device_or(0);
     if (!t) return TG_ERR_OOM;
     tg_status rc = TG_OK;
     {

@@ -231,6 +231,18 @@ int num_sms();
 #endif
 cudaError_t dev_malloc(void **p, size_t bytes, cudaStream_t s);
 
+// Streams (non-blocking) and events (timing or not) of the current device from a library-owned pool:
+// a tree takes a side stream and up to four events and a walk two timing events on every call, and
+// creating and destroying them cost host time between the GPU's launches. A released stream may
+// still have work queued; work put on it later runs after that work. A released event may be
+// recorded again; waits already enqueued on it are unaffected.
+cudaError_t pool_stream(cudaStream_t *s);
+void release_stream(cudaStream_t s);
+// dev: the device the event was made on (-1: the current device).
+cudaError_t pool_event(cudaEvent_t *e, bool timing);
+void release_event(cudaEvent_t e, bool timing, int dev = -1);
+int current_device_or(int fallback);
+
 // A stream-ordered device array from dev_malloc, freed on `st` when it goes out of scope.
 template <typename T>
 struct DevArray {

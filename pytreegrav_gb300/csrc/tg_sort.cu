@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <mutex>
+#include <vector>
 
 #include "tg_common.cuh"
 
@@ -29,6 +30,72 @@ int num_sms() {
         if (sms <= 0) sms = 1;
     }
     return sms;
+}
+
+namespace {
+constexpr int POOL_DEVICES = 64;
+std::mutex g_res_mu;
+std::vector<cudaStream_t> g_streams[POOL_DEVICES];
+std::vector<cudaEvent_t> g_events[POOL_DEVICES][2];  // [timing]
+int current_device() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= POOL_DEVICES) return -1;
+    return dev;
+}
+}  // namespace
+
+int current_device_or(int fallback) {
+    int dev = 0;
+    return cudaGetDevice(&dev) == cudaSuccess ? dev : fallback;
+}
+
+cudaError_t pool_stream(cudaStream_t *s) {
+    const int dev = current_device();
+    if (dev >= 0) {
+        std::lock_guard<std::mutex> lock(g_res_mu);
+        if (!g_streams[dev].empty()) {
+            *s = g_streams[dev].back();
+            g_streams[dev].pop_back();
+            return cudaSuccess;
+        }
+    }
+    return cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
+}
+
+void release_stream(cudaStream_t s) {
+    if (!s) return;
+    int dev = -1;
+    if (cudaStreamGetDevice(s, &dev) != cudaSuccess || dev < 0 || dev >= POOL_DEVICES) {
+        cudaStreamDestroy(s);
+        return;
+    }
+    std::lock_guard<std::mutex> lock(g_res_mu);
+    g_streams[dev].push_back(s);
+}
+
+cudaError_t pool_event(cudaEvent_t *e, bool timing) {
+    const int dev = current_device();
+    if (dev >= 0) {
+        std::lock_guard<std::mutex> lock(g_res_mu);
+        auto &v = g_events[dev][timing ? 1 : 0];
+        if (!v.empty()) {
+            *e = v.back();
+            v.pop_back();
+            return cudaSuccess;
+        }
+    }
+    return cudaEventCreateWithFlags(e, timing ? cudaEventDefault : cudaEventDisableTiming);
+}
+
+void release_event(cudaEvent_t e, bool timing, int dev) {
+    if (!e) return;
+    if (dev < 0) dev = current_device();
+    if (dev < 0 || dev >= POOL_DEVICES) {
+        cudaEventDestroy(e);
+        return;
+    }
+    std::lock_guard<std::mutex> lock(g_res_mu);
+    g_events[dev][timing ? 1 : 0].push_back(e);
 }
 
 cudaError_t dev_malloc(void **p, size_t bytes, cudaStream_t s) {

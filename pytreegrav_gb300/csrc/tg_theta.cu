@@ -53,12 +53,18 @@ __global__ void k_copy_groups(const int2 *groups, const int *node, int64_t ng, i
 
 // The frontier of the top TOP_DEPTH levels under the root (node 0): every node at depth TOP_DEPTH
 // and every shallower node without node children, found level by level from the arena's child
-// ranges. One block; *ntop receives the count.
-__global__ void k_top_nodes(Arena<float> ar, int *top, int *ntop) {
-    __shared__ int cur[TOP_MAX], nxt[TOP_MAX];
+// ranges and listed in ascending node order, and its FP32 records relative to the root's centre of
+// mass: (x, y, z, m) and the square of half the node size (the field's softening), with the root's
+// centre (float3 + pad). One block; *ntop receives the count.
+__global__ void k_top_nodes(Arena<float> ar, int64_t ntot, const double *coord, const double *mass,
+                            const double *size, int *top, int *ntop, float4 *rec, float *hs2, float4 *origin) {
+    __shared__ int cur[TOP_MAX], nxt[TOP_MAX], fr[TOP_MAX];
     __shared__ int ncur, nnxt, nout;
     if (ar.bad && *ar.bad) {  // the arena is invalid (the walk reports it): no frontier
-        if (threadIdx.x == 0) *ntop = 0;
+        if (threadIdx.x == 0) {
+            *ntop = 0;
+            *origin = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
         return;
     }
     if (threadIdx.x == 0) {
@@ -77,7 +83,7 @@ __global__ void k_top_nodes(Arena<float> ar, int *top, int *ntop) {
             if (nc == 0) {
                 if (d > 0) {
                     int q = atomicAdd(&nout, 1);
-                    if (q < TOP_MAX) top[q] = j;
+                    if (q < TOP_MAX) fr[q] = j;
                 }
             } else {
                 int q = atomicAdd(&nnxt, nc);
@@ -91,26 +97,30 @@ __global__ void k_top_nodes(Arena<float> ar, int *top, int *ntop) {
     }
     for (int i = threadIdx.x; i < ncur; i += blockDim.x) {
         int q = atomicAdd(&nout, 1);
-        if (q < TOP_MAX) top[q] = cur[i];
+        if (q < TOP_MAX) fr[q] = cur[i];
     }
     __syncthreads();
-    if (threadIdx.x == 0) *ntop = min(nout, TOP_MAX);
-}
-
-// FP32 records of the top nodes, relative to the root's centre of mass: (x, y, z, m), and the
-// square of half the node size (the field's softening). Also the root's centre (float3 + pad).
-__global__ void k_top_records(int64_t ntot, const double *coord, const double *mass, const double *size,
-                              const int *top, const int *ntop_p, float4 *rec, float *hs2, float4 *origin) {
-    const int ntop = *ntop_p;
+    // ascending node order (the atomics' order varies from run to run; the features' sums do not)
+    const int nt = min(nout, TOP_MAX);
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+        const int j = fr[i];
+        int r = 0;
+        for (int k = 0; k < nt; k++) r += fr[k] < j ? 1 : 0;  // node indices are distinct
+        nxt[r] = j;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *ntop = nt;
     const double ox = coord[3 * ntot], oy = coord[3 * ntot + 1], oz = coord[3 * ntot + 2];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ntop; i += gridDim.x * blockDim.x) {
-        const int64_t f = ntot + top[i];
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+        const int j = nxt[i];
+        top[i] = j;
+        const int64_t f = ntot + j;
         rec[i] = make_float4((float)(coord[3 * f] - ox), (float)(coord[3 * f + 1] - oy), (float)(coord[3 * f + 2] - oz),
                              (float)mass[f]);
         const float hs = 0.5f * (float)size[f];
         hs2[i] = hs * hs;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) *origin = make_float4((float)ox, (float)oy, (float)oz, 0.f);
+    if (threadIdx.x == 0) *origin = make_float4((float)ox, (float)oy, (float)oz, 0.f);
 }
 
 // One warp per group (see tg_theta_features for the list), in FP32 on coordinates relative to the
@@ -122,98 +132,109 @@ __global__ void k_features(int64_t ntot, const double *coord, const double *mass
                            int64_t ngroups,
                            const float4 *rec, const float *hs2, const int *ntop_p, const float4 *origin, int quad,
                            float log10n, float *feat, unsigned long long *field_sums) {
+    // the tolerance unit's sums, added per block and then once to field_sums
+    __shared__ unsigned long long red[2];
+    if (threadIdx.x == 0) red[0] = red[1] = 0ull;
+    __syncthreads();
     const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (g >= ngroups) return;
-    const int2 gr = groups[g];
-    const float4 o4 = *origin;
-    // targets: box and softening
-    float lo[3], hi[3], hm;
-    {
-        const int64_t t = gr.x + (lane < gr.y ? lane : 0);
-        const float o[3] = {o4.x, o4.y, o4.z};
-        for (int k = 0; k < 3; k++) {  // (hi - o) + lo: the offset from the origin to ~1 float ulp
-            float ch, cl;
-            d2f_split(tcoord[3 * t + k], ch, cl);
-            lo[k] = hi[k] = (ch - o[k]) + cl;
+    if (g < ngroups) {  // warp-uniform
+        const int2 gr = groups[g];
+        const float4 o4 = *origin;
+        // targets: box and softening
+        float lo[3], hi[3], hm;
+        {
+            const int64_t t = gr.x + (lane < gr.y ? lane : 0);
+            const float o[3] = {o4.x, o4.y, o4.z};
+            for (int k = 0; k < 3; k++) {  // (hi - o) + lo: the offset from the origin to ~1 float ulp
+                float ch, cl;
+                d2f_split(tcoord[3 * t + k], ch, cl);
+                lo[k] = hi[k] = (ch - o[k]) + cl;
+            }
+            hm = d2f(tsoft[t]);
         }
-        hm = d2f(tsoft[t]);
-    }
-#pragma unroll
-    for (int s = 16; s; s >>= 1) {
-#pragma unroll
+    #pragma unroll
+        for (int s = 16; s; s >>= 1) {
+    #pragma unroll
+            for (int k = 0; k < 3; k++) {
+                lo[k] = fminf(lo[k], __shfl_xor_sync(FULL, lo[k], s));
+                hi[k] = fmaxf(hi[k], __shfl_xor_sync(FULL, hi[k], s));
+            }
+            hm = fmaxf(hm, __shfl_xor_sync(FULL, hm, s));
+        }
+        float gc[3], ext[3];
+    #pragma unroll
         for (int k = 0; k < 3; k++) {
-            lo[k] = fminf(lo[k], __shfl_xor_sync(FULL, lo[k], s));
-            hi[k] = fmaxf(hi[k], __shfl_xor_sync(FULL, hi[k], s));
+            gc[k] = 0.5f * (lo[k] + hi[k]);
+            ext[k] = hi[k] - lo[k];
         }
-        hm = fmaxf(hm, __shfl_xor_sync(FULL, hm, s));
+        // coarse field of the top levels at the group centre, each node softened by half its size
+        const int ntop = *ntop_p;
+        float s1 = 0.f, s3 = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
+        for (int i = lane; i < ntop; i += 32) {
+            const float4 r = rec[i];
+            const float dx = r.x - gc[0], dy = r.y - gc[1], dz = r.z - gc[2];
+            const float r2 = dx * dx + dy * dy + dz * dz + hs2[i];
+            const float rinv = r2 > 0.f ? rsqrtf(r2) : 0.f;
+            const float mr = r.w * rinv;
+            s1 += mr * rinv;
+            s3 += mr;
+            const float m3 = mr * rinv * rinv;
+            vx += m3 * dx;
+            vy += m3 * dy;
+            vz += m3 * dz;
+        }
+    #pragma unroll
+        for (int s = 16; s; s >>= 1) {
+            s1 += __shfl_xor_sync(FULL, s1, s);
+            s3 += __shfl_xor_sync(FULL, s3, s);
+            vx += __shfl_xor_sync(FULL, vx, s);
+            vy += __shfl_xor_sync(FULL, vy, s);
+            vz += __shfl_xor_sync(FULL, vz, s);
+        }
+        if (lane == 0) {
+            const int64_t R = ntot, P = ntot + group_node[g];  // system root (node 0) and the group's node
+            // FP64 compares and conversions as integer work (finite inputs: x > 0 iff its bits are a positive int64)
+            auto pos = [](double x) { return __double_as_longlong(x) > 0; };
+            const float S = pos(size[R]) ? d2f(size[R]) : 1.f, Mt = pos(mass[R]) ? d2f(mass[R]) : 1.f;
+            const float tiny = 1e-9f * S;
+            const float emax = fmaxf(ext[0], fmaxf(ext[1], ext[2])), emin = fminf(ext[0], fminf(ext[1], ext[2]));
+            const float dcen = sqrtf(gc[0] * gc[0] + gc[1] * gc[1] + gc[2] * gc[2]);
+            const float sP = pos(size[P]) ? d2f(size[P]) : tiny, mP = d2f(mass[P]);
+            const float fa = s1 * S * S / Mt, fv = sqrtf(vx * vx + vy * vy + vz * vz) * S * S / Mt, fp = s3 * S / Mt;
+            const float lmP = logf(mP / Mt + 1e-30f), lsP = logf(sP / S);
+            float *o = feat + g * NF;
+            o[0] = log2f((float)gr.y);
+            o[1] = logf(emax / S + 1e-9f);
+            o[2] = lsP;
+            o[3] = lmP;
+            o[4] = lmP - 3.f * lsP;
+            o[5] = logf(dcen / S + 1e-6f);
+            o[6] = logf(fa + 1e-30f);
+            o[7] = logf(fv + 1e-30f);
+            o[8] = logf(fp + 1e-30f);
+            o[9] = logf(fv + 1e-30f) - logf(fa + 1e-30f);
+            o[10] = logf(hm / S + 1e-9f);
+            o[11] = emin / (emax + tiny);
+            o[12] = logf((ext[0] + tiny) * (ext[1] + tiny) * (ext[2] + tiny) / gr.y) / 3.f - logf(S);
+            o[TG_THETA_FEAT_LAMBDA] = 0.f;
+            o[14] = quad ? 1.f : 0.f;
+            o[15] = log10n;
+            // group-size weighted sum of the field's square (units M / S^2, fixed point 2^-32: integer
+            // sums do not depend on the order of the atomics) and of the weights, for the tolerance unit
+            // of tg_theta_tolerances
+            const uint32_t qb = __float_as_uint(fminf((float)gr.y * fv * fv, 1e8f) * 4294967296.f) & 0x7fffffffu;
+            const int qe = (int)(qb >> 23) - 150;  // truncation to an integer, without a 64-bit conversion
+            const unsigned long long qm = (qb & 0x7fffffu) | 0x800000u;
+            atomicAdd(&red[0], qb < 0x3f800000u ? 0ull : (qe >= 0 ? qm << qe : qm >> -qe));
+            atomicAdd(&red[1], (unsigned long long)gr.y);
+        }  // lane 0
     }
-    float gc[3], ext[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        gc[k] = 0.5f * (lo[k] + hi[k]);
-        ext[k] = hi[k] - lo[k];
+    __syncthreads();
+    if (threadIdx.x == 0 && red[1] != 0ull) {
+        atomicAdd(field_sums, red[0]);
+        atomicAdd(field_sums + 1, red[1]);
     }
-    // coarse field of the top levels at the group centre, each node softened by half its size
-    const int ntop = *ntop_p;
-    float s1 = 0.f, s3 = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
-    for (int i = lane; i < ntop; i += 32) {
-        const float4 r = rec[i];
-        const float dx = r.x - gc[0], dy = r.y - gc[1], dz = r.z - gc[2];
-        const float r2 = dx * dx + dy * dy + dz * dz + hs2[i];
-        const float rinv = r2 > 0.f ? rsqrtf(r2) : 0.f;
-        const float mr = r.w * rinv;
-        s1 += mr * rinv;
-        s3 += mr;
-        const float m3 = mr * rinv * rinv;
-        vx += m3 * dx;
-        vy += m3 * dy;
-        vz += m3 * dz;
-    }
-#pragma unroll
-    for (int s = 16; s; s >>= 1) {
-        s1 += __shfl_xor_sync(FULL, s1, s);
-        s3 += __shfl_xor_sync(FULL, s3, s);
-        vx += __shfl_xor_sync(FULL, vx, s);
-        vy += __shfl_xor_sync(FULL, vy, s);
-        vz += __shfl_xor_sync(FULL, vz, s);
-    }
-    if (lane != 0) return;
-    const int64_t R = ntot, P = ntot + group_node[g];  // system root (node 0) and the group's node
-    // FP64 compares and conversions as integer work (finite inputs: x > 0 iff its bits are a positive int64)
-    auto pos = [](double x) { return __double_as_longlong(x) > 0; };
-    const float S = pos(size[R]) ? d2f(size[R]) : 1.f, Mt = pos(mass[R]) ? d2f(mass[R]) : 1.f;
-    const float tiny = 1e-9f * S;
-    const float emax = fmaxf(ext[0], fmaxf(ext[1], ext[2])), emin = fminf(ext[0], fminf(ext[1], ext[2]));
-    const float dcen = sqrtf(gc[0] * gc[0] + gc[1] * gc[1] + gc[2] * gc[2]);
-    const float sP = pos(size[P]) ? d2f(size[P]) : tiny, mP = d2f(mass[P]);
-    const float fa = s1 * S * S / Mt, fv = sqrtf(vx * vx + vy * vy + vz * vz) * S * S / Mt, fp = s3 * S / Mt;
-    const float lmP = logf(mP / Mt + 1e-30f), lsP = logf(sP / S);
-    float *o = feat + g * NF;
-    o[0] = log2f((float)gr.y);
-    o[1] = logf(emax / S + 1e-9f);
-    o[2] = lsP;
-    o[3] = lmP;
-    o[4] = lmP - 3.f * lsP;
-    o[5] = logf(dcen / S + 1e-6f);
-    o[6] = logf(fa + 1e-30f);
-    o[7] = logf(fv + 1e-30f);
-    o[8] = logf(fp + 1e-30f);
-    o[9] = logf(fv + 1e-30f) - logf(fa + 1e-30f);
-    o[10] = logf(hm / S + 1e-9f);
-    o[11] = emin / (emax + tiny);
-    o[12] = logf((ext[0] + tiny) * (ext[1] + tiny) * (ext[2] + tiny) / gr.y) / 3.f - logf(S);
-    o[TG_THETA_FEAT_LAMBDA] = 0.f;
-    o[14] = quad ? 1.f : 0.f;
-    o[15] = log10n;
-    // group-size weighted sum of the field's square (units M / S^2, fixed point 2^-32: integer
-    // sums do not depend on the order of the atomics) and of the weights, for the tolerance unit
-    // of tg_theta_tolerances
-    const uint32_t qb = __float_as_uint(fminf((float)gr.y * fv * fv, 1e8f) * 4294967296.f) & 0x7fffffffu;
-    const int qe = (int)(qb >> 23) - 150;  // truncation to an integer, without a 64-bit conversion
-    const unsigned long long qm = (qb & 0x7fffffu) | 0x800000u;
-    atomicAdd(field_sums, qb < 0x3f800000u ? 0ull : (qe >= 0 ? qm << qe : qm >> -qe));
-    atomicAdd(field_sums + 1, (unsigned long long)gr.y);
 }
 
 }  // namespace
@@ -384,10 +405,31 @@ __device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], uint32
 }
 
 constexpr int INF_WARPS = 4;
+// The tolerance unit A * M / S^2 (see tg_theta_tolerances) from the features kernel's field sums.
+__device__ __forceinline__ float tol_scale(const unsigned long long *field_sums, const double *mass,
+                                           const double *size, int64_t ntot) {
+    const double S = size[ntot] > 0 ? size[ntot] : 1.0, M = mass[ntot] > 0 ? mass[ntot] : 1.0;
+    const double w = field_sums[1] > 0 ? (double)field_sums[1] : 1.0;
+    return (float)(sqrt((double)field_sums[0] / 4294967296.0 / w) * M / (S * S));
+}
+
+// Output per row: the model's value u in [tmin, tmax] into theta; or, with ts.tol set (a tolerance
+// model), the tolerance 10^u times the unit into ts.tol, a non-finite u taking umin (the strictest).
+struct TolOut {
+    float *tol = nullptr;
+    const unsigned long long *field_sums = nullptr;
+    const double *mass = nullptr, *size = nullptr;
+    int64_t ntot = 0;
+    float umin = 0.f;
+};
+
 __global__ void __launch_bounds__(INF_WARPS * 32) k_theta_infer(ModelDev md, const float *feat, int64_t n,
-                                                                float loglam, float tmin, float tmax, float *theta) {
+                                                                float loglam, float tmin, float tmax, float *theta,
+                                                                TolOut ts) {
     __shared__ uint32_t sw1[H * NF / 2], sw2[H * H / 2];
     __shared__ float sb1[H], sb2[H], sw3[H], smu[NF], sis[NF];
+    __shared__ float sscale;
+    if (ts.tol && threadIdx.x == 0) sscale = tol_scale(ts.field_sums, ts.mass, ts.size, ts.ntot);
     for (int i = threadIdx.x; i < H * NF / 2; i += blockDim.x) sw1[i] = md.w1[i];
     for (int i = threadIdx.x; i < H * H / 2; i += blockDim.x) sw2[i] = md.w2[i];
     for (int i = threadIdx.x; i < H; i += blockDim.x) {
@@ -454,8 +496,16 @@ __global__ void __launch_bounds__(INF_WARPS * 32) k_theta_infer(ModelDev md, con
         s1 += __shfl_xor_sync(FULL, s1, 1);
         s1 += __shfl_xor_sync(FULL, s1, 2);
         if (c == 0) {
-            if (r0 < n) theta[r0] = tmin + (tmax - tmin) * sigm(s0 + b3);
-            if (r1 < n) theta[r1] = tmin + (tmax - tmin) * sigm(s1 + b3);
+            float u0 = tmin + (tmax - tmin) * sigm(s0 + b3), u1 = tmin + (tmax - tmin) * sigm(s1 + b3);
+            if (ts.tol) {
+                if (!isfinite(u0)) u0 = ts.umin;
+                if (!isfinite(u1)) u1 = ts.umin;
+                if (r0 < n) ts.tol[r0] = exp10f(u0) * sscale;
+                if (r1 < n) ts.tol[r1] = exp10f(u1) * sscale;
+            } else {
+                if (r0 < n) theta[r0] = u0;
+                if (r1 < n) theta[r1] = u1;
+            }
         }
     }
 }
@@ -476,9 +526,7 @@ __global__ void k_theta_guard(float *theta, int64_t n, float fallback, float tmi
 // Tolerance unit A * M / S^2 (see tg_theta_tolerances) from the features kernel's field sums.
 __global__ void k_tol_scale(const unsigned long long *field_sums, const double *mass, const double *size,
                             int64_t ntot, float *scale) {
-    const double S = size[ntot] > 0 ? size[ntot] : 1.0, M = mass[ntot] > 0 ? mass[ntot] : 1.0;
-    const double w = field_sums[1] > 0 ? (double)field_sums[1] : 1.0;
-    *scale = (float)(sqrt((double)field_sums[0] / 4294967296.0 / w) * M / (S * S));
+    *scale = tol_scale(field_sums, mass, size, ntot);
 }
 
 __global__ void k_u_to_tol(const float *u, int64_t ng, const float *scale, float umin, float *tol) {
@@ -526,9 +574,7 @@ tg_status features_of_groups(tg_tree_s *t, const double *tcoord, const double *t
     float *hs2 = (float *)(origin + 1);
     unsigned long long *sums = field_sums ? field_sums : (unsigned long long *)(origin + 1 + TOP_MAX / 4);
     TG_CUDA(cudaMemsetAsync(sums, 0, 2 * sizeof(unsigned long long), st));
-    { k_top_nodes<<<1, 256, 0, st>>>(t->arena32, top + 1, top); note_launch(); }
-    { k_top_records<<<div_up(TOP_MAX, 128), 128, 0, st>>>(t->ntot, t->coord, t->mass, t->size, top + 1, top, rec, hs2,
-                                                         origin); note_launch(); }
+    { k_top_nodes<<<1, 256, 0, st>>>(t->arena32, t->ntot, t->coord, t->mass, t->size, top + 1, top, rec, hs2, origin); note_launch(); }
     if (ng > 0) {
         k_features<<<div_up(ng * 32, 256), 256, 0, st>>>(t->ntot, t->coord, t->mass, t->size, tcoord, tsoft, groups,
                                                          group_node, ng, rec, hs2, top, origin, quadrupole,
@@ -571,11 +617,11 @@ tg_status tolerances_device(tg_tree_s *t, const unsigned long long *field_sums, 
 }
 
 tg_status infer_device(const tg_theta_model_s *m, const float *feat, int64_t n, float loglam, float *theta,
-                       cudaStream_t st) {
+                       cudaStream_t st, TolOut ts = TolOut()) {
     if (n <= 0) return TG_OK;
     const int64_t tiles = (n + 15) / 16;
     const int grid = (int)std::min<int64_t>((tiles + INF_WARPS - 1) / INF_WARPS, (int64_t)num_sms() * 8);
-    { k_theta_infer<<<grid, INF_WARPS * 32, 0, st>>>(m->dev, feat, n, loglam, m->tmin, m->tmax, theta); note_launch(); }
+    { k_theta_infer<<<grid, INF_WARPS * 32, 0, st>>>(m->dev, feat, n, loglam, m->tmin, m->tmax, theta, ts); note_launch(); }
     TG_CUDA(cudaGetLastError());
     return TG_OK;
 }
@@ -603,18 +649,23 @@ tg_status learned_walk(tg_tree_s *t, FeatFn feats, const double *tpos, const dou
     if (m) {
         const int64_t ng1 = std::max<int64_t>(ng, 1);
         TG_CUDA(dev_malloc((void **)&feat, sizeof(float) * (NF * ng1 + 8), st));
-        TG_CUDA(dev_malloc((void **)&tg_theta, sizeof(float) * ng1, st));
         unsigned long long *sums = (unsigned long long *)(feat + (NF * ng1 + 1) / 2 * 2);
         TG_TRY(feats(feat, sums));
-        TG_TRY(infer_device(m, feat, ng, log10_lambda, tg_theta, st));
         if (m->kind == TG_THETA_KIND_ANGLE) {
+            TG_CUDA(dev_malloc((void **)&tg_theta, sizeof(float) * ng1, st));
+            TG_TRY(infer_device(m, feat, ng, log10_lambda, tg_theta, st));
             { k_theta_guard<<<div_up(ng, 256), 256, 0, st>>>(tg_theta, ng, (float)theta_fallback, m->tmin, m->tmax); note_launch(); }
             TG_CUDA(cudaGetLastError());
-        } else {
+        } else {  // the tolerances straight from the inference (tolerances_device's values)
             TG_CUDA(dev_malloc((void **)&tol, sizeof(float) * ng1, st));
-            TG_TRY(tolerances_device(t, sums, tg_theta, ng, m->tmin, tol, (float *)(sums + 2), st));
-            cudaFreeAsync(tg_theta, st);
-            tg_theta = nullptr;
+            TolOut ts;
+            ts.tol = tol;
+            ts.field_sums = sums;
+            ts.mass = t->mass;
+            ts.size = t->size;
+            ts.ntot = t->ntot;
+            ts.umin = m->tmin;
+            TG_TRY(infer_device(m, feat, ng, log10_lambda, nullptr, st, ts));
             theta = m->theta_max;
         }
     }

@@ -53,6 +53,7 @@ struct tg_tree_s {
     int64_t ntot = 0;       // particles in the arena (all systems)
     int64_t mtot = 0;       // nodes in the arena (all systems)
     int32_t nsys = 1;
+    int dev = 0;  // the CUDA device it lives on
     int has_quads = 0;
     int has_coincident = 0;
     int compute_moments = 1;

@@ -1858,9 +1858,16 @@ template <typename T>
 static tg_status walk_with_fallback(tg_tree_s *t, WalkArgs<T> &a, Arena<T> &ar, int fields, bool quad, int warps,
                                     int first_stack, int *scratch, bool split_heavy, cudaStream_t st, int *status_out,
                                     float *kernel_ms) {
-    cudaEvent_t e0, e1;
-    TG_CUDA(cudaEventCreate(&e0));
-    TG_CUDA(cudaEventCreate(&e1));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    struct Events {  // back to the pool on every exit
+        cudaEvent_t *a, *b;
+        ~Events() {
+            release_event(*a, true);
+            release_event(*b, true);
+        }
+    } evs{&e0, &e1};
+    TG_CUDA(pool_event(&e0, true));
+    TG_CUDA(pool_event(&e1, true));
     TG_CUDA(cudaEventRecord(e0, st));
     tg_status rc = enqueue_walk<T>(a, fields, quad, warps, first_stack, scratch, st, split_heavy);
     int hdr[WS_RETRY_LIST] = {0};
@@ -1875,8 +1882,6 @@ static tg_status walk_with_fallback(tg_tree_s *t, WalkArgs<T> &a, Arena<T> &ar, 
     TG_CUDA(cudaMemcpyAsync(&status, scratch + WS_STATUS, sizeof(int), cudaMemcpyDeviceToHost, st));
     TG_CUDA(cudaStreamSynchronize(st));
     TG_CUDA(cudaEventElapsedTime(kernel_ms, e0, e1));
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     *status_out = status;
     return rc;
 }
@@ -2082,9 +2087,9 @@ tg_status tree_groups(tg_tree_s *t, int G, cudaStream_t st) {
 // The tree's side stream and its two events, made on first use.
 tg_status tree_side_stream(tg_tree_s *t) {
     if (!t->side) {
-        TG_CUDA(cudaStreamCreateWithFlags(&t->side, cudaStreamNonBlocking));
-        TG_CUDA(cudaEventCreateWithFlags(&t->ev_fork, cudaEventDisableTiming));
-        TG_CUDA(cudaEventCreateWithFlags(&t->ev_join, cudaEventDisableTiming));
+        TG_CUDA(pool_stream(&t->side));
+        TG_CUDA(pool_event(&t->ev_fork, false));
+        TG_CUDA(pool_event(&t->ev_join, false));
     }
     return TG_OK;
 }
