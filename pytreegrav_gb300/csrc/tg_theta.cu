@@ -171,6 +171,7 @@ __global__ void k_features(int64_t ntot, const double *coord, const double *mass
         // coarse field of the top levels at the group centre, each node softened by half its size
         const int ntop = *ntop_p;
         float s1 = 0.f, s3 = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
+#pragma unroll 4
         for (int i = lane; i < ntop; i += 32) {
             const float4 r = rec[i];
             const float dx = r.x - gc[0], dy = r.y - gc[1], dz = r.z - gc[2];
@@ -192,43 +193,59 @@ __global__ void k_features(int64_t ntot, const double *coord, const double *mass
             vy += __shfl_xor_sync(FULL, vy, s);
             vz += __shfl_xor_sync(FULL, vz, s);
         }
+        // the features, one per lane (the sums above are on every lane after the butterfly)
+        const int64_t R = ntot, P = ntot + group_node[g];  // system root (node 0) and the group's node
+        // FP64 compares and conversions as integer work (finite inputs: x > 0 iff its bits are a
+        // positive int64)
+        auto pos = [](double x) { return __double_as_longlong(x) > 0; };
+        const double sR = size[R], mR = mass[R], sPd = size[P], mPd = mass[P];
+        const float S = pos(sR) ? d2f(sR) : 1.f, Mt = pos(mR) ? d2f(mR) : 1.f;
+        const float tiny = 1e-9f * S;
+        const float fa = s1 * S * S / Mt, fv = sqrtf(vx * vx + vy * vy + vz * vz) * S * S / Mt;
+        // every lane takes one logarithm (lane k: feature k's argument; lane 13, the lambda slot,
+        // log S for feature 12), then the differences come from the neighbours' values
+        const float emax = fmaxf(ext[0], fmaxf(ext[1], ext[2])), emin = fminf(ext[0], fminf(ext[1], ext[2]));
+        const float sP = pos(sPd) ? d2f(sPd) : tiny, mP = d2f(mPd);
+        float arg = 1.f;
+        switch (lane) {  // selects only
+            case 1: arg = emax / S + 1e-9f; break;
+            case 2: arg = sP / S; break;
+            case 3: arg = mP / Mt + 1e-30f; break;
+            case 5: arg = sqrtf(gc[0] * gc[0] + gc[1] * gc[1] + gc[2] * gc[2]) / S + 1e-6f; break;
+            case 6: arg = fa + 1e-30f; break;
+            case 7: arg = fv + 1e-30f; break;
+            case 8: arg = s3 * S / Mt + 1e-30f; break;
+            case 10: arg = hm / S + 1e-9f; break;
+            case 12: arg = (ext[0] + tiny) * (ext[1] + tiny) * (ext[2] + tiny) / gr.y; break;
+            case 13: arg = S; break;
+            default: break;
+        }
+        const float lg = logf(arg);
+        const float l2 = __shfl_sync(FULL, lg, 2), l3 = __shfl_sync(FULL, lg, 3), l6 = __shfl_sync(FULL, lg, 6),
+                    l7 = __shfl_sync(FULL, lg, 7), l13 = __shfl_sync(FULL, lg, 13);
+        const float lgn = log2f((float)gr.y);
+        if (lane < NF) {
+            float v = lg;
+            if (lane == 0) v = lgn;
+            else if (lane == 4) v = l3 - 3.f * l2;
+            else if (lane == 9) v = l7 - l6;
+            else if (lane == 11) v = emin / (emax + tiny);
+            else if (lane == 12) v = lg / 3.f - l13;
+            else if (lane == TG_THETA_FEAT_LAMBDA) v = 0.f;
+            else if (lane == 14) v = quad ? 1.f : 0.f;
+            else if (lane == 15) v = log10n;
+            feat[g * NF + lane] = v;
+        }
         if (lane == 0) {
-            const int64_t R = ntot, P = ntot + group_node[g];  // system root (node 0) and the group's node
-            // FP64 compares and conversions as integer work (finite inputs: x > 0 iff its bits are a positive int64)
-            auto pos = [](double x) { return __double_as_longlong(x) > 0; };
-            const float S = pos(size[R]) ? d2f(size[R]) : 1.f, Mt = pos(mass[R]) ? d2f(mass[R]) : 1.f;
-            const float tiny = 1e-9f * S;
-            const float emax = fmaxf(ext[0], fmaxf(ext[1], ext[2])), emin = fminf(ext[0], fminf(ext[1], ext[2]));
-            const float dcen = sqrtf(gc[0] * gc[0] + gc[1] * gc[1] + gc[2] * gc[2]);
-            const float sP = pos(size[P]) ? d2f(size[P]) : tiny, mP = d2f(mass[P]);
-            const float fa = s1 * S * S / Mt, fv = sqrtf(vx * vx + vy * vy + vz * vz) * S * S / Mt, fp = s3 * S / Mt;
-            const float lmP = logf(mP / Mt + 1e-30f), lsP = logf(sP / S);
-            float *o = feat + g * NF;
-            o[0] = log2f((float)gr.y);
-            o[1] = logf(emax / S + 1e-9f);
-            o[2] = lsP;
-            o[3] = lmP;
-            o[4] = lmP - 3.f * lsP;
-            o[5] = logf(dcen / S + 1e-6f);
-            o[6] = logf(fa + 1e-30f);
-            o[7] = logf(fv + 1e-30f);
-            o[8] = logf(fp + 1e-30f);
-            o[9] = logf(fv + 1e-30f) - logf(fa + 1e-30f);
-            o[10] = logf(hm / S + 1e-9f);
-            o[11] = emin / (emax + tiny);
-            o[12] = logf((ext[0] + tiny) * (ext[1] + tiny) * (ext[2] + tiny) / gr.y) / 3.f - logf(S);
-            o[TG_THETA_FEAT_LAMBDA] = 0.f;
-            o[14] = quad ? 1.f : 0.f;
-            o[15] = log10n;
             // group-size weighted sum of the field's square (units M / S^2, fixed point 2^-32: integer
-            // sums do not depend on the order of the atomics) and of the weights, for the tolerance unit
-            // of tg_theta_tolerances
+            // sums do not depend on the order of the atomics) and of the weights, for the tolerance
+            // unit of tg_theta_tolerances
             const uint32_t qb = __float_as_uint(fminf((float)gr.y * fv * fv, 1e8f) * 4294967296.f) & 0x7fffffffu;
             const int qe = (int)(qb >> 23) - 150;  // truncation to an integer, without a 64-bit conversion
             const unsigned long long qm = (qb & 0x7fffffu) | 0x800000u;
             atomicAdd(&red[0], qb < 0x3f800000u ? 0ull : (qe >= 0 ? qm << qe : qm >> -qe));
             atomicAdd(&red[1], (unsigned long long)gr.y);
-        }  // lane 0
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0 && red[1] != 0ull) {

@@ -1662,6 +1662,9 @@ static tg_status launch_walk(WalkArgs<T> &a, int warps, cudaStream_t st) {
     if (!a.ngroups_dev) {
         int64_t need = (a.ngroups + warps - 1) / warps;
         if (blocks > need) blocks = need;
+    } else {  // a pass over a list counted on the device (groups that overflowed the small stack or
+              // went over their error budget): usually empty or short, one block per SM
+        blocks = num_sms();
     }
     if (blocks < 1) blocks = 1;
     { kern<<<(unsigned)blocks, warps * 32, smem, st>>>(a); tg::note_launch(); }
