@@ -405,8 +405,9 @@ def run_ours(args):
                          "targets), plain theta=0.7, quadrupole; the reference arm's configuration")
 
     # the build alone (device arrays, L2 flushed before each), against the HBM copy rate on its
-    # algorithmic bytes: 638 B per particle and 969 B per node, summed over the build's kernels
-    # (profiles/build_plummer1e6.md)
+    # algorithmic bytes (bench_configs.build_roofline)
+    import bench_configs
+
     vp = ctypes.c_void_p
     bev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(10)]
     nodes = 0
@@ -424,18 +425,7 @@ def run_ours(args):
         nodes = int(info.node_hi) - n
         L.tg_tree_free(th_)
     torch.cuda.synchronize()
-    build_ms = statistics.mean(a_.elapsed_time(b_) for a_, b_ in bev)
-    alg_bytes = 638 * n + 969 * nodes
-    hbm = None
-    try:
-        hbm = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs")
-    except Exception:
-        pass
-    build = {"ms": round(build_ms, 4), "nodes": nodes, "algorithmic_bytes": alg_bytes,
-             "achieved_gbs": round(alg_bytes / (build_ms * 1e-3) / 1e9, 1),
-             "hbm_peak_gbs": hbm, "frac_of_hbm": round(alg_bytes / (build_ms * 1e-3) / 1e9 / hbm, 4) if hbm else None,
-             "bound": "latency at this size (dependent launches) and FP64 issue in the moment pass; per-kernel "
-                      "traffic in profiles/build_plummer1e6.md"}
+    build = bench_configs.build_roofline(n, nodes, statistics.mean(a_.elapsed_time(b_) for a_, b_ in bev))
 
     base = cpu_baseline(x, m, h, os.cpu_count() or 1)
     return {
@@ -693,9 +683,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--config", choices=["plummer", "batched", "column", "uniform", "precision", "clustered",
-                                         "largest", "corr"], default="plummer",
+                                         "largest", "corr", "build"], default="plummer",
                     help="batched: the 4096-system configuration; column: ray-traced column density; uniform, "
-                         "precision, clustered, largest, corr: see bench_configs.py (each its own JSON line)")
+                         "precision, clustered, largest, corr, build: see bench_configs.py (each its own JSON line)")
     ap.add_argument("--sources", type=int, default=32_000_000, help="source count of --config largest")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -703,7 +693,7 @@ def main():
         res = run_batched(args)
     elif args.config == "column" and args.impl == "ours":
         res = run_column(args)
-    elif args.config in ("uniform", "precision", "clustered", "largest", "corr") and args.impl == "ours":
+    elif args.config in ("uniform", "precision", "clustered", "largest", "corr", "build") and args.impl == "ours":
         import bench_configs
 
         res = getattr(bench_configs, "run_" + args.config)(args)

@@ -17,6 +17,9 @@
   sums, over all sources on 1e4 sampled targets and over a 2e5-source subset.
 * ``corr``: VelocityStructFunc with pytreegrav's defaults on N = 1e6 Plummer particles with velocities
   (0.3 x + unit normal noise): tree build, velocity moments and the FP64 walk of every particle.
+* ``build``: the octree build alone (quadrupole moments) of the headline's 1e6 Plummer sphere, from
+  device arrays: build time, particles/s, and the build's algorithmic bytes per second against the
+  measured HBM copy rate.
 
 Every input is seeded synthetic data with the configuration's shapes and distributions. Steps are
 timed with CUDA events on the launching stream, inputs resident in HBM, L2 flushed (256 MiB
@@ -24,6 +27,7 @@ written) between timed steps outside the events.
 """
 
 import ctypes
+import json
 import os
 import statistics
 import time
@@ -109,6 +113,27 @@ def fp32_peak(L, st):
     tf, ms = ctypes.c_double(), ctypes.c_double()
     L.tg_measure_fp32_fma(ctypes.byref(tf), ctypes.byref(ms), st)
     return tf.value
+
+
+# The build's algorithmic bytes: 638 B per particle and 969 B per node, summed over its kernels (keys,
+# eight sort passes, gather, split round, numbering sort, final arrays, moment pass; the per-kernel
+# figures are in profiles/build_plummer1e6.md).
+BUILD_BYTES_PER_PARTICLE, BUILD_BYTES_PER_NODE = 638, 969
+
+
+def build_roofline(n, nodes, build_ms):
+    alg = BUILD_BYTES_PER_PARTICLE * n + BUILD_BYTES_PER_NODE * nodes
+    hbm = None
+    try:
+        hbm = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json"))).get(
+            "hbm_gbs")
+    except Exception:
+        pass
+    gbs = alg / (build_ms * 1e-3) / 1e9
+    return {"ms": round(build_ms, 4), "nodes": nodes, "algorithmic_bytes": alg, "achieved_gbs": round(gbs, 1),
+            "hbm_peak_gbs": hbm, "frac_of_hbm": round(gbs / hbm, 4) if hbm else None,
+            "bound": "latency at this size (dependent launches) and FP64 issue in the moment pass; per-kernel "
+                     "traffic in profiles/build_plummer1e6.md"}
 
 
 def ball(n, seed, radius=5.0):
@@ -536,3 +561,35 @@ def run_corr(args):
                              "sample": "oracle build and velocity moments of all N + the structure-function walk "
                                        f"(C, FP64, OpenMP) of every 64th target, extrapolated; {cpu_s:.2f} s per step"},
             "gpu_launches": int(launches)}
+
+
+def run_build(args):
+    """The octree build alone (see the module docstring)."""
+    torch, _lib, L, st = _env()
+    import bench
+
+    n = args.n
+    x = bench.plummer(n, SEED)
+    dx = torch.from_numpy(x).cuda()
+    dm = torch.from_numpy(np.full(n, 1.0 / n)).cuda()
+    dh = torch.from_numpy(np.full(n, bench.SOFT)).cuda()
+    nodes = [0]
+
+    def step():
+        h = build(L, _lib, st, dx, dm, dh, n, True)
+        info = _lib.TreeInfo()
+        L.tg_tree_info_get(h, ctypes.byref(info))
+        nodes[0] = int(info.node_hi) - n
+        L.tg_tree_free(h)
+
+    l0 = L.tg_launch_count()
+    ms, _ = timed(torch, step, args.steps, args.warmup)
+    launches = (L.tg_launch_count() - l0) // (args.steps + args.warmup)
+    roof = build_roofline(n, nodes[0], ms)
+    return {"metric": "octree build particles/s, 1e6 Plummer (quadrupole moments)", "value": round(n / (ms * 1e-3), 1),
+            "unit": "particles/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Plummer sphere, a=1, r<50)",
+            "config": {"workload": f"tg_tree_build of N={n} Plummer particles (m=1/N, h={bench.SOFT}) from device arrays, "
+                                   "quadrupole moments", "l2": "flushed (256 MiB written) before each step"},
+            "build": roof, "gpu_launches": launches}
