@@ -586,7 +586,8 @@ def run_build(args):
     ms, _ = timed(torch, step, args.steps, args.warmup)
     launches = (L.tg_launch_count() - l0) // (args.steps + args.warmup)
     roof = build_roofline(n, nodes[0], ms)
-    return {"metric": "octree build particles/s, 1e6 Plummer (quadrupole moments)", "value": round(n / (ms * 1e-3), 1),
+    return {"metric": f"octree build particles/s, {n:.2g}-particle Plummer sphere (quadrupole moments)",
+            "value": round(n / (ms * 1e-3), 1),
             "unit": "particles/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Plummer sphere, a=1, r<50)",
