@@ -193,6 +193,44 @@ def test_groups_over_the_error_budget_are_rewalked_at_the_global_theta(env, plum
         model.close()
 
 
+def test_learned_walk_is_its_parts_and_repeats(env, plummer_tree):
+    """tg_tree_fields_learned with the shipped tolerance model (no error budget) equals its parts run
+    one by one, bit for bit: the features (tg_theta_features), the network (tg_theta_infer), the
+    tolerances (tg_theta_tolerances), then tg_tree_fields_grouped at the model's angle cap with those
+    tolerances -- inside the learned call the inference kernel writes the tolerances itself. The
+    features (whose top-level frontier is listed in node order) and the learned walk repeat bit for
+    bit."""
+    torch, _lib, L, theta = env
+    tree, keep, x = plummer_tree
+    n = len(x)
+    model = theta.ThetaModel.load()
+    if model.kind != "tolerance":
+        pytest.skip("the shipped model is not a tolerance model")
+    l10 = theta.default_lambda(model, True)
+    f1 = theta.features(tree, 32, True)
+    f2 = theta.features(tree, 32, True)
+    assert np.array_equal(f1, f2)
+    u = torch.from_numpy(theta.predict(model, f1, l10)).cuda()
+    tol = torch.empty(len(f1), dtype=torch.float32, device="cuda")
+    assert L.tg_theta_tolerances(tree, 32, 1, vp(u), vp(tol), None) == 0
+    parts = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    assert L.tg_tree_fields_grouped(tree, _lib.TG_FIELD_ACCEL, 1, 1.0, 32, model.theta_max, None, vp(tol),
+                                    _lib.TG_MEM_DEVICE, vp(parts), None) == 0
+    a = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    b = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    h = model.handle()
+    try:
+        assert L.tg_theta_model_set_error_budget(h, 0.0) == 0
+        for out in (a, b):
+            assert L.tg_tree_fields_learned(tree, _lib.TG_FIELD_ACCEL, 1, 1.0, 32, h, l10, 0.7, _lib.TG_MEM_DEVICE,
+                                            vp(out), None) == 0
+        torch.cuda.synchronize()
+        assert torch.equal(a, b)
+        assert torch.equal(a, parts)
+    finally:
+        model.close()
+
+
 def test_shipped_model_error_budget_rewalks_few_groups(env, plummer_tree):
     """The shipped budget (twice the worst estimate over the training systems) leaves a held-out
     Plummer system's groups alone, or nearly so."""

@@ -250,3 +250,30 @@ def test_tree_used_on_other_streams_right_after_the_build(tg):
         assert mass[n] == ref_tree.Masses[n]  # the root's mass comes from the moment pass
         L.tg_tree_free(t)
         torch.cuda.synchronize()
+
+
+def test_trees_share_pooled_streams_and_events(tg):
+    """Trees take their side streams and events from the library's pool and return them when freed
+    (with work possibly still queued on them): many trees built, walked and freed, two alive at a
+    time and freed in either order, give the first tree's results every time."""
+    import gc
+
+    from pytreegrav_gb300 import synthetic
+
+    x = synthetic.plummer(20_000, 17)
+    n = len(x)
+    m = np.full(n, 1.0 / n)
+    h = np.full(n, 0.01)
+    kw = dict(accel=True, quadrupole=True, group_size=32, theta=0.7, grouping="tree")
+    ref = tg.ConstructTree(x, m, h, quadrupole=True).fields(**kw)["accel"]
+    alive = []
+    for i in range(24):
+        t = tg.ConstructTree(x, m, h, quadrupole=True)
+        alive.append(t)
+        assert np.array_equal(t.fields(**kw)["accel"], ref), i
+        if len(alive) == 2:
+            alive.pop(i % 2)  # free the older or the newer one
+            gc.collect()
+    alive.clear()
+    gc.collect()
+    assert np.array_equal(tg.ConstructTree(x, m, h, quadrupole=True).fields(**kw)["accel"], ref)
