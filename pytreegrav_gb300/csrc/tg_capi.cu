@@ -116,7 +116,7 @@ void destroy(tg_tree_s *t) {
     free_arena(t->arena32, st);
     free_arena(t->arena64, st);
     if (t->stats_dev) cudaFreeAsync(t->stats_dev, st);
-    f(t->groups); f(t->group_root); f(t->group_node); f(t->gstats); f(t->gerr); f(t->sort_err); f(t->vel); f(t->vdisp); f(t->quad32); f(t->lvl_list); f(t->fdepth);
+    f(t->groups); f(t->group_root); f(t->group_node); f(t->gstats); f(t->gerr); f(t->sort_err); f(t->vel); f(t->vdisp); f(t->quad32); f(t->lvl_list); f(t->fdepth); f(t->own32);
     release_stream(t->side);  // back to the library's pool, its queued work still to run
     release_event(t->ev_fork, false, t->dev);
     release_event(t->ev_join, false, t->dev);

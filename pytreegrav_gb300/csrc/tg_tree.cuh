@@ -91,6 +91,9 @@ struct tg_tree_s {
 
     tg::Arena<float> arena32;
     tg::Arena<double> arena64;
+    // FP32 walk targets of the tree's own particles in walk order (ntot hi rows, then ntot lo rows),
+    // made on the side stream beside the first grouping; null until then.
+    float4 *own32 = nullptr;
     tg::WalkStats last_stats;
     int64_t *stats_dev = nullptr;  // 8 counters
 

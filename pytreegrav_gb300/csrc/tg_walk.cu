@@ -1985,16 +1985,22 @@ tg_status run_walk(tg_tree_s *t, const double *tpos, const double *th, int64_t n
         a.gstats = gstats;
         a.prefetch = arena_exceeds_l2(t->arena32);
         vec4<float> *thi = nullptr, *tlo = nullptr;
-        TG_CUDA(tg::dev_malloc((void **)&thi, sizeof(vec4<float>) * std::max<int64_t>(ntargets, 1), st));
-        TG_CUDA(tg::dev_malloc((void **)&tlo, sizeof(vec4<float>) * std::max<int64_t>(ntargets, 1), st));
-        { k_prep_targets<float><<<div_up(ntargets, 256), 256, 0, st>>>(tpos, th, ntargets, thi, tlo); tg::note_launch(); }
-        a.thi = thi;
-        a.tlo = tlo;
+        const bool own = t->own32 && tpos == t->coord && th == t->soft && ntargets == t->ntot;
+        if (own) {  // the tree's own particles, prepared beside the first grouping
+            a.thi = t->own32;
+            a.tlo = t->own32 + t->ntot;
+        } else {
+            TG_CUDA(tg::dev_malloc((void **)&thi, sizeof(vec4<float>) * std::max<int64_t>(ntargets, 1), st));
+            TG_CUDA(tg::dev_malloc((void **)&tlo, sizeof(vec4<float>) * std::max<int64_t>(ntargets, 1), st));
+            { k_prep_targets<float><<<div_up(ntargets, 256), 256, 0, st>>>(tpos, th, ntargets, thi, tlo); tg::note_launch(); }
+            a.thi = thi;
+            a.tlo = tlo;
+        }
         rc = walk_with_fallback<float>(t, a, t->arena32, fields, quadrupole != 0, t->walk_warps, t->walk_stack,
                                        scratch, split_heavy, st, &status,
                                        &kms);
-        cudaFreeAsync(thi, st);
-        cudaFreeAsync(tlo, st);
+        if (thi) cudaFreeAsync(thi, st);
+        if (tlo) cudaFreeAsync(tlo, st);
     }
     if (rc != TG_OK) return rc;
     unsigned long long stats[8];
@@ -2112,6 +2118,17 @@ tg_status tree_groups_with_arena(tg_tree_s *t, int G, bool fp64, cudaStream_t st
         tg_status r = tree_groups(t, G, t->side);
         const bool topo = r == TG_OK && need_arena;
         if (topo) r = fp64 ? build_arena_topology(t, t->arena64, t->side) : build_arena_topology(t, t->arena32, t->side);
+        if (r == TG_OK && !fp64 && !t->own32 && t->ntot > 0) {  // the FP32 walk's own targets, here too
+            const cudaError_t ea = tg::dev_malloc((void **)&t->own32, sizeof(float4) * 2 * t->ntot, t->side);
+            if (ea != cudaSuccess) {
+                t->own32 = nullptr;
+                r = TG_ERR_CUDA;
+            } else {
+                k_prep_targets<float><<<div_up(t->ntot, 256), 256, 0, t->side>>>(t->coord, t->soft, t->ntot, t->own32,
+                                                                                 t->own32 + t->ntot);
+                tg::note_launch();
+            }
+        }
         const cudaError_t ej = cudaEventRecord(t->ev_join, t->side);
         if (ej != cudaSuccess) {  // the join could not be recorded: wait for the side stream from the host
             cudaStreamSynchronize(t->side);
