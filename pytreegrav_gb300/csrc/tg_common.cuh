@@ -220,6 +220,12 @@ LoopLimits &loop_limits();
 
 int num_sms();
 
+// The calling thread's current CUDA context (the driver's cuCtxGetCurrent, reached through the
+// runtime's entry-point query so that the library needs no link to the driver library), or null.
+// Library state tied to a device (pooled streams, events and memory, cached addresses) is kept with
+// the context it belongs to and made again after a device reset.
+void *current_cuda_context();
+
 // Stream-ordered device allocation from the library's own memory pool on the current device.
 // The pool keeps freed memory mapped for later calls, up to a quarter of the device's memory and at
 // least TG_POOL_KEEP_BYTES: a build and a walk allocate and free their temporaries on every call, and

@@ -88,24 +88,6 @@ struct ScratchAddr {
 };
 ScratchAddr g_addr[MAX_DEVICES];
 
-// The calling thread's current CUDA context (the driver's cuCtxGetCurrent, reached through the
-// runtime's entry-point query so that the library needs no link to the driver library), or null.
-void *current_context() {
-    using CtxGetCurrent = int (*)(void **);
-    static CtxGetCurrent fn = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = (CtxGetCurrent)p;
-    });
-    void *ctx = nullptr;
-    if (fn && fn(&ctx) != 0) ctx = nullptr;
-    return ctx;
-}
-
 // Device address of the scratch array on the current device, looked up once per device and context.
 tg_status scratch_on_current_device(unsigned char **out) {
     int dev = 0;
@@ -116,12 +98,12 @@ tg_status scratch_on_current_device(unsigned char **out) {
     }
     std::lock_guard<std::mutex> lock(g_addr_mutex);
     ScratchAddr &c = g_addr[dev];
-    void *ctx = current_context();
+    void *ctx = current_cuda_context();
     if (!c.addr || !ctx || c.ctx != ctx) {
         void *p = nullptr;
         TG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));  // makes the device's context current if needed
         c.addr = (unsigned char *)p;
-        c.ctx = current_context();
+        c.ctx = current_cuda_context();
     }
     *out = c.addr;
     return TG_OK;

@@ -32,15 +32,51 @@ int num_sms() {
     return sms;
 }
 
+void *current_cuda_context() {
+    using CtxGetCurrent = int (*)(void **);
+    static CtxGetCurrent fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (CtxGetCurrent)p;
+    });
+    void *ctx = nullptr;
+    if (fn && fn(&ctx) != 0) ctx = nullptr;
+    return ctx;
+}
+
 namespace {
 constexpr int POOL_DEVICES = 64;
 std::mutex g_res_mu;
-std::vector<cudaStream_t> g_streams[POOL_DEVICES];
-std::vector<cudaEvent_t> g_events[POOL_DEVICES][2];  // [timing]
+// Per device: the context the pooled streams and events belong to, and the pools. After a device
+// reset (a new context) the old handles are dropped, not reused.
+struct ResPool {
+    void *ctx = nullptr;
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> events[2];  // [timing]
+};
+ResPool g_res[POOL_DEVICES];
 int current_device() {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= POOL_DEVICES) return -1;
     return dev;
+}
+// The pool of device dev for the current context (g_res_mu held). A thread that has not bound a
+// context yet (null) keeps the pool.
+ResPool &res_pool(int dev) {
+    ResPool &r = g_res[dev];
+    void *ctx = current_cuda_context();
+    if (ctx && !r.ctx) r.ctx = ctx;  // filled before a context was bound
+    if (ctx && r.ctx != ctx) {
+        r.streams.clear();
+        r.events[0].clear();
+        r.events[1].clear();
+        r.ctx = ctx;
+    }
+    return r;
 }
 }  // namespace
 
@@ -53,9 +89,10 @@ cudaError_t pool_stream(cudaStream_t *s) {
     const int dev = current_device();
     if (dev >= 0) {
         std::lock_guard<std::mutex> lock(g_res_mu);
-        if (!g_streams[dev].empty()) {
-            *s = g_streams[dev].back();
-            g_streams[dev].pop_back();
+        ResPool &r = res_pool(dev);
+        if (!r.streams.empty()) {
+            *s = r.streams.back();
+            r.streams.pop_back();
             return cudaSuccess;
         }
     }
@@ -70,14 +107,14 @@ void release_stream(cudaStream_t s) {
         return;
     }
     std::lock_guard<std::mutex> lock(g_res_mu);
-    g_streams[dev].push_back(s);
+    res_pool(dev).streams.push_back(s);
 }
 
 cudaError_t pool_event(cudaEvent_t *e, bool timing) {
     const int dev = current_device();
     if (dev >= 0) {
         std::lock_guard<std::mutex> lock(g_res_mu);
-        auto &v = g_events[dev][timing ? 1 : 0];
+        auto &v = res_pool(dev).events[timing ? 1 : 0];
         if (!v.empty()) {
             *e = v.back();
             v.pop_back();
@@ -95,13 +132,14 @@ void release_event(cudaEvent_t e, bool timing, int dev) {
         return;
     }
     std::lock_guard<std::mutex> lock(g_res_mu);
-    g_events[dev][timing ? 1 : 0].push_back(e);
+    res_pool(dev).events[timing ? 1 : 0].push_back(e);
 }
 
 cudaError_t dev_malloc(void **p, size_t bytes, cudaStream_t s) {
     constexpr int MAX_DEVICES = 64;
     static std::mutex mu;
     static cudaMemPool_t pools[MAX_DEVICES] = {};
+    static void *pool_ctx[MAX_DEVICES] = {};  // a device reset makes a new context: a new pool
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -109,6 +147,9 @@ cudaError_t dev_malloc(void **p, size_t bytes, cudaStream_t s) {
     cudaMemPool_t pool;
     {
         std::lock_guard<std::mutex> lock(mu);
+        void *ctx = current_cuda_context();  // null on a thread that has not bound a context yet
+        if (pools[dev] && ctx && !pool_ctx[dev]) pool_ctx[dev] = ctx;          // made before a context was bound
+        if (pools[dev] && ctx && pool_ctx[dev] != ctx) pools[dev] = nullptr;  // the old pool died with its context
         if (!pools[dev]) {
             cudaMemPoolProps props = {};
             props.allocType = cudaMemAllocationTypePinned;
@@ -119,6 +160,7 @@ cudaError_t dev_malloc(void **p, size_t bytes, cudaStream_t s) {
                 pools[dev] = nullptr;
                 return e;
             }
+            pool_ctx[dev] = current_cuda_context();
             size_t free_b = 0, total_b = 0;
             unsigned long long keep = TG_POOL_KEEP_BYTES;
             if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && total_b / 4 > keep) keep = total_b / 4;
