@@ -1329,6 +1329,7 @@ __global__ void k_fold_only(MomentArgs a) {
 // build's own stream, with its fork and join events; created once.
 struct BuildSide {
     int dev = -1;
+    unsigned long long ctx = 0;  // id of the CUDA context the stream and events belong to
     cudaStream_t s = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
 };
@@ -1336,13 +1337,18 @@ static tg_status build_side(BuildSide *&out) {
     static thread_local BuildSide side;
     int dev = 0;
     TG_CUDA(cudaGetDevice(&dev));
-    if (side.s && side.dev != dev) side = BuildSide();  // another device: this thread's old one is kept alive
+    // another device (this thread's old one is kept alive), or a new context after a device reset
+    // (the old handles died with it)
+    const unsigned long long ctx = tg::current_cuda_context_id();
+    if (side.s && (side.dev != dev || (ctx && side.ctx && side.ctx != ctx))) side = BuildSide();
     if (!side.s) {
         TG_CUDA(cudaStreamCreateWithFlags(&side.s, cudaStreamNonBlocking));
         TG_CUDA(cudaEventCreateWithFlags(&side.fork, cudaEventDisableTiming));
         TG_CUDA(cudaEventCreateWithFlags(&side.join, cudaEventDisableTiming));
         side.dev = dev;
+        side.ctx = tg::current_cuda_context_id();
     }
+    if (!side.ctx) side.ctx = ctx;
     out = &side;
     return TG_OK;
 }

@@ -220,11 +220,13 @@ LoopLimits &loop_limits();
 
 int num_sms();
 
-// The calling thread's current CUDA context (the driver's cuCtxGetCurrent, reached through the
-// runtime's entry-point query so that the library needs no link to the driver library), or null.
-// Library state tied to a device (pooled streams, events and memory, cached addresses) is kept with
-// the context it belongs to and made again after a device reset.
-void *current_cuda_context();
+// The unique id of the calling thread's current CUDA context (the driver's cuCtxGetCurrent and
+// cuCtxGetId, reached through the runtime's entry-point query so that the library needs no link to
+// the driver library), the runtime's context bound first if none is (as after a device reset), or
+// 0 if that fails. A context made after a device reset has a new id, even where its handle is the
+// old one's. Library state tied to a device (pooled streams, events and memory, cached addresses)
+// is kept with the id of the context it belongs to and made again when the id changes.
+unsigned long long current_cuda_context_id();
 
 // Stream-ordered device allocation from the library's own memory pool on the current device.
 // The pool keeps freed memory mapped for later calls, up to a quarter of the device's memory and at

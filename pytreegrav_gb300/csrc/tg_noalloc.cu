@@ -83,7 +83,7 @@ std::mutex g_addr_mutex;
 // (cudaDeviceReset, or a reset of the primary context by the host application) the context is a
 // new one and the address is looked up again.
 struct ScratchAddr {
-    void *ctx = nullptr;
+    unsigned long long ctx = 0;  // context id
     unsigned char *addr = nullptr;
 };
 ScratchAddr g_addr[MAX_DEVICES];
@@ -98,12 +98,12 @@ tg_status scratch_on_current_device(unsigned char **out) {
     }
     std::lock_guard<std::mutex> lock(g_addr_mutex);
     ScratchAddr &c = g_addr[dev];
-    void *ctx = current_cuda_context();
+    const unsigned long long ctx = current_cuda_context_id();
     if (!c.addr || !ctx || c.ctx != ctx) {
         void *p = nullptr;
         TG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));  // makes the device's context current if needed
         c.addr = (unsigned char *)p;
-        c.ctx = current_cuda_context();
+        c.ctx = current_cuda_context_id();
     }
     *out = c.addr;
     return TG_OK;

@@ -32,20 +32,33 @@ int num_sms() {
     return sms;
 }
 
-void *current_cuda_context() {
+unsigned long long current_cuda_context_id() {
     using CtxGetCurrent = int (*)(void **);
-    static CtxGetCurrent fn = nullptr;
+    using CtxGetId = int (*)(void *, unsigned long long *);
+    static CtxGetCurrent get = nullptr;
+    static CtxGetId get_id = nullptr;
     static std::once_flag once;
     std::call_once(once, [] {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = (CtxGetCurrent)p;
+            get = (CtxGetCurrent)p;
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (CtxGetId)p;
     });
+    if (!get || !get_id) return 0;
     void *ctx = nullptr;
-    if (fn && fn(&ctx) != 0) ctx = nullptr;
-    return ctx;
+    if (get(&ctx) != 0) ctx = nullptr;
+    if (!ctx) {  // none bound to this thread yet (or just reset): let the runtime bind its context
+        cudaFree(nullptr);
+        if (get(&ctx) != 0) ctx = nullptr;
+    }
+    unsigned long long id = 0;
+    if (!ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
 }
 
 namespace {
@@ -54,7 +67,7 @@ std::mutex g_res_mu;
 // Per device: the context the pooled streams and events belong to, and the pools. After a device
 // reset (a new context) the old handles are dropped, not reused.
 struct ResPool {
-    void *ctx = nullptr;
+    unsigned long long ctx = 0;  // context id
     std::vector<cudaStream_t> streams;
     std::vector<cudaEvent_t> events[2];  // [timing]
 };
@@ -64,12 +77,11 @@ int current_device() {
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= POOL_DEVICES) return -1;
     return dev;
 }
-// The pool of device dev for the current context (g_res_mu held). A thread that has not bound a
-// context yet (null) keeps the pool.
+// The pool of device dev for the current context (g_res_mu held).
 ResPool &res_pool(int dev) {
     ResPool &r = g_res[dev];
-    void *ctx = current_cuda_context();
-    if (ctx && !r.ctx) r.ctx = ctx;  // filled before a context was bound
+    const unsigned long long ctx = current_cuda_context_id();
+    if (ctx && !r.ctx) r.ctx = ctx;  // filled before the context could be identified
     if (ctx && r.ctx != ctx) {
         r.streams.clear();
         r.events[0].clear();
@@ -139,7 +151,7 @@ cudaError_t dev_malloc(void **p, size_t bytes, cudaStream_t s) {
     constexpr int MAX_DEVICES = 64;
     static std::mutex mu;
     static cudaMemPool_t pools[MAX_DEVICES] = {};
-    static void *pool_ctx[MAX_DEVICES] = {};  // a device reset makes a new context: a new pool
+    static unsigned long long pool_ctx[MAX_DEVICES] = {};  // context ids: a device reset makes a new context
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -147,7 +159,7 @@ cudaError_t dev_malloc(void **p, size_t bytes, cudaStream_t s) {
     cudaMemPool_t pool;
     {
         std::lock_guard<std::mutex> lock(mu);
-        void *ctx = current_cuda_context();  // null on a thread that has not bound a context yet
+        const unsigned long long ctx = current_cuda_context_id();
         if (pools[dev] && ctx && !pool_ctx[dev]) pool_ctx[dev] = ctx;          // made before a context was bound
         if (pools[dev] && ctx && pool_ctx[dev] != ctx) pools[dev] = nullptr;  // the old pool died with its context
         if (!pools[dev]) {
@@ -160,7 +172,7 @@ cudaError_t dev_malloc(void **p, size_t bytes, cudaStream_t s) {
                 pools[dev] = nullptr;
                 return e;
             }
-            pool_ctx[dev] = current_cuda_context();
+            pool_ctx[dev] = current_cuda_context_id();
             size_t free_b = 0, total_b = 0;
             unsigned long long keep = TG_POOL_KEEP_BYTES;
             if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && total_b / 4 > keep) keep = total_b / 4;
