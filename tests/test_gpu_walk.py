@@ -3,7 +3,7 @@
 Tolerances: the FP64 walk evaluates the reference's accepted node set in double precision, so it
 agrees with the oracle to summation-order rounding (1e-12 relative). The FP32 walk (the engine's
 default) evaluates the same accepted set in single precision with compensated accumulation: it is
-held to 1e-5 relative RMS (the spec bar) and 1e-4 relative max per target. FP64 brute force
+held to 1e-5 relative RMS against the FP64 walk and 1e-4 relative max per target. FP64 brute force
 is the reference's arithmetic in the reference's order: bit-exact.
 """
 
