@@ -246,7 +246,8 @@ cudaError_t dev_malloc(void **p, size_t bytes, cudaStream_t s);
 // recorded again; waits already enqueued on it are unaffected.
 cudaError_t pool_stream(cudaStream_t *s);
 void release_stream(cudaStream_t s);
-// dev: the device the event was made on (-1: the current device).
+// dev: the device the event was made on (-1: the current device). A stream or event of another
+// device than the current one is destroyed instead of pooled.
 cudaError_t pool_event(cudaEvent_t *e, bool timing);
 void release_event(cudaEvent_t e, bool timing, int dev = -1);
 int current_device_or(int fallback);

@@ -114,7 +114,8 @@ cudaError_t pool_stream(cudaStream_t *s) {
 void release_stream(cudaStream_t s) {
     if (!s) return;
     int dev = -1;
-    if (cudaStreamGetDevice(s, &dev) != cudaSuccess || dev < 0 || dev >= POOL_DEVICES) {
+    // pooled only on the current device, whose context the pool's key is checked against
+    if (cudaStreamGetDevice(s, &dev) != cudaSuccess || dev < 0 || dev >= POOL_DEVICES || dev != current_device()) {
         cudaStreamDestroy(s);
         return;
     }
@@ -138,8 +139,9 @@ cudaError_t pool_event(cudaEvent_t *e, bool timing) {
 
 void release_event(cudaEvent_t e, bool timing, int dev) {
     if (!e) return;
-    if (dev < 0) dev = current_device();
-    if (dev < 0 || dev >= POOL_DEVICES) {
+    const int cur = current_device();
+    if (dev < 0) dev = cur;
+    if (dev < 0 || dev >= POOL_DEVICES || dev != cur) {  // pooled only on the current device (as streams)
         cudaEventDestroy(e);
         return;
     }
